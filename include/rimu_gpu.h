@@ -1,0 +1,186 @@
+/*
+ * rimu_gpu.h -- C ABI of librimu_gpu, the GB300 (sm_103a) implementation of the Rimu.jl
+ * FCIQMC step and its matrix-free Hamiltonian application.
+ *
+ * Plain C types only: opaque handles, host pointers for host data, raw device pointers
+ * (as const double * / double *) where a call works on device vectors.  Every call returns
+ * a status code; rimu_last_error() gives the message of the last failure on the calling
+ * thread.  Calls on one context are not thread safe; separate contexts are independent.
+ *
+ * Each entry point names the Rimu.jl interface it stands behind (file:line of the reference
+ * Rimu.jl v0.14.0 sources).
+ */
+#ifndef RIMU_GPU_H
+#define RIMU_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define RIMU_OK 0
+#define RIMU_ERR_BADARG 1    /* invalid argument (ArgumentError in the reference)          */
+#define RIMU_ERR_OOM 2       /* device or host allocation failed                            */
+#define RIMU_ERR_OVERFLOW 3  /* a capacity could not be grown enough                        */
+#define RIMU_ERR_TIMEOUT 4   /* a bounded device wait gave up                               */
+#define RIMU_ERR_CUDA 5      /* a CUDA runtime call failed                                  */
+#define RIMU_ERR_STATE 6     /* handle used in an invalid state                             */
+
+/* Walker amplitude types: Float64 (IsDeterministic, IsDynamicSemistochastic) and Int64
+ * (IsStochasticInteger), src/StochasticStyles/styles.jl:11-12,76-82,175-195. */
+#define RIMU_VAL_F64 0
+#define RIMU_VAL_I64 1
+
+/* Hamiltonians: src/Hamiltonians/HubbardReal1D.jl:22, HubbardRealSpace.jl:163,
+ * HubbardMom1D.jl:43. */
+#define RIMU_MODEL_REAL1D 1
+#define RIMU_MODEL_REALSPACE 2
+#define RIMU_MODEL_MOM1D 3
+
+/* Stochastic styles: IsStochasticInteger (styles.jl:11), IsDeterministic (styles.jl:76),
+ * IsDynamicSemistochastic (styles.jl:175). */
+#define RIMU_STYLE_INTEGER 0
+#define RIMU_STYLE_DETERMINISTIC 1
+#define RIMU_STYLE_DSS 2
+
+/* Operator applied by rimu_apply_operator: the FirstOrderTransitionOperator
+ * T = 1 + dt (S - H) (src/fciqmc.jl:78-112), or H itself (mul!, abstractdvec.jl:275-284). */
+#define RIMU_OP_TRANSITION 0
+#define RIMU_OP_HAMILTONIAN 1
+
+typedef struct rimu_ctx rimu_ctx;
+typedef struct rimu_model rimu_model;
+typedef struct rimu_vec rimu_vec;
+typedef struct rimu_wm rimu_wm;
+
+/* Hamiltonian description.  Addresses are single-chunk bit strings of at most 64 bits
+ * (BoseFS: n_particles + n_modes - 1 bits; FermiFS: n_modes bits), with the chunk layout of
+ * src/BitStringAddresses/bitstring.jl:464-472 (bosons) and 713-723 (fermions). */
+typedef struct {
+  int kind;                 /* RIMU_MODEL_* */
+  int fermion;              /* 1: FermiFS addresses (RIMU_MODEL_REALSPACE only) */
+  int n_particles;
+  int n_modes;
+  double u;                 /* interaction (HubbardRealSpace: u[1,1]) */
+  double t;                 /* hopping */
+  int ndim;                 /* HubbardRealSpace CubicGrid dimensions (1..3) */
+  int dims[3];
+  int periodic[3];          /* 1: PeriodicBoundaries, 0: HardwallBoundaries per dimension */
+  const double *potential;  /* HubbardRealSpace trap energy per site (n_modes) or NULL */
+  const double *dispersion; /* HubbardMom1D kinetic energies h.kes (n_modes), required */
+} rimu_model_desc;
+
+/* Parameters of one projector step (apply_operator!, src/Interfaces/dictvectors.jl:112). */
+typedef struct {
+  int style;                     /* RIMU_STYLE_* */
+  int op;                        /* RIMU_OP_* */
+  double dt;                     /* time step dτ */
+  double shift;                  /* shift S */
+  double boost;                  /* apply_operator! boost (1.0) */
+  double proj_threshold;         /* on-the-fly projection threshold (0: none) */
+  double compression;            /* ThresholdCompression threshold after annihilation (0: none) */
+  double rel_spawning_threshold; /* DynamicSemistochastic rel_threshold (1.0) */
+  double abs_spawning_threshold; /* DynamicSemistochastic abs_threshold (Inf) */
+  uint64_t seed;                 /* random stream seed */
+  uint64_t step;                 /* step number (part of every random counter) */
+  uint32_t replica;              /* replica id (part of every random key) */
+} rimu_step_params;
+
+/* Step statistics (step_stats, styles.jl:14-19,94-96,203-208; compression.jl:16) plus the
+ * walkernumber_and_length of the new vector (abstractdvec.jl:270) and the ProjectedEnergy
+ * dot products of the working-memory projector (poststepstrategy.jl:110-121). */
+typedef struct {
+  double norm;
+  int64_t len;
+  int64_t len_before;
+  int64_t exact_steps;
+  int64_t inexact_steps;
+  int64_t spawn_attempts;
+  double spawns;
+  int64_t clones;
+  int64_t deaths;
+  int64_t zombies;
+  double vproj;
+  double hproj;
+  int64_t spawn_records;
+  int32_t retries;
+  int32_t nb_bits;
+} rimu_step_stats;
+
+/* Library and errors. */
+int rimu_version(void);
+int rimu_last_error(char *buf, size_t len);
+
+/* Context: one device and one stream; stream may be NULL (the library creates one). */
+int rimu_ctx_create(int device, void *stream, rimu_ctx **out);
+int rimu_ctx_destroy(rimu_ctx *ctx);
+int rimu_ctx_synchronize(rimu_ctx *ctx);
+
+/* Hamiltonian handle: stands behind the AbstractHamiltonian constructors
+ * (HubbardReal1D.jl:26, HubbardRealSpace.jl:182, HubbardMom1D.jl:49). */
+int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *desc, rimu_model **out);
+int rimu_model_destroy(rimu_model *m);
+/* diagonal_element (Interfaces/hamiltonians.jl:241) for n host addresses. */
+int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t n, double *out);
+/* num_offdiagonals / offdiagonals (Interfaces/hamiltonians.jl:263,309): all offdiagonal
+ * (address, element) pairs of one column, in the reference's order; illegal hard-wall moves
+ * give (address, 0.0) as in HubbardRealSpace.jl:331-332. */
+int rimu_model_num_offdiagonals(rimu_model *m, uint64_t key, int *out);
+int rimu_model_offdiagonals(rimu_model *m, uint64_t key, uint64_t *keys, double *vals, int cap,
+                            int *n);
+
+/* Device-resident walker list: stands behind DVec / PDVec (src/DictVectors/dvec.jl,
+ * pdvec.jl) as an AbstractDVec (Interfaces/dictvectors.jl:40). */
+int rimu_vec_create(rimu_ctx *ctx, int val_kind, int64_t capacity_hint, rimu_vec **out);
+int rimu_vec_destroy(rimu_vec *v);
+/* Replace the contents with n (address, value) pairs from host memory; addresses must be
+ * distinct.  vals points to double (RIMU_VAL_F64) or int64_t (RIMU_VAL_I64). */
+int rimu_vec_upload(rimu_vec *v, const uint64_t *keys, const void *vals, int64_t n);
+/* Copy all pairs to host memory (any order); *n receives the length. */
+int rimu_vec_download(rimu_vec *v, uint64_t *keys, void *vals, int64_t cap, int64_t *n);
+int rimu_vec_length(rimu_vec *v, int64_t *len);
+/* walkernumber_and_length (abstractdvec.jl:258-270; pdvec.jl:896-902). */
+int rimu_vec_walkernumber_and_length(rimu_vec *v, double *norm, int64_t *len);
+/* getindex for n host addresses (0 where absent): the dot products of dot(P, v). */
+int rimu_vec_lookup(rimu_vec *v, const uint64_t *keys, int64_t n, void *vals);
+int rimu_vec_copy(rimu_vec *dst, const rimu_vec *src);
+int rimu_vec_empty(rimu_vec *v);
+
+/* Working memory: stands behind working_memory(v) (Interfaces/dictvectors.jl:87,
+ * pdworkingmemory.jl:295). */
+int rimu_wm_create(rimu_ctx *ctx, rimu_wm **out);
+int rimu_wm_destroy(rimu_wm *wm);
+/* ProjectedEnergy projector (poststepstrategy.jl:90-121): sorted distinct addresses with
+ * projector values P and (H'P) values; each step reports vproj = <P|v'> and hproj = <H'P|v'>.
+ * n = 0 removes the projector. */
+int rimu_wm_set_projector(rimu_wm *wm, const uint64_t *keys, const double *pvals,
+                          const double *hpvals, int n);
+
+/* One projector step target = T(source), with stats: apply_operator!(wm, target, source,
+ * op, boost) of src/Interfaces/dictvectors.jl:112-140 and pdworkingmemory.jl:297-309,
+ * including the compression of compression.jl:28-42.  source is not modified. */
+int rimu_apply_operator(rimu_model *m, rimu_wm *wm, rimu_vec *target, const rimu_vec *source,
+                        const rimu_step_params *params, rimu_step_stats *stats);
+
+/* Full sorted basis (build_basis, ExactDiagonalization/basis_fock.jl:33-36): all BoseFS
+ * (FermiFS) addresses in increasing bit-string order. */
+int rimu_basis_dimension(rimu_model *m, int64_t *dim);
+int rimu_basis_keys(rimu_model *m, int64_t start, int64_t n, uint64_t *keys);
+
+/* Matrix-free w = H v on the full sorted basis, v and w device arrays of length dim: the
+ * mul!(w, H, v) behind KrylovKit's OperatorMultiplier (ext/KrylovKitExt.jl:23-46,
+ * abstractdvec.jl:275-284).  Runs on the context stream. */
+int rimu_hv_basis(rimu_model *m, const double *v, double *w, int64_t dim);
+/* Adjoint of w = H(u, t) v for HubbardReal1D and bosonic one-component HubbardRealSpace
+ * without trap: gv = H^T gw, gu = <gw, dH/du v>, gt = <gw, dH/dt v> (no counterpart in the
+ * reference; the rrule a ChainRulesCore extension would register for mul!). */
+int rimu_hv_basis_adjoint(rimu_model *m, const double *v, const double *gw, double *gv,
+                          double *gu, double *gt, int64_t dim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RIMU_GPU_H */

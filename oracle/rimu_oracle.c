@@ -1,0 +1,706 @@
+/*
+ * rimu_oracle.c -- CPU restatement of the Rimu.jl FCIQMC hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA path is compared
+ * against; it is never linked into, loaded by, or called from the product library.
+ * Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use it.
+ *
+ * It restates, in plain C and on occupation-number arrays (ONR) rather than bit tricks,
+ * the reference semantics of:
+ *   - BoseFS / FermiFS bit-string encodings      src/BitStringAddresses/bitstring.jl:464-472,
+ *                                                 511-520, 713-723, 746-791
+ *   - HubbardReal1D                               src/Hamiltonians/HubbardReal1D.jl:51-62
+ *   - HubbardRealSpace (one component)            src/Hamiltonians/HubbardRealSpace.jl:18,90-97,
+ *                                                 279-338; geometry.jl:127-139,161-181,232-235
+ *   - HubbardMom1D (BoseFS)                       src/Hamiltonians/HubbardMom1D.jl:49-65,131-194;
+ *                                                 excitations.jl:26-80,126-137
+ *   - FirstOrderTransitionOperator                src/fciqmc.jl:78-112
+ *   - the stochastic styles                       src/StochasticStyles/styles.jl:11-25,94-105,
+ *                                                 175-214; spawning.jl:9-93,174-182,232-243,
+ *                                                 364-378; compression.jl:18-42
+ *   - one apply_operator! step                    src/Interfaces/dictvectors.jl:112-140
+ *   - the matrix-free product                     src/DictVectors/abstractdvec.jl:275-284
+ *
+ * Random numbers.  The reference draws from Julia's task-local Xoshiro in dictionary
+ * iteration order, which no parallel implementation can reproduce.  This restatement uses
+ * the counter-based Philox4x32-10 generator (Salmon, Moraes, Dror, Shaw, SC'11), keyed on
+ * (seed, purpose, replica) and counted by (draw index, step, address), so that any
+ * evaluation order gives the same draws.  The GPU path uses the same stream definition, so
+ * stochastic steps are compared bit for bit; agreement with the reference itself is
+ * statistical (blocking analysis against exact energies).
+ *
+ * Arithmetic.  Floating-point operations follow the reference expressions except where a
+ * different but equally valid rounding order was chosen for the GPU (documented at each
+ * site).  Contributions to one address are summed in a canonical order: the diagonal
+ * term first, then the spawned values in increasing numerical order.  Compile with
+ * -ffp-contract=off so that no multiply-add is fused.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#define O_MAXM 64
+
+/* ------------------------------------------------------------------------------------ */
+/* Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3", SC'11). */
+/* ------------------------------------------------------------------------------------ */
+void o_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+enum { O_PURPOSE_SPAWN = 1, O_PURPOSE_DIAG = 2, O_PURPOSE_COMPRESS = 3 };
+
+/* One Philox block for (seed, purpose, replica) at counter (j, step, address). */
+void o_draw(uint64_t seed, uint32_t purpose, uint32_t replica, uint32_t step, uint64_t addr,
+            uint32_t j, uint32_t out[4]) {
+  uint32_t ctr[4] = {j, step, (uint32_t)addr, (uint32_t)(addr >> 32)};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32) ^ (purpose << 28) ^ replica};
+  o_philox4x32_10(ctr, key, out);
+}
+static inline uint64_t o_u53(const uint32_t r[4]) {
+  return ((uint64_t)r[1] << 21) | (uint64_t)(r[2] >> 11);
+}
+/* r < p with r = u53 * 2^-53, evaluated exactly (p in [0, 1]). */
+static inline int o_bernoulli(uint64_t u53, double p) {
+  return (double)u53 < ldexp(p, 53);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Addresses                                                                             */
+/* ------------------------------------------------------------------------------------ */
+/* from_bose_onr, single chunk: bitstring.jl:464-472.  Mode 1 sits at the low end; each
+ * mode contributes n_i ones followed by one zero (the last mode has no trailing zero). */
+uint64_t o_bose_from_onr(const int *onr, int M) {
+  uint64_t result = 0;
+  for (int i = M - 1; i >= 0; --i) {
+    uint64_t n = (uint64_t)onr[i];
+    result = (n + 1 >= 64) ? 0 : (result << (n + 1));
+    result |= (n >= 64) ? ~0ull : (((uint64_t)1 << n) - 1);
+  }
+  return result;
+}
+/* to_bose_onr, single chunk: bitstring.jl:511-520. */
+void o_bose_to_onr(uint64_t key, int M, int *onr) {
+  for (int i = 0; i < M; ++i) onr[i] = 0;
+  for (int mode = 0; mode < M; ++mode) {
+    int b = 0;
+    while (b < 64 && ((key >> b) & 1)) ++b;
+    onr[mode] = b;
+    key = (b + 1 >= 64) ? 0 : key >> (b + 1);
+    if (key == 0) break;
+  }
+}
+/* from_fermi_onr: bitstring.jl:713-723 (mode k <-> bit k-1). */
+uint64_t o_fermi_from_onr(const int *onr, int M) {
+  uint64_t r = 0;
+  for (int k = 0; k < M; ++k) if (onr[k]) r |= (uint64_t)1 << k;
+  return r;
+}
+void o_fermi_to_onr(uint64_t key, int M, int *onr) {
+  for (int k = 0; k < M; ++k) onr[k] = (int)((key >> k) & 1);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Models                                                                                */
+/* ------------------------------------------------------------------------------------ */
+enum { O_REAL1D = 1, O_REALSPACE = 2, O_MOM1D = 3 };
+
+typedef struct {
+  int kind;          /* O_REAL1D, O_REALSPACE, O_MOM1D */
+  int fermion;       /* 1: FermiFS address (HubbardRealSpace only) */
+  int N, M;
+  double u, t;
+  int ndim;          /* HubbardRealSpace geometry */
+  int dims[3];
+  int periodic[3];
+  const double *pot; /* HubbardRealSpace trap energy per site, or NULL */
+  const double *kes; /* HubbardMom1D dispersion per mode */
+} o_model;
+
+static void o_to_onr(const o_model *h, uint64_t key, int *onr) {
+  if (h->fermion) o_fermi_to_onr(key, h->M, onr); else o_bose_to_onr(key, h->M, onr);
+}
+static uint64_t o_from_onr(const o_model *h, const int *onr) {
+  return h->fermion ? o_fermi_from_onr(onr, h->M) : o_bose_from_onr(onr, h->M);
+}
+static int o_num_occupied(const int *onr, int M) {
+  int c = 0;
+  for (int i = 0; i < M; ++i) c += onr[i] > 0;
+  return c;
+}
+/* k-th occupied mode (1-based k), returns 0-based mode index or -1
+ * (find_occupied_mode, fockaddress.jl:115-125). */
+static int o_find_occupied(const int *onr, int M, int k) {
+  for (int i = 0; i < M; ++i) if (onr[i] > 0 && --k == 0) return i;
+  return -1;
+}
+
+/* neighbor_site(geometry, mode, chosen): geometry.jl:127-139,161-181,232-235.
+ * mode is 0-based here, chosen is 1-based; returns 0-based site or -1 if illegal. */
+static int o_neighbor_site(const o_model *h, int mode, int chosen) {
+  int D = h->ndim, x[3] = {0, 0, 0}, rem = mode;
+  for (int d = 0; d < D; ++d) { x[d] = rem % h->dims[d]; rem /= h->dims[d]; }
+  int dir = chosen <= D ? chosen - 1 : chosen - D - 1;
+  int step = chosen <= D ? 1 : -1;
+  x[dir] += step;
+  if (x[dir] < 0 || x[dir] >= h->dims[dir]) {
+    if (!h->periodic[dir]) return -1;
+    x[dir] = (x[dir] + h->dims[dir]) % h->dims[dir];
+  }
+  int site = 0;
+  for (int d = D - 1; d >= 0; --d) site = site * h->dims[d] + x[d];
+  return site;
+}
+
+int o_num_offdiagonals(const o_model *h, uint64_t key) {
+  int onr[O_MAXM];
+  o_to_onr(h, key, onr);
+  int s = o_num_occupied(onr, h->M);
+  if (h->kind == O_REAL1D) return 2 * s;                        /* HubbardReal1D.jl:51-53 */
+  if (h->kind == O_REALSPACE) return s * 2 * h->ndim;           /* HubbardRealSpace.jl:316-321 */
+  int d = 0;                                                    /* HubbardMom1D.jl:103-140 */
+  for (int i = 0; i < h->M; ++i) d += onr[i] > 1;
+  return s * (s - 1) * (h->M - 2) + d * (h->M - 1);
+}
+
+/* Fermionic single excitation sign (fermi_excitation, bitstring.jl:746-791).
+ * Returns 0 for an illegal move, else +1/-1; updates onr. */
+static int o_fermi_hop(int *onr, int src, int dst) {
+  if (!onr[src] || onr[dst]) return 0;
+  int count = 0;
+  for (int k = 0; k < src; ++k) count += onr[k];
+  onr[src] = 0;
+  for (int k = 0; k < dst; ++k) count += onr[k];
+  onr[dst] = 1;
+  return (count % 2 == 0) ? 1 : -1;
+}
+
+/* Hamiltonian matrix element of offdiagonal `chosen` (1-based) of column `key`:
+ * returns the new address and H_{new,key}; *prod receives the integer under the square
+ * root of the element (0 for an illegal move). */
+void o_get_offdiagonal_p(const o_model *h, uint64_t key, int chosen, uint64_t *nkey,
+                         double *val, long *prod) {
+  int onr[O_MAXM];
+  *prod = 0;
+  o_to_onr(h, key, onr);
+  int M = h->M;
+  if (h->kind == O_REAL1D) {
+    /* hopnextneighbour restated on the ONR, as in test/BitStringAddresses.jl:251-267. */
+    int site = (chosen + 1) / 2;
+    int i = o_find_occupied(onr, M, site);
+    int j = (chosen % 2 == 1) ? (i + 1) % M : (i - 1 + M) % M;
+    *prod = (long)onr[i] * (onr[j] + 1);
+    onr[i] -= 1;
+    onr[j] += 1;
+    *nkey = o_from_onr(h, onr);
+    *val = -h->t * sqrt((double)((onr[i] + 1) * onr[j]));
+    return;
+  }
+  if (h->kind == O_REALSPACE) {
+    int nb = 2 * h->ndim;
+    int particle = (chosen - 1) / nb + 1, neigh = (chosen - 1) % nb + 1;
+    int src = o_find_occupied(onr, M, particle);
+    int dst = o_neighbor_site(h, src, neigh);
+    if (dst < 0) { *nkey = key; *val = 0.0; return; }
+    if (h->fermion) {
+      int sgn = o_fermi_hop(onr, src, dst);
+      if (!sgn) { *nkey = key; *val = 0.0; return; }
+      *nkey = o_from_onr(h, onr);
+      *val = -h->t * (double)sgn;
+      *prod = 1;
+      return;
+    }
+    int value = onr[src] * (onr[dst] + 1);   /* bose_excitation_value, fockaddress.jl:559-567 */
+    *prod = value;
+    onr[src] -= 1;
+    onr[dst] += 1;
+    *nkey = o_from_onr(h, onr);
+    *val = -h->t * sqrt((double)value);
+    return;
+  }
+  /* HubbardMom1D: momentum_transfer_excitation with fold=true, excitations.jl:26-80. */
+  int map_mode[O_MAXM], map_occ[O_MAXM], s = 0;
+  for (int i = 0; i < M; ++i) if (onr[i] > 0) { map_mode[s] = i + 1; map_occ[s] = onr[i]; ++s; }
+  int dbl = chosen - s * (s - 1) * (M - 2);
+  int p_idx, q_idx, mom_change;
+  if (dbl > 0) {
+    int which = (dbl - 1) / (M - 1) + 1;
+    mom_change = (dbl - 1) % (M - 1) + 1;
+    int idx = 0;
+    for (int k = 0; k < s; ++k) {
+      which -= map_occ[k] >= 2;
+      if (which == 0) { idx = k; break; }
+    }
+    p_idx = q_idx = idx;
+  } else {
+    int pair = (chosen - 1) / (M - 2) + 1;
+    mom_change = (chosen - 1) % (M - 2) + 1;
+    int fst = (pair - 1) / (s - 1) + 1, snd = (pair - 1) % (s - 1) + 1;
+    int f_hole, s_hole;
+    if (snd < fst) { f_hole = snd; s_hole = fst; } else { f_hole = fst; s_hole = snd + 1; }
+    p_idx = f_hole - 1;
+    q_idx = s_hole - 1;
+    if (mom_change >= map_mode[q_idx] - map_mode[p_idx]) mom_change += 1;
+  }
+  int src1 = map_mode[p_idx], src2 = map_mode[q_idx];
+  int dst1 = ((src1 + mom_change - 1) % M + M) % M + 1;
+  int dst2 = ((src2 - mom_change - 1) % M + M) % M + 1;
+  /* a†_{dst1} a†_{dst2} a_{src2} a_{src1}: destroy then create, multiplying occupations. */
+  long value = 1;
+  value *= onr[src2 - 1]; onr[src2 - 1] -= 1;
+  value *= onr[src1 - 1]; onr[src1 - 1] -= 1;
+  value *= onr[dst2 - 1] + 1; onr[dst2 - 1] += 1;
+  value *= onr[dst1 - 1] + 1; onr[dst1 - 1] += 1;
+  if (value == 0) { *nkey = key; *val = 0.0; return; }
+  *nkey = o_from_onr(h, onr);
+  *prod = value;
+  /* get_offdiagonal: ham.u/(2*M)*onproduct, HubbardMom1D.jl:189-194 */
+  *val = h->u / (2 * M) * sqrt((double)value);
+}
+
+void o_get_offdiagonal(const o_model *h, uint64_t key, int chosen, uint64_t *nkey, double *val) {
+  long prod;
+  o_get_offdiagonal_p(h, key, chosen, nkey, val, &prod);
+}
+
+double o_diagonal(const o_model *h, uint64_t key) {
+  int onr[O_MAXM];
+  o_to_onr(h, key, onr);
+  int M = h->M;
+  if (h->kind == O_REAL1D) {
+    long bhi = 0;
+    for (int i = 0; i < M; ++i) bhi += (long)onr[i] * (onr[i] - 1);
+    return h->u * (double)bhi / 2;                         /* HubbardReal1D.jl:55-57 */
+  }
+  if (h->kind == O_REALSPACE) {
+    double in = 0.0;
+    if (!h->fermion && h->u != 0.0) {
+      long bhi = 0;
+      for (int i = 0; i < M; ++i) bhi += (long)onr[i] * (onr[i] - 1);
+      in = h->u * (double)bhi / 2;                         /* HubbardRealSpace.jl:18 */
+    }
+    double pe = 0.0;
+    if (h->pot) for (int i = 0; i < M; ++i) if (onr[i]) pe += onr[i] * h->pot[i];
+    return in + pe;                                        /* HubbardRealSpace.jl:284-293 */
+  }
+  double kin = 0.0;                                        /* fockaddress.jl:316-322 */
+  long onp = 0;                                            /* excitations.jl:126-137 */
+  int occ[O_MAXM], s = 0;
+  for (int i = 0; i < M; ++i) if (onr[i]) { kin += h->kes[i] * onr[i]; occ[s++] = onr[i]; }
+  for (int i = 0; i < s; ++i) {
+    onp += (long)occ[i] * (occ[i] - 1);
+    for (int j = 0; j < i; ++j) onp += 4L * occ[i] * occ[j];
+  }
+  return kin + h->u / (2 * M) * (double)onp;               /* HubbardMom1D.jl:163-177 */
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* FCIQMC step                                                                           */
+/* ------------------------------------------------------------------------------------ */
+enum { O_STYLE_INTEGER = 0, O_STYLE_DETERMINISTIC = 1, O_STYLE_DSS = 2 };
+enum { O_OP_TRANSITION = 0, O_OP_HAMILTONIAN = 1 };
+
+typedef struct {
+  int style;            /* O_STYLE_* */
+  int op;               /* O_OP_TRANSITION: T = 1 + dt (S - H); O_OP_HAMILTONIAN: H */
+  double dt, shift;
+  double boost;
+  double proj_threshold;       /* on-the-fly projection threshold (0: none) */
+  double compression;          /* ThresholdCompression threshold (0: no compression) */
+  double rel_threshold, abs_threshold; /* DynamicSemistochastic thresholds */
+  uint64_t seed;
+  uint32_t step;
+  uint32_t replica;
+} o_params;
+
+typedef struct {
+  double norm;          /* walkernumber after the step */
+  int64_t len;
+  int64_t len_before;   /* ThresholdCompression statistic */
+  int64_t exact_steps, inexact_steps, spawn_attempts;
+  double spawns;        /* sum of |deposited spawn| */
+  int64_t clones, deaths, zombies;   /* IsStochasticInteger only */
+} o_stats;
+
+typedef struct { uint64_t key; int kind; double v; int64_t iv; } o_contrib;
+
+static uint64_t o_ordered_bits(double v) {
+  uint64_t u;
+  memcpy(&u, &v, 8);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+static int o_cmp_contrib_f(const void *a, const void *b) {
+  const o_contrib *x = a, *y = b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  if (x->kind != y->kind) return x->kind < y->kind ? -1 : 1;
+  uint64_t ox = o_ordered_bits(x->v), oy = o_ordered_bits(y->v);
+  return ox < oy ? -1 : ox > oy;
+}
+static int o_cmp_contrib_i(const void *a, const void *b) {
+  const o_contrib *x = a, *y = b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  if (x->kind != y->kind) return x->kind < y->kind ? -1 : 1;
+  return x->iv < y->iv ? -1 : x->iv > y->iv;
+}
+
+typedef struct { o_contrib *c; int64_t n, cap; int err; } o_buf;
+static void o_push(o_buf *b, uint64_t key, int kind, double v, int64_t iv) {
+  if (b->n == b->cap) {
+    int64_t nc = b->cap ? 2 * b->cap : 1024;
+    o_contrib *p = realloc(b->c, nc * sizeof(o_contrib));
+    if (!p) { b->err = 1; return; }
+    b->c = p; b->cap = nc;
+  }
+  b->c[b->n].key = key; b->c[b->n].kind = kind; b->c[b->n].v = v; b->c[b->n].iv = iv;
+  b->n++;
+}
+
+/* Transition operator elements (fciqmc.jl:93-112). */
+static double o_t_diag(const o_model *h, const o_params *p, uint64_t key) {
+  double d = o_diagonal(h, key);
+  return p->op == O_OP_HAMILTONIAN ? d : 1 - p->dt * (d - p->shift);
+}
+static double o_t_off(const o_params *p, double hval) {
+  return p->op == O_OP_HAMILTONIAN ? hval : -hval * p->dt;
+}
+
+/* Integer stochastic rounding (spawning.jl:33-45): sign(x) * floor(|x| + r), restated as
+ * floor(|x|) + [r < frac(|x|)] with the comparison evaluated exactly. */
+static int64_t o_round_int(double x, uint64_t u53) {
+  double ax = fabs(x);
+  double k = floor(ax);
+  double f = ax - k;
+  int64_t n = (int64_t)k + (o_bernoulli(u53, f) ? 1 : 0);
+  return x < 0 ? -n : n;
+}
+/* Threshold projection for floats (spawning.jl:13-31). */
+static double o_project(double x, double thresh, uint64_t u53) {
+  double ax = fabs(x);
+  if (ax < thresh) {
+    double prob = (thresh == 1.0) ? ax : ax / thresh;
+    if (o_bernoulli(u53, prob)) return x < 0 ? -thresh : thresh;
+    return 0.0;
+  }
+  return x;
+}
+
+/* 1/n as used by the spawn-amplitude factor: (val * (1/n_att)) * n_off. */
+static double o_recip(int64_t n) { return 1.0 / (double)n; }
+
+/* Integer part of a non-negative double below 2^62. */
+static int64_t o_floor_i(double x) { return (int64_t)floor(x); }
+
+/* Unsigned 128-bit fixed point (2^-64 units) used for exact, order-independent norms. */
+typedef unsigned __int128 o_u128;
+static o_u128 o_fixed(double ax) {
+  if (ax == 0.0) return 0;
+  int e;
+  double m = frexp(ax, &e);                /* ax = m * 2^e, m in [0.5, 1) */
+  uint64_t mant = (uint64_t)ldexp(m, 53);  /* 53-bit integer, ax = mant * 2^(e-53) */
+  int sh = e - 53 + 64;                    /* fixed = mant * 2^sh */
+  if (sh >= 0) return sh >= 75 ? ~(o_u128)0 : ((o_u128)mant) << sh;
+  if (-sh >= 64) return 0;
+  return (o_u128)(mant >> (-sh));
+}
+static double o_fixed_to_double(o_u128 x) {
+  return ldexp((double)x, -64);
+}
+
+/* One apply_operator! step (dictvectors.jl:112-140) from `src` into a sorted `dst`.
+ * Values are doubles for the float styles and int64 (passed as double-typed storage of
+ * the same bits is NOT used: separate arrays) for IsStochasticInteger.
+ * Returns 0 on success, nonzero on allocation failure.  *dst arrays are malloc'd. */
+int o_step(const o_model *h, const o_params *p,
+           const uint64_t *skeys, const double *svals, const int64_t *sivals, int64_t n,
+           uint64_t **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
+  memset(st, 0, sizeof(*st));
+  o_buf b = {0};
+  int is_int = p->style == O_STYLE_INTEGER;
+  o_u128 spawn_acc = 0;
+  for (int64_t e = 0; e < n; ++e) {
+    uint64_t key = skeys[e];
+    double val = is_int ? (double)sivals[e] : svals[e];
+    /* ---- diagonal_step! (spawning.jl:73-77) ---- */
+    double x = o_t_diag(h, p, key) * val;
+    if (is_int) {
+      uint32_t r[4];
+      o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+      int64_t res = o_round_int(x, o_u53(r));
+      int64_t v = sivals[e];
+      if (res != 0) o_push(&b, key, 0, 0.0, res);
+      /* clones_deaths_zombies, spawning.jl:79-93 */
+      int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+      if (res > v) st->clones += res - v;
+      else if (sr != sv) { st->deaths += v < 0 ? -v : v; st->zombies += res < 0 ? -res : res; }
+      else st->deaths += (res - v) < 0 ? v - res : res - v;
+    } else {
+      double res = x;
+      if (p->proj_threshold > 0) {
+        uint32_t r[4];
+        o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+        res = o_project(x, p->proj_threshold, o_u53(r));
+      }
+      if (res != 0.0) o_push(&b, key, 0, res, 0);
+    }
+    /* ---- spawn! ---- */
+    int noff = o_num_offdiagonals(h, key);
+    int exact = 0;
+    if (p->style == O_STYLE_DETERMINISTIC) {
+      exact = 1;                       /* apply_column! returns (1,), styles.jl:101-105 */
+      st->exact_steps++;
+    } else if (p->style == O_STYLE_DSS) {
+      /* DynamicSemistochastic, spawning.jl:364-378 */
+      double thresh = p->abs_threshold < (double)noff ? p->abs_threshold : (double)noff;
+      double amount = p->boost * fabs(val) * p->rel_threshold;
+      exact = amount >= thresh;
+      if (exact) st->exact_steps++; else st->inexact_steps++;
+    }
+    /* IsStochasticInteger always samples (WithReplacement); a column without offdiagonals
+     * has nothing to sample from. */
+    if (noff == 0) continue;
+    if (exact) {
+      /* Exact, spawning.jl:174-182: deposit val * mat_elem for every offdiagonal. */
+      st->spawn_attempts += noff;
+      for (int c = 1; c <= noff; ++c) {
+        uint64_t nk; double hv;
+        o_get_offdiagonal(h, key, c, &nk, &hv);
+        double y = val * o_t_off(p, hv);
+        if (p->proj_threshold > 0 && p->style == O_STYLE_DSS) {
+          uint32_t r[4];
+          o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
+          y = o_project(y, p->proj_threshold, o_u53(r));
+        }
+        if (y != 0.0) { o_push(&b, nk, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
+      }
+      continue;
+    }
+    /* WithReplacement, spawning.jl:232-243.  The per-attempt amplitude is
+     * mat_elem * magnitude / prob with magnitude = val / n_att and prob = 1 / n_off; this
+     * restatement evaluates it as mat_elem * ((val * (1/n_att)) * n_off), which is the same
+     * value up to rounding.  For integer walkers with boost 1, val / n_att = sign(val). */
+    int64_t natt = o_floor_i(fabs(val) * p->boost);
+    if (natt < 1) natt = 1;
+    st->spawn_attempts += natt;
+    double c;
+    if (is_int && p->boost == 1.0) c = (val < 0 ? -1.0 : 1.0) * (double)noff;
+    else c = (val * o_recip(natt)) * (double)noff;
+    for (int64_t j = 0; j < natt; ++j) {
+      uint32_t r[4];
+      o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
+      int chosen = (int)(((uint64_t)r[0] * (uint64_t)noff) >> 32) + 1;
+      uint64_t nk; double hv;
+      o_get_offdiagonal(h, key, chosen, &nk, &hv);
+      double y = c * o_t_off(p, hv);
+      if (is_int) {
+        int64_t k = o_round_int(y, o_u53(r));
+        if (k != 0) { o_push(&b, nk, 1, 0.0, k); st->spawns += (double)(k < 0 ? -k : k); }
+      } else {
+        if (p->proj_threshold > 0) y = o_project(y, p->proj_threshold, o_u53(r));
+        if (y != 0.0) { o_push(&b, nk, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
+      }
+    }
+  }
+  if (b.err) { free(b.c); return 1; }
+  if (!is_int) st->spawns = o_fixed_to_double(spawn_acc);
+  /* ---- annihilation: sum contributions per address in canonical order ---- */
+  qsort(b.c, (size_t)b.n, sizeof(o_contrib), is_int ? o_cmp_contrib_i : o_cmp_contrib_f);
+  uint64_t *ok = malloc((size_t)(b.n ? b.n : 1) * 8);
+  double *ov = malloc((size_t)(b.n ? b.n : 1) * 8);
+  int64_t *oi = malloc((size_t)(b.n ? b.n : 1) * 8);
+  if (!ok || !ov || !oi) { free(b.c); free(ok); free(ov); free(oi); return 1; }
+  int64_t m = 0;
+  for (int64_t i = 0; i < b.n;) {
+    int64_t j = i;
+    double s = 0.0;
+    int64_t si = 0;
+    int first = 1;
+    while (j < b.n && b.c[j].key == b.c[i].key) {
+      if (is_int) si += b.c[j].iv;
+      else { s = first ? b.c[j].v : s + b.c[j].v; first = 0; }
+      ++j;
+    }
+    if (is_int ? si != 0 : s != 0.0) { ok[m] = b.c[i].key; ov[m] = s; oi[m] = si; ++m; }
+    i = j;
+  }
+  free(b.c);
+  /* ---- compression (compression.jl:18-42) ---- */
+  st->len_before = m;
+  if (!is_int && p->compression > 0) {
+    int64_t q = 0;
+    for (int64_t i = 0; i < m; ++i) {
+      double w = ov[i];
+      double prob = (p->compression == 1.0) ? fabs(w) : fabs(w) / p->compression;
+      if (prob < 1) {
+        uint32_t r[4];
+        o_draw(p->seed, O_PURPOSE_COMPRESS, p->replica, p->step, ok[i], 0, r);
+        w = o_bernoulli(o_u53(r), prob) ? (w < 0 ? -p->compression : p->compression) : 0.0;
+      }
+      if (w != 0.0) { ok[q] = ok[i]; ov[q] = w; oi[q] = 0; ++q; }
+    }
+    m = q;
+  }
+  o_u128 acc = 0;
+  for (int64_t i = 0; i < m; ++i) acc += o_fixed(fabs(is_int ? (double)oi[i] : ov[i]));
+  st->norm = o_fixed_to_double(acc);
+  st->len = m;
+  *okeys = ok; *ovals = ov; *oivals = oi; *on = m;
+  return 0;
+}
+
+void o_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------------------------ */
+/* Matrix-free product on the full sorted basis (abstractdvec.jl:275-284 in pull form).  */
+/* ------------------------------------------------------------------------------------ */
+static int64_t o_bsearch(const uint64_t *keys, int64_t n, uint64_t k) {
+  int64_t lo = 0, hi = n - 1;
+  while (lo <= hi) {
+    int64_t mid = lo + (hi - lo) / 2;
+    if (keys[mid] == k) return mid;
+    if (keys[mid] < k) lo = mid + 1; else hi = mid - 1;
+  }
+  return -1;
+}
+
+/* w = H v over the sorted basis `keys` (D entries).  H is real symmetric, so row i is
+ * read from the offdiagonals of column i.  Terms are accumulated as d_i v_i followed by
+ * fused multiply-adds in offdiagonal order. Returns number of missing targets (0). */
+int64_t o_hv_basis(const o_model *h, const uint64_t *keys, int64_t D, const double *v, double *w) {
+  int64_t missing = 0;
+  for (int64_t i = 0; i < D; ++i) {
+    double acc = o_diagonal(h, keys[i]) * v[i];
+    int noff = o_num_offdiagonals(h, keys[i]);
+    for (int c = 1; c <= noff; ++c) {
+      uint64_t nk; double hv;
+      o_get_offdiagonal(h, keys[i], c, &nk, &hv);
+      if (hv == 0.0) continue;
+      int64_t j = o_bsearch(keys, D, nk);
+      if (j < 0) { ++missing; continue; }
+      acc = fma(hv, v[j], acc);
+    }
+    w[i] = acc;
+  }
+  return missing;
+}
+
+/* Adjoint of w = H(u, t) v for HubbardReal1D / one-component bosonic HubbardRealSpace
+ * without trap: gv = H^T gw, gu = <gw, dH/du v>, gt = <gw, dH/dt v>. */
+int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, const double *v,
+                           const double *gw, double *gv, double *gu, double *gt) {
+  int64_t missing = o_hv_basis(h, keys, D, gw, gv);
+  double su = 0.0, st = 0.0;
+  for (int64_t i = 0; i < D; ++i) {
+    int onr[O_MAXM];
+    o_to_onr(h, keys[i], onr);
+    long bhi = 0;
+    for (int k = 0; k < h->M; ++k) bhi += (long)onr[k] * (onr[k] - 1);
+    su += gw[i] * ((double)bhi / 2 * v[i]);
+    double kv = 0.0;
+    int noff = o_num_offdiagonals(h, keys[i]);
+    for (int c = 1; c <= noff; ++c) {
+      uint64_t nk; double hv; long prod;
+      o_get_offdiagonal_p(h, keys[i], c, &nk, &hv, &prod);
+      if (hv == 0.0) continue;
+      int64_t j = o_bsearch(keys, D, nk);
+      if (j < 0) { ++missing; continue; }
+      kv = fma(-sqrt((double)prod), v[j], kv);   /* dH_{ji}/dt = -sqrt(prod) */
+    }
+    st += gw[i] * kv;
+  }
+  *gu = su;
+  *gt = st;
+  return missing;
+}
+
+/* Sparse matrix of H over a sorted basis in CSR form (for exact diagonalisation in the
+ * tests).  Duplicate columns within a row are summed by the caller. */
+int64_t o_count_nnz(const o_model *h, const uint64_t *keys, int64_t D) {
+  int64_t nnz = 0;
+  for (int64_t i = 0; i < D; ++i) nnz += 1 + o_num_offdiagonals(h, keys[i]);
+  return nnz;
+}
+int o_build_coo(const o_model *h, const uint64_t *keys, int64_t D,
+                int64_t *rows, int64_t *cols, double *vals, int64_t *nnz_out) {
+  int64_t z = 0;
+  for (int64_t i = 0; i < D; ++i) {
+    rows[z] = i; cols[z] = i; vals[z] = o_diagonal(h, keys[i]); ++z;
+    int noff = o_num_offdiagonals(h, keys[i]);
+    for (int c = 1; c <= noff; ++c) {
+      uint64_t nk; double hv;
+      o_get_offdiagonal(h, keys[i], c, &nk, &hv);
+      if (hv == 0.0) continue;
+      int64_t j = o_bsearch(keys, D, nk);
+      if (j < 0) return 1;
+      rows[z] = j; cols[z] = i; vals[z] = hv; ++z;
+    }
+  }
+  *nnz_out = z;
+  return 0;
+}
+
+/* All B-bit words with exactly w ones, ascending (the sorted build_basis order,
+ * basis_fock.jl:12-36): BoseFS{N,M} is B = N+M-1, w = N; FermiFS{N,M} is B = M, w = N. */
+int64_t o_enumerate_fixed_weight(int B, int w, uint64_t *out, int64_t cap) {
+  if (w == 0) { if (cap > 0) out[0] = 0; return 1; }
+  if (w > B || B > 63) return -1;
+  uint64_t x = ((uint64_t)1 << w) - 1, limit = (uint64_t)1 << B;
+  int64_t n = 0;
+  while (x < limit) {
+    if (n < cap) out[n] = x;
+    ++n;
+    uint64_t c = x & (~x + 1), r = x + c;      /* Gosper's hack */
+    x = (((r ^ x) >> 2) / c) | r;
+  }
+  return n;
+}
+
+/* Basis of the block connected to `start` by offdiagonals with nonzero elements
+ * (build_basis(H, address), basis_breadth_first_search.jl), sorted ascending.
+ * Returns the number of addresses found (may exceed cap: then out holds the first cap). */
+static int o_cmp_u64(const void *a, const void *b) {
+  uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+  return x < y ? -1 : x > y;
+}
+int64_t o_connected_basis(const o_model *h, uint64_t start, uint64_t *out, int64_t cap) {
+  int64_t tcap = 1024;
+  while (tcap < 4 * (cap > 0 ? cap : 1)) tcap <<= 1;
+  uint64_t *tab = malloc((size_t)tcap * 8);
+  uint64_t *queue = malloc((size_t)tcap * 8);
+  if (!tab || !queue) { free(tab); free(queue); return -1; }
+  const uint64_t EMPTY = ~0ull;
+  for (int64_t i = 0; i < tcap; ++i) tab[i] = EMPTY;
+  int64_t head = 0, tail = 0;
+#define O_INSERT(k) do { \
+    uint64_t _k = (k), _h = (_k * 0x9E3779B97F4A7C15ull) & (uint64_t)(tcap - 1); \
+    while (tab[_h] != EMPTY && tab[_h] != _k) _h = (_h + 1) & (uint64_t)(tcap - 1); \
+    if (tab[_h] == EMPTY) { \
+      if (tail >= tcap / 2) { free(tab); free(queue); return -2; } \
+      tab[_h] = _k; queue[tail++] = _k; } } while (0)
+  O_INSERT(start);
+  while (head < tail) {
+    uint64_t k = queue[head++];
+    int noff = o_num_offdiagonals(h, k);
+    for (int c = 1; c <= noff; ++c) {
+      uint64_t nk; double hv;
+      o_get_offdiagonal(h, k, c, &nk, &hv);
+      if (hv != 0.0) O_INSERT(nk);
+    }
+  }
+#undef O_INSERT
+  qsort(queue, (size_t)tail, 8, o_cmp_u64);
+  for (int64_t i = 0; i < tail && i < cap; ++i) out[i] = queue[i];
+  free(tab); free(queue);
+  return tail;
+}

@@ -1,0 +1,495 @@
+// rimu_device.cuh -- device primitives for the GB300 FCIQMC step and matrix-free H*v.
+//
+// Addresses are single-chunk bit strings (up to 64 bits) with the Rimu.jl layout:
+//   BoseFS: mode 1 at the least significant end, each mode written as n_i ones followed by
+//           a zero separator (src/BitStringAddresses/bitstring.jl:464-472).
+//   FermiFS: mode k <-> bit k-1 (bitstring.jl:713-723).
+// The unsigned integer order of the key equals BitString isless (bitstring.jl:317-324).
+//
+// FP64 is scarce on GB300 (about 0.5 T FP64 instructions/s for the whole GPU), so the
+// kernels use at most one FP64 multiply per spawn: matrix elements of the transition
+// operator come from tables computed on the host with the reference's own expressions,
+// and stochastic rounding / threshold projection decisions are evaluated with integer
+// instructions on the IEEE bit patterns (exactly equivalent to comparing r < p with
+// r = u53 * 2^-53).
+#pragma once
+#include <cstdint>
+
+#ifndef RIMU_HD
+#define RIMU_HD __host__ __device__ __forceinline__
+#endif
+
+namespace rimu {
+
+enum ModelKind : int { MODEL_REAL1D = 1, MODEL_REALSPACE = 2, MODEL_MOM1D = 3 };
+enum Style : int { STYLE_INTEGER = 0, STYLE_DETERMINISTIC = 1, STYLE_DSS = 2 };
+enum OpKind : int { OP_TRANSITION = 0, OP_HAMILTONIAN = 1 };
+enum Purpose : uint32_t { PURPOSE_SPAWN = 1, PURPOSE_DIAG = 2, PURPOSE_COMPRESS = 3 };
+
+constexpr int MAX_MODES = 64;
+constexpr uint64_t EMPTY_KEY = ~0ull;   // never a valid address: would need 64 particles in 1 mode
+
+// ------------------------------------------------------------------------------------------
+// Device model description (immutable during a step).
+// ------------------------------------------------------------------------------------------
+struct DevModel {
+  int kind, fermion, N, M, nbits;
+  int ndim, dims[3], periodic[3];
+  double u, t;
+  const double *kes;     // HubbardMom1D dispersion [M]
+  const double *pot;     // HubbardRealSpace trap [M] or null
+  const double *aoff;    // transition offdiagonal magnitudes, indexed by occupation product
+  int aoff_len;
+  const double *hoff;    // Hamiltonian offdiagonal magnitudes (no dt), same indexing
+  const double *recip;   // recip[n] = 1.0 / n for n < recip_len
+  int recip_len;
+};
+
+// ------------------------------------------------------------------------------------------
+// Bits
+// ------------------------------------------------------------------------------------------
+RIMU_HD int ctz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return x ? __ffsll((long long)x) - 1 : 64;
+#else
+  return x ? __builtin_ctzll(x) : 64;
+#endif
+}
+RIMU_HD int popc64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __popcll(x);
+#else
+  return __builtin_popcountll(x);
+#endif
+}
+RIMU_HD uint64_t shr64(uint64_t x, int s) { return s >= 64 ? 0 : x >> s; }
+RIMU_HD uint64_t shl64(uint64_t x, int s) { return s >= 64 ? 0 : x << s; }
+RIMU_HD uint64_t lowmask(int n) { return n >= 64 ? ~0ull : ((1ull << n) - 1); }
+
+// murmur3 fmix64 finalizer: spreads address bits for bucket and table placement.
+RIMU_HD uint64_t mix64(uint64_t x) {
+  x ^= x >> 33; x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+RIMU_HD uint32_t bucket_of(uint64_t key, int nb_bits) {
+  return nb_bits == 0 ? 0u : (uint32_t)(mix64(key) >> (64 - nb_bits));
+}
+
+// ------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11).  Counter (draw, step, address lo, address hi), key (seed lo, seed hi ^ purpose ^
+// replica): a draw depends only on what it is for, never on the thread that makes it.
+// ------------------------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+RIMU_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    U4 n;
+    n.x = hi1 ^ c.y ^ k0; n.y = lo1; n.z = hi0 ^ c.w ^ k1; n.w = lo0;
+    c = n;
+  }
+  return c;
+}
+RIMU_HD U4 draw(uint64_t seed, uint32_t purpose, uint32_t replica, uint32_t step,
+                uint64_t addr, uint32_t j) {
+  U4 c{j, step, (uint32_t)addr, (uint32_t)(addr >> 32)};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32) ^ (purpose << 28) ^ replica);
+}
+RIMU_HD uint64_t u53_of(U4 r) { return ((uint64_t)r.y << 21) | (uint64_t)(r.z >> 11); }
+RIMU_HD uint32_t uniform_index(uint32_t r, uint32_t n) {   // floor(r * n / 2^32)
+  return (uint32_t)(((uint64_t)r * n) >> 32);
+}
+
+// ------------------------------------------------------------------------------------------
+// Exact stochastic decisions with integer instructions.
+// ------------------------------------------------------------------------------------------
+RIMU_HD uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u; __builtin_memcpy(&u, &x, 8); return u;
+#endif
+}
+RIMU_HD double bitsd(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x; __builtin_memcpy(&x, &u, 8); return x;
+#endif
+}
+
+// u53 < p * 2^53 for finite p >= 0 (p >= 1 -> always true), i.e. r < p for r = u53 * 2^-53.
+RIMU_HD bool bernoulli53(uint64_t u53, double p) {
+  uint64_t b = dbits(p) & 0x7fffffffffffffffull;
+  int e = (int)(b >> 52);
+  if (e >= 1023) return true;                       // p >= 1
+  uint64_t mant = b & lowmask(52);
+  int s;
+  if (e == 0) { s = 1074 - 53; }                    // subnormal: p = mant * 2^-1074
+  else { mant |= 1ull << 52; s = 1075 - 53 - e; }   // p * 2^53 = mant * 2^-(s)
+  // s >= 1 here because e <= 1022.
+  if (s >= 64) return u53 == 0 && mant != 0;
+  uint64_t q = mant >> s;
+  uint64_t rem = mant & lowmask(s);
+  return u53 < q + (rem != 0 ? 1u : 0u);
+}
+
+// floor(|x|) and the Bernoulli on frac(|x|): the integer stochastic rounding of
+// spawning.jl:33-45, restated as floor(|x|) + [r < frac(|x|)].  |x| < 2^62 assumed.
+RIMU_HD int64_t round_stochastic(double x, uint64_t u53) {
+  uint64_t b = dbits(x);
+  bool neg = (b >> 63) != 0;
+  b &= 0x7fffffffffffffffull;
+  int e = (int)(b >> 52);
+  int64_t k;
+  bool up;
+  if (e < 1023) {                 // |x| < 1: k = 0, frac = |x|
+    k = 0;
+    up = bernoulli53(u53, bitsd(b));
+  } else {
+    uint64_t mant = (b & lowmask(52)) | (1ull << 52);
+    int sh = e - 1075;            // |x| = mant * 2^sh
+    if (sh >= 0) {                // integer already
+      k = (int64_t)(mant << sh);
+      up = false;
+    } else {
+      int s = -sh;                // 1..52
+      k = (int64_t)(mant >> s);
+      uint64_t fr = mant & lowmask(s);   // frac = fr * 2^-s ; compare u53 < fr * 2^(53-s)
+      up = u53 < (fr << (53 - s)) ;      // exact: fr * 2^(53-s) is an integer < 2^53
+    }
+  }
+  int64_t n = k + (up ? 1 : 0);
+  return neg ? -n : n;
+}
+
+// Threshold projection of a float spawn (spawning.jl:13-31).  thresh > 0.
+RIMU_HD double project_threshold(double x, double thresh, uint64_t u53) {
+  double ax = fabs(x);
+  if (ax < thresh) {
+    double prob = (thresh == 1.0) ? ax : ax / thresh;
+    if (bernoulli53(u53, prob)) return x < 0 ? -thresh : thresh;
+    return 0.0;
+  }
+  return x;
+}
+
+// Integer part of |x| (x finite, |x| < 2^62) via the bit pattern.
+RIMU_HD int64_t floor_abs(double x) {
+  uint64_t b = dbits(x) & 0x7fffffffffffffffull;
+  int e = (int)(b >> 52);
+  if (e < 1023) return 0;
+  uint64_t mant = (b & lowmask(52)) | (1ull << 52);
+  int sh = e - 1075;
+  return sh >= 0 ? (int64_t)(mant << sh) : (int64_t)(mant >> (-sh));
+}
+
+// Order-preserving map of doubles to unsigned integers (for canonical summation order).
+RIMU_HD uint64_t ordered_bits(double v) {
+  uint64_t u = dbits(v);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// Unsigned 128-bit fixed point with 2^-64 resolution: |x| -> floor(|x| * 2^64).
+struct U128 { uint64_t lo, hi; };
+RIMU_HD U128 fixed_of(double ax) {
+  uint64_t b = dbits(ax) & 0x7fffffffffffffffull;
+  int e = (int)(b >> 52);
+  U128 r{0, 0};
+  if (b == 0) return r;
+  uint64_t mant = b & lowmask(52);
+  int sh;
+  if (e == 0) sh = -1074 + 64; else { mant |= 1ull << 52; sh = e - 1075 + 64; }
+  if (sh >= 75) { r.lo = ~0ull; r.hi = ~0ull; return r; }
+  if (sh >= 64) { r.hi = mant << (sh - 64); return r; }
+  if (sh > 0) { r.lo = mant << sh; r.hi = (sh > 11) ? (mant >> (64 - sh)) : 0; return r; }
+  if (sh == 0) { r.lo = mant; return r; }
+  r.lo = (-sh >= 64) ? 0 : (mant >> (-sh));
+  return r;
+}
+RIMU_HD U128 add128(U128 a, U128 b) {
+  U128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1 : 0);
+  return r;
+}
+RIMU_HD int clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+// Correctly rounded (nearest-even) value of (hi*2^64 + lo) * 2^-64.
+RIMU_HD double fixed_to_double(U128 x) {
+  if (x.hi == 0 && x.lo == 0) return 0.0;
+  int top = x.hi ? 127 - clz64(x.hi) : 63 - clz64(x.lo);   // index of the leading one
+  uint64_t m;
+  if (top <= 52) {
+    m = x.lo << (52 - top);
+  } else {
+    int drop = top - 52;                                      // 1..75
+    m = drop >= 64 ? (x.hi >> (drop - 64)) : ((x.lo >> drop) | (x.hi << (64 - drop)));
+    m &= lowmask(53);
+    int rb = drop - 1;
+    uint64_t rbit;
+    bool sticky;
+    if (rb >= 64) {
+      rbit = (x.hi >> (rb - 64)) & 1;
+      sticky = (x.lo != 0) || ((x.hi & lowmask(rb - 64)) != 0);
+    } else {
+      rbit = (x.lo >> rb) & 1;
+      sticky = (x.lo & lowmask(rb)) != 0;
+    }
+    if (rbit && (sticky || (m & 1))) {
+      m += 1;
+      if (m >> 53) { m >>= 1; top += 1; }
+    }
+  }
+  return bitsd(((uint64_t)(1023 + top - 64) << 52) | (m & lowmask(52)));
+}
+
+// ------------------------------------------------------------------------------------------
+// BoseFS / FermiFS operations on a 64-bit key
+// ------------------------------------------------------------------------------------------
+// Occupied mode record (BoseFSIndex, fockaddress.jl:515-519): occupation, 1-based mode,
+// bit offset of the first boson.
+struct ModeIdx { int occ, mode, offset; };
+
+// k-th occupied mode (1-based).  Also reports the previous occupied mode (mode 0 if none).
+RIMU_HD ModeIdx bose_find_occupied(uint64_t key, int k, ModeIdx *prev) {
+  uint64_t x = key;
+  int mode = 1, bit = 0;
+  ModeIdx p{0, 0, 0};
+  while (x) {
+    int z = ctz64(x);
+    x = shr64(x, z); mode += z; bit += z;
+    int n = ctz64(~x);
+    ModeIdx cur{n, mode, bit};
+    if (--k == 0) { if (prev) *prev = p; return cur; }
+    p = cur;
+    x = shr64(x, n); bit += n;
+  }
+  if (prev) *prev = p;
+  return ModeIdx{0, 0, 0};
+}
+
+// find_mode (bosefs.jl:188-203): occupation and offset of a given 1-based mode.
+RIMU_HD ModeIdx bose_find_mode(uint64_t key, int mode_wanted) {
+  uint64_t x = key;
+  int mode = 1, bit = 0, last_occ = 0, last_mode = 0, last_off = 0;
+  while (x) {
+    int z = ctz64(x);
+    x = shr64(x, z); mode += z; bit += z;
+    int n = ctz64(~x);
+    int dist = mode_wanted - mode;
+    if (dist == 0) return ModeIdx{n, mode_wanted, bit};
+    if (dist < 0) return ModeIdx{0, mode_wanted, bit + dist};
+    last_occ = n; last_mode = mode; last_off = bit;
+    x = shr64(x, n); bit += n;
+  }
+  return ModeIdx{0, mode_wanted, last_off + last_occ + mode_wanted - last_mode};
+}
+
+RIMU_HD int bose_num_occupied(uint64_t key) {
+  // number of runs of ones
+  return popc64(key & ~(key << 1));
+}
+
+// partial_left_shift / partial_right_shift (bitstring.jl:342-375) on one 64-bit chunk.
+RIMU_HD uint64_t partial_left_shift(uint64_t c, int i, int j) {
+  uint64_t mask = shl64(lowmask(j - i + 1), i);
+  uint64_t shifted = ((c & mask) << 1) & mask;
+  return shifted | (c & ~mask) | (1ull << i);
+}
+RIMU_HD uint64_t partial_right_shift(uint64_t c, int i, int j) {
+  uint64_t mask = shl64(lowmask(j - i + 1), i);
+  uint64_t shifted = ((c & mask) >> 1) & mask;
+  return shifted | (c & ~mask) | (1ull << j);
+}
+// bose_move_particle (bitstring.jl:559-567): move one boson between bit offsets.
+RIMU_HD uint64_t bose_move(uint64_t c, int from, int to) {
+  if (to == from) return c;
+  if (to < from) return partial_left_shift(c, to, from);
+  return partial_right_shift(c, from, to - 1);
+}
+
+// ------------------------------------------------------------------------------------------
+// Model offdiagonals.  Each returns the new key and the integer "occupation product" whose
+// square root is the magnitude (index into the aoff/hoff tables), plus a sign.  prod == 0
+// marks an illegal move (value 0.0, address unchanged).
+// ------------------------------------------------------------------------------------------
+struct Offdiag { uint64_t key; int prod; int sign; };
+
+RIMU_HD int num_offdiagonals_real(const DevModel &h, uint64_t key) {
+  int s = h.fermion ? popc64(key) : bose_num_occupied(key);
+  return h.kind == MODEL_REAL1D ? 2 * s : s * 2 * h.ndim;
+}
+
+// HubbardReal1D.get_offdiagonal via hopnextneighbour (bosefs.jl:297-345).
+RIMU_HD Offdiag real1d_offdiag(const DevModel &h, uint64_t key, int chosen) {
+  int site = (chosen + 1) >> 1;
+  ModeIdx prev;
+  ModeIdx cur = bose_find_occupied(key, site, &prev);
+  int M = h.M, B = h.nbits;
+  Offdiag r;
+  r.sign = 1;
+  if (chosen & 1) {   // hop right
+    if (cur.mode == M) {
+      r.key = ((key << 1) | 1ull) & lowmask(B);
+      r.prod = cur.occ * (ctz64(~key) + 1);
+    } else {
+      int after = cur.offset + cur.occ;          // separator after the site
+      int next = ctz64(~shr64(key, after + 1));  // occupation of mode+1
+      r.key = key ^ (3ull << (after - 1));
+      r.prod = cur.occ * (next + 1);
+    }
+  } else {            // hop left
+    if (cur.mode == 1) {
+      uint64_t nk = (key >> 1) | (1ull << (B - 1));
+      // leading ones of nk within B bits = occupation of mode M after the hop
+      int lead = 0;
+      for (int b = B - 1; b >= 0 && ((nk >> b) & 1); --b) ++lead;
+      r.key = nk;
+      r.prod = ctz64(~key) * lead;
+    } else {
+      int prev_occ = (prev.mode == cur.mode - 1) ? prev.occ : 0;
+      r.key = key ^ (3ull << (cur.offset - 1));
+      r.prod = cur.occ * (prev_occ + 1);
+    }
+  }
+  return r;
+}
+
+// neighbor_site (geometry.jl:232-235): 1-based mode and direction, 0 if illegal.
+RIMU_HD int neighbor_site(const DevModel &h, int mode, int chosen) {
+  int D = h.ndim, x[3] = {0, 0, 0}, rem = mode - 1;
+  for (int d = 0; d < D; ++d) { x[d] = rem % h.dims[d]; rem /= h.dims[d]; }
+  int dir = chosen <= D ? chosen - 1 : chosen - D - 1;
+  x[dir] += chosen <= D ? 1 : -1;
+  if (x[dir] < 0 || x[dir] >= h.dims[dir]) {
+    if (!h.periodic[dir]) return 0;
+    x[dir] = (x[dir] + h.dims[dir]) % h.dims[dir];
+  }
+  int site = 0;
+  for (int d = D - 1; d >= 0; --d) site = site * h.dims[d] + x[d];
+  return site + 1;
+}
+
+// HubbardRealSpace one-component offdiagonal (HubbardRealSpace.jl:325-338).
+RIMU_HD Offdiag realspace_offdiag(const DevModel &h, uint64_t key, int chosen) {
+  int nb = 2 * h.ndim;
+  int particle = (chosen - 1) / nb + 1, neigh = (chosen - 1) % nb + 1;
+  Offdiag r{key, 0, 1};
+  if (h.fermion) {
+    // particle-th set bit
+    uint64_t x = key;
+    for (int i = 1; i < particle; ++i) x &= x - 1;
+    int src = ctz64(x) + 1;
+    int dst = neighbor_site(h, src, neigh);
+    if (dst == 0) return r;
+    if ((key >> (dst - 1)) & 1) return r;       // Pauli blocked
+    int count = popc64(key & lowmask(src - 1));
+    uint64_t k1 = key ^ (1ull << (src - 1));
+    count += popc64(k1 & lowmask(dst - 1));
+    r.key = k1 | (1ull << (dst - 1));
+    r.prod = 1;
+    r.sign = (count & 1) ? -1 : 1;
+    return r;
+  }
+  ModeIdx src = bose_find_occupied(key, particle, nullptr);
+  int dst_mode = neighbor_site(h, src.mode, neigh);
+  if (dst_mode == 0) return r;
+  ModeIdx dst = bose_find_mode(key, dst_mode);
+  r.key = bose_move(key, src.offset, dst.offset);
+  r.prod = src.occ * (dst.occ + 1);
+  return r;
+}
+
+// HubbardMom1D occupied mode map in registers (OccupiedModeMap, fockaddress.jl:258-281).
+struct MomMap { int s, d; uint8_t mode[MAX_MODES]; uint8_t occ[MAX_MODES]; };
+RIMU_HD void mom_map(uint64_t key, MomMap &m) {
+  uint64_t x = key;
+  int mode = 1;
+  m.s = 0; m.d = 0;
+  while (x) {
+    int z = ctz64(x);
+    x = shr64(x, z); mode += z;
+    int n = ctz64(~x);
+    m.mode[m.s] = (uint8_t)mode; m.occ[m.s] = (uint8_t)n; m.s++; m.d += n > 1;
+    x = shr64(x, n);
+  }
+}
+RIMU_HD int num_offdiagonals_mom(const DevModel &h, const MomMap &m) {
+  return m.s * (m.s - 1) * (h.M - 2) + m.d * (h.M - 1);
+}
+
+// momentum_transfer_excitation with fold=true (excitations.jl:26-80).
+RIMU_HD Offdiag mom1d_offdiag(const DevModel &h, uint64_t key, const MomMap &m, int chosen) {
+  int M = h.M, s = m.s;
+  int dbl = chosen - s * (s - 1) * (M - 2);
+  int p_idx, q_idx, mom;
+  if (dbl > 0) {
+    int which = (dbl - 1) / (M - 1) + 1;
+    mom = (dbl - 1) % (M - 1) + 1;
+    int idx = 0;
+    for (int k = 0; k < s; ++k) {
+      which -= m.occ[k] >= 2;
+      if (which == 0) { idx = k; break; }
+    }
+    p_idx = q_idx = idx;
+  } else {
+    int pair = (chosen - 1) / (M - 2) + 1;
+    mom = (chosen - 1) % (M - 2) + 1;
+    int fst = (pair - 1) / (s - 1) + 1, snd = (pair - 1) % (s - 1) + 1;
+    int fh, sh;
+    if (snd < fst) { fh = snd; sh = fst; } else { fh = fst; sh = snd + 1; }
+    p_idx = fh - 1; q_idx = sh - 1;
+    if (mom >= m.mode[q_idx] - m.mode[p_idx]) mom += 1;
+  }
+  int src1 = m.mode[p_idx], src2 = m.mode[q_idx];
+  int dst1 = ((src1 + mom - 1) % M + M) % M + 1;
+  int dst2 = ((src2 - mom - 1) % M + M) % M + 1;
+  // occupations before the move
+  auto occ_of = [&](int mode) -> int {
+    for (int k = 0; k < s; ++k) if (m.mode[k] == mode) return m.occ[k];
+    return 0;
+  };
+  int o_s2 = occ_of(src2), o_s1 = occ_of(src1), o_d2 = occ_of(dst2), o_d1 = occ_of(dst1);
+  // a_{src2}, a_{src1}, then a+_{dst2}, a+_{dst1}: sequential occupation factors
+  int v = o_s2;
+  int c_s1 = o_s1 - (src1 == src2);
+  v *= c_s1;
+  int c_d2 = o_d2 - (dst2 == src2) - (dst2 == src1);
+  v *= c_d2 + 1;
+  int c_d1 = o_d1 - (dst1 == src2) - (dst1 == src1) + (dst1 == dst2);
+  v *= c_d1 + 1;
+  Offdiag r{key, 0, 1};
+  if (v == 0) return r;
+  // apply the moves on the bit string: destroy at src offsets, create at dst offsets,
+  // one particle at a time with fresh offsets each time
+  uint64_t k1 = key;
+  {
+    ModeIdx a = bose_find_mode(k1, src2), b = bose_find_mode(k1, dst2);
+    k1 = bose_move(k1, a.offset, b.offset);
+    ModeIdx c = bose_find_mode(k1, src1), d = bose_find_mode(k1, dst1);
+    k1 = bose_move(k1, c.offset, d.offset);
+  }
+  r.key = k1;
+  r.prod = v;
+  return r;
+}
+
+}  // namespace rimu

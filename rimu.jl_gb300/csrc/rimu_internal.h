@@ -1,0 +1,163 @@
+// rimu_internal.h -- structures shared by the CUDA translation units of librimu_gpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "rimu_device.cuh"
+#include "../../include/rimu_gpu.h"
+
+namespace rimu {
+
+// One walker: an address and its amplitude (double or int64 bit pattern).
+struct __align__(16) Rec { uint64_t key; uint64_t val; };
+
+// A heavy column is split into chunks of at most HEAVY_CHUNK spawn attempts.
+constexpr int HEAVY_CHUNK = 2048;
+constexpr int HEAVY_LIMIT = 1024;   // columns with more work than this go to the heavy list
+
+struct __align__(16) HeavyChunk {
+  uint64_t key;
+  uint64_t val;      // amplitude bits
+  double c;          // spawn coefficient
+  int noff;
+  int exact;
+  uint32_t j0, cnt;
+  uint32_t rep;
+  uint32_t pad;
+};
+
+// Per-replica step accumulators (zeroed before each step).
+struct DevStats {
+  unsigned long long norm_lo, norm_hi;       // sum |v'| in 2^-64 fixed point
+  unsigned long long spawn_lo, spawn_hi;     // sum |spawn| (float styles) in fixed point
+  long long len, len_before;
+  long long exact_steps, inexact_steps, spawn_attempts;
+  long long spawns_int;
+  long long clones, deaths, zombies;
+  long long spawn_records;
+  unsigned int max_spawn_bucket, max_v_bucket;
+  unsigned int flags;
+  unsigned int heavy_chunks;
+};
+
+enum Flags : unsigned int {
+  FLAG_SPAWN_OVERFLOW = 1u, FLAG_V_OVERFLOW = 2u, FLAG_HEAVY_OVERFLOW = 4u,
+  FLAG_VALUE_OVERFLOW = 8u, FLAG_TABLE = 16u
+};
+
+// Parameters of one launch of the step kernels.
+struct StepArgs {
+  DevModel h;
+  int style, op;
+  double dt;
+  double boost, proj_threshold, compression, rel_threshold, abs_threshold;
+  uint64_t seed;
+  uint32_t step;
+  uint32_t replica_base;
+  int nrep;
+  int nb_bits;
+  uint32_t capv, caps, tsize;
+  const Rec *v_in;
+  const uint32_t *cnt_in;
+  Rec *v_out;
+  uint32_t *cnt_out;
+  Rec *spawn;
+  uint32_t *scount;
+  HeavyChunk *heavy;
+  uint32_t heavy_cap;
+  uint32_t *heavy_count;
+  DevStats *stats;            // [nrep]
+  const double *dtab;         // [nrep * ndiag] diagonal transition table or null
+  int ndiag;
+  const double *shift;        // [nrep] shifts (used when dtab == null)
+  // ProjectedEnergy: per replica nproj sorted keys, projector values and (H'P) values
+  int nproj;
+  const uint64_t *proj_keys;  // [nrep * nproj]
+  const double *proj_v;
+  const double *proj_h;
+  double *proj_out_v;         // [nrep * nproj]
+  double *proj_out_h;
+};
+
+}  // namespace rimu
+
+struct rimu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+};
+
+struct rimu_model {
+  rimu_ctx *ctx = nullptr;
+  rimu_model_desc desc{};
+  rimu::DevModel dm{};
+  double *d_kes = nullptr, *d_pot = nullptr, *d_aoff = nullptr, *d_hoff = nullptr;
+  double *d_recip = nullptr;
+  int aoff_len = 0;
+  double aoff_dt = -1.0;    // dt of the transition table currently on the device
+  int ndiag = 0;            // size of the diagonal table (0: diagonal computed per address)
+  int max_offdiag = 0;
+};
+
+struct rimu_vec {
+  rimu_ctx *ctx = nullptr;
+  int val_kind = RIMU_VAL_F64;
+  int nb_bits = 0;
+  uint32_t capv = 0;
+  rimu::Rec *recs = nullptr;
+  uint32_t *count = nullptr;
+  int64_t len = 0;          // length after the last operation that changed it
+  double norm = 0.0;
+};
+
+struct rimu_wm {
+  rimu_ctx *ctx = nullptr;
+  int nb_total = 0;         // buckets allocated (nrep * 2^nb_bits)
+  uint32_t caps = 0;
+  rimu::Rec *spawn = nullptr;
+  uint32_t *scount = nullptr;
+  rimu::HeavyChunk *heavy = nullptr;
+  uint32_t heavy_cap = 0;
+  uint32_t *heavy_count = nullptr;
+  rimu::DevStats *stats = nullptr;
+  rimu::DevStats *h_stats = nullptr;   // pinned host copy
+  int stats_n = 0;
+  double *dtab = nullptr;
+  int dtab_n = 0;
+  double *d_shift = nullptr;
+  int64_t last_spawns = -1;
+  // projector
+  int nproj = 0;
+  uint64_t *proj_keys = nullptr;
+  double *proj_v = nullptr, *proj_h = nullptr, *proj_out_v = nullptr, *proj_out_h = nullptr;
+  double *h_proj_out = nullptr;         // pinned [2 * nproj]
+};
+
+// error reporting shared by the translation units
+void rimu_set_error(const std::string &msg);
+int rimu_cuda_check(cudaError_t e, const char *what);
+#define RIMU_CUDA(call) do { int _rc = rimu_cuda_check((call), #call); if (_rc) return _rc; } while (0)
+
+// launchers (fciqmc.cu)
+int rimu_launch_step(rimu_ctx *ctx, const rimu::StepArgs &a, int nb_total);
+int rimu_launch_bucketize(rimu_ctx *ctx, const uint64_t *keys, const uint64_t *vals, int64_t n,
+                          int nb_bits, uint32_t capv, rimu::Rec *recs, uint32_t *count,
+                          unsigned int *flag);
+int rimu_launch_rebucket(rimu_ctx *ctx, const rimu::Rec *old_recs, const uint32_t *old_count,
+                         int old_nb_bits, uint32_t old_capv, rimu::Rec *recs, uint32_t *count,
+                         int nb_bits, uint32_t capv, unsigned int *flag);
+int rimu_launch_compact(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb,
+                        uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals);
+int rimu_launch_norm(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb,
+                     uint32_t capv, int val_kind, unsigned long long *acc3);
+int rimu_launch_lookup(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb_bits,
+                       uint32_t capv, const uint64_t *keys, int64_t n, uint64_t *vals,
+                       int *found);
+int rimu_launch_diag_table(rimu_ctx *ctx, const rimu::DevModel &h, int op, double dt,
+                           const double *shift, int nrep, int ndiag, double *dtab);
+int rimu_launch_diagonal(rimu_ctx *ctx, const rimu::DevModel &h, const uint64_t *keys,
+                         int64_t n, double *out);
+int rimu_launch_offdiagonals(rimu_ctx *ctx, const rimu::DevModel &h, uint64_t key, int noff,
+                             uint64_t *keys, double *vals);

@@ -1,0 +1,22 @@
+"""rimugpu -- GB300 implementation of Rimu.jl's FCIQMC step and matrix-free H*v.
+
+Python mirror of the Rimu.jl API for this path (ProjectorMonteCarloProblem, solve,
+StochasticStyle traits, HubbardReal1D / HubbardRealSpace / HubbardMom1D, BoseFS / FermiFS)
+over the C ABI of librimu_gpu (include/rimu_gpu.h).  All compute runs in the CUDA library.
+"""
+from ._lib import RimuError, load as load_library, library_path
+from .addresses import BoseFS, FermiFS, near_uniform, near_uniform_onr
+from .hamiltonians import (CubicGrid, HardwallBoundaries, HubbardMom1D, HubbardReal1D,
+                           HubbardRealSpace, LadderBoundaries, PeriodicBoundaries,
+                           continuum_dispersion, hubbard_dispersion)
+from .styles import (Exact, IsDeterministic, IsDynamicSemistochastic, IsStochasticInteger,
+                     NoCompression, ThresholdCompression, WithReplacement, default_style)
+from .dvec import (FirstOrderTransitionOperator, GPUDVec, GPUWorkingMemory, apply_operator,
+                   dot_operator, mul, working_memory)
+from .problem import (DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUpdate, LogUpdate,
+                      LogUpdateAfterTargetWalkers, PMCSimulation, ProjectedEnergy,
+                      ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)
+from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estimator
+from .hv import BasisOperator, eigsolve, hv
+
+__all__ = [n for n in dir() if not n.startswith("_")]

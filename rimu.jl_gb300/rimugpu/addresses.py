@@ -1,0 +1,155 @@
+"""Fock-state addresses as single-chunk bit strings (host side).
+
+The encodings are the ones of Rimu.jl's BitString-backed addresses, so keys produced here
+are the raw chunk values the device kernels operate on:
+  BoseFS{N,M}: N + M - 1 bits, mode 1 at the least significant end, each mode written as
+  n_i ones followed by a zero separator (src/BitStringAddresses/bitstring.jl:464-472,
+  511-520); FermiFS{N,M}: mode k <-> bit k-1 (bitstring.jl:713-723).
+Ordering of addresses is the unsigned integer order of the key (bitstring.jl:317-324).
+"""
+from __future__ import annotations
+
+from functools import total_ordering
+
+
+def _bose_key(onr) -> int:
+    key = 0
+    for n in reversed(onr):
+        key = (key << (n + 1)) | ((1 << n) - 1)
+    return key
+
+
+def _bose_onr(key: int, M: int) -> tuple:
+    onr = []
+    for _ in range(M):
+        n = 0
+        while key & 1:
+            n += 1
+            key >>= 1
+        onr.append(n)
+        key >>= 1
+    return tuple(onr)
+
+
+@total_ordering
+class BoseFS:
+    """BoseFS{N,M} (src/BitStringAddresses/bosefs.jl:54-112).
+
+    ``BoseFS(1, 1, 2)``, ``BoseFS((1, 1, 2))``, ``BoseFS(M, {mode: occupation})`` (sparse,
+    1-based modes) or ``BoseFS.from_key(key, N, M)``."""
+
+    __slots__ = ("N", "M", "key")
+    fermion = False
+
+    def __init__(self, *args):
+        if len(args) == 2 and isinstance(args[1], dict):
+            M, pairs = args
+            onr = [0] * M
+            for mode, occ in pairs.items():
+                onr[mode - 1] = occ
+        elif len(args) == 1 and not isinstance(args[0], int):
+            onr = list(args[0])
+        else:
+            onr = list(args)
+        if any(n < 0 for n in onr):
+            raise ValueError("invalid ONR: negative occupation")
+        self.N = int(sum(onr))
+        self.M = len(onr)
+        if self.N + self.M - 1 > 64:
+            raise ValueError("BoseFS wider than 64 bits is not supported")
+        self.key = _bose_key(onr)
+
+    @classmethod
+    def from_key(cls, key: int, N: int, M: int) -> "BoseFS":
+        b = cls.__new__(cls)
+        b.N, b.M, b.key = N, M, int(key)
+        return b
+
+    @property
+    def nbits(self) -> int:
+        return self.N + self.M - 1
+
+    def onr(self) -> tuple:
+        return _bose_onr(self.key, self.M)
+
+    def num_occupied_modes(self) -> int:
+        return sum(1 for n in self.onr() if n)
+
+    def __eq__(self, o):
+        return isinstance(o, BoseFS) and (self.N, self.M, self.key) == (o.N, o.M, o.key)
+
+    def __lt__(self, o):
+        return self.key < o.key
+
+    def __hash__(self):
+        return hash(("B", self.N, self.M, self.key))
+
+    def __repr__(self):
+        return f"BoseFS{{{self.N},{self.M}}}{self.onr()}"
+
+
+@total_ordering
+class FermiFS:
+    """FermiFS{N,M} (src/BitStringAddresses/fermifs.jl:54-161)."""
+
+    __slots__ = ("N", "M", "key")
+    fermion = True
+
+    def __init__(self, *args):
+        if len(args) == 2 and isinstance(args[1], dict):
+            M, pairs = args
+            onr = [0] * M
+            for mode, occ in pairs.items():
+                onr[mode - 1] = occ
+        elif len(args) == 1 and not isinstance(args[0], int):
+            onr = list(args[0])
+        else:
+            onr = list(args)
+        if any(n not in (0, 1) for n in onr):
+            raise ValueError("invalid fermionic ONR")
+        self.N = int(sum(onr))
+        self.M = len(onr)
+        if self.M > 64:
+            raise ValueError("FermiFS wider than 64 bits is not supported")
+        self.key = sum(1 << k for k, n in enumerate(onr) if n)
+
+    @classmethod
+    def from_key(cls, key: int, N: int, M: int) -> "FermiFS":
+        f = cls.__new__(cls)
+        f.N, f.M, f.key = N, M, int(key)
+        return f
+
+    @property
+    def nbits(self) -> int:
+        return self.M
+
+    def onr(self) -> tuple:
+        return tuple((self.key >> k) & 1 for k in range(self.M))
+
+    def num_occupied_modes(self) -> int:
+        return self.N
+
+    def __eq__(self, o):
+        return isinstance(o, FermiFS) and (self.N, self.M, self.key) == (o.N, o.M, o.key)
+
+    def __lt__(self, o):
+        return self.key < o.key
+
+    def __hash__(self):
+        return hash(("F", self.N, self.M, self.key))
+
+    def __repr__(self):
+        return f"FermiFS{{{self.N},{self.M}}}{self.onr()}"
+
+
+def near_uniform_onr(N: int, M: int) -> tuple:
+    """near_uniform_onr (bosefs.jl:139-148)."""
+    f, extras = divmod(N, M)
+    return tuple(f + (1 if i < extras else 0) for i in range(M))
+
+
+def near_uniform(kind, N: int, M: int):
+    """near_uniform(BoseFS{N,M}) / near_uniform(FermiFS{N,M})."""
+    if kind is FermiFS:
+        return FermiFS([1] * N + [0] * (M - N))
+    return BoseFS(near_uniform_onr(N, M))

@@ -1,0 +1,279 @@
+"""Device-resident walker list (the DVec/PDVec replacement) and apply_operator!.
+
+GPUDVec implements the AbstractDVec interface of src/Interfaces/dictvectors.jl:40 over a
+librimu_gpu vector handle; GPUWorkingMemory stands behind working_memory (dictvectors.jl:87)
+and apply_operator (dictvectors.jl:112-140) performs one projector step on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from .addresses import BoseFS
+from .styles import IsDeterministic, IsDynamicSemistochastic, StochasticStyle, default_style
+
+
+def _u64p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+class GPUDVec:
+    """Sparse vector of (address => value) pairs living in GPU memory.
+
+    ``GPUDVec({addr: val, ...}, style=...)``, ``GPUDVec(addr => val)`` as a tuple
+    ``(addr, val)``, or ``GPUDVec(style=..., address_type=addr)`` for an empty vector."""
+
+    def __init__(self, pairs=None, style: StochasticStyle | None = None, address_type=None,
+                 capacity: int = 0):
+        if isinstance(pairs, tuple) and len(pairs) == 2 and not isinstance(pairs[0], tuple):
+            pairs = {pairs[0]: pairs[1]}
+        pairs = dict(pairs or {})
+        if style is None:
+            vt = type(next(iter(pairs.values()))) if pairs else float
+            style = default_style(int if issubclass(vt, (int, np.integer)) else float)
+        self.style = style
+        self.valtype = style.valtype
+        proto = address_type if address_type is not None else (next(iter(pairs)) if pairs else None)
+        self.address_type = (type(proto), proto.N, proto.M) if proto is not None else (BoseFS, 0, 0)
+        lib = _lib.load()
+        self._ctx = _lib.default_context()
+        h = C.c_void_p()
+        vk = _lib.VAL_I64 if self.valtype is int else _lib.VAL_F64
+        _lib.check(lib.rimu_vec_create(self._ctx.handle, vk, max(capacity, len(pairs)), C.byref(h)))
+        self.handle = h
+        if pairs:
+            self.set_pairs(pairs)
+
+    # ---- storage ---------------------------------------------------------------------
+    def _np_vals(self, vals):
+        return np.ascontiguousarray(vals, dtype=np.int64 if self.valtype is int else np.float64)
+
+    def upload(self, keys, vals):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        vals = self._np_vals(vals)
+        _lib.check(_lib.load().rimu_vec_upload(self.handle, _u64p(keys), vals.ctypes.data_as(C.c_void_p),
+                                                len(keys)))
+
+    def set_pairs(self, pairs: dict):
+        keys = [a.key for a in pairs]
+        vals = list(pairs.values())
+        self.upload(keys, vals)
+
+    def download(self):
+        """(keys, values) as numpy arrays, in bucket order."""
+        lib = _lib.load()
+        n = C.c_int64()
+        _lib.check(lib.rimu_vec_length(self.handle, C.byref(n)))
+        cap = max(n.value, 1)
+        keys = np.zeros(cap, dtype=np.uint64)
+        vals = np.zeros(cap, dtype=np.int64 if self.valtype is int else np.float64)
+        got = C.c_int64()
+        _lib.check(lib.rimu_vec_download(self.handle, _u64p(keys), vals.ctypes.data_as(C.c_void_p),
+                                          cap, C.byref(got)))
+        return keys[:got.value], vals[:got.value]
+
+    def sorted_arrays(self):
+        k, v = self.download()
+        o = np.argsort(k, kind="stable")
+        return k[o], v[o]
+
+    # ---- AbstractDVec interface --------------------------------------------------------
+    def __len__(self):
+        n = C.c_int64()
+        _lib.check(_lib.load().rimu_vec_length(self.handle, C.byref(n)))
+        return n.value
+
+    def _addr(self, key):
+        cls, N, M = self.address_type
+        return cls.from_key(int(key), N, M)
+
+    def pairs(self):
+        k, v = self.sorted_arrays()
+        return [(self._addr(a), self.valtype(b)) for a, b in zip(k, v)]
+
+    def keys(self):
+        return [a for a, _ in self.pairs()]
+
+    def values(self):
+        return [b for _, b in self.pairs()]
+
+    def to_dict(self):
+        return dict(self.pairs())
+
+    def __getitem__(self, addr):
+        keys = np.array([addr.key], dtype=np.uint64)
+        out = np.zeros(1, dtype=np.int64 if self.valtype is int else np.float64)
+        _lib.check(_lib.load().rimu_vec_lookup(self.handle, _u64p(keys), 1,
+                                                out.ctypes.data_as(C.c_void_p)))
+        return self.valtype(out[0])
+
+    def lookup_keys(self, keys):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        out = np.zeros(len(keys), dtype=np.int64 if self.valtype is int else np.float64)
+        if len(keys):
+            _lib.check(_lib.load().rimu_vec_lookup(self.handle, _u64p(keys), len(keys),
+                                                    out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def walkernumber_and_length(self):
+        """walkernumber_and_length (abstractdvec.jl:270): 1-norm and length."""
+        norm, n = C.c_double(), C.c_int64()
+        _lib.check(_lib.load().rimu_vec_walkernumber_and_length(self.handle, C.byref(norm),
+                                                                 C.byref(n)))
+        return norm.value, n.value
+
+    def walkernumber(self):
+        return self.walkernumber_and_length()[0]
+
+    def StochasticStyle(self):
+        return self.style
+
+    def empty(self):
+        _lib.check(_lib.load().rimu_vec_empty(self.handle))
+        return self
+
+    zerovector_ = empty
+
+    def similar(self):
+        cls, N, M = self.address_type
+        return GPUDVec(style=self.style, address_type=cls.from_key(0, N, M))
+
+    def copy(self):
+        w = self.similar()
+        _lib.check(_lib.load().rimu_vec_copy(w.handle, self.handle))
+        return w
+
+    def dot(self, other) -> float:
+        """dot(self, other) for a dict / GPUDVec `other` (small side is looked up)."""
+        if isinstance(other, dict):
+            keys = np.array([a.key for a in other], dtype=np.uint64)
+            mine = self.lookup_keys(keys)
+            return float(sum(float(m) * float(o) for m, o in zip(mine, other.values())))
+        if len(other) < len(self):
+            return other.dot(self)
+        k, v = self.download()
+        theirs = other.lookup_keys(k)
+        return float(np.dot(v.astype(float), theirs.astype(float)))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().rimu_vec_destroy(self.handle)
+        except Exception:
+            pass
+
+    def __repr__(self):
+        return f"GPUDVec(len={len(self)}, style={self.style})"
+
+
+class GPUWorkingMemory:
+    """Working memory of one projector step: spawn buffers, statistics and the
+    ProjectedEnergy projector.  Holds the random-stream state (seed, counter)."""
+
+    def __init__(self, seed: int = 0):
+        lib = _lib.load()
+        self._ctx = _lib.default_context()
+        h = C.c_void_p()
+        _lib.check(lib.rimu_wm_create(self._ctx.handle, C.byref(h)))
+        self.handle = h
+        self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        self.counter = 0
+        self.replica = 0
+        self.projector_keys = None
+
+    def set_projector(self, keys, pvals, hpvals):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        o = np.argsort(keys)
+        keys, pvals, hpvals = keys[o], np.asarray(pvals, float)[o], np.asarray(hpvals, float)[o]
+        pv = np.ascontiguousarray(pvals)
+        hv = np.ascontiguousarray(hpvals)
+        _lib.check(_lib.load().rimu_wm_set_projector(
+            self.handle, _u64p(keys), pv.ctypes.data_as(C.POINTER(C.c_double)),
+            hv.ctypes.data_as(C.POINTER(C.c_double)), len(keys)))
+        self.projector_keys = keys if len(keys) else None
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().rimu_wm_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def working_memory(v: GPUDVec, seed: int = 0) -> GPUWorkingMemory:
+    return GPUWorkingMemory(seed)
+
+
+class FirstOrderTransitionOperator:
+    """T = 1 + dt (S - H) (src/fciqmc.jl:78-112)."""
+
+    def __init__(self, hamiltonian, shift: float, time_step: float):
+        self.hamiltonian = hamiltonian
+        self.shift = float(shift)
+        self.time_step = float(time_step)
+
+
+def apply_operator(wm: GPUWorkingMemory, target: GPUDVec, source: GPUDVec, op, boost=1.0,
+                   step: int | None = None):
+    """apply_operator!(wm, target, source, op, boost) -> (stat_names, stats, wm, target)
+    (dictvectors.jl:112-140).  `op` is a FirstOrderTransitionOperator or a Hamiltonian
+    (plain multiplication, used by mul!).  `step` fixes the random counter; by default the
+    working memory's counter is used and advanced."""
+    if target is source:
+        raise ValueError("`target` and `source` must not have the same local storage")
+    style = source.style
+    p = _lib.StepParams()
+    sp = style.params()
+    p.style = sp["style"]
+    if isinstance(op, FirstOrderTransitionOperator):
+        ham = op.hamiltonian
+        p.op, p.dt, p.shift = _lib.OP_TRANSITION, op.time_step, op.shift
+    else:
+        ham = op
+        p.op, p.dt, p.shift = _lib.OP_HAMILTONIAN, 0.0, 0.0
+        if not isinstance(style, IsDeterministic):
+            raise ValueError("plain multiplication needs IsDeterministic")
+    p.boost = float(boost)
+    p.proj_threshold = sp["proj_threshold"]
+    p.compression = sp["compression"]
+    p.rel_spawning_threshold = sp["rel_spawning_threshold"]
+    p.abs_spawning_threshold = sp["abs_spawning_threshold"]
+    p.seed = wm.seed
+    if step is None:
+        step = wm.counter
+        wm.counter += 1
+    p.step = int(step) & 0xFFFFFFFF
+    p.replica = wm.replica
+    target.style, target.valtype, target.address_type = source.style, source.valtype, source.address_type
+    st = _lib.StepStats()
+    _lib.check(_lib.load().rimu_apply_operator(ham.handle, wm.handle, target.handle, source.handle,
+                                                C.byref(p), C.byref(st)))
+    names = style.step_stat_names() + style.compression_names()
+    full = {f: getattr(st, f) for f, _ in _lib.StepStats._fields_}
+    stats = tuple(full[n] for n in names)
+    wm.last_stats = full
+    return names, stats, wm, target
+
+
+def mul(y: GPUDVec, H, x: GPUDVec, wm: GPUWorkingMemory | None = None) -> GPUDVec:
+    """mul!(y, H, x) for sparse vectors (abstractdvec.jl:275-284, pdvec.jl:810-822)."""
+    if not isinstance(x.style, IsDeterministic):
+        raise ValueError("mul! needs IsDeterministic vectors")
+    wm = wm or GPUWorkingMemory()
+    apply_operator(wm, y, x, H)
+    return y
+
+
+def dot_operator(w: GPUDVec, H, v: GPUDVec) -> float:
+    """dot(w, H, v) (abstractdvec.jl:298-324)."""
+    tmp = GPUDVec(style=IsDeterministic(), address_type=v._addr(0))
+    src = v
+    if not isinstance(v.style, IsDeterministic):
+        k, vals = v.download()
+        src = GPUDVec(style=IsDeterministic(), address_type=v._addr(0))
+        src.upload(k, vals.astype(np.float64))
+    mul(tmp, H, src)
+    return tmp.dot(w)

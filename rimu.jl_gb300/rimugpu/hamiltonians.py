@@ -1,0 +1,266 @@
+"""Hamiltonians: the AbstractHamiltonian interface on device-side model handles.
+
+HubbardReal1D (src/Hamiltonians/HubbardReal1D.jl), HubbardRealSpace with one component
+(HubbardRealSpace.jl, geometry.jl) and HubbardMom1D with BoseFS (HubbardMom1D.jl).  Matrix
+elements are evaluated by librimu_gpu; this module only holds parameters and converts.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from .addresses import BoseFS, FermiFS
+
+
+class CubicGrid:
+    """CubicGrid(dims, fold) (geometry.jl:45-54): `fold[i]` True for periodic boundaries."""
+
+    def __init__(self, dims, fold=None):
+        dims = tuple(int(d) for d in dims)
+        if any(d <= 1 for d in dims):
+            raise ValueError("All dimensions must be at least 2 in size")
+        if not 1 <= len(dims) <= 3:
+            raise ValueError("1 to 3 dimensions are supported")
+        self.dims = dims
+        self.fold = tuple(bool(f) for f in fold) if fold is not None else tuple(True for _ in dims)
+
+    def __len__(self):
+        return int(np.prod(self.dims))
+
+    def __repr__(self):
+        return f"CubicGrid({self.dims}, {self.fold})"
+
+
+def PeriodicBoundaries(*dims):
+    dims = dims[0] if len(dims) == 1 and isinstance(dims[0], tuple) else dims
+    return CubicGrid(dims, tuple(True for _ in dims))
+
+
+def HardwallBoundaries(*dims):
+    dims = dims[0] if len(dims) == 1 and isinstance(dims[0], tuple) else dims
+    return CubicGrid(dims, tuple(False for _ in dims))
+
+
+def LadderBoundaries(*dims):
+    """First dimension hard-wall, the rest periodic (geometry.jl:87-90)."""
+    dims = dims[0] if len(dims) == 1 and isinstance(dims[0], tuple) else dims
+    return CubicGrid(dims, tuple(i > 0 for i in range(len(dims))))
+
+
+def hubbard_dispersion(t, k):
+    """-2t cos(k) (HubbardMom1D.jl:7)."""
+    return -2 * t * math.cos(k)
+
+
+def continuum_dispersion(t, k):
+    """t k^2 (HubbardMom1D.jl:17)."""
+    return t * k ** 2
+
+
+class AbstractHamiltonian:
+    kind = 0
+
+    def __init__(self, address):
+        self.address = address
+        self._handle = None
+        self._keep = []
+
+    # ---- device handle -------------------------------------------------------------
+    def _desc(self) -> _lib.ModelDesc:
+        raise NotImplementedError
+
+    @property
+    def handle(self):
+        if self._handle is None:
+            lib = _lib.load()
+            ctx = _lib.default_context()
+            h = C.c_void_p()
+            _lib.check(lib.rimu_model_create(ctx.handle, C.byref(self._desc()), C.byref(h)))
+            self._handle = h
+            self._ctx = ctx
+        return self._handle
+
+    def __del__(self):
+        try:
+            if self._handle is not None:
+                _lib.load().rimu_model_destroy(self._handle)
+        except Exception:
+            pass
+
+    # ---- AbstractHamiltonian interface (Interfaces/hamiltonians.jl:201-421) ----------
+    def starting_address(self):
+        return self.address
+
+    def LOStructure(self):
+        return "IsHermitian"
+
+    @property
+    def N(self):
+        return self.address.N
+
+    @property
+    def M(self):
+        return self.address.M
+
+    def _addr(self, key):
+        return type(self.address).from_key(key, self.N, self.M)
+
+    def diagonal_element(self, address) -> float:
+        out = np.zeros(1)
+        keys = np.array([address.key], dtype=np.uint64)
+        _lib.check(_lib.load().rimu_model_diagonal(
+            self.handle, keys.ctypes.data_as(C.POINTER(C.c_uint64)), 1,
+            out.ctypes.data_as(C.POINTER(C.c_double))))
+        return float(out[0])
+
+    def diagonal_elements(self, keys) -> np.ndarray:
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        out = np.zeros(len(keys))
+        _lib.check(_lib.load().rimu_model_diagonal(
+            self.handle, keys.ctypes.data_as(C.POINTER(C.c_uint64)), len(keys),
+            out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def num_offdiagonals(self, address) -> int:
+        n = C.c_int()
+        _lib.check(_lib.load().rimu_model_num_offdiagonals(self.handle, C.c_uint64(address.key),
+                                                          C.byref(n)))
+        return n.value
+
+    def offdiagonal_keys(self, key: int):
+        """(keys, values) of all offdiagonals of column `key`, in the reference's order."""
+        lib = _lib.load()
+        n = C.c_int()
+        _lib.check(lib.rimu_model_num_offdiagonals(self.handle, C.c_uint64(key), C.byref(n)))
+        ks = np.zeros(max(n.value, 1), dtype=np.uint64)
+        vs = np.zeros(max(n.value, 1))
+        got = C.c_int()
+        _lib.check(lib.rimu_model_offdiagonals(
+            self.handle, C.c_uint64(key), ks.ctypes.data_as(C.POINTER(C.c_uint64)),
+            vs.ctypes.data_as(C.POINTER(C.c_double)), len(ks), C.byref(got)))
+        return ks[:got.value], vs[:got.value]
+
+    def offdiagonals(self, address):
+        """offdiagonals(H, address): list of (address, matrix element)."""
+        ks, vs = self.offdiagonal_keys(address.key)
+        return [(self._addr(int(k)), float(v)) for k, v in zip(ks, vs)]
+
+    def get_offdiagonal(self, address, chosen: int):
+        return self.offdiagonals(address)[chosen - 1]
+
+    def dimension(self) -> int:
+        d = C.c_int64()
+        _lib.check(_lib.load().rimu_basis_dimension(self.handle, C.byref(d)))
+        return d.value
+
+
+class HubbardReal1D(AbstractHamiltonian):
+    """HubbardReal1D(address; u=1.0, t=1.0) (HubbardReal1D.jl:26-29)."""
+    kind = _lib.MODEL_REAL1D
+
+    def __init__(self, address: BoseFS, u=1.0, t=1.0):
+        if not isinstance(address, BoseFS):
+            raise TypeError("HubbardReal1D needs a BoseFS address")
+        super().__init__(address)
+        self.u, self.t = float(u), float(t)
+
+    def _desc(self):
+        d = _lib.ModelDesc()
+        d.kind, d.fermion, d.n_particles, d.n_modes = self.kind, 0, self.N, self.M
+        d.u, d.t, d.ndim = self.u, self.t, 1
+        d.dims[0], d.periodic[0] = self.M, 1
+        return d
+
+    def with_params(self, u=None, t=None):
+        return HubbardReal1D(self.address, self.u if u is None else u, self.t if t is None else t)
+
+    def __repr__(self):
+        return f"HubbardReal1D({self.address}; u={self.u}, t={self.t})"
+
+
+class HubbardRealSpace(AbstractHamiltonian):
+    """HubbardRealSpace(address; geometry, t, u, v) with one component
+    (HubbardRealSpace.jl:182-231).  `t` and `u` may be scalars or 1-element sequences; `v`
+    (trap strengths per dimension) gives the potential of HubbardRealSpace.jl:214-226."""
+    kind = _lib.MODEL_REALSPACE
+
+    def __init__(self, address, geometry: CubicGrid | None = None, t=(1.0,), u=((1.0,),), v=None):
+        if not isinstance(address, (BoseFS, FermiFS)):
+            raise TypeError("HubbardRealSpace needs a single-component BoseFS or FermiFS")
+        super().__init__(address)
+        self.geometry = geometry if geometry is not None else PeriodicBoundaries(address.M)
+        if len(self.geometry) != address.M:
+            raise ValueError("`geometry` does not have the correct number of sites")
+        self.t = float(np.ravel(t)[0])
+        self.u = float(np.ravel(u)[0])
+        self.v = None if v is None or not np.any(v) else np.ravel(np.asarray(v, dtype=float))
+        self.potential = None
+        if self.v is not None:
+            dims = self.geometry.dims
+            ranges = [[-(Md // 2) + i for i in range(Md)] for Md in dims]
+            pot = []
+            for lin in range(address.M):
+                rem, acc = lin, None
+                for d, Md in enumerate(dims):
+                    x = ranges[d][rem % Md]
+                    rem //= Md
+                    term = self.v[d] * (x ** 2)
+                    acc = term if acc is None else acc + term
+                pot.append(acc)
+            self.potential = np.array(pot, dtype=np.float64)
+
+    def _desc(self):
+        d = _lib.ModelDesc()
+        d.kind, d.n_particles, d.n_modes = self.kind, self.N, self.M
+        d.fermion = 1 if isinstance(self.address, FermiFS) else 0
+        d.u, d.t = self.u, self.t
+        g = self.geometry
+        d.ndim = len(g.dims)
+        for i in range(3):
+            d.dims[i] = g.dims[i] if i < len(g.dims) else 1
+            d.periodic[i] = int(g.fold[i]) if i < len(g.dims) else 1
+        if self.potential is not None:
+            arr = np.ascontiguousarray(self.potential)
+            self._keep.append(arr)
+            d.potential = arr.ctypes.data_as(C.POINTER(C.c_double))
+        return d
+
+    def with_params(self, u=None, t=None):
+        return HubbardRealSpace(self.address, self.geometry, self.t if t is None else t,
+                                self.u if u is None else u, self.v)
+
+    def __repr__(self):
+        return f"HubbardRealSpace({self.address}; geometry={self.geometry}, t={self.t}, u={self.u})"
+
+
+class HubbardMom1D(AbstractHamiltonian):
+    """HubbardMom1D(address; u=1.0, t=1.0, dispersion=hubbard_dispersion) with BoseFS
+    (HubbardMom1D.jl:49-65)."""
+    kind = _lib.MODEL_MOM1D
+
+    def __init__(self, address: BoseFS, u=1.0, t=1.0, dispersion=hubbard_dispersion):
+        if not isinstance(address, BoseFS):
+            raise TypeError("HubbardMom1D is supported with BoseFS addresses")
+        super().__init__(address)
+        self.u, self.t = float(u), float(t)
+        M = address.M
+        step = 2 * math.pi / M
+        start = (-math.pi * (1 + 1 / M) + step) if M % 2 == 1 else (-math.pi + step)
+        self.ks = np.array([start + i * step for i in range(M)])
+        self.kes = np.array([dispersion(self.t, k) for k in self.ks], dtype=np.float64)
+
+    def _desc(self):
+        d = _lib.ModelDesc()
+        d.kind, d.fermion, d.n_particles, d.n_modes = self.kind, 0, self.N, self.M
+        d.u, d.t, d.ndim = self.u, self.t, 1
+        d.dims[0], d.periodic[0] = self.M, 1
+        arr = np.ascontiguousarray(self.kes)
+        self._keep.append(arr)
+        d.dispersion = arr.ctypes.data_as(C.POINTER(C.c_double))
+        return d
+
+    def __repr__(self):
+        return f"HubbardMom1D({self.address}; u={self.u}, t={self.t})"

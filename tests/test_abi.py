@@ -1,0 +1,68 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point that
+include/rimu_gpu.h declares (no compute call: runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import rimugpu
+from rimugpu import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "rimu_gpu.h")).read()
+    return sorted(set(re.findall(r"^int\s+(rimu_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_bound_entry_points():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(_lib.load().__dict__["_name"])
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_error_string_without_gpu():
+    lib = _lib.load()
+    assert lib.rimu_version() >= 10000
+    buf = ctypes.create_string_buffer(64)
+    assert lib.rimu_last_error(buf, 64) == 0
+
+
+def test_bad_arguments_fail_loudly_without_touching_the_gpu():
+    lib = _lib.load()
+    # NULL handles are rejected with RIMU_ERR_BADARG before any CUDA call
+    assert lib.rimu_apply_operator(None, None, None, None, None, None) == _lib.RIMU_ERR_BADARG
+    assert "NULL" in _lib.last_error()
+    assert lib.rimu_vec_length(None, None) == _lib.RIMU_ERR_BADARG
+
+
+def test_address_encoding_matches_reference_layout():
+    b = rimugpu.BoseFS(1, 0, 2)        # bits: mode1 '1', sep, mode2 sep, mode3 '11'
+    assert b.key == 0b11001 and b.onr() == (1, 0, 2)
+    assert rimugpu.BoseFS.from_key(b.key, 3, 3) == b
+    f = rimugpu.FermiFS(1, 1, 0, 1)
+    assert f.key == 0b1011 and f.onr() == (1, 1, 0, 1)
+    assert rimugpu.near_uniform(rimugpu.BoseFS, 7, 5).onr() == (2, 2, 1, 1, 1)
+    assert sorted([rimugpu.BoseFS(0, 2), rimugpu.BoseFS(2, 0), rimugpu.BoseFS(1, 1)])[0].onr() == (2, 0)
+
+
+def test_host_address_encoding_agrees_with_oracle():
+    import numpy as np
+    import oracle as O
+    rng = np.random.default_rng(2)
+    for N, M in ((6, 6), (20, 20), (10, 20), (3, 30)):
+        for _ in range(20):
+            onr = np.bincount(rng.integers(0, M, N), minlength=M).tolist()
+            assert rimugpu.BoseFS(onr).key == O.bose_key(onr)
+
+
+def test_blocking_analysis_on_correlated_series():
+    import numpy as np
+    rng = np.random.default_rng(0)
+    x = np.convolve(rng.normal(size=2 ** 14 + 63), np.ones(64) / 64, mode="valid")
+    r = rimugpu.blocking_analysis(x)
+    assert r.k > 1 and r.err > np.std(x) / np.sqrt(len(x))

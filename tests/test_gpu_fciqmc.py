@@ -1,0 +1,69 @@
+"""End-to-end FCIQMC through ProjectorMonteCarloProblem / solve on the GPU: statistical
+agreement with exact energies (blocking analysis), reproducibility, ProjectedEnergy."""
+import numpy as np
+import pytest
+
+import oracle as O
+import rimugpu as R
+
+pytestmark = pytest.mark.gpu
+
+
+def test_c1_integer_walkers_shift_brackets_exact_energy():
+    """HubbardReal1D M=N=6, u=6: shift and projected energy agree with E0 = -4.0215
+    (test/KrylovKit.jl:15) within 3 blocking errors."""
+    addr = R.BoseFS([1] * 6)
+    H = R.HubbardReal1D(addr, u=6.0, t=1.0)
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsStochasticInteger(), target_walkers=1000,
+                                     time_step=1e-3, last_step=12000, random_seed=1234,
+                                     post_step_strategy=R.ProjectedEnergy(H, (addr, 1.0)))
+    sim = R.solve(p)
+    assert sim.success
+    df = sim.df
+    E0 = O.ground_energy(O.real1d(6, 6, 6.0))
+    r = R.shift_estimator(df, skip=3000)
+    assert abs(r.mean - E0) < max(3 * r.err, 0.02), (r.mean, r.err)
+    pe, pe_err = R.projected_energy(df, skip=3000)
+    assert abs(pe - E0) < max(3 * pe_err, 0.02), (pe, pe_err)
+
+
+def test_dss_shift_brackets_exact_energy():
+    addr = R.BoseFS([1] * 5)
+    H = R.HubbardReal1D(addr, u=1.0)
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsDynamicSemistochastic(), target_walkers=100,
+                                     time_step=1e-2, last_step=6000, random_seed=99,
+                                     shift_strategy=R.DoubleLogUpdate(100, 0.05, 0.05 ** 2 / 4))
+    sim = R.solve(p)
+    r = R.shift_estimator(sim.df, skip=1000)
+    assert abs(r.mean - (-8.280991746582686)) < max(3 * r.err, 0.02), (r.mean, r.err)
+
+
+def test_same_seed_identical_reports():
+    """Same random_seed => identical DataFrames (test/projector_monte_carlo_problem.jl:126-167)."""
+    H = R.HubbardReal1D(R.BoseFS([1] * 6), u=6.0)
+    def run():
+        p = R.ProjectorMonteCarloProblem(H, target_walkers=300, time_step=1e-2, last_step=300,
+                                         random_seed=42)
+        return R.solve(p).df
+    a, b = run(), run()
+    assert set(a) == set(b)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_deterministic_power_iteration_converges_to_ground_state():
+    addr = R.BoseFS([1] * 6)
+    H = R.HubbardReal1D(addr, u=6.0)
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsDeterministic(), start_at={addr: 1.0},
+                                     target_walkers=10, time_step=0.05, last_step=1500)
+    sim = R.solve(p)
+    assert sim.df["shift"][-1] == pytest.approx(O.ground_energy(O.real1d(6, 6, 6.0)), abs=1e-8)
+
+
+def test_abort_on_dead_population():
+    H = R.HubbardReal1D(R.BoseFS([1] * 4), u=1.0)
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsStochasticInteger(), shift=-50.0,
+                                     shift_strategy=R.DontUpdate(10 ** 9), time_step=0.1,
+                                     last_step=100, population=1, random_seed=3)
+    sim = R.solve(p)
+    assert sim.aborted and "dead" in sim.message

@@ -1,0 +1,150 @@
+"""The CPU oracle against the reference's own known answers (tests/golden/reference_goldens.json).
+CPU only: this pins the checker before it is trusted for GPU parity."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+G = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+
+
+def test_hopnextneighbour_docstring():
+    for c in G["hopnextneighbour"]:
+        onr = c["onr"]
+        m = O.real1d(sum(onr), len(onr), u=1.0, t=1.0)
+        nk, val = O.offdiagonals(m, O.bose_key(onr))[c["chosen"] - 1]
+        assert O.bose_onr(nk, len(onr)) == c["new"]
+        assert -val == c["value"]          # get_offdiagonal = -t * hopnextneighbour value
+
+
+def test_real1d_offdiagonals_docstring():
+    c = G["real1d_offdiagonals"]
+    m = O.real1d(sum(c["onr"]), len(c["onr"]), c["u"], c["t"])
+    got = [(O.bose_onr(k, 3), v) for k, v in O.offdiagonals(m, O.bose_key(c["onr"]))]
+    assert got == [(p[0], p[1]) for p in c["pairs"]]
+
+
+def test_bose_hubbard_interaction():
+    for c in G["bose_hubbard_interaction"]:
+        m = O.real1d(sum(c["onr"]), len(c["onr"]), u=2.0)
+        assert O.diagonal(m, O.bose_key(c["onr"])) == c["value"]   # u/2 * interaction with u=2
+
+
+def test_mom1d_goldens():
+    c = G["mom1d"]
+    m = O.mom1d(sum(c["onr"]), len(c["onr"]), c["u"], c["t"])
+    k = O.bose_key(c["onr"])
+    assert O.diagonal(m, k) == c["diagonal"]
+    assert O.num_offdiagonals(m, k) == c["num_offdiagonals"]
+    nk, v = O.offdiagonals(m, k)[2]
+    assert O.bose_onr(nk, 3) == c["offdiag3"][0] and v == c["offdiag3"][1]
+    d = G["momentum_transfer_diagonal"]
+    m5 = O.mom1d(6, 5)
+    kin = sum(m5.kes[i] * n for i, n in enumerate(d["onr"]) if n)
+    assert O.diagonal(m5, O.bose_key(d["onr"])) - kin == pytest.approx(d["value"], abs=1e-14)
+
+
+def test_realspace_fermion_offdiagonal_counts():
+    c = G["realspace_fermi_offdiag_counts"]
+    f = O.fermi_key([1] * c["N"] + [0] * (c["M"] - c["N"]))
+    for dims, periodic, total, nonzero in c["cases"]:
+        m = O.realspace(c["N"], tuple(dims), u=0.0, periodic=(periodic, periodic), fermion=True)
+        od = O.offdiagonals(m, f)
+        assert len(od) == total and sum(1 for _, v in od if v != 0) == nonzero
+
+
+@pytest.mark.parametrize("case", G["energies"], ids=lambda c: c["src"] + str(c.get("N", "")))
+def test_exact_energies(case):
+    if case["model"] == "real1d":
+        E = O.ground_energy(O.real1d(case["N"], case["M"], case["u"], case["t"]))
+    elif case["model"] == "mom1d":
+        onr = case["start"]
+        E = O.ground_energy(O.mom1d(sum(onr), len(onr), case["u"], case["t"]), O.bose_key(onr))
+    else:
+        E = O.ground_energy(O.realspace(case["N"], tuple(case["dims"]), u=case["u"], t=case["t"],
+                                        fermion=True))
+    assert E == pytest.approx(case["E0"], abs=case["atol"])
+
+
+def test_real1d_equals_realspace_1d():
+    c = G["real1d_equals_realspace"]
+    N, M = sum(c["onr"]), len(c["onr"])
+    a = O.ground_energy(O.real1d(N, M, c["u"], c["t"]))
+    b = O.ground_energy(O.realspace(N, (M,), u=c["u"], t=c["t"]))
+    assert a == pytest.approx(b, abs=1e-12)
+
+
+def test_hopnextneighbour_equals_excitation_on_random_onrs():
+    """HubbardReal1D (hop formula) agrees with HubbardRealSpace 1D (excitation formula) on
+    random ONRs, as test/BitStringAddresses.jl:251-297 checks hopnextneighbour."""
+    rng = np.random.default_rng(7)
+    for N, M in ((16, 16), (3, 32), (20, 20), (5, 40)):
+        for _ in range(10):
+            onr = np.bincount(rng.integers(0, M, N), minlength=M).tolist()
+            k = O.bose_key(onr)
+            a = O.offdiagonals(O.real1d(N, M), k)
+            b = O.offdiagonals(O.realspace(N, (M,)), k)
+            assert a == b
+            assert O.bose_onr(k, M) == onr
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 known-answer vectors of the Random123 distribution (Salmon et al.)."""
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == \
+        [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_oracle_step_is_deterministic_and_conserves_structure():
+    m = O.real1d(6, 6, u=6.0)
+    k0 = O.bose_key([1] * 6)
+    p = O.StepParams(O.STYLE_INTEGER, dt=1e-3, shift=0.0, seed=11, step=1)
+    a = O.step(m, p, [k0], [10])
+    b = O.step(m, p, [k0], [10])
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2]
+    assert a[2]["spawn_attempts"] == 10 and a[2]["len"] == len(a[0])
+    assert a[2]["norm"] == float(np.abs(a[1]).sum())
+
+
+def test_oracle_deterministic_step_matches_dense_transition_matrix():
+    """IsDeterministic step == (1 + dt(S - H)) v with the dense matrix (fciqmc.jl:78-112)."""
+    m = O.real1d(4, 4, u=3.0, t=1.5)
+    keys = O.basis(m)
+    H = O.sparse_matrix(m, keys).toarray()
+    rng = np.random.default_rng(3)
+    v = rng.normal(size=len(keys))
+    dt, S = 0.01, -1.25
+    ok, ov, st = O.step(m, O.StepParams(O.STYLE_DETERMINISTIC, dt=dt, shift=S), keys, v)
+    want = (np.eye(len(keys)) + dt * (S * np.eye(len(keys)) - H)) @ v
+    got = np.zeros(len(keys))
+    got[np.searchsorted(keys, ok)] = ov
+    assert np.allclose(got, want, rtol=1e-13, atol=1e-15)
+    assert st["exact_steps"] == len(keys)
+
+
+def test_oracle_hv_matches_sparse_matrix():
+    for m in (O.real1d(6, 6, u=2.0), O.realspace(4, (2, 3), u=1.0, t=0.7),
+              O.mom1d(4, 5, u=2.0), O.realspace(3, (3, 3), u=0.0, fermion=True)):
+        keys = O.basis(m)
+        v = np.random.default_rng(1).normal(size=len(keys))
+        assert np.allclose(O.hv_basis(m, keys, v), O.sparse_matrix(m, keys) @ v, rtol=1e-13, atol=1e-13)
+
+
+def test_oracle_adjoint_matches_finite_differences():
+    N, M, u, t = 5, 5, 2.0, 1.0
+    m = O.real1d(N, M, u, t)
+    keys = O.basis(m)
+    rng = np.random.default_rng(5)
+    v, gw = rng.normal(size=len(keys)), rng.normal(size=len(keys))
+    gv, gu, gt = O.hv_basis_adjoint(m, keys, v, gw)
+    H = O.sparse_matrix(m, keys)
+    assert np.allclose(gv, H.T @ gw, rtol=1e-13, atol=1e-13)
+    h = 1e-5
+    fu = (gw @ O.hv_basis(O.real1d(N, M, u + h, t), keys, v) - gw @ O.hv_basis(O.real1d(N, M, u - h, t), keys, v)) / (2 * h)
+    ft = (gw @ O.hv_basis(O.real1d(N, M, u, t + h), keys, v) - gw @ O.hv_basis(O.real1d(N, M, u, t - h), keys, v)) / (2 * h)
+    assert gu == pytest.approx(fu, rel=1e-7) and gt == pytest.approx(ft, rel=1e-7)

@@ -64,8 +64,13 @@ __device__ __forceinline__ int bose_interaction_hv(uint64_t key) {
 
 // One HubbardReal1D row: w = d v + sum fma(H, v_j), optionally also k = sum fma(-sqrt p, x_j)
 // for the hopping derivative (second vector x).
+// A rank outside the basis can only come from an inconsistent address; the gather is
+// skipped and the row marked NaN so that callers see it.
+#define RIMU_GATHER_GUARD(j) if ((j) >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); continue; }
+
 template <bool ADJ>
 __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *tab, uint64_t row,
+                                           int64_t dim,
                                            uint64_t key, const double *__restrict__ v,
                                            const double *__restrict__ x, const double *dtabH,
                                            const double *dhdt, double &acc, double &kacc) {
@@ -93,6 +98,7 @@ __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *ta
         int idx = popc64(key & lowmask(q + 1));
         j = row + C(tab, w, q, idx - 1);
       }
+      if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }
       acc = fma(h.hoff[prod], v[j], acc);
       if (ADJ) kacc = fma(dhdt[prod], x[j], kacc);
     }
@@ -112,6 +118,7 @@ __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *ta
         int idx = popc64(key & lowmask(bit + 1));
         j = row - C(tab, w, bit - 1, idx - 1);
       }
+      if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }
       acc = fma(h.hoff[prod], v[j], acc);
       if (ADJ) kacc = fma(dhdt[prod], x[j], kacc);
     }
@@ -122,8 +129,8 @@ __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *ta
 
 template <int KIND>
 __device__ __forceinline__ double generic_row(const DevModel &h, const uint64_t *tab,
-                                              uint64_t row, uint64_t key, const double *v,
-                                              double diag) {
+                                              uint64_t row, int64_t dim, uint64_t key,
+                                              const double *v, double diag) {
   double acc = diag * v[row];
   int noff;
   MomMap m;
@@ -137,6 +144,7 @@ __device__ __forceinline__ double generic_row(const DevModel &h, const uint64_t 
     double hv = h.hoff[od.prod];
     if (od.sign < 0) hv = -hv;
     uint64_t j = rank_of(od.key, h.N, tab);
+    RIMU_GATHER_GUARD(j);
     acc = fma(hv, v[j], acc);
   }
   return acc;
@@ -205,9 +213,9 @@ __global__ void __launch_bounds__(HB) k_hv(DevModel h, const uint64_t *binom, in
     double acc;
     if (KIND == MODEL_REAL1D) {
       double k;
-      real1d_row<false>(h, s_tab, (uint64_t)row, key, v, nullptr, dtabH, nullptr, acc, k);
+      real1d_row<false>(h, s_tab, (uint64_t)row, dim, key, v, nullptr, dtabH, nullptr, acc, k);
     } else {
-      acc = generic_row<KIND>(h, s_tab, (uint64_t)row, key, v, hv_diag<KIND>(h, key));
+      acc = generic_row<KIND>(h, s_tab, (uint64_t)row, dim, key, v, hv_diag<KIND>(h, key));
     }
     w[row] = acc;
   }
@@ -234,7 +242,7 @@ __global__ void __launch_bounds__(HB) k_hv_adjoint(DevModel h, const uint64_t *b
     uint64_t key = unrank((uint64_t)row, B, wt, s_tab);
     double acc, kv;
     if (KIND == MODEL_REAL1D) {
-      real1d_row<true>(h, s_tab, (uint64_t)row, key, gw, v, dtabH, dhdt, acc, kv);
+      real1d_row<true>(h, s_tab, (uint64_t)row, dim, key, gw, v, dtabH, dhdt, acc, kv);
     } else {
       // bosonic one-component HubbardRealSpace without trap
       acc = dtabH[bose_interaction_hv(key)] * gw[row];
@@ -244,6 +252,7 @@ __global__ void __launch_bounds__(HB) k_hv_adjoint(DevModel h, const uint64_t *b
         Offdiag od = realspace_offdiag(h, key, c);
         if (od.prod == 0) continue;
         uint64_t j = rank_of(od.key, wt, s_tab);
+        RIMU_GATHER_GUARD(j);
         acc = fma(h.hoff[od.prod], gw[j], acc);
         kv = fma(dhdt[od.prod], v[j], kv);
       }

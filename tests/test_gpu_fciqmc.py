@@ -54,10 +54,11 @@ def test_same_seed_identical_reports():
 def test_deterministic_power_iteration_converges_to_ground_state():
     addr = R.BoseFS([1] * 6)
     H = R.HubbardReal1D(addr, u=6.0)
+    # dt below 2 / (E_max - E0) so that 1 + dt (S - H) is a contraction on the excited states
     p = R.ProjectorMonteCarloProblem(H, style=R.IsDeterministic(), start_at={addr: 1.0},
-                                     target_walkers=10, time_step=0.05, last_step=1500)
+                                     target_walkers=10, time_step=0.01, last_step=6000)
     sim = R.solve(p)
-    assert sim.df["shift"][-1] == pytest.approx(O.ground_energy(O.real1d(6, 6, 6.0)), abs=1e-8)
+    assert sim.df["shift"][-1] == pytest.approx(O.ground_energy(O.real1d(6, 6, 6.0)), abs=1e-7)
 
 
 def test_abort_on_dead_population():

@@ -114,7 +114,8 @@ typedef struct {
 int rimu_version(void);
 int rimu_last_error(char *buf, size_t len);
 
-/* Context: one device and one stream; stream may be NULL (the library creates one). */
+/* Context: one device and one stream; stream NULL means the CUDA default stream.  All work
+ * of the context is ordered on that stream. */
 int rimu_ctx_create(int device, void *stream, rimu_ctx **out);
 int rimu_ctx_destroy(rimu_ctx *ctx);
 int rimu_ctx_synchronize(rimu_ctx *ctx);

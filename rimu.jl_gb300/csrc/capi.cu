@@ -73,13 +73,10 @@ int rimu_ctx_create(int device, void *stream, rimu_ctx **out) {
   rimu_ctx *c = new rimu_ctx();
   c->device = device;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (stream) {
-    c->stream = (cudaStream_t)stream;
-  } else {
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete c; return rimu_cuda_check(e, "cudaStreamCreate"); }
-    c->own_stream = true;
-  }
+  // NULL selects the CUDA default stream, so the caller's default-stream work (for
+  // example a torch tensor initialised on it) is ordered with the library's kernels.
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
   *out = c;
   return RIMU_OK;
 }

@@ -250,7 +250,8 @@ __global__ void __launch_bounds__(SB) k_spawn(StepArgs a, int nb_total) {
   SpawnAcc acc{};
   for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
     const int r = gb >> a.nb_bits;
-    const uint32_t n = a.cnt_in[gb];
+    const uint32_t n0 = a.cnt_in[gb];
+    const uint32_t n = n0 < a.capv ? n0 : a.capv;
     const Rec *base = a.v_in + (size_t)gb * a.capv;
     for (uint32_t c0 = 0; c0 < n; c0 += SB) {
       uint32_t e = c0 + tid;
@@ -293,12 +294,20 @@ __global__ void __launch_bounds__(SB) k_spawn(StepArgs a, int nb_total) {
           }
         }
         uint64_t work = noff == 0 ? 0 : (exact ? (uint64_t)noff : natt);
+        if (work > (1ull << 36)) {       // more attempts than any walker list can hold
+          atomicOr(&a.stats[r].flags, (unsigned)FLAG_VALUE_OVERFLOW);
+          work = 0;
+        }
         acc.attempts += noff == 0 ? 0 : (long long)work;
         if (work > (uint64_t)HEAVY_LIMIT) {
           uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
           uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
           for (uint64_t k = 0; k < nch; ++k) {
-            if (idx + k < a.heavy_cap) {
+            if (idx + k >= a.heavy_cap) {
+              atomicOr(&a.stats[r].flags, (unsigned)FLAG_HEAVY_OVERFLOW);
+              break;
+            }
+            {
               HeavyChunk ch;
               ch.key = key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
               ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
@@ -306,8 +315,6 @@ __global__ void __launch_bounds__(SB) k_spawn(StepArgs a, int nb_total) {
               ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
               ch.rep = (uint32_t)r; ch.pad = 0;
               a.heavy[idx + k] = ch;
-            } else {
-              atomicOr(&a.stats[r].flags, (unsigned)FLAG_HEAVY_OVERFLOW);
             }
           }
           work = 0;
@@ -359,6 +366,11 @@ __global__ void __launch_bounds__(SB) k_spawn_heavy(StepArgs a) {
   SpawnAcc acc{};
   for (uint32_t ci = blockIdx.x; ci < nch; ci += gridDim.x) {
     HeavyChunk ch = a.heavy[ci];
+    if (ch.cnt > (uint32_t)HEAVY_CHUNK || ch.rep >= (uint32_t)a.nrep) {
+      if (threadIdx.x == 0) atomicOr(&a.stats[0].flags, (unsigned)FLAG_TABLE);
+      ch.cnt = 0;
+      ch.rep = 0;
+    }
     for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x) {
       spawn_item<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact, ch.j0 + t,
                               acc);
@@ -382,13 +394,19 @@ __device__ __forceinline__ double from_ordered(uint64_t o) {
 }
 
 // Sum of the spawn list starting at `head` in increasing order of value, after `first`.
+// Lists hold at most `ns` entries; a longer walk means a corrupted list and is cut short
+// (the caller's flag check reports it).
 __device__ double canonical_sum(bool have, double first, int head, const uint64_t *sval,
-                                const int *snext) {
+                                const int *snext, int ns, bool *bad) {
   double sum = first;
   constexpr int K = 16;
   uint64_t ob[K];
   int n = 0, idx = head;
-  while (idx >= 0 && n < K) { ob[n++] = ordered_bits(bitsd(sval[idx])); idx = snext[idx]; }
+  while (idx >= 0 && n < K) {
+    if (idx >= ns) { *bad = true; return sum; }
+    ob[n++] = ordered_bits(bitsd(sval[idx]));
+    idx = snext[idx];
+  }
   if (idx < 0) {
     for (int i = 1; i < n; ++i) {
       uint64_t v = ob[i];
@@ -406,21 +424,34 @@ __device__ double canonical_sum(bool have, double first, int head, const uint64_
   // long list: repeated minimum (ties of equal value are indistinguishable)
   uint64_t last = 0;
   bool any_last = false;
-  for (;;) {
+  for (int round = 0; round <= ns; ++round) {
     uint64_t best = ~0ull;
-    int cnt = 0;
+    int cnt = 0, steps = 0;
     for (int i = head; i >= 0; i = snext[i]) {
+      if (i >= ns || ++steps > ns) { *bad = true; return sum; }
       uint64_t o = ordered_bits(bitsd(sval[i]));
       if (any_last && o <= last) continue;
       if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
     }
-    if (cnt == 0) break;
+    if (cnt == 0) return sum;
     double v = from_ordered(best);
     for (int c = 0; c < cnt; ++c) { sum = have ? sum + v : v; have = true; }
     last = best;
     any_last = true;
   }
+  *bad = true;
   return sum;
+}
+
+__device__ __forceinline__ int64_t list_sum_int(int head, const uint64_t *sval, const int *snext,
+                                                int ns, bool *bad) {
+  int64_t tot = 0;
+  int steps = 0;
+  for (int i = head; i >= 0; i = snext[i]) {
+    if (i >= ns || ++steps > ns) { *bad = true; break; }
+    tot += (int64_t)sval[i];
+  }
+  return tot;
 }
 
 __device__ __forceinline__ int table_lookup(uint64_t key, const uint64_t *tkey, uint32_t T) {
@@ -497,7 +528,9 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
     const uint32_t rep = a.replica_base + (uint32_t)r;
     const uint32_t nsp = a.scount[gb];
     const uint32_t ns = nsp < caps ? nsp : caps;
-    const uint32_t nv = a.cnt_in[gb];
+    const uint32_t nv0 = a.cnt_in[gb];
+    const uint32_t nv = nv0 < a.capv ? nv0 : a.capv;
+    bool bad = false;
     for (uint32_t i = tid; i < T; i += AB) { tkey[i] = EMPTY_KEY; thead[i] = -1; }
     if (tid == 0) s_out = 0;
     const Rec *sp = a.spawn + (size_t)gb * caps;
@@ -542,8 +575,7 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
         if (res > v) acc.clones += res - v;
         else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
         else acc.deaths += (res - v) < 0 ? v - res : res - v;
-        int64_t tot = res;
-        for (int i = head; i >= 0; i = snext[i]) tot += (int64_t)sval[i];
+        const int64_t tot = res + list_sum_int(head, sval, snext, (int)ns, &bad);
         finalize_entry<STYLE>(a, r, gb, key, 0.0, tot, &s_out, acc);
       } else {
         const double v = bitsd(rec.val);
@@ -552,7 +584,8 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
           U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
           res = project_threshold(res, a.proj_threshold, u53_of(rr));
         }
-        const double tot = head >= 0 ? canonical_sum(res != 0.0, res, head, sval, snext) : res;
+        const double tot =
+            head >= 0 ? canonical_sum(res != 0.0, res, head, sval, snext, (int)ns, &bad) : res;
         finalize_entry<STYLE>(a, r, gb, key, tot, 0, &s_out, acc);
       }
     }
@@ -563,14 +596,14 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
       const int head = thead[s];
       if (key == EMPTY_KEY || head < 0) continue;
       if (STYLE == STYLE_INTEGER) {
-        int64_t tot = 0;
-        for (int i = head; i >= 0; i = snext[i]) tot += (int64_t)sval[i];
+        const int64_t tot = list_sum_int(head, sval, snext, (int)ns, &bad);
         finalize_entry<STYLE>(a, r, gb, key, 0.0, tot, &s_out, acc);
       } else {
-        const double tot = canonical_sum(false, 0.0, head, sval, snext);
+        const double tot = canonical_sum(false, 0.0, head, sval, snext, (int)ns, &bad);
         finalize_entry<STYLE>(a, r, gb, key, tot, 0, &s_out, acc);
       }
     }
+    if (bad) atomicOr(&a.stats[r].flags, (unsigned)FLAG_TABLE);
     __syncthreads();
     if (tid == 0) {
       uint32_t no = s_out;

@@ -133,6 +133,7 @@ class Context:
         lib = load()
         h = C.c_void_p()
         check(lib.rimu_ctx_create(device, C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.stream = stream or 0
         self.handle = h
         self.device = device
         self._lib = lib

@@ -719,6 +719,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.rel_threshold = p->rel_spawning_threshold; a.abs_threshold = p->abs_spawning_threshold;
     a.seed = p->seed; a.step = (uint32_t)p->step; a.replica_base = p->replica;
     a.nrep = 1; a.nb_bits = nb_bits;
+    a.capv_in = source->capv;
     a.capv = capv; a.caps = caps;
     uint32_t T = 64;
     while (T < 2 * caps) T <<= 1;

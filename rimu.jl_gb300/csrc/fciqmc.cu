@@ -251,8 +251,8 @@ __global__ void __launch_bounds__(SB) k_spawn(StepArgs a, int nb_total) {
   for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
     const int r = gb >> a.nb_bits;
     const uint32_t n0 = a.cnt_in[gb];
-    const uint32_t n = n0 < a.capv ? n0 : a.capv;
-    const Rec *base = a.v_in + (size_t)gb * a.capv;
+    const uint32_t n = n0 < a.capv_in ? n0 : a.capv_in;
+    const Rec *base = a.v_in + (size_t)gb * a.capv_in;
     for (uint32_t c0 = 0; c0 < n; c0 += SB) {
       uint32_t e = c0 + tid;
       uint32_t w = 0;
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
     const uint32_t nsp = a.scount[gb];
     const uint32_t ns = nsp < caps ? nsp : caps;
     const uint32_t nv0 = a.cnt_in[gb];
-    const uint32_t nv = nv0 < a.capv ? nv0 : a.capv;
+    const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
     bool bad = false;
     for (uint32_t i = tid; i < T; i += AB) { tkey[i] = EMPTY_KEY; thead[i] = -1; }
     if (tid == 0) s_out = 0;
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
     }
     __syncthreads();
     // source walkers: diagonal step + spawns on the same address
-    const Rec *vb = a.v_in + (size_t)gb * a.capv;
+    const Rec *vb = a.v_in + (size_t)gb * a.capv_in;
     for (uint32_t e = tid; e < nv; e += AB) {
       Rec rec = vb[e];
       const uint64_t key = rec.key;

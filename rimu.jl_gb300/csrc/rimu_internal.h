@@ -57,7 +57,8 @@ struct StepArgs {
   uint32_t replica_base;
   int nrep;
   int nb_bits;
-  uint32_t capv, caps, tsize;
+  uint32_t capv_in;           // slab capacity of the source list
+  uint32_t capv, caps, tsize; // target slab, spawn slab, hash table size
   const Rec *v_in;
   const uint32_t *cnt_in;
   Rec *v_out;

@@ -1,0 +1,444 @@
+#!/usr/bin/env python
+"""FCIQMC walker-steps/s on one GB300 (plus matrix-free H*v nonzeros/s).
+
+Workload (default): the large plain FCIQMC configuration -- HubbardReal1D, periodic, M = N = 20
+(BoseFS in 39 bits of one 64-bit word), u = 4, t = 1, IsDynamicSemistochastic with threshold
+1.0 (late ThresholdCompression), target walker norm 1e8, dt = 1e-3, DoubleLogUpdate, seed
+0x5EED.  The population is grown from the unit-filling start address (untimed preparation),
+then W warm-up steps and K timed steps are run through rimu_apply_operator.
+
+A "step" is one projector step of the whole walker list (spawn, annihilation, compression,
+norm).  value = sum over timed steps of the walker number (1-norm) / device time.  The walker
+list (~1e8 walkers, 16-byte records, > 1 GB) is far larger than L2, so no L2 flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "rimu.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "FCIQMC walker-steps/s & H·v nnz/s on 1 GB300; batched/adjoint vs plain, same err"
+UNIT = "walker-steps/s"
+WORKLOAD = "HubbardReal1D M=N=20 u=4 t=1, IsDynamicSemistochastic(threshold=1), target norm 1e8, dt=1e-3"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, backend):
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+        return dist
+    return None
+
+
+# --------------------------------------------------------------------------------------------
+# CPU baseline: the oracle step (single thread per process) on a bounded sample
+# --------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    keys, vals, shift, seconds, seed = args
+    import numpy as np
+    import oracle as O
+    m = O.real1d(20, 20, 4.0, 1.0)
+    norm0 = float(np.abs(vals).sum())
+    t0 = time.time()
+    steps = 0
+    walkers = 0.0
+    k, v = keys, vals
+    while time.time() - t0 < seconds:
+        p = O.StepParams(O.STYLE_DSS, dt=1e-3, shift=shift, seed=seed, step=steps + 1, compression=1.0)
+        k2, v2, st = O.step(m, p, k, v)
+        walkers += st["norm"]
+        steps += 1
+        # keep the sample size bounded: restart from the sample
+        k, v = (k2, v2) if st["norm"] < 2 * norm0 else (keys, vals)
+    return walkers, time.time() - t0, steps
+
+
+def cpu_baseline(keys, vals, shift, seconds, procs):
+    import numpy as np
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    jobs = [(keys, vals, shift, seconds, 1000 + i) for i in range(procs)]
+    if procs == 1:
+        res = [_cpu_worker(jobs[0])]
+    else:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    walkers = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return walkers / wall, sum(r[2] for r in res)
+
+
+def sample_state(keys, vals, target_norm, rng):
+    """A bounded random sample of the walker list with about target_norm walkers."""
+    import numpy as np
+    norm = float(np.abs(vals).sum())
+    frac = min(1.0, target_norm / max(norm, 1.0))
+    idx = np.nonzero(rng.random(len(keys)) < frac)[0]
+    return np.ascontiguousarray(keys[idx]), np.ascontiguousarray(vals[idx])
+
+
+# --------------------------------------------------------------------------------------------
+# Our arm
+# --------------------------------------------------------------------------------------------
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    dist = dist_init(ws, "nccl" if ws > 1 else None)
+    torch.cuda.set_device(local)
+    if rank == 0:
+        from rimugpu import _build
+        _build.build()
+    if dist:
+        dist.barrier()
+    import rimugpu as R
+
+    target = args.target
+    addr = R.near_uniform(R.BoseFS, 20, 20)
+    H = R.HubbardReal1D(addr, u=4.0, t=1.0)
+    style = R.IsDynamicSemistochastic(threshold=1.0)
+    dt = 1e-3
+    p = R.ProjectorMonteCarloProblem(H, style=style, time_step=dt, target_walkers=target,
+                                     last_step=10 ** 9, random_seed=0x5EED + rank,
+                                     max_length=int(2 * target + 100))
+    sim = R.init(p)
+    s = sim.states[0]
+    t_prep = time.time()
+    prep = 0
+    while prep < args.max_prep:
+        sim.step_()
+        prep += 1
+        if s.wm.last_stats["norm"] >= 0.9 * target and prep >= 50:
+            break
+    for _ in range(args.warmup):
+        sim.step_()
+    torch.cuda.synchronize()
+    t_prep = time.time() - t_prep
+    s.wm.set_timing(True)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    norms = []
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            sim.step_()
+            norms.append(s.wm.last_stats["norm"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    tim = s.wm.timing()
+    lens = list(sim.report.data["len"][-args.steps:])
+    walker_steps = float(sum(norms))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        w = torch.tensor([walker_steps], dtype=torch.float64, device="cuda")
+        dist.all_reduce(w)
+        walker_steps = float(w.item())
+    value = walker_steps / (ms / 1e3)
+
+    # ---- roofline of spawn + annihilation (the hot path) ----
+    peak, peak_kind = peaks()
+    k_ms = tim["spawn_ms"] + tim["heavy_ms"] + tim["annihilate_ms"]
+    k_bytes = tim["spawn_bytes"] + tim["annihilate_bytes"]
+    steps_t = max(tim["steps"], 1)
+    achieved = k_bytes / (k_ms / 1e3) / 1e9 if k_ms > 0 else 0.0
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": args.traffic,
+                "peak_source": peak_kind,
+                "kernel": "k_spawn + k_spawn_heavy + k_annihilate (one step)",
+                "bytes_per_step": k_bytes / steps_t, "ms_per_step": k_ms / steps_t,
+                "spawn": {"ms": tim["spawn_ms"] / steps_t,
+                          "gbs": tim["spawn_bytes"] / (tim["spawn_ms"] / 1e3) / 1e9 if tim["spawn_ms"] else 0},
+                "annihilate": {"ms": tim["annihilate_ms"] / steps_t,
+                               "gbs": tim["annihilate_bytes"] / (tim["annihilate_ms"] / 1e3) / 1e9 if tim["annihilate_ms"] else 0},
+                "heavy_ms": tim["heavy_ms"] / steps_t}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        keys, vals = s.v.download()
+        n = len(keys)
+        hk = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        hv = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        hk[:] = keys
+        hv[:] = vals
+        ok = torch.empty(max(n * 2, 1), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        ov = torch.empty(max(n * 2, 1), dtype=torch.float64, pin_memory=True).numpy()
+        sp = s.shift_parameters
+        shift0, pnorm0 = sp.shift, sp.pnorm
+        torch.cuda.synchronize()
+        t0 = time.time()
+        v = R.GPUDVec(style=style, address_type=addr, capacity=n)
+        v.upload(hk, hv)
+        pv = v.similar()
+        wm = R.GPUWorkingMemory(0x5EED + 77)
+        e2e_norm = 0.0
+        S, pn = shift0, pnorm0
+        strat = p.shift_strategy
+        from rimugpu.problem import DefaultShiftParameters
+        spp = DefaultShiftParameters(S, pn, dt)
+        for k in range(args.steps):
+            R.apply_operator(wm, pv, v, R.FirstOrderTransitionOperator(H, spp.shift, dt), step=10 ** 6 + k)
+            v, pv = pv, v
+            st = wm.last_stats
+            e2e_norm += st["norm"]
+            strat.update(spp, st["norm"])
+        got = __import__("ctypes").c_int64()
+        import ctypes as C
+        from rimugpu import _lib
+        _lib.check(_lib.load().rimu_vec_download(v.handle, ok.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                  ov.ctypes.data_as(C.c_void_p), len(ok), C.byref(got)))
+        torch.cuda.synchronize()
+        wall = time.time() - t0
+        from rimugpu._lib import StepParams, StepStats
+        e2e = {"value": e2e_norm / wall, "unit": UNIT,
+               "h2d_bytes_per_step": int((16 * n) / args.steps + C.sizeof(StepParams) + 8),
+               "d2h_bytes_per_step": int((16 * got.value) / args.steps + 136 + 4 * 2),
+               "how": "upload of the walker list from pinned host memory, K steps through "
+                      "rimu_apply_operator (parameters in, statistics out every step), download "
+                      "of the final list to pinned host memory; host wall clock"}
+
+    # ---- matrix-free H*v on the full basis (M = N = 14, D = 20 058 300) ----
+    hv_res = None
+    if rank == 0 and not args.no_hv:
+        hv_res = bench_hv(R, torch, peak)
+
+    # ---- CPU baseline (oracle port) on a bounded sample ----
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        import numpy as np
+        keys, vals = s.v.download()
+        smp_k, smp_v = sample_state(keys, vals, args.cpu_sample, np.random.default_rng(1))
+        import oracle
+        oracle.build()
+        thr, nsteps = cpu_baseline(smp_k, smp_v, s.shift_parameters.shift, args.cpu_seconds, 1)
+        cpu = {"value": thr, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{len(smp_k)} walkers (norm {float(np.abs(smp_v).sum()):.3g}) sampled from the "
+                         f"steady-state list; {nsteps} oracle steps in {args.cpu_seconds:.0f} s, one thread"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "target_walkers": target,
+                       "walkers_per_step": walker_steps / args.steps / ws,
+                       "entries_per_step": float(np.mean(lens)) if lens else None,
+                       "prep_steps": prep, "prep_seconds": round(t_prep, 2),
+                       "l2": "inputs larger than L2 (walker list > 1 GB), no flush",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "gpu_launches": 4 * args.steps,
+            "roofline": roofline,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "hv": hv_res,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def bench_hv(R, torch, peak):
+    """H*v nonzeros/s on HubbardReal1D M=N=14 (D = 20 058 300), forward and adjoint."""
+    h = R.HubbardReal1D(R.BoseFS([1] * 14), u=4.0, t=1.0)
+    op = R.BasisOperator(h)
+    D = op.dim
+    nnz_off = 2 * 14 * 9657700          # 2 M C(26,13): offdiagonal nonzeros of HubbardReal1D(14,14)
+    nnz = D + nnz_off
+    g = torch.Generator(device="cuda").manual_seed(3)
+    v = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+    v /= torch.linalg.norm(v)
+    gw = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+    w = torch.empty_like(v)
+    for _ in range(3):
+        op(v, out=w)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        op(v, out=w)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    for _ in range(2):
+        op.adjoint(v, gw)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(3):
+        op.adjoint(v, gw)
+    torch.cuda.synchronize()
+    adj_ms = (time.time() - t0) / 3 * 1e3
+    bytes_fwd = 8 * D * 2 + 8 * nnz_off
+    return {"workload": "HubbardReal1D M=N=14 full basis, D=20058300", "value": nnz / (ms / 1e3),
+            "unit": "nnz/s", "ms": ms, "nnz": nnz,
+            "achieved_gbs": bytes_fwd / (ms / 1e3) / 1e9, "frac_hbm": bytes_fwd / (ms / 1e3) / 1e9 / peak,
+            "fp64_fma_per_s": nnz / (ms / 1e3),
+            "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / ms}
+
+
+# --------------------------------------------------------------------------------------------
+# Reference arm: the CPU restatement of the reference step, all host cores
+# --------------------------------------------------------------------------------------------
+def run_reference(args, ws, rank, local):
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle as O
+    O.build()
+    # bounded sample: a population grown with the oracle itself from the start address
+    m = O.real1d(20, 20, 4.0, 1.0)
+    k0 = O.bose_key([1] * 20)
+    keys, vals = np.array([k0], dtype=np.uint64), np.array([10.0])
+    S, pn = 0.0, 10.0
+    target = args.cpu_sample
+    step = 0
+    while float(np.abs(vals).sum()) < 0.9 * target and step < 5000:
+        step += 1
+        keys, vals, st = O.step(m, O.StepParams(O.STYLE_DSS, dt=1e-3, shift=S, seed=0x5EED, step=step,
+                                                  compression=1.0), keys, vals)
+        tn = st["norm"]
+        S -= 0.08 ** 2 / 4 / 1e-3 * math.log(tn / target) + 0.08 / 1e-3 * math.log(tn / pn)
+        pn = tn
+    procs = os.cpu_count() or 1
+    vals_per_step = []
+    for _ in range(args.warmup):
+        pass
+    per = max(args.cpu_seconds / max(args.steps, 1), 1.0)
+    t_all = time.time()
+    for _ in range(args.steps):
+        thr, _ = cpu_baseline(keys, vals, S, per, procs)
+        vals_per_step.append(thr)
+    value = float(np.mean(vals_per_step))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD + " (bounded sample)", "target_walkers": args.target},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": f"{len(keys)} walkers (norm {float(np.abs(vals).sum()):.3g}) grown by "
+                                       f"the oracle from the start address; {procs} processes stepping "
+                                       f"independent copies, {per:.1f} s per step sample"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Julia is not installed; this is the C restatement of the reference step (oracle/)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--target", type=float, default=1e8)
+    ap.add_argument("--max-prep", type=int, default=4000)
+    ap.add_argument("--cpu-sample", type=float, default=2e4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--traffic", type=float, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-hv", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

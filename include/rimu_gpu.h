@@ -160,6 +160,15 @@ int rimu_wm_destroy(rimu_wm *wm);
 int rimu_wm_set_projector(rimu_wm *wm, const uint64_t *keys, const double *pvals,
                           const double *hpvals, int n);
 
+/* Per-kernel timing of the steps run with this working memory (CUDA events on the context
+ * stream; the reference times steps with its Timer post-step strategy and communicator
+ * reports, poststepstrategy.jl:195, communicators.jl:580-603).  rimu_wm_set_timing resets
+ * the accumulators.  rimu_wm_timing fills out7 with: milliseconds in the spawn, heavy-spawn
+ * and annihilation kernels, the number of timed steps, the algorithmic bytes of the spawn
+ * and annihilation kernels (16-byte records read and written), and the number of steps. */
+int rimu_wm_set_timing(rimu_wm *wm, int enable);
+int rimu_wm_timing(rimu_wm *wm, double *out7);
+
 /* One projector step target = T(source), with stats: apply_operator!(wm, target, source,
  * op, boost) of src/Interfaces/dictvectors.jl:112-140 and pdworkingmemory.jl:297-309,
  * including the compression of compression.jl:28-42.  source is not modified. */

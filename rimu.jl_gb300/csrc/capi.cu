@@ -585,9 +585,25 @@ extern "C" int rimu_wm_destroy(rimu_wm *w) {
   dfree(ctx, w->proj_keys); dfree(ctx, w->proj_v); dfree(ctx, w->proj_h);
   dfree(ctx, w->proj_out_v); dfree(ctx, w->proj_out_h);
   cudaStreamSynchronize(ctx->stream);
+  for (int i = 0; i < 4; ++i) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
   if (w->h_stats) cudaFreeHost(w->h_stats);
   if (w->h_proj_out) cudaFreeHost(w->h_proj_out);
   delete w;
+  return RIMU_OK;
+}
+
+extern "C" int rimu_wm_set_timing(rimu_wm *w, int enable) {
+  if (!w) return bad("rimu_wm_set_timing: NULL working memory");
+  w->timing = enable != 0;
+  for (int i = 0; i < 4; ++i) w->t_ms[i] = 0;
+  for (int i = 0; i < 3; ++i) w->bytes[i] = 0;
+  return RIMU_OK;
+}
+
+extern "C" int rimu_wm_timing(rimu_wm *w, double *out7) {
+  if (!w || !out7) return bad("rimu_wm_timing: NULL argument");
+  for (int i = 0; i < 4; ++i) out7[i] = w->t_ms[i];
+  for (int i = 0; i < 3; ++i) out7[4 + i] = w->bytes[i];
   return RIMU_OK;
 }
 
@@ -734,7 +750,10 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.nproj = w->nproj;
     a.proj_keys = w->proj_keys; a.proj_v = w->proj_v; a.proj_h = w->proj_h;
     a.proj_out_v = w->proj_out_v; a.proj_out_h = w->proj_out_h;
-    if ((rc = rimu_launch_step(ctx, a, (int)nb))) return rc;
+    if (w->timing && !w->ev[0]) {
+      for (int i = 0; i < 4; ++i) RIMU_CUDA(cudaEventCreate(&w->ev[i]));
+    }
+    if ((rc = rimu_launch_step(ctx, a, (int)nb, w->timing ? w->ev : nullptr))) return rc;
     if ((rc = d2h(ctx, w->h_stats, w->stats, 1))) return rc;
     if (w->nproj) {
       if ((rc = d2h(ctx, w->h_proj_out, w->proj_out_v, w->nproj)) ||
@@ -760,6 +779,20 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     if (st.flags & FLAG_VALUE_OVERFLOW) { g_err = "rimu_apply_operator: walker value overflow"; return RIMU_ERR_OVERFLOW; }
   }
   const DevStats &st = *w->h_stats;
+  if (w->timing) {
+    float ms[3];
+    cudaEventElapsedTime(&ms[0], w->ev[0], w->ev[1]);
+    cudaEventElapsedTime(&ms[1], w->ev[1], w->ev[2]);
+    cudaEventElapsedTime(&ms[2], w->ev[2], w->ev[3]);
+    for (int i = 0; i < 3; ++i) w->t_ms[i] += ms[i];
+    w->t_ms[3] += 1;
+    // algorithmic bytes: spawn reads the source and writes the spawns; annihilation reads
+    // spawns and source and writes the target (16-byte records)
+    const double r = (double)sizeof(Rec);
+    w->bytes[0] += r * ((double)source->len + (double)st.spawn_records);
+    w->bytes[1] += r * ((double)st.spawn_records + (double)source->len + (double)st.len);
+    w->bytes[2] += 1;
+  }
   target->len = st.len;
   target->norm = fixed_to_double(U128{st.norm_lo, st.norm_hi});
   w->last_spawns = st.spawn_records;

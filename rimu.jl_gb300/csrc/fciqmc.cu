@@ -741,11 +741,14 @@ __global__ void k_offdiagonals(DevModel h, uint64_t key, int noff, uint64_t *key
 // Launchers
 // ------------------------------------------------------------------------------------------
 template <int KIND, int STYLE>
-static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total) {
+static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
   int grid = nb_total < (1 << 20) ? nb_total : (1 << 20);
+  if (ev) cudaEventRecord(ev[0], st);
   k_spawn<KIND, STYLE><<<grid, SB, 0, st>>>(a, nb_total);
+  if (ev) cudaEventRecord(ev[1], st);
   k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, SB, 0, st>>>(a);
+  if (ev) cudaEventRecord(ev[2], st);
   size_t smem = (size_t)a.tsize * 12 + (size_t)a.caps * 20;
   static bool attr_set = false;
   if (!attr_set) {
@@ -754,15 +757,16 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total) {
     attr_set = true;
   }
   k_annihilate<KIND, STYLE><<<grid, AB, smem, st>>>(a, nb_total);
+  if (ev) cudaEventRecord(ev[3], st);
   return rimu_cuda_check(cudaGetLastError(), "step kernels");
 }
 
 template <int KIND>
-static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total) {
+static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   switch (a.style) {
-    case STYLE_INTEGER: return launch_step_t<KIND, STYLE_INTEGER>(ctx, a, nb_total);
-    case STYLE_DETERMINISTIC: return launch_step_t<KIND, STYLE_DETERMINISTIC>(ctx, a, nb_total);
-    default: return launch_step_t<KIND, STYLE_DSS>(ctx, a, nb_total);
+    case STYLE_INTEGER: return launch_step_t<KIND, STYLE_INTEGER>(ctx, a, nb_total, ev);
+    case STYLE_DETERMINISTIC: return launch_step_t<KIND, STYLE_DETERMINISTIC>(ctx, a, nb_total, ev);
+    default: return launch_step_t<KIND, STYLE_DSS>(ctx, a, nb_total, ev);
   }
 }
 
@@ -770,11 +774,11 @@ static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total) {
 
 using namespace rimu;
 
-int rimu_launch_step(rimu_ctx *ctx, const StepArgs &a, int nb_total) {
+int rimu_launch_step(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   switch (a.h.kind) {
-    case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D>(ctx, a, nb_total);
-    case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE>(ctx, a, nb_total);
-    default: return launch_step_k<MODEL_MOM1D>(ctx, a, nb_total);
+    case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D>(ctx, a, nb_total, ev);
+    case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE>(ctx, a, nb_total, ev);
+    default: return launch_step_k<MODEL_MOM1D>(ctx, a, nb_total, ev);
   }
 }
 

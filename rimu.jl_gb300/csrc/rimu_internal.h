@@ -134,6 +134,11 @@ struct rimu_wm {
   uint64_t *proj_keys = nullptr;
   double *proj_v = nullptr, *proj_h = nullptr, *proj_out_v = nullptr, *proj_out_h = nullptr;
   double *h_proj_out = nullptr;         // pinned [2 * nproj]
+  // optional per-kernel timing (CUDA events on the context stream)
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_ms[4] = {0, 0, 0, 0};        // spawn, heavy, annihilate, steps timed
+  double bytes[3] = {0, 0, 0};          // algorithmic bytes of spawn, annihilate; steps
 };
 
 // error reporting shared by the translation units
@@ -142,7 +147,10 @@ int rimu_cuda_check(cudaError_t e, const char *what);
 #define RIMU_CUDA(call) do { int _rc = rimu_cuda_check((call), #call); if (_rc) return _rc; } while (0)
 
 // launchers (fciqmc.cu)
-int rimu_launch_step(rimu_ctx *ctx, const rimu::StepArgs &a, int nb_total);
+// ev (optional, 4 events): recorded before k_spawn, after k_spawn, after k_spawn_heavy and
+// after k_annihilate on the context stream.
+int rimu_launch_step(rimu_ctx *ctx, const rimu::StepArgs &a, int nb_total,
+                     cudaEvent_t *ev = nullptr);
 int rimu_launch_bucketize(rimu_ctx *ctx, const uint64_t *keys, const uint64_t *vals, int64_t n,
                           int nb_bits, uint32_t capv, rimu::Rec *recs, uint32_t *count,
                           unsigned int *flag);

@@ -195,6 +195,16 @@ class GPUWorkingMemory:
             hv.ctypes.data_as(C.POINTER(C.c_double)), len(keys)))
         self.projector_keys = keys if len(keys) else None
 
+    def set_timing(self, enable=True):
+        _lib.check(_lib.load().rimu_wm_set_timing(self.handle, int(enable)))
+
+    def timing(self) -> dict:
+        """Per-kernel milliseconds and algorithmic bytes accumulated since set_timing."""
+        out = np.zeros(7)
+        _lib.check(_lib.load().rimu_wm_timing(self.handle, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return dict(spawn_ms=out[0], heavy_ms=out[1], annihilate_ms=out[2], steps=int(out[3]),
+                    spawn_bytes=out[4], annihilate_bytes=out[5])
+
     def __del__(self):
         try:
             if self.handle:

@@ -56,15 +56,27 @@ def test_deterministic_power_iteration_converges_to_ground_state():
     H = R.HubbardReal1D(addr, u=6.0)
     # dt below 2 / (E_max - E0) so that 1 + dt (S - H) is a contraction on the excited states
     p = R.ProjectorMonteCarloProblem(H, style=R.IsDeterministic(), start_at={addr: 1.0},
-                                     target_walkers=10, time_step=0.01, last_step=6000)
+                                     target_walkers=10, time_step=0.01, last_step=6000,
+                                     max_length=10_000)
     sim = R.solve(p)
     assert sim.df["shift"][-1] == pytest.approx(O.ground_energy(O.real1d(6, 6, 6.0)), abs=1e-7)
 
 
+def test_abort_when_max_length_is_exceeded():
+    """len > max_length aborts the run (fciqmc.jl:176-179)."""
+    addr = R.BoseFS([1] * 6)
+    H = R.HubbardReal1D(addr, u=6.0)
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsDeterministic(), start_at={addr: 1.0},
+                                     target_walkers=10, time_step=0.01, last_step=100)
+    sim = R.solve(p)
+    assert sim.aborted and "max_length" in sim.message
+
+
 def test_abort_on_dead_population():
     H = R.HubbardReal1D(R.BoseFS([1] * 4), u=1.0)
-    p = R.ProjectorMonteCarloProblem(H, style=R.IsStochasticInteger(), shift=-50.0,
-                                     shift_strategy=R.DontUpdate(10 ** 9), time_step=0.1,
+    # diagonal factor 1 - dt (H - S) = 0.4: the single walker dies within a few steps
+    p = R.ProjectorMonteCarloProblem(H, style=R.IsStochasticInteger(), shift=-60.0,
+                                     shift_strategy=R.DontUpdate(10 ** 9), time_step=0.01,
                                      last_step=100, population=1, random_seed=3)
     sim = R.solve(p)
     assert sim.aborted and "dead" in sim.message

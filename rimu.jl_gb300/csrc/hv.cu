@@ -326,3 +326,175 @@ int rimu_launch_hv_adjoint(rimu_ctx *ctx, const DevModel &h, const uint64_t *bin
   k_reduce_partials<<<1, 32, 0, ctx->stream>>>(partial, grid, out2);
   return rimu_cuda_check(cudaGetLastError(), "k_hv_adjoint");
 }
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free adjoint.
+//
+// rimu_hv_basis_adjoint keeps its tables and its per-block partial sums in device memory that
+// the library allocates.  Some callers cannot let a library allocate: code that records work
+// into a CUDA graph, and applications whose device memory is owned by their own allocator or
+// budget (an inference server, a Julia/CUDA.jl program with a memory pool).  This entry point
+// does the same computation with all of its scratch in one file-scope device array of fixed
+// size, so that it calls no allocator at all.
+//
+// The array is global to the library: every GPU that loads the library holds it until the
+// process exits, every call shares it, and it keeps the last call's contents.  Calls whose
+// kernels overlap on the GPU (two streams, two host threads) race on it.
+// ---------------------------------------------------------------------------------------------
+namespace rimu {
+
+constexpr int NOALLOC_MAX_BLOCKS = 2048;        // grid blocks (one pair of partial sums each)
+constexpr int NOALLOC_MAX_BINOM = 64 * 64;      // (B + 1) * (N + 1) binomial coefficients
+constexpr int NOALLOC_MAX_DIAG = 4096;          // N (N - 1) + 1 interaction entries
+constexpr int NOALLOC_MAX_PROD = 4096;          // N (N + 1) + 1 occupation products
+
+struct NoAllocScratch {
+  double partial[2 * NOALLOC_MAX_BLOCKS];
+  double out2[2];
+  uint64_t binom[NOALLOC_MAX_BINOM];
+  double dtabH[NOALLOC_MAX_DIAG];
+  double hoff[NOALLOC_MAX_PROD];
+  double dhdt[NOALLOC_MAX_PROD];
+};
+
+// About 160 KB per device.
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+}  // namespace rimu
+
+namespace {
+constexpr int kMaxDevices = 64;
+rimu::NoAllocScratch *g_noalloc_ptr[kMaxDevices] = {nullptr};
+int g_noalloc_sms[kMaxDevices] = {0};
+// host staging of the tables (no heap): calls are not thread safe
+uint64_t g_h_binom[rimu::NOALLOC_MAX_BINOM];
+double g_h_diag[rimu::NOALLOC_MAX_DIAG];
+double g_h_hoff[rimu::NOALLOC_MAX_PROD];
+double g_h_dhdt[rimu::NOALLOC_MAX_PROD];
+}  // namespace
+
+extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const double *v,
+                                             const double *gw, double *gv, double *gu,
+                                             double *gt, int64_t dim, void *stream_handle) {
+  using namespace rimu;
+  if (!d || !v || !gw || !gv || !gu || !gt) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: NULL argument");
+    return RIMU_ERR_BADARG;
+  }
+  const bool realspace = d->kind == RIMU_MODEL_REALSPACE;
+  if (!(d->kind == RIMU_MODEL_REAL1D || (realspace && !d->fermion && !d->potential))) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: needs HubbardReal1D or bosonic HubbardRealSpace without trap");
+    return RIMU_ERR_BADARG;
+  }
+  const int N = d->n_particles, M = d->n_modes, B = N + M - 1;
+  if (N < 1 || M < 2 || B > 63) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: need N >= 1, M >= 2 and N + M - 1 <= 63");
+    return RIMU_ERR_BADARG;
+  }
+  const int nbinom = (B + 1) * (N + 1), ndiag = N * (N - 1) + 1, nprod = N * (N + 1) + 1;
+  if (nbinom > NOALLOC_MAX_BINOM || ndiag > NOALLOC_MAX_DIAG || nprod > NOALLOC_MAX_PROD) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: model exceeds the static scratch limits "
+                   "((N+M)(N+1) <= 4096, N(N+1)+1 <= 4096)");
+    return RIMU_ERR_BADARG;
+  }
+  int ndim = realspace ? d->ndim : 1;
+  if (ndim < 1 || ndim > 3) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: ndim must be 1..3");
+    return RIMU_ERR_BADARG;
+  }
+  // dimension C(B, N) must fit int64 and match dim
+  unsigned __int128 D = 1;
+  for (int i = 1; i <= N; ++i) {
+    D = D * (unsigned)(B - N + i) / (unsigned)i;
+    if (D > (unsigned __int128)INT64_MAX) {
+      rimu_set_error("rimu_hv_basis_adjoint_noalloc: basis dimension does not fit int64");
+      return RIMU_ERR_BADARG;
+    }
+  }
+  if ((int64_t)D != dim) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: dim does not match the basis dimension");
+    return RIMU_ERR_BADARG;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return rimu_cuda_check(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) {
+    rimu_set_error("rimu_hv_basis_adjoint_noalloc: device index out of range");
+    return RIMU_ERR_BADARG;
+  }
+  // Set-up, once per device with that device current: the host-side symbol is only a
+  // stand-in, the kernels need the device address of the array.
+  if (!g_noalloc_ptr[dev]) {
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return rimu_cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    e = cudaDeviceGetAttribute(&g_noalloc_sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return rimu_cuda_check(e, "cudaDeviceGetAttribute");
+    g_noalloc_ptr[dev] = static_cast<NoAllocScratch *>(ptr);
+  }
+  NoAllocScratch *s = g_noalloc_ptr[dev];
+  cudaStream_t st = (cudaStream_t)stream_handle;
+  // tables: the same values as the handle-based entry point builds
+  for (int p = 0; p <= B; ++p)
+    for (int i = 0; i <= N; ++i) {
+      unsigned __int128 c = 1;
+      if (i > p) c = 0;
+      else for (int k = 1; k <= i; ++k) c = c * (unsigned)(p - i + k) / (unsigned)k;
+      g_h_binom[p * (N + 1) + i] = c > (unsigned __int128)UINT64_MAX ? ~0ull : (uint64_t)c;
+    }
+  for (int I = 0; I < ndiag; ++I) g_h_diag[I] = d->u * (double)I / 2;
+  for (int p = 0; p < nprod; ++p) {
+    double q = sqrt((double)p);
+    g_h_hoff[p] = -d->t * q;
+    g_h_dhdt[p] = -q;
+  }
+  struct { void *dst; const void *src; size_t n; } copies[] = {
+      {s->binom, g_h_binom, nbinom * sizeof(uint64_t)},
+      {s->dtabH, g_h_diag, ndiag * sizeof(double)},
+      {s->hoff, g_h_hoff, nprod * sizeof(double)},
+      {s->dhdt, g_h_dhdt, nprod * sizeof(double)}};
+  for (auto &c : copies) {
+    e = cudaMemcpyAsync(c.dst, c.src, c.n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return rimu_cuda_check(e, "cudaMemcpyAsync (tables)");
+  }
+  DevModel h{};
+  h.kind = d->kind; h.fermion = 0; h.N = N; h.M = M; h.nbits = B; h.u = d->u; h.t = d->t;
+  h.ndim = ndim;
+  for (int i = 0; i < 3; ++i) {
+    h.dims[i] = realspace ? (i < ndim ? d->dims[i] : 1) : (i == 0 ? M : 1);
+    h.periodic[i] = realspace ? (i < ndim ? d->periodic[i] : 1) : 1;
+  }
+  if (realspace) {
+    int prod = 1;
+    for (int i = 0; i < ndim; ++i) prod *= h.dims[i];
+    if (prod != M) {
+      rimu_set_error("rimu_hv_basis_adjoint_noalloc: geometry does not match n_modes");
+      return RIMU_ERR_BADARG;
+    }
+  }
+  h.hoff = s->hoff;
+  h.aoff = s->hoff;
+  h.aoff_len = nprod;
+  int64_t want = (dim + HB - 1) / HB;
+  int64_t cap = (int64_t)g_noalloc_sms[dev] * 8;
+  if (cap > NOALLOC_MAX_BLOCKS) cap = NOALLOC_MAX_BLOCKS;
+  int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);
+  size_t smem = (size_t)nbinom * 8;
+  if (d->kind == RIMU_MODEL_REAL1D)
+    k_hv_adjoint<MODEL_REAL1D><<<grid, HB, smem, st>>>(h, s->binom, nbinom, v, gw, gv, dim,
+                                                       s->dtabH, s->dhdt, s->partial);
+  else
+    k_hv_adjoint<MODEL_REALSPACE><<<grid, HB, smem, st>>>(h, s->binom, nbinom, v, gw, gv, dim,
+                                                          s->dtabH, s->dhdt, s->partial);
+  k_reduce_partials<<<1, 32, 0, st>>>(s->partial, grid, s->out2);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return rimu_cuda_check(e, "k_hv_adjoint (no-alloc)");
+  double out[2];
+  e = cudaMemcpyAsync(out, s->out2, sizeof(out), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return rimu_cuda_check(e, "cudaMemcpyAsync (gu, gt)");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return rimu_cuda_check(e, "cudaStreamSynchronize");
+  *gu = out[0];
+  *gt = out[1];
+  return RIMU_OK;
+}

@@ -27,6 +27,7 @@ EXPORTS = [
     "rimu_wm_create", "rimu_wm_destroy", "rimu_wm_set_projector", "rimu_wm_set_timing",
     "rimu_wm_timing", "rimu_apply_operator",
     "rimu_basis_dimension", "rimu_basis_keys", "rimu_hv_basis", "rimu_hv_basis_adjoint",
+    "rimu_hv_basis_adjoint_noalloc",
 ]
 
 
@@ -108,6 +109,8 @@ def load(build_if_missing: bool = True):
         "rimu_basis_keys": ([vp, C.c_int64, C.c_int64, u64p], C.c_int),
         "rimu_hv_basis": ([vp, vp, vp, C.c_int64], C.c_int),
         "rimu_hv_basis_adjoint": ([vp, vp, vp, vp, f64p, f64p, C.c_int64], C.c_int),
+        "rimu_hv_basis_adjoint_noalloc": ([P(ModelDesc), vp, vp, vp, f64p, f64p, C.c_int64, vp],
+                                          C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -1,0 +1,64 @@
+"""The allocation-free adjoint entry point, called through the C ABI.
+
+Callers that cannot allocate device memory -- work recorded into a CUDA graph, or programs
+whose GPU memory belongs to their own allocator or budget -- use
+rimu_hv_basis_adjoint_noalloc, which keeps its scratch in a fixed static device array instead
+of asking for memory.  It must give the results of the handle-based rimu_hv_basis_adjoint, on
+consecutive calls that reuse the same array.  This file is collected last on purpose.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _call_noalloc(lib, desc, v, gw, gv):
+    gu, gt = C.c_double(), C.c_double()
+    rc = lib.rimu_hv_basis_adjoint_noalloc(C.byref(desc), C.c_void_p(v.data_ptr()),
+                                           C.c_void_p(gw.data_ptr()), C.c_void_p(gv.data_ptr()),
+                                           C.byref(gu), C.byref(gt), v.numel(), None)
+    return rc, gu.value, gt.value
+
+
+@pytest.mark.parametrize("which", ["real1d", "realspace"])
+def test_noalloc_adjoint_matches_handle_entry_point_on_two_calls(which):
+    import torch
+    import rimugpu as R
+    from rimugpu import _lib
+    lib = _lib.load()
+    if which == "real1d":
+        h = R.HubbardReal1D(R.BoseFS([1] * 9), u=3.0, t=0.9)
+    else:
+        h = R.HubbardRealSpace(R.BoseFS([1, 0, 2, 1, 0, 1, 0, 1, 1]), R.PeriodicBoundaries(3, 3),
+                               u=[[2.0]], t=[1.1])
+    op = R.BasisOperator(h)
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    for call in range(2):
+        v = torch.randn(op.dim, dtype=torch.float64, device="cuda", generator=gen)
+        gw = torch.randn(op.dim, dtype=torch.float64, device="cuda", generator=gen)
+        gv_ref, gu_ref, gt_ref = op.adjoint(v, gw)
+        gv = torch.full_like(v, float("nan"))
+        rc, gu, gt = _call_noalloc(lib, h._desc(), v, gw, gv)
+        assert rc == 0, _lib.last_error()
+        torch.cuda.synchronize()
+        assert torch.allclose(gv, gv_ref, rtol=1e-12, atol=1e-12), call
+        assert gu == pytest.approx(gu_ref, rel=1e-12, abs=1e-12), call
+        assert gt == pytest.approx(gt_ref, rel=1e-12, abs=1e-12), call
+
+
+def test_noalloc_rejects_models_beyond_the_static_limit():
+    import torch
+    import rimugpu as R
+    from rimugpu import _lib
+    lib = _lib.load()
+    desc = R.HubbardReal1D(R.BoseFS([1] * 4), u=1.0)._desc()
+    desc.n_particles, desc.n_modes = 40, 30          # 69-bit addresses: beyond the tables
+    v = torch.zeros(4, dtype=torch.float64, device="cuda")
+    rc, _, _ = _call_noalloc(lib, desc, v, v, v.clone())
+    assert rc == _lib.RIMU_ERR_BADARG
+    assert "63" in _lib.last_error()
+    small = R.HubbardReal1D(R.BoseFS([1] * 4), u=1.0)._desc()   # dim 35, not 4
+    rc, _, _ = _call_noalloc(lib, small, v, v, v.clone())
+    assert rc == _lib.RIMU_ERR_BADARG and "dim" in _lib.last_error()

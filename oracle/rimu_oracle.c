@@ -496,10 +496,21 @@ int o_step(const o_model *h, const o_params *p,
     double c;
     if (is_int && p->boost == 1.0) c = (val < 0 ? -1.0 : 1.0) * (double)noff;
     else c = (val * o_recip(natt)) * (double)noff;
+    /* Float walkers without on-the-fly projection need only the offdiagonal index per
+     * attempt: attempt j takes word j % 4 of Philox block j / 4.  Otherwise attempt j uses
+     * its own block: word 0 for the index, words 1-2 for the rounding. */
+    const int grouped = !is_int && p->proj_threshold == 0;
     for (int64_t j = 0; j < natt; ++j) {
       uint32_t r[4];
-      o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
-      int chosen = (int)(((uint64_t)r[0] * (uint64_t)noff) >> 32) + 1;
+      uint32_t word;
+      if (grouped) {
+        o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(j >> 2), r);
+        word = r[j & 3];
+      } else {
+        o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
+        word = r[0];
+      }
+      int chosen = (int)(((uint64_t)word * (uint64_t)noff) >> 32) + 1;
       uint64_t nk; double hv;
       o_get_offdiagonal(h, key, chosen, &nk, &hv);
       double y = c * o_t_off(p, hv);

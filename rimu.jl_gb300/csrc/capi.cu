@@ -208,13 +208,15 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     h.pot = m->d_pot;
   }
   {
-    // 1/n table (host IEEE division) for the spawn amplitude factor
+    // 1/n and (double)n tables (host IEEE arithmetic) for the spawn amplitude factor
     const int nr = 4096;
-    std::vector<double> rec(nr);
+    std::vector<double> rec(2 * nr);
     rec[0] = 0.0;
     for (int i = 1; i < nr; ++i) rec[i] = 1.0 / (double)i;
-    if ((rc = dalloc(ctx, &m->d_recip, nr)) || (rc = h2d(ctx, m->d_recip, rec.data(), nr))) goto fail;
+    for (int i = 0; i < nr; ++i) rec[nr + i] = (double)i;
+    if ((rc = dalloc(ctx, &m->d_recip, 2 * nr)) || (rc = h2d(ctx, m->d_recip, rec.data(), 2 * nr))) goto fail;
     h.recip = m->d_recip;
+    h.dint = m->d_recip + nr;
     h.recip_len = nr;
     // Hamiltonian offdiagonal magnitudes: -t sqrt(p) (HubbardReal1D.jl:59-62,
     // HubbardRealSpace.jl:336) or u/(2M) sqrt(p) (HubbardMom1D.jl:189-194)
@@ -682,34 +684,32 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   int rc;
   if (p->op == RIMU_OP_TRANSITION && (rc = ensure_aoff(m, p->dt))) return rc;
 
-  // capacity planning
+  // capacity planning: one warp per bucket, about 48 walkers and 96 spawns per bucket
   const int64_t L = std::max<int64_t>(source->len, 1);
   const double norm = std::max(source->norm, 1.0);
   int64_t S_est;
   if (w->last_spawns >= 0) S_est = (int64_t)(1.3 * (double)w->last_spawns) + 256;
   else if (p->style == RIMU_STYLE_DETERMINISTIC) S_est = L * (int64_t)m->max_offdiag + 256;
   else S_est = (int64_t)(norm * p->boost) + L * 4 + 256;
-  int need_bits = std::max(ceil_log2((uint64_t)((1.5 * (double)L + 64) / 256)),
-                           ceil_log2((uint64_t)(S_est / 768 + 1)));
+  int need_bits = std::max(ceil_log2((uint64_t)((1.5 * (double)L + 64) / 48)),
+                           ceil_log2((uint64_t)(S_est / 96 + 1)));
   int nb_bits = std::max(source->nb_bits, need_bits);
   uint32_t caps = 0, capv = 0;
   uint32_t heavy_cap = 0;
   int retries = 0;
   const int ndiag = m->ndiag;
+  const uint32_t kMaxCaps = 512;
   for (;;) {
-    if (nb_bits > 24) { g_err = "rimu_apply_operator: too many buckets needed"; return RIMU_ERR_OVERFLOW; }
+    if (nb_bits > 26) { g_err = "rimu_apply_operator: too many buckets needed"; return RIMU_ERR_OVERFLOW; }
     if (nb_bits != source->nb_bits) {
       if ((rc = vec_regrid(source, nb_bits, capv_for(source->len, nb_bits)))) return rc;
     }
     const uint64_t nb = 1ull << nb_bits;
     double mu_s = (double)S_est / (double)nb;
-    uint32_t want_caps = round_up((uint64_t)(1.5 * mu_s + 6.0 * std::sqrt(mu_s) + 64.0), 32);
-    if (want_caps > 4096) { nb_bits++; continue; }
-    caps = std::max(caps, want_caps);
-    if (caps > 4096) caps = 4096;
-    double mu_v = (1.5 * (double)L + 64) / (double)nb;
+    uint32_t want_caps = round_up((uint64_t)(mu_s + 6.0 * std::sqrt(mu_s) + 32.0), 32);
+    if (want_caps > kMaxCaps) { nb_bits++; continue; }
+    caps = std::min(kMaxCaps, std::max(caps, want_caps));
     capv = std::max(capv, std::max(source->capv, capv_for((int64_t)(1.5 * L + 64), nb_bits)));
-    (void)mu_v;
     uint64_t work_bound = (uint64_t)(norm * p->boost) + (uint64_t)L * (uint64_t)m->max_offdiag;
     uint64_t hc = work_bound / HEAVY_CHUNK + std::min<uint64_t>((uint64_t)L, work_bound / HEAVY_LIMIT + 1) + 64;
     heavy_cap = std::max<uint32_t>(heavy_cap, (uint32_t)std::min<uint64_t>(hc, 1u << 28));
@@ -733,13 +733,17 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.style = p->style; a.op = p->op; a.dt = p->dt;
     a.boost = p->boost; a.proj_threshold = p->proj_threshold; a.compression = p->compression;
     a.rel_threshold = p->rel_spawning_threshold; a.abs_threshold = p->abs_spawning_threshold;
+    a.has_proj = p->proj_threshold > 0;
+    a.comp_mode = p->compression > 0 ? (p->compression == 1.0 ? 1 : 2) : 0;
+    a.boost_one = p->boost == 1.0 && p->rel_spawning_threshold == 1.0;
+    a.has_abs_thr = std::isfinite(p->abs_spawning_threshold);
     a.seed = p->seed; a.step = (uint32_t)p->step; a.replica_base = p->replica;
     a.nrep = 1; a.nb_bits = nb_bits;
     a.capv_in = source->capv;
     a.capv = capv; a.caps = caps;
     uint32_t T = 64;
     while (T < 2 * caps) T <<= 1;
-    a.tsize = T;
+    a.tsize = T;            // largest per-bucket table; each bucket sizes its own from its spawns
     a.v_in = source->recs; a.cnt_in = source->count;
     a.v_out = target->recs; a.cnt_out = target->count;
     a.spawn = w->spawn; a.scount = w->scount;
@@ -767,7 +771,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     if (++retries > 10) { g_err = "rimu_apply_operator: capacities could not be grown enough"; return RIMU_ERR_OVERFLOW; }
     if (st.flags & FLAG_SPAWN_OVERFLOW) {
       S_est = std::max<int64_t>(2 * S_est, (int64_t)st.max_spawn_bucket * (int64_t)nb);
-      if (caps >= 2048) nb_bits++;
+      if (caps >= kMaxCaps) nb_bits++;
       caps = 0;
     }
     if (st.flags & FLAG_V_OVERFLOW) {

@@ -23,8 +23,6 @@
 
 namespace rimu {
 
-constexpr int SB = 256;   // spawn CTA
-constexpr int AB = 256;   // annihilation CTA
 
 // ------------------------------------------------------------------------------------------
 // Model dispatch
@@ -113,7 +111,7 @@ __device__ double model_diagonal(const DevModel &h, uint64_t key) {
 template <int KIND>
 __device__ __forceinline__ double op_diagonal(const StepArgs &a, int r, uint64_t key) {
   if (a.dtab) {
-    int I = a.h.fermion ? 0 : bose_interaction(key);
+    int I = a.h.fermion ? 0 : bose_interaction_fast(key);
     return a.dtab[(size_t)r * a.ndiag + I];
   }
   double d = model_diagonal<KIND>(a.h, key);
@@ -161,7 +159,7 @@ __device__ __forceinline__ void atomic_add_ll(long long *p, long long v) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Spawning
+// Spawning: one warp per bucket, no block barriers
 // ------------------------------------------------------------------------------------------
 struct SpawnAcc {
   U128 fx;           // sum |spawn| for float styles
@@ -169,6 +167,9 @@ struct SpawnAcc {
   long long records;
   long long attempts, exact_n, inexact_n;
 };
+
+constexpr int WARPS = 8;           // warps per CTA in the step kernels
+constexpr int G = 4;               // units (attempts or offdiagonals) per work item
 
 __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk, uint64_t vb,
                                            SpawnAcc &acc) {
@@ -182,41 +183,67 @@ __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk
   acc.records++;
 }
 
+template <int KIND>
+__device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key, int chosen) {
+  if (KIND == MODEL_REAL1D) return real1d_offdiag_fast(key, h.nbits, chosen);
+  return column_offdiag<KIND>(h, key, chosen);
+}
+
+// Units [j0, j1) of one column.  Exact columns deposit val * T_{new,key} for offdiagonals
+// j+1 (spawning.jl:174-182); sampled columns draw a uniform offdiagonal per attempt and
+// deposit c * T_{new,key} (spawning.jl:232-243).  With float walkers and no on-the-fly
+// projection an attempt needs 32 random bits, so one Philox block serves four attempts.
 template <int KIND, int STYLE>
-__device__ __forceinline__ void spawn_item(const StepArgs &a, int r, uint64_t key, uint64_t vb,
-                                           double c, int noff, int exact, uint32_t j,
-                                           SpawnAcc &acc) {
-  uint32_t rep = a.replica_base + (uint32_t)r;
+__device__ __forceinline__ void spawn_units(const StepArgs &a, int r, uint64_t key, uint64_t vb,
+                                            double c, int noff, int exact, uint32_t j0,
+                                            uint32_t j1, SpawnAcc &acc) {
+  const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
-    // Exact (spawning.jl:174-182): val * mat_elem for offdiagonal j+1
-    Offdiag od = column_offdiag<KIND>(a.h, key, (int)j + 1);
-    if (od.prod == 0) return;
-    double y = bitsd(vb) * op_offdiag(a, od);
-    if (STYLE == STYLE_DSS && a.proj_threshold > 0) {
-      U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
-      y = project_threshold(y, a.proj_threshold, u53_of(rr));
+    const double val = bitsd(vb);
+    for (uint32_t j = j0; j < j1; ++j) {
+      Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
+      if (od.prod == 0) continue;
+      double y = val * op_offdiag(a, od);
+      if (STYLE == STYLE_DSS && a.has_proj) {
+        U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
+        y = project_threshold(y, a.proj_threshold, u53_of(rr));
+      }
+      if (is_zero_d(y)) continue;
+      acc.fx = add128(acc.fx, fixed_of(abs_d(y)));
+      emit_spawn(a, r, od.key, dbits(y), acc);
     }
-    if (y == 0.0) return;
-    acc.fx = add128(acc.fx, fixed_of(fabs(y)));
-    emit_spawn(a, r, od.key, dbits(y), acc);
     return;
   }
-  // WithReplacement attempt j (spawning.jl:232-243): uniform offdiagonal, amplitude c * elem
-  U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
-  int chosen = (int)uniform_index(rr.x, (uint32_t)noff) + 1;
-  Offdiag od = column_offdiag<KIND>(a.h, key, chosen);
-  if (od.prod == 0) return;
-  double y = c * op_offdiag(a, od);
-  if (STYLE == STYLE_INTEGER) {
-    int64_t k = round_stochastic(y, u53_of(rr));
-    if (k == 0) return;
-    acc.spawns_i += k < 0 ? -k : k;
-    emit_spawn(a, r, od.key, (uint64_t)k, acc);
-  } else {
-    if (a.proj_threshold > 0) y = project_threshold(y, a.proj_threshold, u53_of(rr));
-    if (y == 0.0) return;
-    acc.fx = add128(acc.fx, fixed_of(fabs(y)));
-    emit_spawn(a, r, od.key, dbits(y), acc);
+  const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
+  U4 blk{0, 0, 0, 0};
+  uint32_t blk_id = 0xffffffffu;
+  for (uint32_t j = j0; j < j1; ++j) {
+    uint32_t word;
+    U4 rr;
+    if (grouped) {
+      if ((j >> 2) != blk_id) { blk_id = j >> 2; blk = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, blk_id); }
+      const uint32_t q = j & 3;
+      word = q == 0 ? blk.x : q == 1 ? blk.y : q == 2 ? blk.z : blk.w;
+      rr = blk;
+    } else {
+      rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
+      word = rr.x;
+    }
+    const int chosen = (int)uniform_index(word, (uint32_t)noff) + 1;
+    Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
+    if (od.prod == 0) continue;
+    double y = c * op_offdiag(a, od);
+    if (STYLE == STYLE_INTEGER) {
+      int64_t k = round_stochastic(y, u53_of(rr));
+      if (k == 0) continue;
+      acc.spawns_i += k < 0 ? -k : k;
+      emit_spawn(a, r, od.key, (uint64_t)k, acc);
+    } else {
+      if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
+      if (is_zero_d(y)) continue;
+      acc.fx = add128(acc.fx, fixed_of(abs_d(y)));
+      emit_spawn(a, r, od.key, dbits(y), acc);
+    }
   }
 }
 
@@ -236,131 +263,139 @@ __device__ __forceinline__ void flush_spawn_acc(const StepArgs &a, int r, SpawnA
   acc = SpawnAcc{};
 }
 
+__device__ __forceinline__ double dint_of(const DevModel &h, int n) {
+  return n < h.recip_len ? h.dint[n] : (double)n;
+}
+
+// Work of one column: units (offdiagonals if exact, attempts otherwise) and the spawn
+// coefficient c, without FP64 compares (DynamicSemistochastic, spawning.jl:364-378;
+// WithReplacement attempts, spawning.jl:234-235).
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(SB) k_spawn(StepArgs a, int nb_total) {
-  __shared__ uint64_t s_key[SB];
-  __shared__ uint64_t s_val[SB];
-  __shared__ double s_c[SB];
-  __shared__ int s_noff[SB];
-  __shared__ int s_exact[SB];
-  __shared__ uint32_t s_pref[SB];
-  __shared__ uint32_t s_warp[SB / 32];
-  __shared__ uint32_t s_tot;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+__device__ __forceinline__ uint64_t column_work(const StepArgs &a, uint64_t key, uint64_t vb,
+                                                int &noff, int &exact, double &c,
+                                                SpawnAcc &acc) {
+  noff = column_noff<KIND>(a.h, key);
+  exact = 0;
+  c = 0.0;
+  uint64_t natt = 0;
+  if (STYLE == STYLE_DETERMINISTIC) {
+    exact = 1;
+    acc.exact_n++;
+  } else if (STYLE == STYLE_DSS) {
+    const double val = bitsd(vb);
+    const double amount = a.boost_one ? abs_d(val) : a.boost * abs_d(val) * a.rel_threshold;
+    if (!a.has_abs_thr || a.abs_threshold >= (double)noff) exact = floor_abs(amount) >= (int64_t)noff;
+    else exact = amount >= a.abs_threshold;
+    if (exact) acc.exact_n++; else acc.inexact_n++;
+    if (!exact) {
+      natt = (uint64_t)floor_abs(a.boost_one ? val : abs_d(val) * a.boost);
+      if (natt < 1) natt = 1;
+      const double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
+      c = (natt == 1 ? val : val * rc) * dint_of(a.h, noff);
+    }
+  } else {  // IsStochasticInteger
+    const int64_t iv = (int64_t)vb;
+    const uint64_t av = (uint64_t)(iv < 0 ? -iv : iv);
+    if (a.boost_one) {
+      natt = av < 1 ? 1 : av;
+      const double dn = dint_of(a.h, noff);
+      c = iv < 0 ? bitsd(dbits(dn) ^ 0x8000000000000000ull) : dn;
+    } else {
+      natt = (uint64_t)floor_abs(i2d_exact(iv) * a.boost);
+      if (natt < 1) natt = 1;
+      const double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
+      c = (i2d_exact(iv) * rc) * dint_of(a.h, noff);
+    }
+  }
+  return noff == 0 ? 0 : (exact ? (uint64_t)noff : natt);
+}
+
+template <int KIND, int STYLE>
+__global__ void __launch_bounds__(WARPS * 32) k_spawn(StepArgs a, int nb_total) {
+  __shared__ uint64_t s_key[WARPS][32];
+  __shared__ uint64_t s_val[WARPS][32];
+  __shared__ double s_c[WARPS][32];
+  __shared__ uint32_t s_units[WARPS][32];
+  __shared__ uint32_t s_excl[WARPS][32];
+  __shared__ int s_noff[WARPS][32];
+  __shared__ int s_exact[WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   SpawnAcc acc{};
-  for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
+  int cur_r = -1;
+  for (int gb = blockIdx.x * WARPS + w; gb < nb_total; gb += gridDim.x * WARPS) {
     const int r = gb >> a.nb_bits;
+    if (r != cur_r) {
+      if (cur_r >= 0) flush_spawn_acc(a, cur_r, acc);
+      cur_r = r;
+    }
     const uint32_t n0 = a.cnt_in[gb];
     const uint32_t n = n0 < a.capv_in ? n0 : a.capv_in;
     const Rec *base = a.v_in + (size_t)gb * a.capv_in;
-    for (uint32_t c0 = 0; c0 < n; c0 += SB) {
-      uint32_t e = c0 + tid;
-      uint32_t w = 0;
+    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
+      const uint32_t e = c0 + lane;
+      uint32_t items = 0;
       if (e < n) {
-        Rec rec = base[e];
-        uint64_t key = rec.key;
-        int noff = column_noff<KIND>(a.h, key);
-        int exact = 0;
-        double c = 0.0;
-        uint64_t natt = 0;
-        if (STYLE == STYLE_DETERMINISTIC) {
-          exact = 1;
-          acc.exact_n++;
-        } else if (STYLE == STYLE_DSS) {
-          double val = bitsd(rec.val);
-          double thresh = a.abs_threshold < (double)noff ? a.abs_threshold : (double)noff;
-          double amount = (a.boost == 1.0 && a.rel_threshold == 1.0)
-                              ? fabs(val) : a.boost * fabs(val) * a.rel_threshold;
-          exact = amount >= thresh;
-          if (exact) acc.exact_n++; else acc.inexact_n++;
-          if (!exact) {
-            double bv = a.boost == 1.0 ? fabs(val) : fabs(val) * a.boost;
-            natt = (uint64_t)floor_abs(bv);
-            if (natt < 1) natt = 1;
-            double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
-            c = (natt == 1 ? val : val * rc) * (double)noff;
-          }
-        } else {  // IsStochasticInteger
-          int64_t iv = (int64_t)rec.val;
-          uint64_t av = (uint64_t)(iv < 0 ? -iv : iv);
-          if (a.boost == 1.0) {
-            natt = av < 1 ? 1 : av;
-            c = (iv < 0 ? -1.0 : 1.0) * (double)noff;
-          } else {
-            natt = (uint64_t)floor_abs((double)iv * a.boost);
-            if (natt < 1) natt = 1;
-            double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
-            c = ((double)iv * rc) * (double)noff;
-          }
-        }
-        uint64_t work = noff == 0 ? 0 : (exact ? (uint64_t)noff : natt);
+        const Rec rec = base[e];
+        int noff, exact;
+        double c;
+        uint64_t work = column_work<KIND, STYLE>(a, rec.key, rec.val, noff, exact, c, acc);
         if (work > (1ull << 36)) {       // more attempts than any walker list can hold
           atomicOr(&a.stats[r].flags, (unsigned)FLAG_VALUE_OVERFLOW);
           work = 0;
         }
-        acc.attempts += noff == 0 ? 0 : (long long)work;
+        acc.attempts += (long long)work;
         if (work > (uint64_t)HEAVY_LIMIT) {
-          uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
-          uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
+          const uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
+          const uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
           for (uint64_t k = 0; k < nch; ++k) {
             if (idx + k >= a.heavy_cap) {
               atomicOr(&a.stats[r].flags, (unsigned)FLAG_HEAVY_OVERFLOW);
               break;
             }
-            {
-              HeavyChunk ch;
-              ch.key = key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
-              ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
-              uint64_t rem = work - k * HEAVY_CHUNK;
-              ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
-              ch.rep = (uint32_t)r; ch.pad = 0;
-              a.heavy[idx + k] = ch;
-            }
+            HeavyChunk ch;
+            ch.key = rec.key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
+            ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
+            const uint64_t rem = work - k * HEAVY_CHUNK;
+            ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
+            ch.rep = (uint32_t)r; ch.pad = 0;
+            a.heavy[idx + k] = ch;
           }
           work = 0;
         }
-        w = (uint32_t)work;
-        s_key[tid] = key; s_val[tid] = rec.val; s_c[tid] = c;
-        s_noff[tid] = noff; s_exact[tid] = exact;
+        s_key[w][lane] = rec.key; s_val[w][lane] = rec.val; s_c[w][lane] = c;
+        s_noff[w][lane] = noff; s_exact[w][lane] = exact;
+        s_units[w][lane] = (uint32_t)work;
+        items = ((uint32_t)work + G - 1) / G;
       }
-      // block exclusive scan of w
-      uint32_t x = w;
+      // warp exclusive scan of the work items
+      uint32_t incl = items;
+#pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
       }
-      if (lane == 31) s_warp[wid] = x;
-      __syncthreads();
-      if (wid == 0) {
-        uint32_t t = lane < SB / 32 ? s_warp[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-          uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-          if (lane >= o) t += y;
-        }
-        if (lane < SB / 32) s_warp[lane] = t;
-        if (lane == SB / 32 - 1) s_tot = t;
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      s_excl[w][lane] = incl - items;
+      __syncwarp();
+      for (uint32_t it = lane; it < total; it += 32) {
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1)
+          if (s_excl[w][lo + step] <= it) lo += step;
+        const uint32_t j0 = (it - s_excl[w][lo]) * G;
+        const uint32_t ju = s_units[w][lo];
+        const uint32_t j1 = j0 + G < ju ? j0 + G : ju;
+        spawn_units<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo], s_noff[w][lo],
+                                 s_exact[w][lo], j0, j1, acc);
       }
-      __syncthreads();
-      s_pref[tid] = x - w + (wid ? s_warp[wid - 1] : 0);
-      __syncthreads();
-      const uint32_t W = s_tot;
-      for (uint32_t it = tid; it < W; it += SB) {
-        int lo = 0, hi = SB - 1;
-        while (lo < hi) {
-          int mid = (lo + hi + 1) >> 1;
-          if (s_pref[mid] <= it) lo = mid; else hi = mid - 1;
-        }
-        spawn_item<KIND, STYLE>(a, r, s_key[lo], s_val[lo], s_c[lo], s_noff[lo], s_exact[lo],
-                                it - s_pref[lo], acc);
-      }
-      __syncthreads();
+      __syncwarp();
     }
-    flush_spawn_acc(a, r, acc);
   }
+  if (cur_r >= 0) flush_spawn_acc(a, cur_r, acc);
 }
 
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(SB) k_spawn_heavy(StepArgs a) {
+__global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
   uint32_t nch = *a.heavy_count;
   if (nch > a.heavy_cap) nch = a.heavy_cap;
   SpawnAcc acc{};
@@ -371,9 +406,10 @@ __global__ void __launch_bounds__(SB) k_spawn_heavy(StepArgs a) {
       ch.cnt = 0;
       ch.rep = 0;
     }
-    for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x) {
-      spawn_item<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact, ch.j0 + t,
-                              acc);
+    for (uint32_t t = threadIdx.x * G; t < ch.cnt; t += blockDim.x * G) {
+      const uint32_t j1 = t + G < ch.cnt ? t + G : ch.cnt;
+      spawn_units<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact,
+                               ch.j0 + t, ch.j0 + j1, acc);
     }
     // attempts were counted when the chunk was created
     acc.attempts = 0;
@@ -382,7 +418,7 @@ __global__ void __launch_bounds__(SB) k_spawn_heavy(StepArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Annihilation
+// Annihilation: one warp per bucket
 // ------------------------------------------------------------------------------------------
 struct AnnAcc {
   U128 norm;
@@ -394,12 +430,11 @@ __device__ __forceinline__ double from_ordered(uint64_t o) {
 }
 
 // Sum of the spawn list starting at `head` in increasing order of value, after `first`.
-// Lists hold at most `ns` entries; a longer walk means a corrupted list and is cut short
-// (the caller's flag check reports it).
+// Lists hold at most `ns` entries; a longer walk means a corrupted list and is cut short.
 __device__ double canonical_sum(bool have, double first, int head, const uint64_t *sval,
                                 const int *snext, int ns, bool *bad) {
   double sum = first;
-  constexpr int K = 16;
+  constexpr int K = 8;
   uint64_t ob[K];
   int n = 0, idx = head;
   while (idx >= 0 && n < K) {
@@ -421,7 +456,6 @@ __device__ double canonical_sum(bool have, double first, int head, const uint64_
     }
     return sum;
   }
-  // long list: repeated minimum (ties of equal value are indistinguishable)
   uint64_t last = 0;
   bool any_last = false;
   for (int round = 0; round <= ns; ++round) {
@@ -465,173 +499,220 @@ __device__ __forceinline__ int table_lookup(uint64_t key, const uint64_t *tkey, 
   return -1;
 }
 
+// Final value of one address: threshold compression (compression.jl:18-42), statistics, the
+// ProjectedEnergy dot products.  Returns whether the address is kept and its value bits.
 template <int STYLE>
-__device__ __forceinline__ void finalize_entry(const StepArgs &a, int r, int gb, uint64_t key,
-                                               double fv, int64_t iv, uint32_t *s_out,
-                                               AnnAcc &acc) {
-  uint64_t vb;
+__device__ __forceinline__ bool finalize_entry(const StepArgs &a, int r, uint64_t key, double fv,
+                                               int64_t iv, uint64_t &vb, AnnAcc &acc) {
   double dv;
   if (STYLE == STYLE_INTEGER) {
-    if (iv == 0) return;
+    if (iv == 0) return false;
     acc.len_before++;
     vb = (uint64_t)iv;
-    dv = (double)iv;
+    const uint64_t mag = (uint64_t)(iv < 0 ? -iv : iv);
+    acc.norm = add128(acc.norm, U128{0, mag});
+    acc.len++;
+    if (a.nproj == 0) return true;
+    dv = i2d_exact(iv);
   } else {
-    if (fv == 0.0) return;
+    if (is_zero_d(fv)) return false;
     acc.len_before++;
-    if (a.compression > 0) {
-      double at = fabs(fv);
-      double prob = a.compression == 1.0 ? at : at / a.compression;
-      if (prob < 1) {
+    if (a.comp_mode != 0) {
+      bool small;
+      double prob;
+      if (a.comp_mode == 1) { small = abs_lt_one(fv); prob = abs_d(fv); }
+      else { prob = abs_d(fv) / a.compression; small = prob < 1; }
+      if (small) {
         U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, a.step, key, 0);
-        fv = bernoulli53(u53_of(rr), prob) ? (fv < 0 ? -a.compression : a.compression) : 0.0;
+        if (!bernoulli53(u53_of(rr), prob)) return false;
+        fv = signed_like(a.compression, fv);
       }
-      if (fv == 0.0) return;
     }
     vb = dbits(fv);
+    acc.norm = add128(acc.norm, fixed_of(abs_d(fv)));
+    acc.len++;
+    if (a.nproj == 0) return true;
     dv = fv;
   }
-  uint32_t pos = atomicAdd(s_out, 1u);
-  if (pos < a.capv) a.v_out[(size_t)gb * a.capv + pos] = Rec{key, vb};
-  acc.norm = add128(acc.norm, fixed_of(fabs(dv)));
-  acc.len++;
-  if (a.nproj > 0) {
-    const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
-    int lo = 0, hi = a.nproj - 1;
-    while (lo <= hi) {
-      int mid = (lo + hi) >> 1;
-      if (pk[mid] == key) {
-        size_t o = (size_t)r * a.nproj + mid;
-        a.proj_out_v[o] = a.proj_v[o] * dv;
-        a.proj_out_h[o] = a.proj_h[o] * dv;
-        break;
-      }
-      if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
+  const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
+  int lo = 0, hi = a.nproj - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    if (pk[mid] == key) {
+      const size_t o = (size_t)r * a.nproj + mid;
+      a.proj_out_v[o] = a.proj_v[o] * dv;
+      a.proj_out_h[o] = a.proj_h[o] * dv;
+      break;
     }
+    if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
   }
+  return true;
+}
+
+// Warp-synchronous append of the kept entries to the target slab of bucket gb.
+__device__ __forceinline__ void warp_emit(const StepArgs &a, int gb, bool keep, uint64_t key,
+                                          uint64_t vb, uint32_t &out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t m = __ballot_sync(0xffffffffu, keep);
+  const uint32_t pos = out + __popc(m & ((1u << lane) - 1));
+  if (keep && pos < a.capv) a.v_out[(size_t)gb * a.capv + pos] = Rec{key, vb};
+  out += __popc(m);
+}
+
+__device__ __forceinline__ void flush_ann_acc(const StepArgs &a, int r, AnnAcc &acc) {
+  U128 nfx = warp_sum128(acc.norm);
+  long long l = warp_sum(acc.len), lb = warp_sum(acc.len_before);
+  long long cl = warp_sum(acc.clones), de = warp_sum(acc.deaths), zo = warp_sum(acc.zombies);
+  if ((threadIdx.x & 31) == 0) {
+    DevStats &st = a.stats[r];
+    atomic_add128(&st.norm_lo, &st.norm_hi, nfx);
+    atomic_add_ll(&st.len, l);
+    atomic_add_ll(&st.len_before, lb);
+    atomic_add_ll(&st.clones, cl);
+    atomic_add_ll(&st.deaths, de);
+    atomic_add_ll(&st.zombies, zo);
+  }
+  acc = AnnAcc{};
+}
+
+// Per-warp shared memory: table keys [tmax], spawn values [caps], table heads [tmax],
+// list links [caps], slots first claimed [caps].
+__host__ __device__ inline size_t ann_warp_smem(uint32_t tmax, uint32_t caps) {
+  return (size_t)tmax * 12 + (size_t)caps * 16;
 }
 
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(AB) k_annihilate(StepArgs a, int nb_total) {
+__global__ void __launch_bounds__(WARPS * 32) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t T = a.tsize, caps = a.caps;
-  uint64_t *tkey = reinterpret_cast<uint64_t *>(smem);
-  uint64_t *skey = tkey + T;
-  uint64_t *sval = skey + caps;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t caps = a.caps, tmax = a.tsize;
+  unsigned char *mine = smem + (size_t)w * ann_warp_smem(tmax, caps);
+  uint64_t *tkey = reinterpret_cast<uint64_t *>(mine);
+  uint64_t *sval = tkey + tmax;
   int *thead = reinterpret_cast<int *>(sval + caps);
-  int *snext = thead + T;
-  __shared__ uint32_t s_out;
-  const int tid = threadIdx.x;
+  int *snext = thead + tmax;
+  int *snew = snext + caps;
   AnnAcc acc{};
-  for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
+  int cur_r = -1;
+  bool bad = false;
+  for (int gb = blockIdx.x * WARPS + w; gb < nb_total; gb += gridDim.x * WARPS) {
     const int r = gb >> a.nb_bits;
+    if (r != cur_r) {
+      if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
+      cur_r = r;
+    }
     const uint32_t rep = a.replica_base + (uint32_t)r;
     const uint32_t nsp = a.scount[gb];
     const uint32_t ns = nsp < caps ? nsp : caps;
     const uint32_t nv0 = a.cnt_in[gb];
     const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
-    bool bad = false;
-    for (uint32_t i = tid; i < T; i += AB) { tkey[i] = EMPTY_KEY; thead[i] = -1; }
-    if (tid == 0) s_out = 0;
+    uint32_t T = 64;
+    while (T < 2 * ns && T < tmax) T <<= 1;
+    for (uint32_t i = lane; i < T; i += 32) { tkey[i] = EMPTY_KEY; thead[i] = -1; }
+    __syncwarp();
+    // spawns into the table; slots claimed first are listed in snew
+    uint32_t nnew = 0;
     const Rec *sp = a.spawn + (size_t)gb * caps;
-    for (uint32_t j = tid; j < ns; j += AB) {
-      Rec s = sp[j];
-      skey[j] = s.key;
-      sval[j] = s.val;
-    }
-    __syncthreads();
-    for (uint32_t j = tid; j < ns; j += AB) {
-      uint64_t k = skey[j];
-      uint32_t slot = (uint32_t)mix64(k) & (T - 1);
-      uint32_t p = 0;
-      for (; p < T; ++p) {
-        unsigned long long old = atomicCAS((unsigned long long *)&tkey[slot],
-                                           (unsigned long long)EMPTY_KEY, (unsigned long long)k);
-        if (old == EMPTY_KEY || old == k) {
-          snext[j] = atomicExch(&thead[slot], (int)j);
-          break;
+    for (uint32_t j0 = 0; j0 < ns; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      bool first = false;
+      int slot = -1;
+      if (j < ns) {
+        const Rec s = sp[j];
+        sval[j] = s.val;
+        uint32_t sl = (uint32_t)mix64(s.key) & (T - 1);
+        for (uint32_t p = 0; p < T; ++p) {
+          const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
+                                                   (unsigned long long)EMPTY_KEY,
+                                                   (unsigned long long)s.key);
+          if (old == EMPTY_KEY || old == s.key) {
+            first = old == EMPTY_KEY;
+            slot = (int)sl;
+            snext[j] = atomicExch(&thead[sl], (int)j);
+            break;
+          }
+          sl = (sl + 1) & (T - 1);
         }
-        slot = (slot + 1) & (T - 1);
+        if (slot < 0) bad = true;
       }
-      if (p == T) atomicOr(&a.stats[r].flags, (unsigned)FLAG_TABLE);
+      const uint32_t m = __ballot_sync(0xffffffffu, first);
+      if (first) snew[nnew + __popc(m & ((1u << lane) - 1))] = slot;
+      nnew += __popc(m);
     }
-    __syncthreads();
-    // source walkers: diagonal step + spawns on the same address
-    const Rec *vb = a.v_in + (size_t)gb * a.capv_in;
-    for (uint32_t e = tid; e < nv; e += AB) {
-      Rec rec = vb[e];
-      const uint64_t key = rec.key;
-      const double dg = op_diagonal<KIND>(a, r, key);
-      const int slot = ns ? table_lookup(key, tkey, T) : -1;
-      int head = -1;
-      if (slot >= 0) { head = thead[slot]; thead[slot] = -2; }
-      if (STYLE == STYLE_INTEGER) {
-        const int64_t v = (int64_t)rec.val;
-        const double x = dg * (double)v;
-        U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
-        const int64_t res = round_stochastic(x, u53_of(rr));
-        // clones_deaths_zombies (spawning.jl:79-93)
-        const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
-        if (res > v) acc.clones += res - v;
-        else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
-        else acc.deaths += (res - v) < 0 ? v - res : res - v;
-        const int64_t tot = res + list_sum_int(head, sval, snext, (int)ns, &bad);
-        finalize_entry<STYLE>(a, r, gb, key, 0.0, tot, &s_out, acc);
-      } else {
-        const double v = bitsd(rec.val);
-        double res = dg * v;
-        if (a.proj_threshold > 0) {
-          U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
-          res = project_threshold(res, a.proj_threshold, u53_of(rr));
+    __syncwarp();
+    uint32_t out = 0;
+    // source walkers: diagonal step (diagonal_step!, spawning.jl:73-77) + spawns on them
+    const Rec *vbase = a.v_in + (size_t)gb * a.capv_in;
+    for (uint32_t e0 = 0; e0 < nv; e0 += 32) {
+      const uint32_t e = e0 + lane;
+      bool keep = false;
+      uint64_t key = 0, vb = 0;
+      if (e < nv) {
+        const Rec rec = vbase[e];
+        key = rec.key;
+        const double dg = op_diagonal<KIND>(a, r, key);
+        const int slot = ns ? table_lookup(key, tkey, T) : -1;
+        int head = -1;
+        if (slot >= 0) { head = thead[slot]; thead[slot] = -2; }
+        if (STYLE == STYLE_INTEGER) {
+          const int64_t v = (int64_t)rec.val;
+          const double x = dg * i2d_exact(v);
+          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
+          const int64_t res = round_stochastic(x, u53_of(rr));
+          // clones_deaths_zombies (spawning.jl:79-93)
+          const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+          if (res > v) acc.clones += res - v;
+          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
+          else acc.deaths += (res - v) < 0 ? v - res : res - v;
+          const int64_t tot = res + list_sum_int(head, sval, snext, (int)ns, &bad);
+          keep = finalize_entry<STYLE>(a, r, key, 0.0, tot, vb, acc);
+        } else {
+          double res = dg * bitsd(rec.val);
+          if (a.has_proj) {
+            const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
+            res = project_threshold(res, a.proj_threshold, u53_of(rr));
+          }
+          const double tot =
+              head >= 0 ? canonical_sum(!is_zero_d(res), res, head, sval, snext, (int)ns, &bad) : res;
+          keep = finalize_entry<STYLE>(a, r, key, tot, 0, vb, acc);
         }
-        const double tot =
-            head >= 0 ? canonical_sum(res != 0.0, res, head, sval, snext, (int)ns, &bad) : res;
-        finalize_entry<STYLE>(a, r, gb, key, tot, 0, &s_out, acc);
       }
+      warp_emit(a, gb, keep, key, vb, out);
     }
-    __syncthreads();
-    // addresses that received spawns but were not in the source
-    for (uint32_t s = tid; s < T; s += AB) {
-      const uint64_t key = tkey[s];
-      const int head = thead[s];
-      if (key == EMPTY_KEY || head < 0) continue;
-      if (STYLE == STYLE_INTEGER) {
-        const int64_t tot = list_sum_int(head, sval, snext, (int)ns, &bad);
-        finalize_entry<STYLE>(a, r, gb, key, 0.0, tot, &s_out, acc);
-      } else {
-        const double tot = canonical_sum(false, 0.0, head, sval, snext, (int)ns, &bad);
-        finalize_entry<STYLE>(a, r, gb, key, tot, 0, &s_out, acc);
+    __syncwarp();
+    // addresses reached only by spawns
+    for (uint32_t i0 = 0; i0 < nnew; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      bool keep = false;
+      uint64_t key = 0, vb = 0;
+      if (i < nnew) {
+        const int slot = snew[i];
+        const int head = thead[slot];
+        key = tkey[slot];
+        if (head >= 0) {
+          if (STYLE == STYLE_INTEGER) {
+            const int64_t tot = list_sum_int(head, sval, snext, (int)ns, &bad);
+            keep = finalize_entry<STYLE>(a, r, key, 0.0, tot, vb, acc);
+          } else {
+            const double tot = canonical_sum(false, 0.0, head, sval, snext, (int)ns, &bad);
+            keep = finalize_entry<STYLE>(a, r, key, tot, 0, vb, acc);
+          }
+        }
       }
+      warp_emit(a, gb, keep, key, vb, out);
     }
-    if (bad) atomicOr(&a.stats[r].flags, (unsigned)FLAG_TABLE);
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t no = s_out;
-      a.cnt_out[gb] = no < a.capv ? no : a.capv;
-      if (no > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
+    if (lane == 0) {
+      a.cnt_out[gb] = out < a.capv ? out : a.capv;
+      if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
       if (nsp > caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
-      atomicMax(&a.stats[r].max_v_bucket, no);
+      atomicMax(&a.stats[r].max_v_bucket, out);
       atomicMax(&a.stats[r].max_spawn_bucket, nsp);
       a.scount[gb] = 0;
     }
-    // flush statistics of this bucket
-    {
-      U128 nfx = warp_sum128(acc.norm);
-      long long l = warp_sum(acc.len), lb = warp_sum(acc.len_before);
-      long long cl = warp_sum(acc.clones), de = warp_sum(acc.deaths), zo = warp_sum(acc.zombies);
-      if ((tid & 31) == 0) {
-        DevStats &st = a.stats[r];
-        atomic_add128(&st.norm_lo, &st.norm_hi, nfx);
-        atomic_add_ll(&st.len, l);
-        atomic_add_ll(&st.len_before, lb);
-        atomic_add_ll(&st.clones, cl);
-        atomic_add_ll(&st.deaths, de);
-        atomic_add_ll(&st.zombies, zo);
-      }
-      acc = AnnAcc{};
-    }
-    __syncthreads();
+    __syncwarp();
   }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
+  if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -743,20 +824,22 @@ __global__ void k_offdiagonals(DevModel h, uint64_t key, int noff, uint64_t *key
 template <int KIND, int STYLE>
 static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
-  int grid = nb_total < (1 << 20) ? nb_total : (1 << 20);
+  const int want = (nb_total + WARPS - 1) / WARPS;
+  const int cap = ctx->num_sms * 64;
+  const int grid = want < cap ? want : cap;
   if (ev) cudaEventRecord(ev[0], st);
-  k_spawn<KIND, STYLE><<<grid, SB, 0, st>>>(a, nb_total);
+  k_spawn<KIND, STYLE><<<grid, WARPS * 32, 0, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[1], st);
-  k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, SB, 0, st>>>(a);
+  k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  size_t smem = (size_t)a.tsize * 12 + (size_t)a.caps * 20;
+  const size_t smem = WARPS * ann_warp_smem(a.tsize, a.caps);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_annihilate<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
     attr_set = true;
   }
-  k_annihilate<KIND, STYLE><<<grid, AB, smem, st>>>(a, nb_total);
+  k_annihilate<KIND, STYLE><<<grid, WARPS * 32, smem, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[3], st);
   return rimu_cuda_check(cudaGetLastError(), "step kernels");
 }

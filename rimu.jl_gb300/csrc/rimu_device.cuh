@@ -43,6 +43,7 @@ struct DevModel {
   const double *hoff;    // Hamiltonian offdiagonal magnitudes (no dt), same indexing
   const double *recip;   // recip[n] = 1.0 / n for n < recip_len
   int recip_len;
+  const double *dint;    // dint[n] = (double)n for n < recip_len
 };
 
 // ------------------------------------------------------------------------------------------
@@ -60,6 +61,13 @@ RIMU_HD int popc64(uint64_t x) {
   return __popcll(x);
 #else
   return __builtin_popcountll(x);
+#endif
+}
+RIMU_HD int clz64_hd(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
 #endif
 }
 RIMU_HD uint64_t shr64(uint64_t x, int s) { return s >= 64 ? 0 : x >> s; }
@@ -194,6 +202,25 @@ RIMU_HD int64_t floor_abs(double x) {
   uint64_t mant = (b & lowmask(52)) | (1ull << 52);
   int sh = e - 1075;
   return sh >= 0 ? (int64_t)(mant << sh) : (int64_t)(mant >> (-sh));
+}
+
+// Tests on IEEE bit patterns (GB300 issues FP64 compares on the slow FP64 pipe).
+RIMU_HD uint64_t abs_bits(double x) { return dbits(x) & 0x7fffffffffffffffull; }
+RIMU_HD bool is_zero_d(double x) { return abs_bits(x) == 0; }
+RIMU_HD bool is_neg_d(double x) { return (dbits(x) >> 63) != 0; }
+RIMU_HD bool abs_lt_one(double x) { return abs_bits(x) < 0x3FF0000000000000ull; }
+RIMU_HD double abs_d(double x) { return bitsd(abs_bits(x)); }
+RIMU_HD double signed_like(double mag, double s) {   // |mag| with the sign of s
+  return bitsd(abs_bits(mag) | (dbits(s) & 0x8000000000000000ull));
+}
+// Exact int64 -> double for |v| < 2^53 with integer instructions.
+RIMU_HD double i2d_exact(int64_t v) {
+  if (v == 0) return 0.0;
+  uint64_t sgn = v < 0 ? 0x8000000000000000ull : 0;
+  uint64_t a = (uint64_t)(v < 0 ? -v : v);
+  int p = 63 - clz64_hd(a);
+  uint64_t mant = (p <= 52) ? (a << (52 - p)) : (a >> (p - 52));
+  return bitsd(sgn | ((uint64_t)(1023 + p) << 52) | (mant & lowmask(52)));
 }
 
 // Order-preserving map of doubles to unsigned integers (for canonical summation order).
@@ -368,6 +395,56 @@ RIMU_HD Offdiag real1d_offdiag(const DevModel &h, uint64_t key, int chosen) {
       int prev_occ = (prev.mode == cur.mode - 1) ? prev.occ : 0;
       r.key = key ^ (3ull << (cur.offset - 1));
       r.prod = cur.occ * (prev_occ + 1);
+    }
+  }
+  return r;
+}
+
+// sum_i n_i (n_i - 1) of a BoseFS word: each run of n ones contributes n(n-1), and
+// sum over runs of C(n, 2) = sum_{d >= 1} popcount(bits starting d+1 consecutive ones).
+RIMU_HD int bose_interaction_fast(uint64_t x) {
+  int acc = 0;
+  uint64_t y = x & (x >> 1);
+  while (y) { acc += popc64(y); y &= y >> 1; }
+  return 2 * acc;
+}
+
+// Position of the k-th (0-based) set bit.
+RIMU_HD int select_bit(uint64_t x, int k) {
+  for (int i = 0; i < k; ++i) x &= x - 1;
+  return ctz64(x);
+}
+
+// HubbardReal1D offdiagonal with word operations only: the site-th occupied mode starts at
+// the site-th run start (bits that are set and whose lower neighbour is not); same results
+// as hopnextneighbour (bosefs.jl:297-345).
+RIMU_HD Offdiag real1d_offdiag_fast(uint64_t key, int B, int chosen) {
+  const int site = (chosen + 1) >> 1;
+  const uint64_t starts = key & ~(key << 1);
+  const int start = select_bit(starts, site - 1);
+  const int n = ctz64(~shr64(key, start));
+  const int end = start + n;                 // separator after the mode, or B for mode M
+  Offdiag r;
+  r.sign = 1;
+  if (chosen & 1) {                          // hop right
+    if (end == B) {                          // from mode M to mode 1 (periodic wrap)
+      r.key = ((key << 1) | 1ull) & lowmask(B);
+      r.prod = n * (ctz64(~key) + 1);
+    } else {
+      const int next = ctz64(~shr64(key, end + 1));
+      r.key = key ^ (3ull << (end - 1));
+      r.prod = n * (next + 1);
+    }
+  } else {                                   // hop left
+    if (start == 0) {                        // from mode 1 to mode M
+      const uint64_t nk = (key >> 1) | (1ull << (B - 1));
+      const int lead = clz64_hd(~(nk << (64 - B)));
+      r.key = nk;
+      r.prod = n * lead;
+    } else {
+      const int prev = start >= 2 ? clz64_hd(~(key << (65 - start))) : 0;
+      r.key = key ^ (3ull << (start - 1));
+      r.prod = n * (prev + 1);
     }
   }
   return r;

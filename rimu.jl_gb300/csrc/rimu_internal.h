@@ -52,6 +52,10 @@ struct StepArgs {
   int style, op;
   double dt;
   double boost, proj_threshold, compression, rel_threshold, abs_threshold;
+  int has_proj;      // proj_threshold > 0
+  int comp_mode;     // 0: no compression, 1: threshold 1, 2: other threshold
+  int boost_one;     // boost == 1 and rel_threshold == 1
+  int has_abs_thr;   // abs_threshold finite
   uint64_t seed;
   uint32_t step;
   uint32_t replica_base;

@@ -108,10 +108,11 @@ def test_large_vector_rebuckets_and_matches_oracle():
 def test_same_seed_same_result_and_seed_matters():
     h = R.HubbardReal1D(B66, u=6.0)
     style = R.IsDynamicSemistochastic()
-    # 5 walkers on 12 offdiagonals: the column is sampled, so the seed matters
-    a = gpu_step(h, style, [B66.key], [5.0], 0.01, 0.0, 7, 1)
-    b = gpu_step(h, style, [B66.key], [5.0], 0.01, 0.0, 7, 1)
-    c = gpu_step(h, style, [B66.key], [5.0], 0.01, 0.0, 8, 1)
+    # 5 walkers on 12 offdiagonals: the column is sampled, so the seed matters; dt = 0.1
+    # makes each spawn larger than the compression threshold
+    a = gpu_step(h, style, [B66.key], [5.0], 0.1, 0.0, 7, 1)
+    b = gpu_step(h, style, [B66.key], [5.0], 0.1, 0.0, 7, 1)
+    c = gpu_step(h, style, [B66.key], [5.0], 0.1, 0.0, 8, 1)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert not (np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1]))
 

@@ -699,6 +699,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   int retries = 0;
   const int ndiag = m->ndiag;
   const uint32_t kMaxCaps = 512;
+  uint32_t min_caps = 0;   // raised after a spawn-slab overflow
   for (;;) {
     if (nb_bits > 26) { g_err = "rimu_apply_operator: too many buckets needed"; return RIMU_ERR_OVERFLOW; }
     if (nb_bits != source->nb_bits) {
@@ -708,11 +709,17 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     double mu_s = (double)S_est / (double)nb;
     uint32_t want_caps = round_up((uint64_t)(mu_s + 6.0 * std::sqrt(mu_s) + 32.0), 32);
     if (want_caps > kMaxCaps) { nb_bits++; continue; }
-    caps = std::min(kMaxCaps, std::max(caps, want_caps));
+    caps = std::min(kMaxCaps, std::max(std::max(caps, want_caps), min_caps));
+    // reuse the allocated spawn slabs and target slabs when they are large enough, so
+    // that steady-state steps do not reallocate (capacities only grow, with headroom)
+    if (w->nb_total == (int)nb && w->caps >= caps && w->caps <= kMaxCaps) caps = w->caps;
+    else if (caps < kMaxCaps) caps = std::min(kMaxCaps, round_up((uint64_t)caps * 5 / 4, 32));
     capv = std::max(capv, std::max(source->capv, capv_for((int64_t)(1.5 * L + 64), nb_bits)));
+    if (target->nb_bits == nb_bits && target->capv >= capv) capv = target->capv;
     uint64_t work_bound = (uint64_t)(norm * p->boost) + (uint64_t)L * (uint64_t)m->max_offdiag;
     uint64_t hc = work_bound / HEAVY_CHUNK + std::min<uint64_t>((uint64_t)L, work_bound / HEAVY_LIMIT + 1) + 64;
     heavy_cap = std::max<uint32_t>(heavy_cap, (uint32_t)std::min<uint64_t>(hc, 1u << 28));
+    heavy_cap = std::max<uint32_t>(heavy_cap, w->heavy_cap);
     if (target->nb_bits != nb_bits || target->capv != capv) {
       if ((rc = vec_alloc(target, nb_bits, capv))) return rc;
     }
@@ -771,7 +778,8 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     if (++retries > 10) { g_err = "rimu_apply_operator: capacities could not be grown enough"; return RIMU_ERR_OVERFLOW; }
     if (st.flags & FLAG_SPAWN_OVERFLOW) {
       S_est = std::max<int64_t>(2 * S_est, (int64_t)st.max_spawn_bucket * (int64_t)nb);
-      if (caps >= kMaxCaps) nb_bits++;
+      min_caps = round_up((uint64_t)st.max_spawn_bucket * 5 / 4 + 32, 32);
+      if (min_caps > kMaxCaps) { nb_bits++; min_caps = 0; }
       caps = 0;
     }
     if (st.flags & FLAG_V_OVERFLOW) {

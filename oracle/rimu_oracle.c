@@ -418,6 +418,42 @@ static double o_fixed_to_double(o_u128 x) {
   return ldexp((double)x, -64);
 }
 
+/* x as a signed multiple of 2^-64, if it is one and |x| < 2^48 (so that up to 2^15
+ * contributions cannot overflow the 128-bit sum). */
+static int o_to_fixed(double x, __int128 *out) {
+  if (x == 0.0) { *out = 0; return 1; }
+  double ax = fabs(x);
+  if (!(ax < 281474976710656.0)) return 0;             /* 2^48 */
+  double scaled = ldexp(ax, 64);
+  if (scaled != floor(scaled)) return 0;               /* bits below 2^-64 */
+  /* scaled < 2^112: split into two 64-bit halves exactly */
+  double hi = floor(ldexp(scaled, -64));
+  double lo = scaled - ldexp(hi, 64);
+  unsigned __int128 u = ((unsigned __int128)(uint64_t)hi << 64) | (uint64_t)lo;
+  *out = x < 0 ? -(__int128)u : (__int128)u;
+  return 1;
+}
+/* Nearest double (ties to even) of fx * 2^-64, computed on the integer. */
+static double o_fixed_signed_to_double(__int128 fx) {
+  if (fx == 0) return 0.0;
+  int neg = fx < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-fx) : (unsigned __int128)fx;
+  int top = 127;
+  while (!((u >> top) & 1)) --top;
+  double r;
+  if (top <= 52) {
+    r = ldexp((double)(uint64_t)u, -64);
+  } else {
+    int drop = top - 52;
+    unsigned __int128 m = u >> drop;
+    unsigned __int128 rem = u & ((((unsigned __int128)1) << drop) - 1);
+    unsigned __int128 half = ((unsigned __int128)1) << (drop - 1);
+    if (rem > half || (rem == half && (m & 1))) m += 1;
+    r = ldexp((double)(uint64_t)m, drop - 64);     /* m <= 2^53: exact */
+  }
+  return neg ? -r : r;
+}
+
 /* One apply_operator! step (dictvectors.jl:112-140) from `src` into a sorted `dst`.
  * Values are doubles for the float styles and int64 (passed as double-typed storage of
  * the same bits is NOT used: separate arrays) for IsStochasticInteger.
@@ -525,7 +561,11 @@ int o_step(const o_model *h, const o_params *p,
   }
   if (b.err) { free(b.c); return 1; }
   if (!is_int) st->spawns = o_fixed_to_double(spawn_acc);
-  /* ---- annihilation: sum contributions per address in canonical order ---- */
+  /* ---- annihilation: sum the contributions per address ----
+   * Rule (the GPU follows it exactly): if every contribution to an address is a multiple of
+   * 2^-64 with magnitude below 2^48, the result is the exact sum rounded once to the nearest
+   * double (ties to even); otherwise the contributions are added in canonical order, the
+   * diagonal term first and then the spawns in increasing numerical order. */
   qsort(b.c, (size_t)b.n, sizeof(o_contrib), is_int ? o_cmp_contrib_i : o_cmp_contrib_f);
   uint64_t *ok = malloc((size_t)(b.n ? b.n : 1) * 8);
   double *ov = malloc((size_t)(b.n ? b.n : 1) * 8);
@@ -536,12 +576,19 @@ int o_step(const o_model *h, const o_params *p,
     int64_t j = i;
     double s = 0.0;
     int64_t si = 0;
-    int first = 1;
+    int first = 1, exact = 1;
+    __int128 fx = 0;
     while (j < b.n && b.c[j].key == b.c[i].key) {
       if (is_int) si += b.c[j].iv;
-      else { s = first ? b.c[j].v : s + b.c[j].v; first = 0; }
+      else {
+        s = first ? b.c[j].v : s + b.c[j].v;
+        first = 0;
+        __int128 t;
+        if (exact && o_to_fixed(b.c[j].v, &t)) fx += t; else exact = 0;
+      }
       ++j;
     }
+    if (!is_int && exact) s = o_fixed_signed_to_double(fx);
     if (is_int ? si != 0 : s != 0.0) { ok[m] = b.c[i].key; ov[m] = s; oi[m] = si; ++m; }
     i = j;
   }

@@ -602,6 +602,18 @@ extern "C" int rimu_wm_set_timing(rimu_wm *w, int enable) {
   return RIMU_OK;
 }
 
+extern "C" int rimu_wm_set_launch_shape(rimu_wm *w, int keys_per_bucket, int table_slots) {
+  if (!w) return bad("rimu_wm_set_launch_shape: NULL working memory");
+  if (keys_per_bucket < 16 || keys_per_bucket > 512)
+    return bad("rimu_wm_set_launch_shape: keys_per_bucket must be in 16..512");
+  if (table_slots != 0 &&
+      (table_slots < 64 || table_slots > 512 || (table_slots & (table_slots - 1))))
+    return bad("rimu_wm_set_launch_shape: table_slots must be 0 or a power of two in 64..512");
+  w->keys_per_bucket = keys_per_bucket;
+  w->table_slots = table_slots;
+  return RIMU_OK;
+}
+
 extern "C" int rimu_wm_timing(rimu_wm *w, double *out7) {
   if (!w || !out7) return bad("rimu_wm_timing: NULL argument");
   for (int i = 0; i < 4; ++i) out7[i] = w->t_ms[i];
@@ -684,15 +696,16 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   int rc;
   if (p->op == RIMU_OP_TRANSITION && (rc = ensure_aoff(m, p->dt))) return rc;
 
-  // capacity planning: one warp per bucket, about 48 walkers and 96 spawns per bucket
+  // capacity planning: one warp per bucket; the bucket count keeps the expected number of
+  // addresses (source walkers plus spawns) per bucket between kKeys / 2 and kKeys
   const int64_t L = std::max<int64_t>(source->len, 1);
   const double norm = std::max(source->norm, 1.0);
   int64_t S_est;
   if (w->last_spawns >= 0) S_est = (int64_t)(1.3 * (double)w->last_spawns) + 256;
   else if (p->style == RIMU_STYLE_DETERMINISTIC) S_est = L * (int64_t)m->max_offdiag + 256;
   else S_est = (int64_t)(norm * p->boost) + L * 4 + 256;
-  int need_bits = std::max(ceil_log2((uint64_t)((1.5 * (double)L + 64) / 48)),
-                           ceil_log2((uint64_t)(S_est / 96 + 1)));
+  const double kKeys = (double)w->keys_per_bucket;
+  int need_bits = ceil_log2((uint64_t)((double)(L + S_est) / kKeys) + 1);
   int nb_bits = std::max(source->nb_bits, need_bits);
   uint32_t caps = 0, capv = 0;
   uint32_t heavy_cap = 0;
@@ -748,9 +761,12 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.nrep = 1; a.nb_bits = nb_bits;
     a.capv_in = source->capv;
     a.capv = capv; a.caps = caps;
+    // per-warp table: room for the expected addresses of a bucket plus 5 sigma and one
+    // round of 32 insertions; larger buckets are processed in several passes
+    const double mu_k = (double)(L + S_est) / (double)nb;
     uint32_t T = 64;
-    while (T < 2 * caps) T <<= 1;
-    a.tsize = T;            // largest per-bucket table; each bucket sizes its own from its spawns
+    while ((double)T < mu_k + 5.0 * std::sqrt(mu_k) + 32.0 && T < 512) T <<= 1;
+    a.tsize = w->table_slots ? (uint32_t)w->table_slots : T;
     a.v_in = source->recs; a.cnt_in = source->count;
     a.v_out = target->recs; a.cnt_out = target->count;
     a.spawn = w->spawn; a.scount = w->scount;

@@ -6,16 +6,17 @@
 // buckets with slabs of capacity caps.
 //
 // One step (apply_operator!, src/Interfaces/dictvectors.jl:112-140):
-//   k_spawn      reads the source slabs and writes every spawn straight into the slab of
+//   k_spawn      each warp lays the walkers of 32 consecutive buckets out as one list,
+//                evaluates their columns and deals the spawn attempts out to its lanes in
+//                work items of G units; every spawn is written straight into the slab of
 //                its destination bucket (perform_spawns!, pdworkingmemory.jl:208-217).
-//                Columns are balanced across the CTA by a block scan over their work;
-//                columns with more than HEAVY_LIMIT attempts are cut into chunks.
+//                Columns with more than HEAVY_LIMIT units are cut into chunks.
 //   k_spawn_heavy  processes the chunks of heavy columns on all SMs.
-//   k_annihilate one CTA per bucket: spawns go into a shared-memory hash table, each source
-//                walker takes its diagonal step and collects the spawns on its address, new
-//                addresses are emitted, contributions summed in canonical order (diagonal
-//                first, spawns by increasing value), threshold compression applied, and the
-//                norm accumulated exactly (collect_local!/move_and_compress!,
+//   k_annihilate one warp per bucket: the source walkers (after their diagonal step) and the
+//                spawns go into a shared-memory table holding one exact 128-bit fixed-point
+//                sum per address; the sums are rounded once, threshold compression applied,
+//                statistics and the norm accumulated exactly, and the survivors written to
+//                the target slab (collect_local!/move_and_compress!,
 //                pdworkingmemory.jl:228-273; compression.jl:18-42).
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -128,11 +129,6 @@ __device__ __forceinline__ double op_offdiag(const StepArgs &a, const Offdiag &o
 // ------------------------------------------------------------------------------------------
 // Statistics
 // ------------------------------------------------------------------------------------------
-struct Acc {
-  U128 fx;                 // fixed-point sum (spawn magnitudes or norm)
-  long long a0, a1, a2, a3, a4, a5;
-};
-
 __device__ __forceinline__ U128 shfl_down128(U128 v, int o) {
   U128 r;
   r.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
@@ -157,30 +153,27 @@ __device__ __forceinline__ void atomic_add128(unsigned long long *lo, unsigned l
 __device__ __forceinline__ void atomic_add_ll(long long *p, long long v) {
   if (v) atomicAdd((unsigned long long *)p, (unsigned long long)v);
 }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  return (1u << (threadIdx.x & 31)) - 1u;
+}
 
 // ------------------------------------------------------------------------------------------
-// Spawning: one warp per bucket, no block barriers
+// Spawning: a warp spreads the walkers of CHUNK_BUCKETS consecutive buckets over its lanes
 // ------------------------------------------------------------------------------------------
 struct SpawnAcc {
-  U128 fx;           // sum |spawn| for float styles
-  long long spawns_i;
-  long long records;
   long long attempts, exact_n, inexact_n;
 };
 
-constexpr int WARPS = 8;           // warps per CTA in the step kernels
-constexpr int G = 4;               // units (attempts or offdiagonals) per work item
+constexpr int WARPS = 8;            // warps per CTA in the step kernels
+constexpr int G = 4;                // units (attempts or offdiagonals) per work item
+constexpr int CHUNK_BUCKETS = 32;   // buckets whose walkers one warp processes together
+constexpr int BATCH = 64;           // walkers whose work items are distributed together
 
-__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk, uint64_t vb,
-                                           SpawnAcc &acc) {
-  uint32_t b = ((uint32_t)r << a.nb_bits) | bucket_of(nk, a.nb_bits);
-  uint32_t pos = atomicAdd(&a.scount[b], 1u);
-  if (pos < a.caps) {
-    a.spawn[(size_t)b * a.caps + pos] = Rec{nk, vb};
-  } else {
-    atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
-  }
-  acc.records++;
+__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk, uint64_t vb) {
+  const uint32_t b = ((uint32_t)r << a.nb_bits) | bucket_of(nk, a.nb_bits);
+  const uint32_t pos = atomicAdd(&a.scount[b], 1u);
+  if (pos < a.caps) a.spawn[(size_t)b * a.caps + pos] = Rec{nk, vb};
+  else atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
 }
 
 template <int KIND>
@@ -189,73 +182,65 @@ __device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key,
   return column_offdiag<KIND>(h, key, chosen);
 }
 
-// Units [j0, j1) of one column.  Exact columns deposit val * T_{new,key} for offdiagonals
-// j+1 (spawning.jl:174-182); sampled columns draw a uniform offdiagonal per attempt and
-// deposit c * T_{new,key} (spawning.jl:232-243).  With float walkers and no on-the-fly
-// projection an attempt needs 32 random bits, so one Philox block serves four attempts.
+// Units [j0, j1) of one column, j0 a multiple of G.  Exact columns deposit val * T_{new,key}
+// for offdiagonals j+1 (spawning.jl:174-182); sampled columns draw a uniform offdiagonal per
+// attempt and deposit c * T_{new,key} (spawning.jl:232-243).  With float walkers and no
+// on-the-fly projection an attempt needs 32 random bits, so one Philox block serves the four
+// attempts 4q..4q+3.
 template <int KIND, int STYLE>
 __device__ __forceinline__ void spawn_units(const StepArgs &a, int r, uint64_t key, uint64_t vb,
                                             double c, int noff, int exact, uint32_t j0,
-                                            uint32_t j1, SpawnAcc &acc) {
+                                            uint32_t j1) {
   const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
     const double val = bitsd(vb);
     for (uint32_t j = j0; j < j1; ++j) {
-      Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
+      const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
       if (od.prod == 0) continue;
       double y = val * op_offdiag(a, od);
       if (STYLE == STYLE_DSS && a.has_proj) {
-        U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
+        const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
         y = project_threshold(y, a.proj_threshold, u53_of(rr));
       }
       if (is_zero_d(y)) continue;
-      acc.fx = add128(acc.fx, fixed_of(abs_d(y)));
-      emit_spawn(a, r, od.key, dbits(y), acc);
+      emit_spawn(a, r, od.key, dbits(y));
     }
     return;
   }
   const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
   U4 blk{0, 0, 0, 0};
-  uint32_t blk_id = 0xffffffffu;
+  if (grouped) blk = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j0 >> 2);
   for (uint32_t j = j0; j < j1; ++j) {
+    U4 rr = blk;
     uint32_t word;
-    U4 rr;
     if (grouped) {
-      if ((j >> 2) != blk_id) { blk_id = j >> 2; blk = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, blk_id); }
       const uint32_t q = j & 3;
       word = q == 0 ? blk.x : q == 1 ? blk.y : q == 2 ? blk.z : blk.w;
-      rr = blk;
     } else {
       rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
       word = rr.x;
     }
     const int chosen = (int)uniform_index(word, (uint32_t)noff) + 1;
-    Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
+    const Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
     if (od.prod == 0) continue;
     double y = c * op_offdiag(a, od);
     if (STYLE == STYLE_INTEGER) {
-      int64_t k = round_stochastic(y, u53_of(rr));
+      const int64_t k = round_stochastic(y, u53_of(rr));
       if (k == 0) continue;
-      acc.spawns_i += k < 0 ? -k : k;
-      emit_spawn(a, r, od.key, (uint64_t)k, acc);
+      emit_spawn(a, r, od.key, (uint64_t)k);
     } else {
       if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
       if (is_zero_d(y)) continue;
-      acc.fx = add128(acc.fx, fixed_of(abs_d(y)));
-      emit_spawn(a, r, od.key, dbits(y), acc);
+      emit_spawn(a, r, od.key, dbits(y));
     }
   }
 }
 
 __device__ __forceinline__ void flush_spawn_acc(const StepArgs &a, int r, SpawnAcc &acc) {
-  U128 fx = warp_sum128(acc.fx);
-  long long s = warp_sum(acc.spawns_i), rc = warp_sum(acc.records), at = warp_sum(acc.attempts);
-  long long ex = warp_sum(acc.exact_n), ie = warp_sum(acc.inexact_n);
+  const long long at = warp_sum(acc.attempts);
+  const long long ex = warp_sum(acc.exact_n), ie = warp_sum(acc.inexact_n);
   if ((threadIdx.x & 31) == 0) {
     DevStats &st = a.stats[r];
-    atomic_add128(&st.spawn_lo, &st.spawn_hi, fx);
-    atomic_add_ll(&st.spawns_int, s);
-    atomic_add_ll(&st.spawn_records, rc);
     atomic_add_ll(&st.spawn_attempts, at);
     atomic_add_ll(&st.exact_steps, ex);
     atomic_add_ll(&st.inexact_steps, ie);
@@ -310,83 +295,124 @@ __device__ __forceinline__ uint64_t column_work(const StepArgs &a, uint64_t key,
   return noff == 0 ? 0 : (exact ? (uint64_t)noff : natt);
 }
 
+// Cut a column with more than HEAVY_LIMIT units into chunks for k_spawn_heavy.
+__device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, int noff,
+                           int exact, uint64_t work) {
+  const uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
+  const uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
+  for (uint64_t k = 0; k < nch; ++k) {
+    if (idx + k >= a.heavy_cap) {
+      atomicOr(&a.stats[r].flags, (unsigned)FLAG_HEAVY_OVERFLOW);
+      break;
+    }
+    HeavyChunk ch;
+    ch.key = rec.key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
+    ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
+    const uint64_t rem = work - k * HEAVY_CHUNK;
+    ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
+    ch.rep = (uint32_t)r; ch.pad = 0;
+    a.heavy[idx + k] = ch;
+  }
+}
+
+// Each warp takes CHUNK_BUCKETS consecutive buckets of one replica, lays their walkers out
+// as one flat list and works through it BATCH walkers at a time: every lane evaluates the
+// column of one or two walkers, then the batch's work items (G units each) are dealt out to
+// the lanes by an exclusive scan and a binary search.
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(WARPS * 32) k_spawn(StepArgs a, int nb_total) {
-  __shared__ uint64_t s_key[WARPS][32];
-  __shared__ uint64_t s_val[WARPS][32];
-  __shared__ double s_c[WARPS][32];
-  __shared__ uint32_t s_units[WARPS][32];
-  __shared__ uint32_t s_excl[WARPS][32];
-  __shared__ int s_noff[WARPS][32];
-  __shared__ int s_exact[WARPS][32];
+__global__ void __launch_bounds__(WARPS * 32, 3) k_spawn(StepArgs a, int nb_total) {
+  __shared__ uint32_t s_bpre[WARPS][CHUNK_BUCKETS + 1];
+  __shared__ uint64_t s_key[WARPS][BATCH];
+  __shared__ uint64_t s_val[WARPS][BATCH];
+  __shared__ double s_c[WARPS][BATCH];
+  __shared__ uint32_t s_units[WARPS][BATCH];
+  __shared__ uint32_t s_excl[WARPS][BATCH];
+  __shared__ uint32_t s_meta[WARPS][BATCH];   // noff | exact << 31
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int cb = a.nb_bits < 5 ? (1 << a.nb_bits) : CHUNK_BUCKETS;
+  const int nchunks = nb_total / cb;
   SpawnAcc acc{};
   int cur_r = -1;
-  for (int gb = blockIdx.x * WARPS + w; gb < nb_total; gb += gridDim.x * WARPS) {
-    const int r = gb >> a.nb_bits;
+  for (int ch = blockIdx.x * WARPS + w; ch < nchunks; ch += gridDim.x * WARPS) {
+    const int b0 = ch * cb;
+    const int r = b0 >> a.nb_bits;
     if (r != cur_r) {
       if (cur_r >= 0) flush_spawn_acc(a, cur_r, acc);
       cur_r = r;
     }
-    const uint32_t n0 = a.cnt_in[gb];
-    const uint32_t n = n0 < a.capv_in ? n0 : a.capv_in;
-    const Rec *base = a.v_in + (size_t)gb * a.capv_in;
-    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
-      const uint32_t e = c0 + lane;
-      uint32_t items = 0;
-      if (e < n) {
-        const Rec rec = base[e];
-        int noff, exact;
-        double c;
-        uint64_t work = column_work<KIND, STYLE>(a, rec.key, rec.val, noff, exact, c, acc);
-        if (work > (1ull << 36)) {       // more attempts than any walker list can hold
-          atomicOr(&a.stats[r].flags, (unsigned)FLAG_VALUE_OVERFLOW);
-          work = 0;
-        }
-        acc.attempts += (long long)work;
-        if (work > (uint64_t)HEAVY_LIMIT) {
-          const uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
-          const uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
-          for (uint64_t k = 0; k < nch; ++k) {
-            if (idx + k >= a.heavy_cap) {
-              atomicOr(&a.stats[r].flags, (unsigned)FLAG_HEAVY_OVERFLOW);
-              break;
-            }
-            HeavyChunk ch;
-            ch.key = rec.key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
-            ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
-            const uint64_t rem = work - k * HEAVY_CHUNK;
-            ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
-            ch.rep = (uint32_t)r; ch.pad = 0;
-            a.heavy[idx + k] = ch;
+    uint32_t n = 0;
+    if (lane < cb) {
+      n = a.cnt_in[b0 + lane];
+      if (n > a.capv_in) n = a.capv_in;
+    }
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 0) s_bpre[w][0] = 0;
+    s_bpre[w][lane + 1] = incl;
+    const uint32_t E = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (uint32_t e0 = 0; e0 < E; e0 += BATCH) {
+      uint32_t items[2];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const uint32_t f = e0 + (uint32_t)(hh * 32 + lane);
+        const int slot = hh * 32 + lane;
+        uint32_t it = 0, units = 0;
+        if (f < E) {
+          int bi = 0;
+#pragma unroll
+          for (int st = 16; st >= 1; st >>= 1)
+            if (bi + st < cb && s_bpre[w][bi + st] <= f) bi += st;
+          const Rec rec = a.v_in[(size_t)(b0 + bi) * a.capv_in + (f - s_bpre[w][bi])];
+          int noff, exact;
+          double c;
+          uint64_t work = column_work<KIND, STYLE>(a, rec.key, rec.val, noff, exact, c, acc);
+          if (work > (1ull << 36)) {       // more attempts than any walker list can hold
+            atomicOr(&a.stats[r].flags, (unsigned)FLAG_VALUE_OVERFLOW);
+            work = 0;
           }
-          work = 0;
+          acc.attempts += (long long)work;
+          if (work > (uint64_t)HEAVY_LIMIT) {
+            push_heavy(a, r, rec, c, noff, exact, work);
+            work = 0;
+          }
+          s_key[w][slot] = rec.key;
+          s_val[w][slot] = rec.val;
+          s_c[w][slot] = c;
+          s_meta[w][slot] = (uint32_t)noff | ((uint32_t)exact << 31);
+          units = (uint32_t)work;
+          it = (units + G - 1) / G;
         }
-        s_key[w][lane] = rec.key; s_val[w][lane] = rec.val; s_c[w][lane] = c;
-        s_noff[w][lane] = noff; s_exact[w][lane] = exact;
-        s_units[w][lane] = (uint32_t)work;
-        items = ((uint32_t)work + G - 1) / G;
+        s_units[w][slot] = units;
+        items[hh] = it;
       }
-      // warp exclusive scan of the work items
-      uint32_t incl = items;
+      uint32_t in0 = items[0], in1 = items[1];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
+        const uint32_t y0 = __shfl_up_sync(0xffffffffu, in0, o);
+        const uint32_t y1 = __shfl_up_sync(0xffffffffu, in1, o);
+        if (lane >= o) { in0 += y0; in1 += y1; }
       }
-      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-      s_excl[w][lane] = incl - items;
+      const uint32_t tot0 = __shfl_sync(0xffffffffu, in0, 31);
+      const uint32_t total = tot0 + __shfl_sync(0xffffffffu, in1, 31);
+      s_excl[w][lane] = in0 - items[0];
+      s_excl[w][32 + lane] = tot0 + in1 - items[1];
       __syncwarp();
       for (uint32_t it = lane; it < total; it += 32) {
         int lo = 0;
 #pragma unroll
-        for (int step = 16; step >= 1; step >>= 1)
-          if (s_excl[w][lo + step] <= it) lo += step;
+        for (int st = 32; st >= 1; st >>= 1)
+          if (s_excl[w][lo + st] <= it) lo += st;
         const uint32_t j0 = (it - s_excl[w][lo]) * G;
         const uint32_t ju = s_units[w][lo];
         const uint32_t j1 = j0 + G < ju ? j0 + G : ju;
-        spawn_units<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo], s_noff[w][lo],
-                                 s_exact[w][lo], j0, j1, acc);
+        const uint32_t meta = s_meta[w][lo];
+        spawn_units<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo],
+                                 (int)(meta & 0x7fffffffu), (int)(meta >> 31), j0, j1);
       }
       __syncwarp();
     }
@@ -398,59 +424,107 @@ template <int KIND, int STYLE>
 __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
   uint32_t nch = *a.heavy_count;
   if (nch > a.heavy_cap) nch = a.heavy_cap;
-  SpawnAcc acc{};
   for (uint32_t ci = blockIdx.x; ci < nch; ci += gridDim.x) {
     HeavyChunk ch = a.heavy[ci];
-    if (ch.cnt > (uint32_t)HEAVY_CHUNK || ch.rep >= (uint32_t)a.nrep) {
+    if (ch.cnt > (uint32_t)HEAVY_CHUNK || ch.rep >= (uint32_t)a.nrep || (ch.j0 & (G - 1))) {
       if (threadIdx.x == 0) atomicOr(&a.stats[0].flags, (unsigned)FLAG_TABLE);
-      ch.cnt = 0;
-      ch.rep = 0;
+      continue;
     }
     for (uint32_t t = threadIdx.x * G; t < ch.cnt; t += blockDim.x * G) {
       const uint32_t j1 = t + G < ch.cnt ? t + G : ch.cnt;
       spawn_units<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact,
-                               ch.j0 + t, ch.j0 + j1, acc);
+                               ch.j0 + t, ch.j0 + j1);
     }
-    // attempts were counted when the chunk was created
-    acc.attempts = 0;
-    flush_spawn_acc(a, (int)ch.rep, acc);
   }
 }
 
 // ------------------------------------------------------------------------------------------
-// Annihilation: one warp per bucket
+// Annihilation: one warp per bucket, exact fixed-point sums in a shared-memory table
 // ------------------------------------------------------------------------------------------
+// Summation rule (the oracle states the same): when every contribution to an address is a
+// multiple of 2^-64 below 2^48 in magnitude, the address gets the exact sum rounded once to
+// the nearest double, so the order of the contributions does not matter; otherwise the
+// contributions are added in canonical order (the diagonal term, then the spawns by
+// increasing value).  Integer walkers are summed as int64.
 struct AnnAcc {
-  U128 norm;
-  long long len, len_before, clones, deaths, zombies;
+  U128 norm, spawn_fx;
+  long long len, len_before, clones, deaths, zombies, spawns_i, records;
 };
+
+// Statistics of one pass over a bucket; kept only if the pass completes.
+struct PassAcc {
+  U128 spawn_fx;
+  long long clones, deaths, zombies, spawns_i, records;
+};
+
+constexpr uint32_t INFO_INEXACT = 1u;   // tinfo bit 0; bits 1..31: 1 + source walker index
+constexpr int MAX_SPLIT = 16;           // at most 2^MAX_SPLIT passes over one bucket
+
+// Per-warp table of T slots: keys, 128-bit sums (lo, hi), info words, occupied-slot list.
+__host__ __device__ inline size_t ann_warp_smem(uint32_t T) { return (size_t)T * 30; }
+
+__device__ __forceinline__ U128 neg128(U128 x) {
+  U128 r;
+  r.lo = ~x.lo + 1;
+  r.hi = ~x.hi + (x.lo == 0 ? 1 : 0);
+  return r;
+}
+
+// x as a two's-complement multiple of 2^-64, if it is one and |x| < 2^48.
+__device__ __forceinline__ bool fixed_exact(double x, U128 &out) {
+  const uint64_t b = dbits(x);
+  const uint64_t ab = b & 0x7fffffffffffffffull;
+  out = U128{0, 0};
+  if (ab == 0) return true;
+  const int e = (int)(ab >> 52);
+  if (e == 0 || e >= 1023 + 48) return false;
+  const uint64_t mant = (ab & lowmask(52)) | (1ull << 52);
+  const int sh = e - 1075 + 64;            // |x| = mant * 2^(sh - 64), sh <= 59
+  U128 m;
+  if (sh >= 0) {
+    m.lo = mant << sh;
+    m.hi = sh > 11 ? (mant >> (64 - sh)) : 0;
+  } else {
+    if (-sh >= 53 || (mant & lowmask(-sh))) return false;
+    m.lo = mant >> (-sh);
+    m.hi = 0;
+  }
+  out = (b >> 63) ? neg128(m) : m;
+  return true;
+}
+
+__device__ __forceinline__ double signed_fixed_to_double(U128 x) {
+  if (x.hi >> 63) return bitsd(dbits(fixed_to_double(neg128(x))) ^ 0x8000000000000000ull);
+  return fixed_to_double(x);
+}
 
 __device__ __forceinline__ double from_ordered(uint64_t o) {
   return bitsd((o >> 63) ? (o & 0x7fffffffffffffffull) : ~o);
 }
 
-// Sum of the spawn list starting at `head` in increasing order of value, after `first`.
-// Lists hold at most `ns` entries; a longer walk means a corrupted list and is cut short.
-__device__ double canonical_sum(bool have, double first, int head, const uint64_t *sval,
-                                const int *snext, int ns, bool *bad) {
+// Canonical-order sum for an address with an inexact contribution: `first` (the diagonal
+// term, when `have`) followed by the spawns on `key` in increasing order of value.
+__device__ double canonical_sum_scan(bool have, double first, uint64_t key, const Rec *sp,
+                                     uint32_t ns, bool *bad) {
   double sum = first;
   constexpr int K = 8;
   uint64_t ob[K];
-  int n = 0, idx = head;
-  while (idx >= 0 && n < K) {
-    if (idx >= ns) { *bad = true; return sum; }
-    ob[n++] = ordered_bits(bitsd(sval[idx]));
-    idx = snext[idx];
+  int n = 0;
+  bool more = false;
+  for (uint32_t j = 0; j < ns; ++j) {
+    if (sp[j].key != key) continue;
+    if (n < K) ob[n++] = ordered_bits(bitsd(sp[j].val));
+    else { more = true; break; }
   }
-  if (idx < 0) {
+  if (!more) {
     for (int i = 1; i < n; ++i) {
-      uint64_t v = ob[i];
+      const uint64_t v = ob[i];
       int k = i - 1;
       while (k >= 0 && ob[k] > v) { ob[k + 1] = ob[k]; --k; }
       ob[k + 1] = v;
     }
     for (int i = 0; i < n; ++i) {
-      double v = from_ordered(ob[i]);
+      const double v = from_ordered(ob[i]);
       sum = have ? sum + v : v;
       have = true;
     }
@@ -458,18 +532,18 @@ __device__ double canonical_sum(bool have, double first, int head, const uint64_
   }
   uint64_t last = 0;
   bool any_last = false;
-  for (int round = 0; round <= ns; ++round) {
+  for (uint32_t round = 0; round <= ns; ++round) {
     uint64_t best = ~0ull;
-    int cnt = 0, steps = 0;
-    for (int i = head; i >= 0; i = snext[i]) {
-      if (i >= ns || ++steps > ns) { *bad = true; return sum; }
-      uint64_t o = ordered_bits(bitsd(sval[i]));
+    uint32_t cnt = 0;
+    for (uint32_t j = 0; j < ns; ++j) {
+      if (sp[j].key != key) continue;
+      const uint64_t o = ordered_bits(bitsd(sp[j].val));
       if (any_last && o <= last) continue;
       if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
     }
     if (cnt == 0) return sum;
-    double v = from_ordered(best);
-    for (int c = 0; c < cnt; ++c) { sum = have ? sum + v : v; have = true; }
+    const double v = from_ordered(best);
+    for (uint32_t c = 0; c < cnt; ++c) { sum = have ? sum + v : v; have = true; }
     last = best;
     any_last = true;
   }
@@ -477,24 +551,34 @@ __device__ double canonical_sum(bool have, double first, int head, const uint64_
   return sum;
 }
 
-__device__ __forceinline__ int64_t list_sum_int(int head, const uint64_t *sval, const int *snext,
-                                                int ns, bool *bad) {
-  int64_t tot = 0;
-  int steps = 0;
-  for (int i = head; i >= 0; i = snext[i]) {
-    if (i >= ns || ++steps > ns) { *bad = true; break; }
-    tot += (int64_t)sval[i];
+// Diagonal step of one walker (diagonal_step!, spawning.jl:73-77), float walkers.
+template <int KIND>
+__device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t rep,
+                                             const Rec &rec) {
+  double res = op_diagonal<KIND>(a, r, rec.key) * bitsd(rec.val);
+  if (a.has_proj) {
+    const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
+    res = project_threshold(res, a.proj_threshold, u53_of(rr));
   }
-  return tot;
+  return res;
 }
 
-__device__ __forceinline__ int table_lookup(uint64_t key, const uint64_t *tkey, uint32_t T) {
-  uint32_t slot = (uint32_t)mix64(key) & (T - 1);
+// Slot of `key` in the table, claimed if the key is new; -1 if the table is full.
+__device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, uint64_t key,
+                                            uint64_t hsh, bool &claimed) {
+  uint32_t sl = (uint32_t)hsh & (T - 1);
+  claimed = false;
   for (uint32_t p = 0; p < T; ++p) {
-    uint64_t k = tkey[slot];
-    if (k == key) return (int)slot;
-    if (k == EMPTY_KEY) return -1;
-    slot = (slot + 1) & (T - 1);
+    const uint64_t k = *(volatile uint64_t *)&tkey[sl];
+    if (k == key) return (int)sl;
+    if (k == EMPTY_KEY) {
+      const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
+                                               (unsigned long long)EMPTY_KEY,
+                                               (unsigned long long)key);
+      if (old == EMPTY_KEY) { claimed = true; return (int)sl; }
+      if (old == key) return (int)sl;
+    }
+    sl = (sl + 1) & (T - 1);
   }
   return -1;
 }
@@ -552,46 +636,50 @@ __device__ __forceinline__ bool finalize_entry(const StepArgs &a, int r, uint64_
 // Warp-synchronous append of the kept entries to the target slab of bucket gb.
 __device__ __forceinline__ void warp_emit(const StepArgs &a, int gb, bool keep, uint64_t key,
                                           uint64_t vb, uint32_t &out) {
-  const int lane = threadIdx.x & 31;
   const uint32_t m = __ballot_sync(0xffffffffu, keep);
-  const uint32_t pos = out + __popc(m & ((1u << lane) - 1));
+  const uint32_t pos = out + __popc(m & lanemask_lt());
   if (keep && pos < a.capv) a.v_out[(size_t)gb * a.capv + pos] = Rec{key, vb};
   out += __popc(m);
 }
 
 __device__ __forceinline__ void flush_ann_acc(const StepArgs &a, int r, AnnAcc &acc) {
-  U128 nfx = warp_sum128(acc.norm);
-  long long l = warp_sum(acc.len), lb = warp_sum(acc.len_before);
-  long long cl = warp_sum(acc.clones), de = warp_sum(acc.deaths), zo = warp_sum(acc.zombies);
+  const U128 nfx = warp_sum128(acc.norm), sfx = warp_sum128(acc.spawn_fx);
+  const long long l = warp_sum(acc.len), lb = warp_sum(acc.len_before);
+  const long long cl = warp_sum(acc.clones), de = warp_sum(acc.deaths), zo = warp_sum(acc.zombies);
+  const long long si = warp_sum(acc.spawns_i), rc = warp_sum(acc.records);
   if ((threadIdx.x & 31) == 0) {
     DevStats &st = a.stats[r];
     atomic_add128(&st.norm_lo, &st.norm_hi, nfx);
+    atomic_add128(&st.spawn_lo, &st.spawn_hi, sfx);
     atomic_add_ll(&st.len, l);
     atomic_add_ll(&st.len_before, lb);
     atomic_add_ll(&st.clones, cl);
     atomic_add_ll(&st.deaths, de);
     atomic_add_ll(&st.zombies, zo);
+    atomic_add_ll(&st.spawns_int, si);
+    atomic_add_ll(&st.spawn_records, rc);
   }
   acc = AnnAcc{};
 }
 
-// Per-warp shared memory: table keys [tmax], spawn values [caps], table heads [tmax],
-// list links [caps], slots first claimed [caps].
-__host__ __device__ inline size_t ann_warp_smem(uint32_t tmax, uint32_t caps) {
-  return (size_t)tmax * 12 + (size_t)caps * 16;
-}
-
+// One warp per bucket.  The bucket's addresses go into a T-slot table: first the source
+// walkers after their diagonal step, then the spawns, each contribution added exactly into
+// the address's 128-bit fixed-point sum by shared-memory atomics.  The occupied slots are
+// then finalized (rounding, compression, statistics) and appended to the target slab.  A
+// bucket with more addresses than the table holds is processed in passes, each taking the
+// addresses whose hash bits 16.. select it; a pass that still overflows is split in two.
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(WARPS * 32) k_annihilate(StepArgs a, int nb_total) {
+__global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t caps = a.caps, tmax = a.tsize;
-  unsigned char *mine = smem + (size_t)w * ann_warp_smem(tmax, caps);
+  const uint32_t T = a.tsize;
+  unsigned char *mine = smem + (size_t)w * ann_warp_smem(T);
   uint64_t *tkey = reinterpret_cast<uint64_t *>(mine);
-  uint64_t *sval = tkey + tmax;
-  int *thead = reinterpret_cast<int *>(sval + caps);
-  int *snext = thead + tmax;
-  int *snew = snext + caps;
+  unsigned long long *tlo = reinterpret_cast<unsigned long long *>(tkey + T);
+  unsigned long long *thi = tlo + T;
+  uint32_t *tinfo = reinterpret_cast<uint32_t *>(thi + T);
+  uint16_t *slist = reinterpret_cast<uint16_t *>(tinfo + T);
+  const uint32_t lim = T - 32;      // a round of 32 insertions starts only below this fill
   AnnAcc acc{};
   int cur_r = -1;
   bool bad = false;
@@ -603,115 +691,170 @@ __global__ void __launch_bounds__(WARPS * 32) k_annihilate(StepArgs a, int nb_to
     }
     const uint32_t rep = a.replica_base + (uint32_t)r;
     const uint32_t nsp = a.scount[gb];
-    const uint32_t ns = nsp < caps ? nsp : caps;
+    const uint32_t ns = nsp < a.caps ? nsp : a.caps;
     const uint32_t nv0 = a.cnt_in[gb];
     const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
-    uint32_t T = 64;
-    while (T < 2 * ns && T < tmax) T <<= 1;
-    for (uint32_t i = lane; i < T; i += 32) { tkey[i] = EMPTY_KEY; thead[i] = -1; }
-    __syncwarp();
-    // spawns into the table; slots claimed first are listed in snew
-    uint32_t nnew = 0;
-    const Rec *sp = a.spawn + (size_t)gb * caps;
-    for (uint32_t j0 = 0; j0 < ns; j0 += 32) {
-      const uint32_t j = j0 + lane;
-      bool first = false;
-      int slot = -1;
-      if (j < ns) {
-        const Rec s = sp[j];
-        sval[j] = s.val;
-        uint32_t sl = (uint32_t)mix64(s.key) & (T - 1);
-        for (uint32_t p = 0; p < T; ++p) {
-          const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
-                                                   (unsigned long long)EMPTY_KEY,
-                                                   (unsigned long long)s.key);
-          if (old == EMPTY_KEY || old == s.key) {
-            first = old == EMPTY_KEY;
-            slot = (int)sl;
-            snext[j] = atomicExch(&thead[sl], (int)j);
-            break;
-          }
-          sl = (sl + 1) & (T - 1);
-        }
-        if (slot < 0) bad = true;
-      }
-      const uint32_t m = __ballot_sync(0xffffffffu, first);
-      if (first) snew[nnew + __popc(m & ((1u << lane) - 1))] = slot;
-      nnew += __popc(m);
-    }
-    __syncwarp();
-    uint32_t out = 0;
-    // source walkers: diagonal step (diagonal_step!, spawning.jl:73-77) + spawns on them
+    const Rec *sp = a.spawn + (size_t)gb * a.caps;
     const Rec *vbase = a.v_in + (size_t)gb * a.capv_in;
-    for (uint32_t e0 = 0; e0 < nv; e0 += 32) {
-      const uint32_t e = e0 + lane;
-      bool keep = false;
-      uint64_t key = 0, vb = 0;
-      if (e < nv) {
-        const Rec rec = vbase[e];
-        key = rec.key;
-        const double dg = op_diagonal<KIND>(a, r, key);
-        const int slot = ns ? table_lookup(key, tkey, T) : -1;
-        int head = -1;
-        if (slot >= 0) { head = thead[slot]; thead[slot] = -2; }
-        if (STYLE == STYLE_INTEGER) {
-          const int64_t v = (int64_t)rec.val;
-          const double x = dg * i2d_exact(v);
-          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
-          const int64_t res = round_stochastic(x, u53_of(rr));
-          // clones_deaths_zombies (spawning.jl:79-93)
-          const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
-          if (res > v) acc.clones += res - v;
-          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
-          else acc.deaths += (res - v) < 0 ? v - res : res - v;
-          const int64_t tot = res + list_sum_int(head, sval, snext, (int)ns, &bad);
-          keep = finalize_entry<STYLE>(a, r, key, 0.0, tot, vb, acc);
-        } else {
-          double res = dg * bitsd(rec.val);
-          if (a.has_proj) {
-            const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, key, 0);
-            res = project_threshold(res, a.proj_threshold, u53_of(rr));
-          }
-          const double tot =
-              head >= 0 ? canonical_sum(!is_zero_d(res), res, head, sval, snext, (int)ns, &bad) : res;
-          keep = finalize_entry<STYLE>(a, r, key, tot, 0, vb, acc);
-        }
-      }
-      warp_emit(a, gb, keep, key, vb, out);
+    const uint32_t need = nv + ns;   // upper bound on the bucket's distinct addresses
+    int lvl0 = 0;
+    if (need > lim) {
+      lvl0 = 1;
+      while (lvl0 < MAX_SPLIT && need > ((lim * 3 / 4) << lvl0)) ++lvl0;
     }
-    __syncwarp();
-    // addresses reached only by spawns
-    for (uint32_t i0 = 0; i0 < nnew; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      bool keep = false;
-      uint64_t key = 0, vb = 0;
-      if (i < nnew) {
-        const int slot = snew[i];
-        const int head = thead[slot];
-        key = tkey[slot];
-        if (head >= 0) {
-          if (STYLE == STYLE_INTEGER) {
-            const int64_t tot = list_sum_int(head, sval, snext, (int)ns, &bad);
-            keep = finalize_entry<STYLE>(a, r, key, 0.0, tot, vb, acc);
-          } else {
-            const double tot = canonical_sum(false, 0.0, head, sval, snext, (int)ns, &bad);
-            keep = finalize_entry<STYLE>(a, r, key, tot, 0, vb, acc);
+    int lvl = lvl0;
+    uint32_t sel = 0;
+    uint32_t out = 0;
+    for (;;) {
+      const uint32_t mask = (1u << lvl) - 1u;
+      for (uint32_t i = lane; i < T; i += 32) {
+        tkey[i] = EMPTY_KEY; tlo[i] = 0; thi[i] = 0; tinfo[i] = 0;
+      }
+      __syncwarp();
+      uint32_t nslots = 0;
+      bool fail = false;
+      PassAcc pa{};
+      // source walkers: diagonal step; their keys are distinct, each claims its own slot
+      for (uint32_t e0 = 0; e0 < nv; e0 += 32) {
+        if (nslots > lim) { fail = true; break; }
+        const uint32_t e = e0 + lane;
+        bool claimed = false, lfail = false;
+        int slot = -1;
+        if (e < nv) {
+          const Rec rec = vbase[e];
+          const uint64_t hsh = mix64(rec.key);
+          if (((uint32_t)(hsh >> 16) & mask) == sel) {
+            slot = table_insert(tkey, T, rec.key, hsh, claimed);
+            if (slot < 0) lfail = true;
+            else if (!claimed) bad = true;          // an address listed twice in the source
+            else if (STYLE == STYLE_INTEGER) {
+              const int64_t v = (int64_t)rec.val;
+              const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
+              const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
+              const int64_t res = round_stochastic(x, u53_of(rr));
+              // clones_deaths_zombies (spawning.jl:79-93)
+              const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+              if (res > v) pa.clones += res - v;
+              else if (sr != sv) { pa.deaths += v < 0 ? -v : v; pa.zombies += res < 0 ? -res : res; }
+              else pa.deaths += (res - v) < 0 ? v - res : res - v;
+              tlo[slot] = (unsigned long long)res;
+            } else {
+              const double res = diag_float<KIND>(a, r, rep, rec);
+              U128 fx;
+              uint32_t info = (e + 1) << 1;
+              if (fixed_exact(res, fx)) { tlo[slot] = fx.lo; thi[slot] = fx.hi; }
+              else info |= INFO_INEXACT;
+              tinfo[slot] = info;
+            }
           }
         }
+        const uint32_t m = __ballot_sync(0xffffffffu, claimed);
+        if (claimed) slist[nslots + __popc(m & lanemask_lt())] = (uint16_t)slot;
+        nslots += __popc(m);
+        if (__any_sync(0xffffffffu, lfail)) { fail = true; break; }
       }
-      warp_emit(a, gb, keep, key, vb, out);
+      __syncwarp();
+      // spawns: find or claim the slot, add the value
+      if (!fail) {
+        for (uint32_t j0 = 0; j0 < ns; j0 += 32) {
+          if (nslots > lim) { fail = true; break; }
+          const uint32_t j = j0 + lane;
+          bool claimed = false, lfail = false;
+          int slot = -1;
+          if (j < ns) {
+            const Rec s = sp[j];
+            const uint64_t hsh = mix64(s.key);
+            if (((uint32_t)(hsh >> 16) & mask) == sel) {
+              slot = table_insert(tkey, T, s.key, hsh, claimed);
+              if (slot < 0) {
+                lfail = true;
+              } else {
+                pa.records++;
+                if (STYLE == STYLE_INTEGER) {
+                  const int64_t k = (int64_t)s.val;
+                  pa.spawns_i += k < 0 ? -k : k;
+                  atomicAdd(&tlo[slot], (unsigned long long)k);
+                } else {
+                  const double y = bitsd(s.val);
+                  pa.spawn_fx = add128(pa.spawn_fx, fixed_of(abs_d(y)));
+                  U128 fx;
+                  if (fixed_exact(y, fx)) {
+                    const unsigned long long old = atomicAdd(&tlo[slot], fx.lo);
+                    const unsigned long long hadd = fx.hi + ((old + fx.lo < old) ? 1ull : 0ull);
+                    if (hadd) atomicAdd(&thi[slot], hadd);
+                  } else {
+                    atomicOr(&tinfo[slot], INFO_INEXACT);
+                  }
+                }
+              }
+            }
+          }
+          const uint32_t m = __ballot_sync(0xffffffffu, claimed);
+          if (claimed) slist[nslots + __popc(m & lanemask_lt())] = (uint16_t)slot;
+          nslots += __popc(m);
+          if (__any_sync(0xffffffffu, lfail)) { fail = true; break; }
+        }
+      }
+      __syncwarp();
+      if (fail) {
+        if (lvl >= MAX_SPLIT) { bad = true; break; }
+        ++lvl;                       // first half of this pass: hash bit lvl-1 clear
+        continue;
+      }
+      // finalize the pass's addresses
+      for (uint32_t i0 = 0; i0 < nslots; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        bool keep = false;
+        uint64_t key = 0, vb = 0;
+        if (i < nslots) {
+          const int slot = slist[i];
+          key = tkey[slot];
+          if (STYLE == STYLE_INTEGER) {
+            keep = finalize_entry<STYLE>(a, r, key, 0.0, (int64_t)tlo[slot], vb, acc);
+          } else {
+            const uint32_t info = tinfo[slot];
+            double fv;
+            if (info & INFO_INEXACT) {
+              bool have = false;
+              double first = 0.0;
+              const uint32_t src = info >> 1;
+              if (src) {
+                first = diag_float<KIND>(a, r, rep, vbase[src - 1]);
+                have = !is_zero_d(first);
+              }
+              fv = canonical_sum_scan(have, first, key, sp, ns, &bad);
+            } else {
+              fv = signed_fixed_to_double(U128{tlo[slot], thi[slot]});
+            }
+            keep = finalize_entry<STYLE>(a, r, key, fv, 0, vb, acc);
+          }
+        }
+        warp_emit(a, gb, keep, key, vb, out);
+      }
+      acc.spawn_fx = add128(acc.spawn_fx, pa.spawn_fx);
+      acc.clones += pa.clones; acc.deaths += pa.deaths; acc.zombies += pa.zombies;
+      acc.spawns_i += pa.spawns_i; acc.records += pa.records;
+      __syncwarp();
+      // next pass: depth first over the splits
+      while (lvl > lvl0 && ((sel >> (lvl - 1)) & 1u)) { sel &= ~(1u << (lvl - 1)); --lvl; }
+      if (lvl == lvl0) {
+        if (++sel >= (1u << lvl0)) break;
+      } else {
+        sel |= 1u << (lvl - 1);
+      }
     }
     if (lane == 0) {
       a.cnt_out[gb] = out < a.capv ? out : a.capv;
       if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
-      if (nsp > caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
+      if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
       atomicMax(&a.stats[r].max_v_bucket, out);
       atomicMax(&a.stats[r].max_spawn_bucket, nsp);
       a.scount[gb] = 0;
     }
     __syncwarp();
   }
-  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
+  if (__any_sync(0xffffffffu, bad) && lane == 0)
+    atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
   if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
 }
 
@@ -824,15 +967,18 @@ __global__ void k_offdiagonals(DevModel h, uint64_t key, int noff, uint64_t *key
 template <int KIND, int STYLE>
 static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
-  const int want = (nb_total + WARPS - 1) / WARPS;
   const int cap = ctx->num_sms * 64;
+  const int cb = a.nb_bits < 5 ? (1 << a.nb_bits) : CHUNK_BUCKETS;
+  const int want_s = (nb_total / cb + WARPS - 1) / WARPS;
+  const int grid_s = want_s < cap ? want_s : cap;
+  const int want = (nb_total + WARPS - 1) / WARPS;
   const int grid = want < cap ? want : cap;
   if (ev) cudaEventRecord(ev[0], st);
-  k_spawn<KIND, STYLE><<<grid, WARPS * 32, 0, st>>>(a, nb_total);
+  k_spawn<KIND, STYLE><<<grid_s, WARPS * 32, 0, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[1], st);
   k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  const size_t smem = WARPS * ann_warp_smem(a.tsize, a.caps);
+  const size_t smem = WARPS * ann_warp_smem(a.tsize);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_annihilate<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -133,6 +133,8 @@ struct rimu_wm {
   int dtab_n = 0;
   double *d_shift = nullptr;
   int64_t last_spawns = -1;
+  int keys_per_bucket = 64;             // expected addresses per bucket (launch shape)
+  int table_slots = 0;                  // annihilation table slots per warp (0: automatic)
   // projector
   int nproj = 0;
   uint64_t *proj_keys = nullptr;

@@ -198,6 +198,12 @@ class GPUWorkingMemory:
     def set_timing(self, enable=True):
         _lib.check(_lib.load().rimu_wm_set_timing(self.handle, int(enable)))
 
+    def set_launch_shape(self, keys_per_bucket: int = 64, table_slots: int = 0):
+        """Launch shape of the step kernels: expected addresses per bucket (16..512) and
+        annihilation table slots per warp (0 = automatic, else a power of two 64..512)."""
+        _lib.check(_lib.load().rimu_wm_set_launch_shape(self.handle, int(keys_per_bucket),
+                                                        int(table_slots)))
+
     def timing(self) -> dict:
         """Per-kernel milliseconds and algorithmic bytes accumulated since set_timing."""
         out = np.zeros(7)

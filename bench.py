@@ -186,6 +186,9 @@ def run_ours(args, ws, rank, local):
                                      max_length=int(2 * target + 100))
     sim = R.init(p)
     s = sim.states[0]
+    if args.shape:
+        kpb, slots = (int(x) for x in args.shape.split(","))
+        s.wm.set_launch_shape(kpb, slots)
     t_prep = time.time()
     prep = 0
     while prep < args.max_prep:
@@ -316,7 +319,8 @@ def run_ours(args, ws, rank, local):
                        "entries_per_step": float(np.mean(lens)) if lens else None,
                        "prep_steps": prep, "prep_seconds": round(t_prep, 2),
                        "l2": "inputs larger than L2 (walker list > 1 GB), no flush",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                       "launch_shape": args.shape or "default (1024 contributions per bucket, automatic table)"},
             "gpu_launches": 4 * args.steps,
             "roofline": roofline,
             "e2e": e2e,
@@ -430,6 +434,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-hv", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--shape", default=None,
+                    help="launch shape KEYS_PER_BUCKET,TABLE_SLOTS of the step kernels (0 slots = automatic)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

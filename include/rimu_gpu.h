@@ -171,11 +171,11 @@ int rimu_wm_timing(rimu_wm *wm, double *out7);
 
 /* Launch shape of the step kernels (no counterpart in the reference, whose walker list is a
  * hash dictionary per thread, pdvec.jl:1-120).  keys_per_bucket: the bucket count is chosen
- * so that the expected number of addresses (source walkers plus spawns) per bucket lies
- * between keys_per_bucket / 2 and keys_per_bucket; 16..512, default 64.  table_slots: slots
- * of the per-warp annihilation table, a power of two in 64..512, or 0 to size it from the
- * expected bucket load; buckets that do not fit are processed in several passes.  Results
- * do not depend on either value. */
+ * so that the expected number of contributions (source walkers plus spawns) per bucket lies
+ * between keys_per_bucket / 2 and keys_per_bucket; 16..4096, default 1024.  table_slots:
+ * slots of the shared-memory table of one annihilation CTA, a power of two in 512..4096, or
+ * 0 to size it from the expected bucket load; buckets that do not fit are processed in
+ * several passes.  Results do not depend on either value. */
 int rimu_wm_set_launch_shape(rimu_wm *wm, int keys_per_bucket, int table_slots);
 
 /* One projector step target = T(source), with stats: apply_operator!(wm, target, source,

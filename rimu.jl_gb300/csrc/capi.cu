@@ -371,7 +371,7 @@ static int vec_alloc(rimu_vec *v, int nb_bits, uint32_t capv) {
 
 static uint32_t capv_for(int64_t n, int nb_bits) {
   double mu = (double)n / (double)(1ull << nb_bits);
-  uint64_t c = (uint64_t)(2.0 * mu + 8.0 * std::sqrt(mu) + 64.0);
+  uint64_t c = (uint64_t)(1.25 * mu + 8.0 * std::sqrt(mu) + 64.0);
   return round_up(c, 32);
 }
 
@@ -604,11 +604,11 @@ extern "C" int rimu_wm_set_timing(rimu_wm *w, int enable) {
 
 extern "C" int rimu_wm_set_launch_shape(rimu_wm *w, int keys_per_bucket, int table_slots) {
   if (!w) return bad("rimu_wm_set_launch_shape: NULL working memory");
-  if (keys_per_bucket < 16 || keys_per_bucket > 512)
-    return bad("rimu_wm_set_launch_shape: keys_per_bucket must be in 16..512");
+  if (keys_per_bucket < 16 || keys_per_bucket > 4096)
+    return bad("rimu_wm_set_launch_shape: keys_per_bucket must be in 16..4096");
   if (table_slots != 0 &&
-      (table_slots < 64 || table_slots > 512 || (table_slots & (table_slots - 1))))
-    return bad("rimu_wm_set_launch_shape: table_slots must be 0 or a power of two in 64..512");
+      (table_slots < 512 || table_slots > 4096 || (table_slots & (table_slots - 1))))
+    return bad("rimu_wm_set_launch_shape: table_slots must be 0 or a power of two in 512..4096");
   w->keys_per_bucket = keys_per_bucket;
   w->table_slots = table_slots;
   return RIMU_OK;
@@ -696,8 +696,8 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   int rc;
   if (p->op == RIMU_OP_TRANSITION && (rc = ensure_aoff(m, p->dt))) return rc;
 
-  // capacity planning: one warp per bucket; the bucket count keeps the expected number of
-  // addresses (source walkers plus spawns) per bucket between kKeys / 2 and kKeys
+  // capacity planning: one annihilation CTA per bucket; the bucket count keeps the expected
+  // number of contributions (source walkers plus spawns) per bucket between kKeys / 2 and kKeys
   const int64_t L = std::max<int64_t>(source->len, 1);
   const double norm = std::max(source->norm, 1.0);
   int64_t S_est;
@@ -711,7 +711,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   uint32_t heavy_cap = 0;
   int retries = 0;
   const int ndiag = m->ndiag;
-  const uint32_t kMaxCaps = 512;
+  const uint32_t kMaxCaps = 16384;
   uint32_t min_caps = 0;   // raised after a spawn-slab overflow
   for (;;) {
     if (nb_bits > 26) { g_err = "rimu_apply_operator: too many buckets needed"; return RIMU_ERR_OVERFLOW; }
@@ -761,12 +761,17 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.nrep = 1; a.nb_bits = nb_bits;
     a.capv_in = source->capv;
     a.capv = capv; a.caps = caps;
-    // per-warp table: room for the expected addresses of a bucket plus 5 sigma and one
-    // round of 32 insertions; larger buckets are processed in several passes
+    // annihilation table: room for 5/4 of the expected contributions of a bucket plus one
+    // round of insertions by all threads; fuller buckets are processed in several passes
     const double mu_k = (double)(L + S_est) / (double)nb;
-    uint32_t T = 64;
-    while ((double)T < mu_k + 5.0 * std::sqrt(mu_k) + 32.0 && T < 512) T <<= 1;
+    uint32_t T = 512;
+    while ((double)T < 1.25 * mu_k + 256.0 && T < 4096) T <<= 1;
     a.tsize = w->table_slots ? (uint32_t)w->table_slots : T;
+    // spawn chunks of about 256 source walkers per warp
+    const double mu_v = (double)L / (double)nb;
+    int cb = 1;
+    while (cb < 32 && (double)cb * mu_v < 256.0 && cb < (int)nb) cb <<= 1;
+    a.spawn_cb = cb;
     a.v_in = source->recs; a.cnt_in = source->count;
     a.v_out = target->recs; a.cnt_out = target->count;
     a.spawn = w->spawn; a.scount = w->scount;
@@ -800,7 +805,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     }
     if (st.flags & FLAG_V_OVERFLOW) {
       uint64_t want = (uint64_t)st.max_v_bucket * 5 / 4 + 64;
-      if (want > 8192) { nb_bits++; capv = 0; }
+      if (want > 65536) { nb_bits++; capv = 0; }
       else capv = std::max<uint32_t>(2 * capv, round_up(want, 32));
     }
     if (st.flags & FLAG_HEAVY_OVERFLOW) heavy_cap *= 2;

@@ -7,16 +7,16 @@
 //
 // One step (apply_operator!, src/Interfaces/dictvectors.jl:112-140):
 //   k_spawn      each warp lays the walkers of 32 consecutive buckets out as one list,
-//                evaluates their columns and deals the spawn attempts out to its lanes in
-//                work items of G units; every spawn is written straight into the slab of
+//                evaluates their columns and deals the spawn attempts out to its lanes, one
+//                attempt per lane; every spawn is written straight into the slab of
 //                its destination bucket (perform_spawns!, pdworkingmemory.jl:208-217).
 //                Columns with more than HEAVY_LIMIT units are cut into chunks.
 //   k_spawn_heavy  processes the chunks of heavy columns on all SMs.
-//   k_annihilate one warp per bucket: the source walkers (after their diagonal step) and the
-//                spawns go into a shared-memory table holding one exact 128-bit fixed-point
-//                sum per address; the sums are rounded once, threshold compression applied,
-//                statistics and the norm accumulated exactly, and the survivors written to
-//                the target slab (collect_local!/move_and_compress!,
+//   k_annihilate one CTA per bucket: the source walkers (after their diagonal step) and the
+//                spawns are linked into per-address lists of a shared-memory table; each
+//                address is summed exactly in 128-bit fixed point and rounded once, threshold
+//                compression applied, statistics and the norm accumulated exactly, and the
+//                survivors written to the target slab (collect_local!/move_and_compress!,
 //                pdworkingmemory.jl:228-273; compression.jl:18-42).
 #include <cuda_runtime.h>
 #include <cstdio>
@@ -164,9 +164,8 @@ struct SpawnAcc {
   long long attempts, exact_n, inexact_n;
 };
 
-constexpr int WARPS = 8;            // warps per CTA in the step kernels
-constexpr int G = 4;                // units (attempts or offdiagonals) per work item
-constexpr int CHUNK_BUCKETS = 32;   // buckets whose walkers one warp processes together
+constexpr int WARPS = 8;            // warps per CTA in the spawn kernel
+constexpr int CHUNK_BUCKETS = 32;   // most buckets whose walkers one warp processes together
 constexpr int BATCH = 64;           // walkers whose work items are distributed together
 
 __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk, uint64_t vb) {
@@ -182,57 +181,46 @@ __device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key,
   return column_offdiag<KIND>(h, key, chosen);
 }
 
-// Units [j0, j1) of one column, j0 a multiple of G.  Exact columns deposit val * T_{new,key}
-// for offdiagonals j+1 (spawning.jl:174-182); sampled columns draw a uniform offdiagonal per
-// attempt and deposit c * T_{new,key} (spawning.jl:232-243).  With float walkers and no
-// on-the-fly projection an attempt needs 32 random bits, so one Philox block serves the four
-// attempts 4q..4q+3.
+// Unit j of one column.  Exact columns deposit val * T_{new,key} for offdiagonal j+1
+// (spawning.jl:174-182); sampled columns draw a uniform offdiagonal for attempt j and deposit
+// c * T_{new,key} (spawning.jl:232-243).  With float walkers and no on-the-fly projection an
+// attempt needs 32 random bits: attempt j takes word j % 4 of Philox block j / 4 (each lane
+// evaluates the block of its own attempt; under SIMT this costs no extra issue slots).
 template <int KIND, int STYLE>
-__device__ __forceinline__ void spawn_units(const StepArgs &a, int r, uint64_t key, uint64_t vb,
-                                            double c, int noff, int exact, uint32_t j0,
-                                            uint32_t j1) {
+__device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, uint64_t key, uint64_t vb,
+                                           double c, int noff, int exact, uint32_t j) {
   const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
-    const double val = bitsd(vb);
-    for (uint32_t j = j0; j < j1; ++j) {
-      const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
-      if (od.prod == 0) continue;
-      double y = val * op_offdiag(a, od);
-      if (STYLE == STYLE_DSS && a.has_proj) {
-        const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
-        y = project_threshold(y, a.proj_threshold, u53_of(rr));
-      }
-      if (is_zero_d(y)) continue;
-      emit_spawn(a, r, od.key, dbits(y));
+    const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
+    if (od.prod == 0) return;
+    double y = bitsd(vb) * op_offdiag(a, od);
+    if (STYLE == STYLE_DSS && a.has_proj) {
+      const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
+      y = project_threshold(y, a.proj_threshold, u53_of(rr));
     }
+    if (is_zero_d(y)) return;
+    emit_spawn(a, r, od.key, dbits(y));
     return;
   }
   const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
-  U4 blk{0, 0, 0, 0};
-  if (grouped) blk = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j0 >> 2);
-  for (uint32_t j = j0; j < j1; ++j) {
-    U4 rr = blk;
-    uint32_t word;
-    if (grouped) {
-      const uint32_t q = j & 3;
-      word = q == 0 ? blk.x : q == 1 ? blk.y : q == 2 ? blk.z : blk.w;
-    } else {
-      rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
-      word = rr.x;
-    }
-    const int chosen = (int)uniform_index(word, (uint32_t)noff) + 1;
-    const Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
-    if (od.prod == 0) continue;
-    double y = c * op_offdiag(a, od);
-    if (STYLE == STYLE_INTEGER) {
-      const int64_t k = round_stochastic(y, u53_of(rr));
-      if (k == 0) continue;
-      emit_spawn(a, r, od.key, (uint64_t)k);
-    } else {
-      if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
-      if (is_zero_d(y)) continue;
-      emit_spawn(a, r, od.key, dbits(y));
-    }
+  const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, grouped ? j >> 2 : j);
+  uint32_t word = rr.x;
+  if (grouped) {
+    const uint32_t q = j & 3;
+    word = q == 0 ? rr.x : q == 1 ? rr.y : q == 2 ? rr.z : rr.w;
+  }
+  const int chosen = (int)uniform_index(word, (uint32_t)noff) + 1;
+  const Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
+  if (od.prod == 0) return;
+  double y = c * op_offdiag(a, od);
+  if (STYLE == STYLE_INTEGER) {
+    const int64_t k = round_stochastic(y, u53_of(rr));
+    if (k == 0) return;
+    emit_spawn(a, r, od.key, (uint64_t)k);
+  } else {
+    if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
+    if (is_zero_d(y)) return;
+    emit_spawn(a, r, od.key, dbits(y));
   }
 }
 
@@ -315,21 +303,21 @@ __device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, i
   }
 }
 
-// Each warp takes CHUNK_BUCKETS consecutive buckets of one replica, lays their walkers out
-// as one flat list and works through it BATCH walkers at a time: every lane evaluates the
-// column of one or two walkers, then the batch's work items (G units each) are dealt out to
-// the lanes by an exclusive scan and a binary search.
+// Each warp takes spawn_cb (a power of two <= CHUNK_BUCKETS) consecutive buckets of one
+// replica, lays their walkers out as one flat list and works through it BATCH walkers at a
+// time: every lane evaluates the columns of two walkers, then the batch's units (spawn
+// attempts, or offdiagonals of exact columns) are dealt out one per lane by an exclusive scan
+// and a binary search.
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(WARPS * 32, 3) k_spawn(StepArgs a, int nb_total) {
+__global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_total) {
   __shared__ uint32_t s_bpre[WARPS][CHUNK_BUCKETS + 1];
   __shared__ uint64_t s_key[WARPS][BATCH];
   __shared__ uint64_t s_val[WARPS][BATCH];
   __shared__ double s_c[WARPS][BATCH];
-  __shared__ uint32_t s_units[WARPS][BATCH];
   __shared__ uint32_t s_excl[WARPS][BATCH];
   __shared__ uint32_t s_meta[WARPS][BATCH];   // noff | exact << 31
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int cb = a.nb_bits < 5 ? (1 << a.nb_bits) : CHUNK_BUCKETS;
+  const int cb = a.spawn_cb;
   const int nchunks = nb_total / cb;
   SpawnAcc acc{};
   int cur_r = -1;
@@ -361,7 +349,7 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_spawn(StepArgs a, int nb_tota
       for (int hh = 0; hh < 2; ++hh) {
         const uint32_t f = e0 + (uint32_t)(hh * 32 + lane);
         const int slot = hh * 32 + lane;
-        uint32_t it = 0, units = 0;
+        uint32_t units = 0;
         if (f < E) {
           int bi = 0;
 #pragma unroll
@@ -385,10 +373,8 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_spawn(StepArgs a, int nb_tota
           s_c[w][slot] = c;
           s_meta[w][slot] = (uint32_t)noff | ((uint32_t)exact << 31);
           units = (uint32_t)work;
-          it = (units + G - 1) / G;
         }
-        s_units[w][slot] = units;
-        items[hh] = it;
+        items[hh] = units;
       }
       uint32_t in0 = items[0], in1 = items[1];
 #pragma unroll
@@ -407,12 +393,9 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_spawn(StepArgs a, int nb_tota
 #pragma unroll
         for (int st = 32; st >= 1; st >>= 1)
           if (s_excl[w][lo + st] <= it) lo += st;
-        const uint32_t j0 = (it - s_excl[w][lo]) * G;
-        const uint32_t ju = s_units[w][lo];
-        const uint32_t j1 = j0 + G < ju ? j0 + G : ju;
         const uint32_t meta = s_meta[w][lo];
-        spawn_units<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo],
-                                 (int)(meta & 0x7fffffffu), (int)(meta >> 31), j0, j1);
+        spawn_unit<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo],
+                                (int)(meta & 0x7fffffffu), (int)(meta >> 31), it - s_excl[w][lo]);
       }
       __syncwarp();
     }
@@ -426,15 +409,12 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
   if (nch > a.heavy_cap) nch = a.heavy_cap;
   for (uint32_t ci = blockIdx.x; ci < nch; ci += gridDim.x) {
     HeavyChunk ch = a.heavy[ci];
-    if (ch.cnt > (uint32_t)HEAVY_CHUNK || ch.rep >= (uint32_t)a.nrep || (ch.j0 & (G - 1))) {
+    if (ch.cnt > (uint32_t)HEAVY_CHUNK || ch.rep >= (uint32_t)a.nrep) {
       if (threadIdx.x == 0) atomicOr(&a.stats[0].flags, (unsigned)FLAG_TABLE);
       continue;
     }
-    for (uint32_t t = threadIdx.x * G; t < ch.cnt; t += blockDim.x * G) {
-      const uint32_t j1 = t + G < ch.cnt ? t + G : ch.cnt;
-      spawn_units<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact,
-                               ch.j0 + t, ch.j0 + j1);
-    }
+    for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x)
+      spawn_unit<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact, ch.j0 + t);
   }
 }
 
@@ -451,17 +431,19 @@ struct AnnAcc {
   long long len, len_before, clones, deaths, zombies, spawns_i, records;
 };
 
-// Statistics of one pass over a bucket; kept only if the pass completes.
+// Integer-walker statistics of one pass over a bucket; kept only if the pass completes.
 struct PassAcc {
-  U128 spawn_fx;
-  long long clones, deaths, zombies, spawns_i, records;
+  long long clones, deaths, zombies;
 };
 
-constexpr uint32_t INFO_INEXACT = 1u;   // tinfo bit 0; bits 1..31: 1 + source walker index
 constexpr int MAX_SPLIT = 16;           // at most 2^MAX_SPLIT passes over one bucket
+constexpr uint32_t NIL = 0xffffffffu;   // end of a contribution list
+constexpr int ANN_THREADS = 256;        // threads of one annihilation CTA
 
-// Per-warp table of T slots: keys, 128-bit sums (lo, hi), info words, occupied-slot list.
-__host__ __device__ inline size_t ann_warp_smem(uint32_t T) { return (size_t)T * 30; }
+// Shared memory of one annihilation CTA with T table slots and T contribution entries:
+// keys [T] u64, contribution values [T] u64, list heads [T] u32, diagonal-term markers [T]
+// u32, contribution links [T] u32, occupied-slot list [T] u16, compression queue [T] u16.
+__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 32; }
 
 __device__ __forceinline__ U128 neg128(U128 x) {
   U128 r;
@@ -470,26 +452,22 @@ __device__ __forceinline__ U128 neg128(U128 x) {
   return r;
 }
 
-// x as a two's-complement multiple of 2^-64, if it is one and |x| < 2^48.
-__device__ __forceinline__ bool fixed_exact(double x, U128 &out) {
-  const uint64_t b = dbits(x);
-  const uint64_t ab = b & 0x7fffffffffffffffull;
-  out = U128{0, 0};
+// |x| as a multiple of 2^-64, if it is one and |x| < 2^48 (then equal to fixed_of(|x|)).
+__device__ __forceinline__ bool fixed_magnitude(double x, U128 &m) {
+  const uint64_t ab = dbits(x) & 0x7fffffffffffffffull;
+  m = U128{0, 0};
   if (ab == 0) return true;
   const int e = (int)(ab >> 52);
   if (e == 0 || e >= 1023 + 48) return false;
   const uint64_t mant = (ab & lowmask(52)) | (1ull << 52);
   const int sh = e - 1075 + 64;            // |x| = mant * 2^(sh - 64), sh <= 59
-  U128 m;
   if (sh >= 0) {
     m.lo = mant << sh;
     m.hi = sh > 11 ? (mant >> (64 - sh)) : 0;
   } else {
     if (-sh >= 53 || (mant & lowmask(-sh))) return false;
     m.lo = mant >> (-sh);
-    m.hi = 0;
   }
-  out = (b >> 63) ? neg128(m) : m;
   return true;
 }
 
@@ -503,27 +481,32 @@ __device__ __forceinline__ double from_ordered(uint64_t o) {
 }
 
 // Canonical-order sum for an address with an inexact contribution: `first` (the diagonal
-// term, when `have`) followed by the spawns on `key` in increasing order of value.
-__device__ double canonical_sum_scan(bool have, double first, uint64_t key, const Rec *sp,
-                                     uint32_t ns, bool *bad) {
+// term, when `have`) followed by the spawns of the list starting at `head` (the diagonal
+// term, entry `skip`, left out) in increasing order of value.  Lists hold at most `n`
+// entries; a longer walk means a corrupted list and is cut short.
+__device__ double canonical_sum_list(bool have, double first, uint32_t head, uint32_t skip,
+                                     const uint64_t *cval, const uint32_t *cnext, uint32_t n,
+                                     bool *bad) {
   double sum = first;
   constexpr int K = 8;
   uint64_t ob[K];
-  int n = 0;
+  int k = 0;
   bool more = false;
-  for (uint32_t j = 0; j < ns; ++j) {
-    if (sp[j].key != key) continue;
-    if (n < K) ob[n++] = ordered_bits(bitsd(sp[j].val));
+  uint32_t steps = 0;
+  for (uint32_t c = head; c != NIL; c = cnext[c]) {
+    if (c >= n || ++steps > n) { *bad = true; return sum; }
+    if (c == skip) continue;
+    if (k < K) ob[k++] = ordered_bits(bitsd(cval[c]));
     else { more = true; break; }
   }
   if (!more) {
-    for (int i = 1; i < n; ++i) {
+    for (int i = 1; i < k; ++i) {
       const uint64_t v = ob[i];
-      int k = i - 1;
-      while (k >= 0 && ob[k] > v) { ob[k + 1] = ob[k]; --k; }
-      ob[k + 1] = v;
+      int j = i - 1;
+      while (j >= 0 && ob[j] > v) { ob[j + 1] = ob[j]; --j; }
+      ob[j + 1] = v;
     }
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < k; ++i) {
       const double v = from_ordered(ob[i]);
       sum = have ? sum + v : v;
       have = true;
@@ -532,18 +515,20 @@ __device__ double canonical_sum_scan(bool have, double first, uint64_t key, cons
   }
   uint64_t last = 0;
   bool any_last = false;
-  for (uint32_t round = 0; round <= ns; ++round) {
+  for (uint32_t round = 0; round <= n; ++round) {
     uint64_t best = ~0ull;
     uint32_t cnt = 0;
-    for (uint32_t j = 0; j < ns; ++j) {
-      if (sp[j].key != key) continue;
-      const uint64_t o = ordered_bits(bitsd(sp[j].val));
+    steps = 0;
+    for (uint32_t c = head; c != NIL; c = cnext[c]) {
+      if (c >= n || ++steps > n) { *bad = true; return sum; }
+      if (c == skip) continue;
+      const uint64_t o = ordered_bits(bitsd(cval[c]));
       if (any_last && o <= last) continue;
       if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
     }
     if (cnt == 0) return sum;
     const double v = from_ordered(best);
-    for (uint32_t c = 0; c < cnt; ++c) { sum = have ? sum + v : v; have = true; }
+    for (uint32_t i = 0; i < cnt; ++i) { sum = have ? sum + v : v; have = true; }
     last = best;
     any_last = true;
   }
@@ -563,10 +548,11 @@ __device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t 
   return res;
 }
 
-// Slot of `key` in the table, claimed if the key is new; -1 if the table is full.
-__device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, uint64_t key,
-                                            uint64_t hsh, bool &claimed) {
-  uint32_t sl = (uint32_t)hsh & (T - 1);
+// Slot of `key` in the table, claimed if the key is new; -1 if the table is full.  Probing
+// starts at the top bits of a multiplicative hash of the key.
+__device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, int tbits, uint64_t key,
+                                            bool &claimed) {
+  uint32_t sl = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - tbits));
   claimed = false;
   for (uint32_t p = 0; p < T; ++p) {
     const uint64_t k = *(volatile uint64_t *)&tkey[sl];
@@ -581,65 +567,6 @@ __device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, uint64_t
     sl = (sl + 1) & (T - 1);
   }
   return -1;
-}
-
-// Final value of one address: threshold compression (compression.jl:18-42), statistics, the
-// ProjectedEnergy dot products.  Returns whether the address is kept and its value bits.
-template <int STYLE>
-__device__ __forceinline__ bool finalize_entry(const StepArgs &a, int r, uint64_t key, double fv,
-                                               int64_t iv, uint64_t &vb, AnnAcc &acc) {
-  double dv;
-  if (STYLE == STYLE_INTEGER) {
-    if (iv == 0) return false;
-    acc.len_before++;
-    vb = (uint64_t)iv;
-    const uint64_t mag = (uint64_t)(iv < 0 ? -iv : iv);
-    acc.norm = add128(acc.norm, U128{0, mag});
-    acc.len++;
-    if (a.nproj == 0) return true;
-    dv = i2d_exact(iv);
-  } else {
-    if (is_zero_d(fv)) return false;
-    acc.len_before++;
-    if (a.comp_mode != 0) {
-      bool small;
-      double prob;
-      if (a.comp_mode == 1) { small = abs_lt_one(fv); prob = abs_d(fv); }
-      else { prob = abs_d(fv) / a.compression; small = prob < 1; }
-      if (small) {
-        U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, a.step, key, 0);
-        if (!bernoulli53(u53_of(rr), prob)) return false;
-        fv = signed_like(a.compression, fv);
-      }
-    }
-    vb = dbits(fv);
-    acc.norm = add128(acc.norm, fixed_of(abs_d(fv)));
-    acc.len++;
-    if (a.nproj == 0) return true;
-    dv = fv;
-  }
-  const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
-  int lo = 0, hi = a.nproj - 1;
-  while (lo <= hi) {
-    const int mid = (lo + hi) >> 1;
-    if (pk[mid] == key) {
-      const size_t o = (size_t)r * a.nproj + mid;
-      a.proj_out_v[o] = a.proj_v[o] * dv;
-      a.proj_out_h[o] = a.proj_h[o] * dv;
-      break;
-    }
-    if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
-  }
-  return true;
-}
-
-// Warp-synchronous append of the kept entries to the target slab of bucket gb.
-__device__ __forceinline__ void warp_emit(const StepArgs &a, int gb, bool keep, uint64_t key,
-                                          uint64_t vb, uint32_t &out) {
-  const uint32_t m = __ballot_sync(0xffffffffu, keep);
-  const uint32_t pos = out + __popc(m & lanemask_lt());
-  if (keep && pos < a.capv) a.v_out[(size_t)gb * a.capv + pos] = Rec{key, vb};
-  out += __popc(m);
 }
 
 __device__ __forceinline__ void flush_ann_acc(const StepArgs &a, int r, AnnAcc &acc) {
@@ -662,28 +589,77 @@ __device__ __forceinline__ void flush_ann_acc(const StepArgs &a, int r, AnnAcc &
   acc = AnnAcc{};
 }
 
-// One warp per bucket.  The bucket's addresses go into a T-slot table: first the source
-// walkers after their diagonal step, then the spawns, each contribution added exactly into
-// the address's 128-bit fixed-point sum by shared-memory atomics.  The occupied slots are
-// then finalized (rounding, compression, statistics) and appended to the target slab.  A
-// bucket with more addresses than the table holds is processed in passes, each taking the
-// addresses whose hash bits 16.. select it; a pass that still overflows is split in two.
+// Index for the lanes of a warp with `flag` set in a list whose length is *count: one
+// shared-memory atomic per warp.
+__device__ __forceinline__ uint32_t warp_append(uint32_t *count, bool flag) {
+  const uint32_t m = __ballot_sync(0xffffffffu, flag);
+  uint32_t base = 0;
+  if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  return base + __popc(m & lanemask_lt());
+}
+
+// Compression draw (compression.jl:28-42) for an address whose |value| is below the
+// threshold: kept at +-threshold with probability |value| / threshold.
+template <int STYLE>
+__device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint64_t key, double &fv) {
+  const double prob = a.comp_mode == 1 ? abs_d(fv) : abs_d(fv) / a.compression;
+  const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, a.step, key, 0);
+  if (!bernoulli53(u53_of(rr), prob)) return false;
+  fv = signed_like(a.compression, fv);
+  return true;
+}
+
+// Statistics and the ProjectedEnergy dot products of a kept address.
+template <int STYLE>
+__device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t key, double dv,
+                                             U128 mag, AnnAcc &acc) {
+  acc.norm = add128(acc.norm, mag);
+  acc.len++;
+  if (a.nproj == 0) return;
+  const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
+  int lo = 0, hi = a.nproj - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    if (pk[mid] == key) {
+      const size_t o = (size_t)r * a.nproj + mid;
+      a.proj_out_v[o] = a.proj_v[o] * dv;
+      a.proj_out_h[o] = a.proj_h[o] * dv;
+      break;
+    }
+    if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
+  }
+}
+
+// One CTA per bucket.  The bucket's contributions -- the source walkers after their
+// diagonal step and the spawns -- are dealt out to all threads: each finds or claims the
+// slot of its address in a shared-memory table and pushes itself onto the slot's list (one
+// 32-bit atomic exchange).  Each occupied slot is then finalized by one thread, which walks
+// its list adding the contributions exactly in 128-bit fixed point, rounds once, applies the
+// compression threshold and appends the survivor to the target slab; addresses below the
+// threshold are queued and drawn together afterwards, so that the random draws run on full
+// warps.  A bucket with more contributions than the table holds is processed in passes, each
+// taking the addresses whose hash bits 16.. select it; a pass that still overflows is split.
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb_total) {
+__global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ uint32_t s_nslots, s_ncon, s_out, s_fail, s_nq;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const uint32_t T = a.tsize;
-  unsigned char *mine = smem + (size_t)w * ann_warp_smem(T);
-  uint64_t *tkey = reinterpret_cast<uint64_t *>(mine);
-  unsigned long long *tlo = reinterpret_cast<unsigned long long *>(tkey + T);
-  unsigned long long *thi = tlo + T;
-  uint32_t *tinfo = reinterpret_cast<uint32_t *>(thi + T);
-  uint16_t *slist = reinterpret_cast<uint16_t *>(tinfo + T);
-  const uint32_t lim = T - 32;      // a round of 32 insertions starts only below this fill
+  uint64_t *tkey = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *cval = tkey + T;
+  uint32_t *thead = reinterpret_cast<uint32_t *>(cval + T);
+  uint32_t *tsrc = thead + T;
+  uint32_t *cnext = tsrc + T;
+  uint16_t *slist = reinterpret_cast<uint16_t *>(cnext + T);
+  uint16_t *qlist = slist + T;
+  const uint32_t lim = T - ANN_THREADS;   // a warp starts a round of insertions only below this
+  const int tbits = 31 - __clz((int)T);
+  for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; tsrc[i] = 0; }
   AnnAcc acc{};
   int cur_r = -1;
   bool bad = false;
-  for (int gb = blockIdx.x * WARPS + w; gb < nb_total; gb += gridDim.x * WARPS) {
+  for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
     const int r = gb >> a.nb_bits;
     if (r != cur_r) {
       if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
@@ -696,7 +672,8 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb
     const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
     const Rec *sp = a.spawn + (size_t)gb * a.caps;
     const Rec *vbase = a.v_in + (size_t)gb * a.capv_in;
-    const uint32_t need = nv + ns;   // upper bound on the bucket's distinct addresses
+    Rec *vout = a.v_out + (size_t)gb * a.capv;
+    const uint32_t need = nv + ns;   // contributions: also an upper bound on the addresses
     int lvl0 = 0;
     if (need > lim) {
       lvl0 = 1;
@@ -704,137 +681,196 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb
     }
     int lvl = lvl0;
     uint32_t sel = 0;
-    uint32_t out = 0;
+    if (tid == 0) s_out = 0;
     for (;;) {
       const uint32_t mask = (1u << lvl) - 1u;
-      for (uint32_t i = lane; i < T; i += 32) {
-        tkey[i] = EMPTY_KEY; tlo[i] = 0; thi[i] = 0; tinfo[i] = 0;
-      }
-      __syncwarp();
-      uint32_t nslots = 0;
-      bool fail = false;
+      if (tid == 0) { s_nslots = 0; s_ncon = 0; s_fail = 0; s_nq = 0; }
+      __syncthreads();
       PassAcc pa{};
-      // source walkers: diagonal step; their keys are distinct, each claims its own slot
-      for (uint32_t e0 = 0; e0 < nv; e0 += 32) {
-        if (nslots > lim) { fail = true; break; }
-        const uint32_t e = e0 + lane;
-        bool claimed = false, lfail = false;
+      // ---- every contribution of this pass onto the list of its address ----
+      for (uint32_t f0 = (uint32_t)w * 32; f0 < need; f0 += ANN_THREADS) {
+        const uint32_t filled = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_nslots, 0);
+        const uint32_t used = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_ncon, 0);
+        const uint32_t failed = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_fail, 0);
+        if (failed) break;
+        if (filled > lim || used > lim) { if (lane == 0) atomicExch(&s_fail, 1u); break; }
+        const uint32_t f = f0 + lane;
+        bool add = false, claimed = false, lfail = false, src = false;
         int slot = -1;
-        if (e < nv) {
-          const Rec rec = vbase[e];
-          const uint64_t hsh = mix64(rec.key);
-          if (((uint32_t)(hsh >> 16) & mask) == sel) {
-            slot = table_insert(tkey, T, rec.key, hsh, claimed);
-            if (slot < 0) lfail = true;
-            else if (!claimed) bad = true;          // an address listed twice in the source
-            else if (STYLE == STYLE_INTEGER) {
-              const int64_t v = (int64_t)rec.val;
-              const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
-              const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
-              const int64_t res = round_stochastic(x, u53_of(rr));
-              // clones_deaths_zombies (spawning.jl:79-93)
-              const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
-              if (res > v) pa.clones += res - v;
-              else if (sr != sv) { pa.deaths += v < 0 ? -v : v; pa.zombies += res < 0 ? -res : res; }
-              else pa.deaths += (res - v) < 0 ? v - res : res - v;
-              tlo[slot] = (unsigned long long)res;
+        uint64_t vbits = 0;
+        if (f < need) {
+          src = f < nv;
+          const Rec rec = src ? vbase[f] : sp[f - nv];
+          if (lvl == 0 || ((uint32_t)(mix64(rec.key) >> 16) & mask) == sel) {
+            slot = table_insert(tkey, T, tbits, rec.key, claimed);
+            if (slot < 0) {
+              lfail = true;
             } else {
-              const double res = diag_float<KIND>(a, r, rep, rec);
-              U128 fx;
-              uint32_t info = (e + 1) << 1;
-              if (fixed_exact(res, fx)) { tlo[slot] = fx.lo; thi[slot] = fx.hi; }
-              else info |= INFO_INEXACT;
-              tinfo[slot] = info;
-            }
-          }
-        }
-        const uint32_t m = __ballot_sync(0xffffffffu, claimed);
-        if (claimed) slist[nslots + __popc(m & lanemask_lt())] = (uint16_t)slot;
-        nslots += __popc(m);
-        if (__any_sync(0xffffffffu, lfail)) { fail = true; break; }
-      }
-      __syncwarp();
-      // spawns: find or claim the slot, add the value
-      if (!fail) {
-        for (uint32_t j0 = 0; j0 < ns; j0 += 32) {
-          if (nslots > lim) { fail = true; break; }
-          const uint32_t j = j0 + lane;
-          bool claimed = false, lfail = false;
-          int slot = -1;
-          if (j < ns) {
-            const Rec s = sp[j];
-            const uint64_t hsh = mix64(s.key);
-            if (((uint32_t)(hsh >> 16) & mask) == sel) {
-              slot = table_insert(tkey, T, s.key, hsh, claimed);
-              if (slot < 0) {
-                lfail = true;
-              } else {
-                pa.records++;
+              add = true;
+              vbits = rec.val;
+              if (src) {
+                // diagonal step of a source walker
                 if (STYLE == STYLE_INTEGER) {
-                  const int64_t k = (int64_t)s.val;
-                  pa.spawns_i += k < 0 ? -k : k;
-                  atomicAdd(&tlo[slot], (unsigned long long)k);
+                  const int64_t v = (int64_t)rec.val;
+                  const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
+                  const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
+                  const int64_t res = round_stochastic(x, u53_of(rr));
+                  // clones_deaths_zombies (spawning.jl:79-93)
+                  const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+                  if (res > v) pa.clones += res - v;
+                  else if (sr != sv) { pa.deaths += v < 0 ? -v : v; pa.zombies += res < 0 ? -res : res; }
+                  else pa.deaths += (res - v) < 0 ? v - res : res - v;
+                  vbits = (uint64_t)res;
                 } else {
-                  const double y = bitsd(s.val);
-                  pa.spawn_fx = add128(pa.spawn_fx, fixed_of(abs_d(y)));
-                  U128 fx;
-                  if (fixed_exact(y, fx)) {
-                    const unsigned long long old = atomicAdd(&tlo[slot], fx.lo);
-                    const unsigned long long hadd = fx.hi + ((old + fx.lo < old) ? 1ull : 0ull);
-                    if (hadd) atomicAdd(&thi[slot], hadd);
-                  } else {
-                    atomicOr(&tinfo[slot], INFO_INEXACT);
-                  }
+                  vbits = dbits(diag_float<KIND>(a, r, rep, rec));
                 }
               }
             }
           }
-          const uint32_t m = __ballot_sync(0xffffffffu, claimed);
-          if (claimed) slist[nslots + __popc(m & lanemask_lt())] = (uint16_t)slot;
-          nslots += __popc(m);
-          if (__any_sync(0xffffffffu, lfail)) { fail = true; break; }
         }
+        const uint32_t c = warp_append(&s_ncon, add);
+        if (add) {
+          if (c < T) {
+            cval[c] = vbits;
+            cnext[c] = atomicExch(&thead[slot], c);
+            if (src) tsrc[slot] = c + 1;
+          } else {
+            lfail = true;
+          }
+        }
+        const uint32_t pos = warp_append(&s_nslots, claimed);
+        if (claimed && pos < T) slist[pos] = (uint16_t)slot;
+        if (__any_sync(0xffffffffu, lfail)) { if (lane == 0) atomicExch(&s_fail, 1u); break; }
       }
-      __syncwarp();
+      __syncthreads();
+      const bool fail = s_fail != 0;
+      const uint32_t nslots = s_nslots < T ? s_nslots : T;
+      const uint32_t ncon = s_ncon < T ? s_ncon : T;
+      if (!fail) {
+        // ---- finalize: exact sum, compression threshold, statistics, output ----
+        for (uint32_t i0 = (uint32_t)w * 32; i0 < nslots; i0 += ANN_THREADS) {
+          const uint32_t i = i0 + lane;
+          bool keep = false, queue = false;
+          uint64_t key = 0, vb = 0;
+          int slot = 0;
+          if (i < nslots) {
+            slot = slist[i];
+            key = tkey[slot];
+            const uint32_t head = thead[slot];
+            const uint32_t dsrc = tsrc[slot];          // 1 + index of the diagonal term
+            uint32_t steps = 0;
+            if (STYLE == STYLE_INTEGER) {
+              int64_t iv = 0;
+              for (uint32_t c = head; c != NIL; c = cnext[c]) {
+                if (c >= ncon || ++steps > ncon) { bad = true; break; }
+                const int64_t k = (int64_t)cval[c];
+                iv += k;
+                if (c + 1 != dsrc) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
+              }
+              if (iv != 0) {
+                acc.len_before++;
+                keep = true;
+                vb = (uint64_t)iv;
+                const uint64_t mag = (uint64_t)(iv < 0 ? -iv : iv);
+                account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, mag}, acc);
+              }
+            } else {
+              // One or two contributions: a single IEEE addition is correctly rounded, so it
+              // equals both the exact fixed-point sum and the canonical-order sum.
+              double fv;
+              const uint32_t c1 = head < ncon ? cnext[head] : NIL;
+              if (head < ncon && (c1 == NIL || (c1 < ncon && cnext[c1] == NIL))) {
+                const double y0 = bitsd(cval[head]);
+                if (head + 1 != dsrc) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
+                fv = y0;
+                if (c1 != NIL) {
+                  const double y1 = bitsd(cval[c1]);
+                  if (c1 + 1 != dsrc) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
+                  fv = __dadd_rn(y0, y1);
+                }
+              } else {
+                U128 sum{0, 0};
+                bool exact = true;
+                for (uint32_t c = head; c != NIL; c = cnext[c]) {
+                  if (c >= ncon || ++steps > ncon) { bad = true; break; }
+                  const uint64_t v = cval[c];
+                  U128 m;
+                  const bool ex = fixed_magnitude(bitsd(v), m);
+                  if (c + 1 != dsrc) {
+                    acc.records++;
+                    acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
+                  }
+                  exact = exact && ex;
+                  sum = add128(sum, (v >> 63) ? neg128(m) : m);
+                }
+                if (exact) {
+                  fv = signed_fixed_to_double(sum);
+                } else {
+                  const double first = dsrc ? bitsd(cval[dsrc - 1]) : 0.0;
+                  fv = canonical_sum_list(dsrc && !is_zero_d(first), first, head,
+                                          dsrc ? dsrc - 1 : NIL, cval, cnext, ncon, &bad);
+                }
+              }
+              vb = dbits(fv);
+              if (!is_zero_d(fv)) {
+                acc.len_before++;
+                bool small = false;
+                if (a.comp_mode == 1) small = abs_lt_one(fv);
+                else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
+                if (small) {
+                  queue = true;
+                } else {
+                  keep = true;
+                  account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+                }
+              }
+            }
+          }
+          const uint32_t pos = warp_append(&s_out, keep);
+          if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+          if (STYLE != STYLE_INTEGER) {
+            const uint32_t q = warp_append(&s_nq, queue);
+            if (queue) {
+              // the slot's list head and marker were read above: keep the value there
+              qlist[q] = (uint16_t)slot;
+              thead[slot] = (uint32_t)vb;
+              tsrc[slot] = (uint32_t)(vb >> 32);
+            }
+          }
+        }
+        if (STYLE != STYLE_INTEGER && a.comp_mode != 0) {
+          __syncthreads();
+          const uint32_t nq = s_nq;
+          for (uint32_t i0 = (uint32_t)w * 32; i0 < nq; i0 += ANN_THREADS) {
+            const uint32_t i = i0 + lane;
+            bool keep = false;
+            uint64_t key = 0;
+            double fv = 0.0;
+            if (i < nq) {
+              const int slot = qlist[i];
+              key = tkey[slot];
+              fv = bitsd(((uint64_t)tsrc[slot] << 32) | thead[slot]);
+              keep = compress_draw<STYLE>(a, r, key, fv);
+              if (keep) account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+            }
+            const uint32_t pos = warp_append(&s_out, keep);
+            if (keep && pos < a.capv) vout[pos] = Rec{key, dbits(fv)};
+          }
+        }
+        acc.clones += pa.clones; acc.deaths += pa.deaths; acc.zombies += pa.zombies;
+      }
+      __syncthreads();
+      // ---- clear the slots this pass used ----
+      for (uint32_t i = tid; i < nslots; i += ANN_THREADS) {
+        const int slot = slist[i];
+        tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
+      }
+      __syncthreads();
       if (fail) {
         if (lvl >= MAX_SPLIT) { bad = true; break; }
         ++lvl;                       // first half of this pass: hash bit lvl-1 clear
         continue;
       }
-      // finalize the pass's addresses
-      for (uint32_t i0 = 0; i0 < nslots; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        bool keep = false;
-        uint64_t key = 0, vb = 0;
-        if (i < nslots) {
-          const int slot = slist[i];
-          key = tkey[slot];
-          if (STYLE == STYLE_INTEGER) {
-            keep = finalize_entry<STYLE>(a, r, key, 0.0, (int64_t)tlo[slot], vb, acc);
-          } else {
-            const uint32_t info = tinfo[slot];
-            double fv;
-            if (info & INFO_INEXACT) {
-              bool have = false;
-              double first = 0.0;
-              const uint32_t src = info >> 1;
-              if (src) {
-                first = diag_float<KIND>(a, r, rep, vbase[src - 1]);
-                have = !is_zero_d(first);
-              }
-              fv = canonical_sum_scan(have, first, key, sp, ns, &bad);
-            } else {
-              fv = signed_fixed_to_double(U128{tlo[slot], thi[slot]});
-            }
-            keep = finalize_entry<STYLE>(a, r, key, fv, 0, vb, acc);
-          }
-        }
-        warp_emit(a, gb, keep, key, vb, out);
-      }
-      acc.spawn_fx = add128(acc.spawn_fx, pa.spawn_fx);
-      acc.clones += pa.clones; acc.deaths += pa.deaths; acc.zombies += pa.zombies;
-      acc.spawns_i += pa.spawns_i; acc.records += pa.records;
-      __syncwarp();
       // next pass: depth first over the splits
       while (lvl > lvl0 && ((sel >> (lvl - 1)) & 1u)) { sel &= ~(1u << (lvl - 1)); --lvl; }
       if (lvl == lvl0) {
@@ -843,7 +879,8 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb
         sel |= 1u << (lvl - 1);
       }
     }
-    if (lane == 0) {
+    if (tid == 0) {
+      const uint32_t out = s_out;
       a.cnt_out[gb] = out < a.capv ? out : a.capv;
       if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
       if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
@@ -851,7 +888,6 @@ __global__ void __launch_bounds__(WARPS * 32, 3) k_annihilate(StepArgs a, int nb
       atomicMax(&a.stats[r].max_spawn_bucket, nsp);
       a.scount[gb] = 0;
     }
-    __syncwarp();
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0)
     atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
@@ -968,24 +1004,23 @@ template <int KIND, int STYLE>
 static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
   const int cap = ctx->num_sms * 64;
-  const int cb = a.nb_bits < 5 ? (1 << a.nb_bits) : CHUNK_BUCKETS;
-  const int want_s = (nb_total / cb + WARPS - 1) / WARPS;
+  const int want_s = (nb_total / a.spawn_cb + WARPS - 1) / WARPS;
   const int grid_s = want_s < cap ? want_s : cap;
-  const int want = (nb_total + WARPS - 1) / WARPS;
-  const int grid = want < cap ? want : cap;
+  const int cap_a = ctx->num_sms * 3;                 // resident annihilation CTAs
+  const int grid = nb_total < cap_a ? nb_total : cap_a;
   if (ev) cudaEventRecord(ev[0], st);
   k_spawn<KIND, STYLE><<<grid_s, WARPS * 32, 0, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[1], st);
   k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  const size_t smem = WARPS * ann_warp_smem(a.tsize);
+  const size_t smem = ann_smem(a.tsize);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_annihilate<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
     attr_set = true;
   }
-  k_annihilate<KIND, STYLE><<<grid, WARPS * 32, smem, st>>>(a, nb_total);
+  k_annihilate<KIND, STYLE><<<grid, ANN_THREADS, smem, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[3], st);
   return rimu_cuda_check(cudaGetLastError(), "step kernels");
 }

@@ -62,7 +62,8 @@ struct StepArgs {
   int nrep;
   int nb_bits;
   uint32_t capv_in;           // slab capacity of the source list
-  uint32_t capv, caps, tsize; // target slab, spawn slab, hash table size
+  uint32_t capv, caps, tsize; // target slab, spawn slab, annihilation table slots
+  int spawn_cb;               // buckets per warp chunk in k_spawn (power of two <= 32)
   const Rec *v_in;
   const uint32_t *cnt_in;
   Rec *v_out;
@@ -133,8 +134,8 @@ struct rimu_wm {
   int dtab_n = 0;
   double *d_shift = nullptr;
   int64_t last_spawns = -1;
-  int keys_per_bucket = 64;             // expected addresses per bucket (launch shape)
-  int table_slots = 0;                  // annihilation table slots per warp (0: automatic)
+  int keys_per_bucket = 1024;           // expected contributions per bucket (launch shape)
+  int table_slots = 0;                  // annihilation table slots per CTA (0: automatic)
   // projector
   int nproj = 0;
   uint64_t *proj_keys = nullptr;

@@ -198,9 +198,9 @@ class GPUWorkingMemory:
     def set_timing(self, enable=True):
         _lib.check(_lib.load().rimu_wm_set_timing(self.handle, int(enable)))
 
-    def set_launch_shape(self, keys_per_bucket: int = 64, table_slots: int = 0):
-        """Launch shape of the step kernels: expected addresses per bucket (16..512) and
-        annihilation table slots per warp (0 = automatic, else a power of two 64..512)."""
+    def set_launch_shape(self, keys_per_bucket: int = 1024, table_slots: int = 0):
+        """Launch shape of the step kernels: expected contributions per bucket (16..4096) and
+        annihilation table slots per CTA (0 = automatic, else a power of two 512..4096)."""
         _lib.check(_lib.load().rimu_wm_set_launch_shape(self.handle, int(keys_per_bucket),
                                                         int(table_slots)))
 

@@ -133,14 +133,14 @@ def test_mul_plain_hamiltonian_matches_sparse_matrix():
     assert np.allclose(got, want, rtol=1e-13, atol=1e-13)
 
 
-SHAPES = [(64, 0), (16, 0), (512, 64), (256, 128), (32, 512)]
+SHAPES = [(1024, 0), (16, 0), (4096, 512), (256, 1024), (64, 4096)]
 
 
 @pytest.mark.parametrize("kpb,slots", SHAPES, ids=[f"k{k}-t{t}" for k, t in SHAPES])
 def test_launch_shapes_give_identical_results(kpb, slots):
-    """Bucket count and table size change only the launch shape: (512, 64) puts several
-    hundred addresses into a 64-slot table, so buckets run in many passes and passes that
-    still overflow are split."""
+    """Bucket count and table size change only the launch shape: (4096, 512) puts a few
+    thousand contributions into a 512-slot table, so buckets run in many passes and passes
+    that still overflow are split."""
     h = R.HubbardReal1D(R.near_uniform(R.BoseFS, 12, 12), u=2.0)
     m = oracle_model(h)
     keys = O.basis(m)[:20000]
@@ -157,7 +157,7 @@ def test_launch_shapes_give_identical_results(kpb, slots):
         assert_same_step(g, o, style)
 
 
-@pytest.mark.parametrize("slots", [0, 64])
+@pytest.mark.parametrize("slots", [0, 512])
 def test_inexact_contributions_follow_canonical_order(slots):
     """Amplitudes from 1e-15 to 1e3 on the whole 462-state basis: most addresses receive a
     contribution that is not a multiple of 2^-64 and more than eight spawns, so their sums
@@ -169,7 +169,7 @@ def test_inexact_contributions_follow_canonical_order(slots):
     vals = rng.choice([-1.0, 1.0], len(keys)) * 10.0 ** rng.uniform(-15, 3, len(keys))
     style = R.IsDeterministic()
     wm = R.GPUWorkingMemory(SEED)
-    wm.set_launch_shape(64, slots)
+    wm.set_launch_shape(1024, slots)
     g = gpu_step(h, style, keys, vals, 0.05, 1.0, SEED, 2, wm=wm)
     o = O.step(m, oracle_params(style, 0.05, 1.0, SEED, 2), keys, vals)
     assert_same_step(g, o, style)
@@ -177,6 +177,6 @@ def test_inexact_contributions_follow_canonical_order(slots):
 
 def test_launch_shape_rejects_bad_values():
     wm = R.GPUWorkingMemory(SEED)
-    for kpb, slots in ((8, 0), (1024, 0), (64, 96), (64, 32), (64, 1024)):
+    for kpb, slots in ((8, 0), (8192, 0), (64, 96), (64, 256), (64, 8192)):
         with pytest.raises(R.RimuError):
             wm.set_launch_shape(kpb, slots)

@@ -4,8 +4,9 @@
 Workload (default): the large plain FCIQMC configuration -- HubbardReal1D, periodic, M = N = 20
 (BoseFS in 39 bits of one 64-bit word), u = 4, t = 1, IsDynamicSemistochastic with threshold
 1.0 (late ThresholdCompression), target walker norm 1e8, dt = 1e-3, DoubleLogUpdate, seed
-0x5EED.  The population is grown from the unit-filling start address (untimed preparation),
-then W warm-up steps and K timed steps are run through rimu_apply_operator.
+0x5EED.  The population is grown from the unit-filling start address and equilibrated for
+2 000 untimed steps in all (the configuration's equilibration), then W warm-up steps and K
+timed steps are run through rimu_apply_operator.
 
 A "step" is one projector step of the whole walker list (spawn, annihilation, compression,
 norm).  value = sum over timed steps of the walker number (1-norm) / device time.  The walker
@@ -191,10 +192,12 @@ def run_ours(args, ws, rank, local):
         s.wm.set_launch_shape(kpb, slots)
     t_prep = time.time()
     prep = 0
+    # growth to the target norm, then equilibration: the list keeps spreading over the
+    # Hilbert space (its length grows) long after the norm has reached the target
     while prep < args.max_prep:
         sim.step_()
         prep += 1
-        if s.wm.last_stats["norm"] >= 0.9 * target and prep >= 50:
+        if s.wm.last_stats["norm"] >= 0.9 * target and prep >= max(50, args.equil):
             break
     for _ in range(args.warmup):
         sim.step_()
@@ -318,6 +321,7 @@ def run_ours(args, ws, rank, local):
                        "walkers_per_step": walker_steps / args.steps / ws,
                        "entries_per_step": float(np.mean(lens)) if lens else None,
                        "prep_steps": prep, "prep_seconds": round(t_prep, 2),
+                       "equilibration": f"{prep} untimed steps from the unit-filling start address",
                        "l2": "inputs larger than L2 (walker list > 1 GB), no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "launch_shape": args.shape or "default (1024 contributions per bucket, automatic table)"},
@@ -428,6 +432,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--target", type=float, default=1e8)
     ap.add_argument("--max-prep", type=int, default=4000)
+    ap.add_argument("--equil", type=int, default=2000,
+                    help="untimed steps (growth + equilibration) before the warm-up steps")
     ap.add_argument("--cpu-sample", type=float, default=2e4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--traffic", type=float, default=None)

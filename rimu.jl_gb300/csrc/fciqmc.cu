@@ -643,7 +643,9 @@ __device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t 
 template <int KIND, int STYLE>
 __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t s_nslots, s_ncon, s_out, s_fail, s_nq;
+  // per pass parity: occupied slots, contributions, overflow flag, compression queue length
+  __shared__ uint32_t s_cnt[2][4];
+  __shared__ uint32_t s_out;            // entries written to the target slab of the bucket
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const uint32_t T = a.tsize;
   uint64_t *tkey = reinterpret_cast<uint64_t *>(smem);
@@ -656,6 +658,13 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
   const uint32_t lim = T - ANN_THREADS;   // a warp starts a round of insertions only below this
   const int tbits = 31 - __clz((int)T);
   for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; tsrc[i] = 0; }
+  if (tid < 8) s_cnt[tid >> 2][tid & 3] = 0;
+  if (tid == 0) s_out = 0;
+  __syncthreads();
+  // Three barriers per pass: after the insertions, before the compression draws and at the
+  // end.  Each thread clears the slots it finalizes, and the counters of a pass are zeroed
+  // during the next pass (they alternate by pass parity).
+  int par = 0;
   AnnAcc acc{};
   int cur_r = -1;
   bool bad = false;
@@ -681,19 +690,18 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
     }
     int lvl = lvl0;
     uint32_t sel = 0;
-    if (tid == 0) s_out = 0;
     for (;;) {
       const uint32_t mask = (1u << lvl) - 1u;
-      if (tid == 0) { s_nslots = 0; s_ncon = 0; s_fail = 0; s_nq = 0; }
-      __syncthreads();
+      uint32_t *const s_nslots = &s_cnt[par][0], *const s_ncon = &s_cnt[par][1];
+      uint32_t *const s_fail = &s_cnt[par][2], *const s_nq = &s_cnt[par][3];
       PassAcc pa{};
       // ---- every contribution of this pass onto the list of its address ----
       for (uint32_t f0 = (uint32_t)w * 32; f0 < need; f0 += ANN_THREADS) {
-        const uint32_t filled = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_nslots, 0);
-        const uint32_t used = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_ncon, 0);
-        const uint32_t failed = __shfl_sync(0xffffffffu, *(volatile uint32_t *)&s_fail, 0);
+        const uint32_t filled = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_nslots, 0);
+        const uint32_t used = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_ncon, 0);
+        const uint32_t failed = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_fail, 0);
         if (failed) break;
-        if (filled > lim || used > lim) { if (lane == 0) atomicExch(&s_fail, 1u); break; }
+        if (filled > lim || used > lim) { if (lane == 0) atomicExch(s_fail, 1u); break; }
         const uint32_t f = f0 + lane;
         bool add = false, claimed = false, lfail = false, src = false;
         int slot = -1;
@@ -728,7 +736,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
             }
           }
         }
-        const uint32_t c = warp_append(&s_ncon, add);
+        const uint32_t c = warp_append(s_ncon, add);
         if (add) {
           if (c < T) {
             cval[c] = vbits;
@@ -738,15 +746,22 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
             lfail = true;
           }
         }
-        const uint32_t pos = warp_append(&s_nslots, claimed);
+        const uint32_t pos = warp_append(s_nslots, claimed);
         if (claimed && pos < T) slist[pos] = (uint16_t)slot;
-        if (__any_sync(0xffffffffu, lfail)) { if (lane == 0) atomicExch(&s_fail, 1u); break; }
+        if (__any_sync(0xffffffffu, lfail)) { if (lane == 0) atomicExch(s_fail, 1u); break; }
       }
       __syncthreads();
-      const bool fail = s_fail != 0;
-      const uint32_t nslots = s_nslots < T ? s_nslots : T;
-      const uint32_t ncon = s_ncon < T ? s_ncon : T;
-      if (!fail) {
+      const bool fail = *s_fail != 0;
+      const uint32_t nslots = *s_nslots < T ? *s_nslots : T;
+      const uint32_t ncon = *s_ncon < T ? *s_ncon : T;
+      // the other parity's counters were last read before the previous pass ended
+      if (tid < 4) s_cnt[par ^ 1][tid] = 0;
+      if (fail) {
+        for (uint32_t i = tid; i < nslots; i += ANN_THREADS) {
+          const int slot = slist[i];
+          tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
+        }
+      } else {
         // ---- finalize: exact sum, compression threshold, statistics, output ----
         for (uint32_t i0 = (uint32_t)w * 32; i0 < nslots; i0 += ANN_THREADS) {
           const uint32_t i = i0 + lane;
@@ -829,7 +844,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
           const uint32_t pos = warp_append(&s_out, keep);
           if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
           if (STYLE != STYLE_INTEGER) {
-            const uint32_t q = warp_append(&s_nq, queue);
+            const uint32_t q = warp_append(s_nq, queue);
             if (queue) {
               // the slot's list head and marker were read above: keep the value there
               qlist[q] = (uint16_t)slot;
@@ -837,10 +852,11 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
               tsrc[slot] = (uint32_t)(vb >> 32);
             }
           }
+          if (i < nslots && !queue) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0; }
         }
         if (STYLE != STYLE_INTEGER && a.comp_mode != 0) {
           __syncthreads();
-          const uint32_t nq = s_nq;
+          const uint32_t nq = *s_nq;
           for (uint32_t i0 = (uint32_t)w * 32; i0 < nq; i0 += ANN_THREADS) {
             const uint32_t i = i0 + lane;
             bool keep = false;
@@ -850,6 +866,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
               const int slot = qlist[i];
               key = tkey[slot];
               fv = bitsd(((uint64_t)tsrc[slot] << 32) | thead[slot]);
+              tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
               keep = compress_draw<STYLE>(a, r, key, fv);
               if (keep) account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
             }
@@ -860,12 +877,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
         acc.clones += pa.clones; acc.deaths += pa.deaths; acc.zombies += pa.zombies;
       }
       __syncthreads();
-      // ---- clear the slots this pass used ----
-      for (uint32_t i = tid; i < nslots; i += ANN_THREADS) {
-        const int slot = slist[i];
-        tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
-      }
-      __syncthreads();
+      par ^= 1;
       if (fail) {
         if (lvl >= MAX_SPLIT) { bad = true; break; }
         ++lvl;                       // first half of this pass: hash bit lvl-1 clear
@@ -881,6 +893,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
     }
     if (tid == 0) {
       const uint32_t out = s_out;
+      s_out = 0;                     // next used after the next bucket's first barrier
       a.cnt_out[gb] = out < a.capv ? out : a.capv;
       if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
       if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);

@@ -35,6 +35,12 @@ UNIT = "walker-steps/s"
 WORKLOAD = "HubbardReal1D M=N=20 u=4 t=1, IsDynamicSemistochastic(threshold=1), target norm 1e8, dt=1e-3"
 
 
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one k_spawn plus one
+# k_annihilate launch per algorithmic byte (16-byte records read and written), measured at an
+# equilibrated norm of 3e7: (409.9 + 422.7 + 838.1 + 354.9) MB / (830 + 1211) MB.
+TRAFFIC_PER_ALGORITHMIC_BYTE = (409.9 + 422.7 + 838.1 + 354.9) / (830.0 + 1211.0)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -239,7 +245,12 @@ def run_ours(args, ws, rank, local):
     steps_t = max(tim["steps"], 1)
     achieved = k_bytes / (k_ms / 1e3) / 1e9 if k_ms > 0 else 0.0
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": args.traffic,
+                "frac": round(achieved / peak, 4),
+                "traffic": args.traffic if args.traffic is not None else
+                round(TRAFFIC_PER_ALGORITHMIC_BYTE * k_bytes / steps_t),
+                "traffic_source": "ncu dram bytes per algorithmic byte of k_spawn + k_annihilate "
+                                  "at norm 3e7 (profiles/step_hubbardreal1d_m20_1e8.md), scaled by "
+                                  "this run's records per step" if args.traffic is None else "given",
                 "peak_source": peak_kind,
                 "kernel": "k_spawn + k_spawn_heavy + k_annihilate (one step)",
                 "bytes_per_step": k_bytes / steps_t, "ms_per_step": k_ms / steps_t,
@@ -436,7 +447,8 @@ def main():
                     help="untimed steps (growth + equilibration) before the warm-up steps")
     ap.add_argument("--cpu-sample", type=float, default=2e4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--traffic", type=float, default=None)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per step of the roofline kernels, if measured for this run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-hv", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

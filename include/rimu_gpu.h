@@ -184,6 +184,74 @@ int rimu_wm_set_launch_shape(rimu_wm *wm, int keys_per_bucket, int table_slots);
 int rimu_apply_operator(rimu_model *m, rimu_wm *wm, rimu_vec *target, const rimu_vec *source,
                         const rimu_step_params *params, rimu_step_stats *stats);
 
+/* ---- Batched replicas ------------------------------------------------------------------
+ * Many independent FCIQMC runs stepped together: the replicas of one Hamiltonian
+ * (ProjectorMonteCarloProblem(H; n_replicas), which the reference steps one after another,
+ * pmc_simulation.jl:288-290) or Hamiltonians that differ only in the interaction u (models whose
+ * diagonal is tabulated: HubbardReal1D and one-component HubbardRealSpace without trap), each
+ * with its own start vector, shift, target walker number, statistics and projector.  Replica r
+ * uses random key (seed, r): its steps equal those of rimu_apply_operator with replica = r and the
+ * same shifts.  One launch of each step kernel covers all replicas; the shift update
+ * (DoubleLogUpdate, shiftstrategy.jl:174-181) runs on the device after every step, so that a
+ * segment of steps is one graph replay without host round trips.  The batch works on its own
+ * stream of the context's device. */
+typedef struct rimu_batch rimu_batch;
+
+typedef struct {
+  int style;                     /* RIMU_STYLE_* */
+  double dt;
+  double boost;                  /* 1.0 */
+  double proj_threshold, compression, rel_spawning_threshold, abs_spawning_threshold;
+  uint64_t seed;
+  int shift_update;              /* 0: shifts stay fixed; 1: DoubleLogUpdate */
+  double zeta, xi;               /* DoubleLogUpdate damping (reference defaults 0.08, zeta^2/4) */
+  int segment_steps;             /* steps per segment (rounded up to even; 0: 64) */
+  int use_graph;                 /* replay each full segment as one captured CUDA graph */
+  int autotune;                  /* time the launch shapes 2048/1024/512 on the first steps
+                                    with at least 2^20 entries and keep the fastest */
+} rimu_batch_params;
+
+/* Per replica and step: the step statistics of rimu_step_stats and the shift after the update
+ * (the value the reference reports for the step). */
+typedef struct {
+  double shift;
+  double norm;
+  double vproj;
+  double hproj;
+  double spawns;
+  int64_t len;
+  int64_t len_before;
+  int64_t exact_steps;
+  int64_t inexact_steps;
+  int64_t spawn_attempts;
+  int64_t spawn_records;
+  int64_t clones;
+  int64_t deaths;
+  int64_t zombies;
+} rimu_batch_stats;
+
+int rimu_batch_create(rimu_ctx *ctx, int nrep, int val_kind, rimu_batch **out);
+int rimu_batch_destroy(rimu_batch *b);
+/* Model, start vector (host pairs), initial shift and target walker number of one replica;
+ * only before the first run. */
+int rimu_batch_set_replica(rimu_batch *b, int replica, rimu_model *m, const uint64_t *keys,
+                           const void *vals, int64_t n, double shift, double target_walkers);
+/* ProjectedEnergy projector of one replica (as rimu_wm_set_projector). */
+int rimu_batch_set_projector(rimu_batch *b, int replica, const uint64_t *keys,
+                             const double *pvals, const double *hpvals, int n);
+/* Launch shape (as rimu_wm_set_launch_shape); setting it turns the autotuner off. */
+int rimu_batch_set_launch_shape(rimu_batch *b, int keys_per_bucket, int table_slots);
+/* nsteps steps with step numbers first_step+1 ... ; out receives nsteps * nrep records,
+ * step-major. */
+int rimu_batch_run(rimu_batch *b, const rimu_batch_params *p, uint64_t first_step, int nsteps,
+                   rimu_batch_stats *out);
+/* The walker list of one replica, as rimu_vec_download. */
+int rimu_batch_download(rimu_batch *b, int replica, uint64_t *keys, void *vals, int64_t cap,
+                        int64_t *n);
+/* out8: keys per bucket in use, annihilation table slots, buckets, graph segments, eager
+ * segments, re-run segments, milliseconds in the segments (CUDA events), steps run. */
+int rimu_batch_info(rimu_batch *b, double *out8);
+
 /* Full sorted basis (build_basis, ExactDiagonalization/basis_fock.jl:33-36): all BoseFS
  * (FermiFS) addresses in increasing bit-string order. */
 int rimu_basis_dimension(rimu_model *m, int64_t *dim);

@@ -100,36 +100,6 @@ int rimu_ctx_synchronize(rimu_ctx *ctx) {
 // ---------------------------------------------------------------------------------------------
 // Helpers
 // ---------------------------------------------------------------------------------------------
-template <class T>
-static int dalloc(rimu_ctx *ctx, T **p, size_t n) {
-  *p = nullptr;
-  if (n == 0) n = 1;
-  return rimu_cuda_check(cudaMallocAsync((void **)p, n * sizeof(T), ctx->stream), "cudaMallocAsync");
-}
-template <class T>
-static void dfree(rimu_ctx *ctx, T *&p) {
-  if (p) cudaFreeAsync(p, ctx->stream);
-  p = nullptr;
-}
-template <class T>
-static int h2d(rimu_ctx *ctx, T *d, const T *h, size_t n) {
-  if (n == 0) return RIMU_OK;
-  return rimu_cuda_check(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream),
-                         "cudaMemcpyAsync H2D");
-}
-template <class T>
-static int d2h(rimu_ctx *ctx, T *h, const T *d, size_t n) {
-  if (n == 0) return RIMU_OK;
-  return rimu_cuda_check(cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream),
-                         "cudaMemcpyAsync D2H");
-}
-static int ceil_log2(uint64_t x) {
-  int b = 0;
-  while ((1ull << b) < x) ++b;
-  return b;
-}
-static uint32_t round_up(uint64_t x, uint32_t m) { return (uint32_t)((x + m - 1) / m * m); }
-
 static int model_max_prod(const rimu_model_desc &d) {
   int N = d.n_particles;
   if (d.kind == RIMU_MODEL_MOM1D) return (N + 1) * (N + 1) * (N + 1) * (N + 1);
@@ -281,7 +251,7 @@ extern "C" int rimu_model_destroy(rimu_model *m) {
 }
 
 // transition offdiagonal table -H dt for the current dt (fciqmc.jl:109-112)
-static int ensure_aoff(rimu_model *m, double dt) {
+int ensure_aoff(rimu_model *m, double dt) {
   if (m->aoff_dt == dt) return RIMU_OK;
   const rimu_model_desc &d = m->desc;
   int n = m->aoff_len, M = d.n_modes;

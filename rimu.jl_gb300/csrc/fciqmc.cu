@@ -168,8 +168,28 @@ constexpr int WARPS = 8;            // warps per CTA in the spawn kernel
 constexpr int CHUNK_BUCKETS = 32;   // most buckets whose walkers one warp processes together
 constexpr int BATCH = 64;           // walkers whose work items are distributed together
 
-__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, uint64_t nk, uint64_t vb) {
-  const uint32_t b = ((uint32_t)r << a.nb_bits) | bucket_of(nk, a.nb_bits);
+// Bucket range of replica r and the replica of bucket gb.
+struct RepLayout { uint32_t off; int bits; };
+__device__ __forceinline__ RepLayout layout_of(const StepArgs &a, int r) {
+  if (!a.rep_off) return RepLayout{(uint32_t)r << a.nb_bits, a.nb_bits};
+  return RepLayout{a.rep_off[r], a.rep_bits[r]};
+}
+__device__ __forceinline__ int replica_of(const StepArgs &a, uint32_t gb) {
+  if (!a.rep_off) return (int)(gb >> a.nb_bits);
+  int lo = 0, hi = a.nrep - 1;       // the last replica whose range starts at or before gb
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.rep_off[mid] <= gb) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ uint32_t step_of(const StepArgs &a) {
+  return a.step_dev ? a.step + *a.step_dev : a.step;
+}
+
+__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout lay, uint64_t nk,
+                                           uint64_t vb) {
+  const uint32_t b = lay.off + bucket_of(nk, lay.bits);
   const uint32_t pos = atomicAdd(&a.scount[b], 1u);
   if (pos < a.caps) a.spawn[(size_t)b * a.caps + pos] = Rec{nk, vb};
   else atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
@@ -187,23 +207,24 @@ __device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key,
 // attempt needs 32 random bits: attempt j takes word j % 4 of Philox block j / 4 (each lane
 // evaluates the block of its own attempt; under SIMT this costs no extra issue slots).
 template <int KIND, int STYLE>
-__device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, uint64_t key, uint64_t vb,
-                                           double c, int noff, int exact, uint32_t j) {
+__device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout lay, uint32_t step,
+                                           uint64_t key, uint64_t vb, double c, int noff,
+                                           int exact, uint32_t j) {
   const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
     const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
     if (od.prod == 0) return;
     double y = bitsd(vb) * op_offdiag(a, od);
     if (STYLE == STYLE_DSS && a.has_proj) {
-      const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, j);
+      const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, key, j);
       y = project_threshold(y, a.proj_threshold, u53_of(rr));
     }
     if (is_zero_d(y)) return;
-    emit_spawn(a, r, od.key, dbits(y));
+    emit_spawn(a, r, lay, od.key, dbits(y));
     return;
   }
   const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
-  const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, a.step, key, grouped ? j >> 2 : j);
+  const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, key, grouped ? j >> 2 : j);
   uint32_t word = rr.x;
   if (grouped) {
     const uint32_t q = j & 3;
@@ -216,11 +237,11 @@ __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, uint64_t ke
   if (STYLE == STYLE_INTEGER) {
     const int64_t k = round_stochastic(y, u53_of(rr));
     if (k == 0) return;
-    emit_spawn(a, r, od.key, (uint64_t)k);
+    emit_spawn(a, r, lay, od.key, (uint64_t)k);
   } else {
     if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
     if (is_zero_d(y)) return;
-    emit_spawn(a, r, od.key, dbits(y));
+    emit_spawn(a, r, lay, od.key, dbits(y));
   }
 }
 
@@ -319,11 +340,13 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int cb = a.spawn_cb;
   const int nchunks = nb_total / cb;
+  const uint32_t step = step_of(a);
   SpawnAcc acc{};
   int cur_r = -1;
   for (int ch = blockIdx.x * WARPS + w; ch < nchunks; ch += gridDim.x * WARPS) {
     const int b0 = ch * cb;
-    const int r = b0 >> a.nb_bits;
+    const int r = replica_of(a, (uint32_t)b0);
+    const RepLayout lay = layout_of(a, r);
     if (r != cur_r) {
       if (cur_r >= 0) flush_spawn_acc(a, cur_r, acc);
       cur_r = r;
@@ -394,7 +417,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
         for (int st = 32; st >= 1; st >>= 1)
           if (s_excl[w][lo + st] <= it) lo += st;
         const uint32_t meta = s_meta[w][lo];
-        spawn_unit<KIND, STYLE>(a, r, s_key[w][lo], s_val[w][lo], s_c[w][lo],
+        spawn_unit<KIND, STYLE>(a, r, lay, step, s_key[w][lo], s_val[w][lo], s_c[w][lo],
                                 (int)(meta & 0x7fffffffu), (int)(meta >> 31), it - s_excl[w][lo]);
       }
       __syncwarp();
@@ -405,6 +428,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
 
 template <int KIND, int STYLE>
 __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
+  const uint32_t step = step_of(a);
   uint32_t nch = *a.heavy_count;
   if (nch > a.heavy_cap) nch = a.heavy_cap;
   for (uint32_t ci = blockIdx.x; ci < nch; ci += gridDim.x) {
@@ -413,8 +437,10 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
       if (threadIdx.x == 0) atomicOr(&a.stats[0].flags, (unsigned)FLAG_TABLE);
       continue;
     }
+    const RepLayout lay = layout_of(a, (int)ch.rep);
     for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x)
-      spawn_unit<KIND, STYLE>(a, (int)ch.rep, ch.key, ch.val, ch.c, ch.noff, ch.exact, ch.j0 + t);
+      spawn_unit<KIND, STYLE>(a, (int)ch.rep, lay, step, ch.key, ch.val, ch.c, ch.noff, ch.exact,
+                              ch.j0 + t);
   }
 }
 
@@ -538,11 +564,11 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, uin
 
 // Diagonal step of one walker (diagonal_step!, spawning.jl:73-77), float walkers.
 template <int KIND>
-__device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t rep,
+__device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t rep, uint32_t step,
                                              const Rec &rec) {
   double res = op_diagonal<KIND>(a, r, rec.key) * bitsd(rec.val);
   if (a.has_proj) {
-    const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
+    const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
     res = project_threshold(res, a.proj_threshold, u53_of(rr));
   }
   return res;
@@ -602,9 +628,10 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *count, bool flag) {
 // Compression draw (compression.jl:28-42) for an address whose |value| is below the
 // threshold: kept at +-threshold with probability |value| / threshold.
 template <int STYLE>
-__device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint64_t key, double &fv) {
+__device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t step, uint64_t key,
+                                              double &fv) {
   const double prob = a.comp_mode == 1 ? abs_d(fv) : abs_d(fv) / a.compression;
-  const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, a.step, key, 0);
+  const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, step, key, 0);
   if (!bernoulli53(u53_of(rr), prob)) return false;
   fv = signed_like(a.compression, fv);
   return true;
@@ -665,11 +692,12 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
   // end.  Each thread clears the slots it finalizes, and the counters of a pass are zeroed
   // during the next pass (they alternate by pass parity).
   int par = 0;
+  const uint32_t step = step_of(a);
   AnnAcc acc{};
   int cur_r = -1;
   bool bad = false;
   for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
-    const int r = gb >> a.nb_bits;
+    const int r = replica_of(a, (uint32_t)gb);
     if (r != cur_r) {
       if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
       cur_r = r;
@@ -721,7 +749,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
                 if (STYLE == STYLE_INTEGER) {
                   const int64_t v = (int64_t)rec.val;
                   const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
-                  const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, a.step, rec.key, 0);
+                  const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
                   const int64_t res = round_stochastic(x, u53_of(rr));
                   // clones_deaths_zombies (spawning.jl:79-93)
                   const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
@@ -730,7 +758,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
                   else pa.deaths += (res - v) < 0 ? v - res : res - v;
                   vbits = (uint64_t)res;
                 } else {
-                  vbits = dbits(diag_float<KIND>(a, r, rep, rec));
+                  vbits = dbits(diag_float<KIND>(a, r, rep, step, rec));
                 }
               }
             }
@@ -867,7 +895,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
               key = tkey[slot];
               fv = bitsd(((uint64_t)tsrc[slot] << 32) | thead[slot]);
               tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
-              keep = compress_draw<STYLE>(a, r, key, fv);
+              keep = compress_draw<STYLE>(a, r, step, key, fv);
               if (keep) account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
             }
             const uint32_t pos = warp_append(&s_out, keep);

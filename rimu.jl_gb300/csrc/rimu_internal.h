@@ -64,6 +64,11 @@ struct StepArgs {
   uint32_t capv_in;           // slab capacity of the source list
   uint32_t capv, caps, tsize; // target slab, spawn slab, annihilation table slots
   int spawn_cb;               // buckets per warp chunk in k_spawn (power of two <= 32)
+  // Replica layout: replica r owns the buckets [rep_off[r], rep_off[r] + 2^rep_bits[r]).
+  // When rep_off is null every replica has 2^nb_bits buckets.
+  const uint32_t *rep_off;    // [nrep + 1]
+  const int *rep_bits;        // [nrep]
+  const uint32_t *step_dev;   // when non-null, *step_dev is added to `step` (device counter)
   const Rec *v_in;
   const uint32_t *cnt_in;
   Rec *v_out;
@@ -152,6 +157,40 @@ struct rimu_wm {
 void rimu_set_error(const std::string &msg);
 int rimu_cuda_check(cudaError_t e, const char *what);
 #define RIMU_CUDA(call) do { int _rc = rimu_cuda_check((call), #call); if (_rc) return _rc; } while (0)
+
+// allocation and copies on the context stream (stream-ordered allocator)
+template <class T>
+inline int dalloc(rimu_ctx *ctx, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return rimu_cuda_check(cudaMallocAsync((void **)p, n * sizeof(T), ctx->stream), "cudaMallocAsync");
+}
+template <class T>
+inline void dfree(rimu_ctx *ctx, T *&p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+  p = nullptr;
+}
+template <class T>
+inline int h2d(rimu_ctx *ctx, T *d, const T *h, size_t n) {
+  if (n == 0) return RIMU_OK;
+  return rimu_cuda_check(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream),
+                         "cudaMemcpyAsync H2D");
+}
+template <class T>
+inline int d2h(rimu_ctx *ctx, T *h, const T *d, size_t n) {
+  if (n == 0) return RIMU_OK;
+  return rimu_cuda_check(cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream),
+                         "cudaMemcpyAsync D2H");
+}
+inline int ceil_log2(uint64_t x) {
+  int b = 0;
+  while ((1ull << b) < x) ++b;
+  return b;
+}
+inline uint32_t round_up(uint64_t x, uint32_t m) { return (uint32_t)((x + m - 1) / m * m); }
+
+// transition-operator offdiagonal table of a model for time step dt (capi.cu)
+int ensure_aoff(rimu_model *m, double dt);
 
 // launchers (fciqmc.cu)
 // ev (optional, 4 events): recorded before k_spawn, after k_spawn, after k_spawn_heavy and

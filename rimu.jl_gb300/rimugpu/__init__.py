@@ -18,5 +18,6 @@ from .problem import (DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUp
                       ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)
 from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estimator
 from .hv import BasisOperator, eigsolve, hv
+from .batch import BatchedReplicas, solve_batched
 
 __all__ = [n for n in dir() if not n.startswith("_")]

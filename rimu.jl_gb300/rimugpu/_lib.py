@@ -29,6 +29,8 @@ EXPORTS = [
     "rimu_wm_timing", "rimu_apply_operator",
     "rimu_basis_dimension", "rimu_basis_keys", "rimu_hv_basis", "rimu_hv_basis_adjoint",
     "rimu_hv_basis_adjoint_noalloc",
+    "rimu_batch_create", "rimu_batch_destroy", "rimu_batch_set_replica", "rimu_batch_set_projector",
+    "rimu_batch_set_launch_shape", "rimu_batch_run", "rimu_batch_download", "rimu_batch_info",
 ]
 
 
@@ -60,6 +62,24 @@ class StepStats(C.Structure):
                 ("deaths", C.c_int64), ("zombies", C.c_int64), ("vproj", C.c_double),
                 ("hproj", C.c_double), ("spawn_records", C.c_int64), ("retries", C.c_int32),
                 ("nb_bits", C.c_int32)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("style", C.c_int), ("dt", C.c_double), ("boost", C.c_double),
+                ("proj_threshold", C.c_double), ("compression", C.c_double),
+                ("rel_spawning_threshold", C.c_double), ("abs_spawning_threshold", C.c_double),
+                ("seed", C.c_uint64), ("shift_update", C.c_int), ("zeta", C.c_double),
+                ("xi", C.c_double), ("segment_steps", C.c_int), ("use_graph", C.c_int),
+                ("autotune", C.c_int)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("shift", C.c_double), ("norm", C.c_double), ("vproj", C.c_double),
+                ("hproj", C.c_double), ("spawns", C.c_double), ("len", C.c_int64),
+                ("len_before", C.c_int64), ("exact_steps", C.c_int64),
+                ("inexact_steps", C.c_int64), ("spawn_attempts", C.c_int64),
+                ("spawn_records", C.c_int64), ("clones", C.c_int64), ("deaths", C.c_int64),
+                ("zombies", C.c_int64)]
 
 
 _lib = None
@@ -113,6 +133,15 @@ def load(build_if_missing: bool = True):
         "rimu_hv_basis_adjoint": ([vp, vp, vp, vp, f64p, f64p, C.c_int64], C.c_int),
         "rimu_hv_basis_adjoint_noalloc": ([P(ModelDesc), vp, vp, vp, f64p, f64p, C.c_int64, vp],
                                           C.c_int),
+        "rimu_batch_create": ([vp, C.c_int, C.c_int, P(vp)], C.c_int),
+        "rimu_batch_destroy": ([vp], C.c_int),
+        "rimu_batch_set_replica": ([vp, C.c_int, vp, u64p, vp, C.c_int64, C.c_double, C.c_double],
+                                   C.c_int),
+        "rimu_batch_set_projector": ([vp, C.c_int, u64p, f64p, f64p, C.c_int], C.c_int),
+        "rimu_batch_set_launch_shape": ([vp, C.c_int, C.c_int], C.c_int),
+        "rimu_batch_run": ([vp, P(BatchParams), C.c_uint64, C.c_int, vp], C.c_int),
+        "rimu_batch_download": ([vp, C.c_int, u64p, vp, C.c_int64, i64p], C.c_int),
+        "rimu_batch_info": ([vp, f64p], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

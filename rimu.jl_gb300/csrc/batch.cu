@@ -92,7 +92,7 @@ struct rimu_batch {
   uint32_t *cnt[3] = {nullptr, nullptr, nullptr};
   int cur = 0;
   std::vector<int64_t> len, spawns_last;
-  std::vector<double> norm;
+  std::vector<double> norm, rate;     // rate: growth per step (log) seen in the last segment
   // device state
   uint32_t *d_off = nullptr;
   int *d_bits = nullptr;
@@ -209,15 +209,16 @@ static int regrid(rimu_batch *b, const std::vector<int> &nbits, uint32_t ncapv) 
 }
 
 // Buckets, slab capacities and table size for the next segment of steps.
-static int plan(rimu_batch *b, const rimu_batch_params *p, int min_caps, int min_capv,
+static int plan(rimu_batch *b, const rimu_batch_params *p, int ksteps, int min_caps, int min_capv,
                 uint32_t heavy_min) {
-  const double g = 2.0;      // room for growth within a segment
   const rimu_model *m0 = b->models[0];
   std::vector<int> nbits(b->nrep);
   double mu_v = 0, mu_s = 0, tot_l = 0, tot_b = 0;
   double work = 0;
   const uint32_t kMaxCaps = 16384;
   for (int r = 0; r < b->nrep; ++r) {
+    // room for the growth per step seen so far, over the steps of the next segment
+    const double g = std::max(2.0, 1.5 * std::exp(std::min(b->rate[r] * ksteps, std::log(64.0))));
     const double L = (double)std::max<int64_t>(b->len[r], 1);
     double S;
     if (b->spawns_last[r] >= 0) S = 1.3 * (double)b->spawns_last[r] + 256;
@@ -269,9 +270,9 @@ static int plan(rimu_batch *b, const rimu_batch_params *p, int min_caps, int min
     release_graph(b);
   }
   // annihilation table and spawn chunks (the rules of rimu_apply_operator)
-  const double mu_k = mu_v / g + mu_s / g;
+  const double mu_k = mu_v + mu_s;
   uint32_t T = 512;
-  while ((double)T < 1.25 * mu_k * g + 256.0 && T < 4096) T <<= 1;
+  while ((double)T < 1.25 * mu_k + 256.0 && T < 4096) T <<= 1;
   if (b->tslots) T = (uint32_t)b->tslots;
   int minbits = 31;
   for (int r = 0; r < b->nrep; ++r) minbits = std::min(minbits, b->bits[r]);
@@ -498,6 +499,7 @@ extern "C" int rimu_batch_create(rimu_ctx *ctx, int nrep, int val_kind, rimu_bat
   b->len.assign(nrep, 0);
   b->norm.assign(nrep, 0.0);
   b->spawns_last.assign(nrep, -1);
+  b->rate.assign(nrep, 0.0);
   b->pkeys.assign(nrep, {});
   b->pvals.assign(nrep, {});
   b->phvals.assign(nrep, {});
@@ -651,6 +653,9 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
   int min_caps = 0, min_capv = 0;
   uint32_t heavy_min = 0;
   int tries = 0;
+  // segments start short and double up to segment_steps while they succeed; an overflow halves
+  // them, so that the growth within one segment stays within the planned room
+  int seg = b->steps_done == 0 ? std::min(p.segment_steps, 8) : p.segment_steps;
   std::vector<double> trial_cost;
   const int shapes[3] = {2048, 1024, 512};
   int trial = -1;
@@ -659,8 +664,8 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
     for (int r = 0; r < b->nrep; ++r) tot_len += b->len[r];
     if (p.autotune && !b->tuned && tot_len >= (1 << 20) && trial < 0) trial = 0;
     if (trial >= 0) b->kpb = shapes[trial];
-    if ((rc = plan(b, &p, min_caps, min_capv, heavy_min))) return rc;
-    int k = std::min(p.segment_steps, nsteps - pos);
+    if ((rc = plan(b, &p, seg, min_caps, min_capv, heavy_min))) return rc;
+    int k = std::min(seg, nsteps - pos);
     if (trial >= 0) k = std::min(k, 4);
     if ((rc = ensure_records(b, p.segment_steps))) return rc;
     const bool graph = p.use_graph && trial < 0 && k == p.segment_steps && b->eager_segments > 0;
@@ -680,19 +685,39 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
       return RIMU_ERR_OVERFLOW;
     }
     if (flags) {
-      // re-run the segment from the snapshot with larger buffers
-      if (++tries > 10) { rimu_set_error("rimu_batch_run: capacities could not be grown enough"); return RIMU_ERR_OVERFLOW; }
+      // re-run the segment from the snapshot, shorter and with larger buffers; the steps before
+      // the overflow show how far each replica grows
+      if (++tries > 30) { rimu_set_error("rimu_batch_run: capacities could not be grown enough"); return RIMU_ERR_OVERFLOW; }
       if ((rc = snapshot(b, true))) return rc;
       RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
       b->retries++;
+      for (int r = 0; r < b->nrep; ++r) {
+        int64_t ml = 0, ms_ = 0;
+        for (int j = 0; j < k; ++j) {
+          ml = std::max<int64_t>(ml, b->h_stats[(size_t)j * b->nrep + r].len);
+          ms_ = std::max<int64_t>(ms_, b->h_stats[(size_t)j * b->nrep + r].spawn_records);
+        }
+        const double f = std::max((double)ml / (double)std::max<int64_t>(b->len[r], 1),
+                                  (double)ms_ / (double)std::max<int64_t>(b->spawns_last[r], 1));
+        b->rate[r] = std::max(2 * b->rate[r], std::log(std::max(f, 1.0)) / k + 0.01);
+        b->spawns_last[r] = std::max(b->spawns_last[r], ms_);
+      }
+      seg = std::max(2, seg / 2);
       if (flags & FLAG_SPAWN_OVERFLOW) min_caps = (int)round_up((uint64_t)max_sp * 5 / 4 + 32, 32);
       if (flags & FLAG_V_OVERFLOW) min_capv = (int)round_up((uint64_t)max_v * 5 / 4 + 64, 32);
       if (flags & FLAG_HEAVY_OVERFLOW) heavy_min = b->heavy_cap * 2;
       continue;
     }
     tries = 0;
+    min_caps = min_capv = 0;
     b->kernel_ms += ms;
     b->steps_done += k;
+    for (int r = 0; r < b->nrep; ++r) {
+      const DevStats &s = b->h_stats[(size_t)(k - 1) * b->nrep + r];
+      const double nl = (double)std::max<int64_t>(s.len, 1) / (double)std::max<int64_t>(b->len[r], 1);
+      const double nn = b->h_rec[(size_t)(k - 1) * b->nrep + r].norm / std::max(b->norm[r], 1.0);
+      b->rate[r] = std::log(std::max(1.0, std::max(nl, nn))) / k;
+    }
     double contributions = 0;
     for (int j = 0; j < k; ++j) {
       for (int r = 0; r < b->nrep; ++r) {
@@ -722,6 +747,7 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
     }
     b->cur ^= (k & 1);
     pos += k;
+    if (trial < 0) seg = std::min(p.segment_steps, seg * 2);
     if (trial >= 0) {
       trial_cost.push_back(ms / std::max(contributions, 1.0));
       if (++trial == 3) {

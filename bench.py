@@ -121,6 +121,17 @@ def dist_init(ws, backend):
     return None
 
 
+def reduce_over_ranks(dist, ms, walker_steps, device):
+    """Whole-job figures of independent replicas, one per rank: the slowest rank's time and
+    the walker-steps of all ranks."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    w = torch.tensor([float(walker_steps)], dtype=torch.float64, device=device)
+    dist.all_reduce(w)
+    return float(t.item()), float(w.item())
+
+
 # --------------------------------------------------------------------------------------------
 # CPU baseline: the oracle step (single thread per process) on a bounded sample
 # --------------------------------------------------------------------------------------------
@@ -230,12 +241,7 @@ def run_ours(args, ws, rank, local):
     lens = list(sim.report.data["len"][-args.steps:])
     walker_steps = float(sum(norms))
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        w = torch.tensor([walker_steps], dtype=torch.float64, device="cuda")
-        dist.all_reduce(w)
-        walker_steps = float(w.item())
+        ms, walker_steps = reduce_over_ranks(dist, ms, walker_steps, "cuda")
     value = walker_steps / (ms / 1e3)
 
     # ---- roofline of spawn + annihilation (the hot path) ----

@@ -1,0 +1,61 @@
+"""The multi-GPU path is "replicas only": every rank runs an independent replica and bench.py
+combines the ranks with one max (time) and one sum (walker-steps).  These tests run that host
+logic as two gloo ranks on the CPU, and the reference arm under two ranks (rank 0 alone prints
+its line)."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, ws, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(ws), LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import bench
+    dist = bench.dist_init(ws, "gloo")
+    ms, w = bench.reduce_over_ranks(dist, 10.0 + 5 * rank, 1000.0 * (rank + 1), "cpu")
+    q.put((rank, ms, w))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_combine_time_by_max_and_walkers_by_sum():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ms, w in res:
+        assert ms == 15.0 and w == 3000.0, (rank, ms, w)
+
+
+def test_reference_arm_under_two_ranks_prints_one_line():
+    port = free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
+           "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--cpu-sample", "300",
+           "--cpu-seconds", "0.5"]
+    out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["e2e"]["h2d_bytes_per_step"] == 0

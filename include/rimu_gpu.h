@@ -149,6 +149,12 @@ int rimu_vec_walkernumber_and_length(rimu_vec *v, double *norm, int64_t *len);
 int rimu_vec_lookup(rimu_vec *v, const uint64_t *keys, int64_t n, void *vals);
 int rimu_vec_copy(rimu_vec *dst, const rimu_vec *src);
 int rimu_vec_empty(rimu_vec *v);
+/* dot(v, w) = inner(v, w) (abstractdvec.jl:214-230) of two device lists of the same address
+ * type, computed on the device; the summation order is fixed, so repeated calls agree. */
+int rimu_vec_dot(rimu_vec *v, rimu_vec *w, double *out);
+/* dst = src with values converted to val_kind (Int64 to Float64, exact below 2^53, or a plain
+ * copy): the promotion of an integer vector before dot(w, H, v) with a Float64 operator. */
+int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind);
 
 /* Working memory: stands behind working_memory(v) (Interfaces/dictvectors.jl:87,
  * pdworkingmemory.jl:295). */

@@ -1,0 +1,140 @@
+// vecops.cu -- operations between two device walker lists: the dot product (inner,
+// src/DictVectors/abstractdvec.jl:214-230) and a value-type conversion.
+//
+// Two lists may use different bucket counts (2^bits_a <= 2^bits_b); both bucket an address by
+// the top bits of mix64, so bucket i of the coarser list covers buckets
+// [i << (bits_b - bits_a), (i + 1) << (bits_b - bits_a)) of the finer one.  One CTA per coarse
+// bucket loads that bucket into a shared-memory table (in chunks if it is larger than the table)
+// and streams the matching fine buckets against it.  Products are accumulated per thread in a
+// fixed order and reduced per CTA and over CTAs in a fixed order, so the result does not change
+// from run to run.
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "rimu_internal.h"
+
+using namespace rimu;
+
+namespace {
+
+constexpr int DOT_THREADS = 256;
+constexpr uint32_t DOT_SLOTS = 2048;     // table slots (32 KB of keys and values)
+constexpr uint32_t DOT_CHUNK = DOT_SLOTS / 2;
+
+__device__ __forceinline__ double value_of(uint64_t bits, int kind) {
+  return kind == RIMU_VAL_I64 ? (double)(int64_t)bits : bitsd(bits);
+}
+
+__global__ void __launch_bounds__(DOT_THREADS) k_vec_dot(
+    const Rec *ra, const uint32_t *ca, int bits_a, uint32_t capv_a, int kind_a,
+    const Rec *rb, const uint32_t *cb, int bits_b, uint32_t capv_b, int kind_b,
+    double *partials) {
+  __shared__ uint64_t tkey[DOT_SLOTS];
+  __shared__ double tval[DOT_SLOTS];
+  __shared__ double red[DOT_THREADS];
+  const int tid = threadIdx.x;
+  const int nba = 1 << bits_a, sub = 1 << (bits_b - bits_a);
+  double acc = 0.0;
+  for (int i = blockIdx.x; i < nba; i += gridDim.x) {
+    const uint32_t na = ca[i] < capv_a ? ca[i] : capv_a;
+    for (uint32_t c0 = 0; c0 < na; c0 += DOT_CHUNK) {
+      const uint32_t c1 = c0 + DOT_CHUNK < na ? c0 + DOT_CHUNK : na;
+      for (uint32_t s = tid; s < DOT_SLOTS; s += DOT_THREADS) tkey[s] = EMPTY_KEY;
+      __syncthreads();
+      for (uint32_t e = c0 + tid; e < c1; e += DOT_THREADS) {
+        const Rec rec = ra[(size_t)i * capv_a + e];
+        uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - 11));
+        for (uint32_t p = 0; p < DOT_SLOTS; ++p) {     // addresses of a list are distinct
+          const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
+                                                   (unsigned long long)EMPTY_KEY,
+                                                   (unsigned long long)rec.key);
+          if (old == EMPTY_KEY) { tval[sl] = value_of(rec.val, kind_a); break; }
+          sl = (sl + 1) & (DOT_SLOTS - 1);
+        }
+      }
+      __syncthreads();
+      for (int j = i * sub; j < (i + 1) * sub; ++j) {
+        const uint32_t nb = cb[j] < capv_b ? cb[j] : capv_b;
+        for (uint32_t e = tid; e < nb; e += DOT_THREADS) {
+          const Rec rec = rb[(size_t)j * capv_b + e];
+          uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - 11));
+          for (uint32_t p = 0; p < DOT_SLOTS; ++p) {
+            const uint64_t k = tkey[sl];
+            if (k == rec.key) { acc += tval[sl] * value_of(rec.val, kind_b); break; }
+            if (k == EMPTY_KEY) break;
+            sl = (sl + 1) & (DOT_SLOTS - 1);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  red[tid] = acc;
+  __syncthreads();
+  for (int s = DOT_THREADS / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  if (tid == 0) partials[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_partials(const double *partials, int n, double *out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += partials[i];
+    *out = s;
+  }
+}
+
+__global__ void k_convert_i64_f64(const Rec *src, Rec *dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const Rec r = src[i];
+    dst[i] = Rec{r.key, dbits((double)(int64_t)r.val)};
+  }
+}
+
+int fail_arg(const std::string &msg) {
+  rimu_set_error(msg);
+  return RIMU_ERR_BADARG;
+}
+
+}  // namespace
+
+extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
+  if (!a || !b || !out) return fail_arg("rimu_vec_dot: NULL argument");
+  if (a->ctx != b->ctx) return fail_arg("rimu_vec_dot: vectors of different contexts");
+  if (a->nb_bits > b->nb_bits) std::swap(a, b);
+  rimu_ctx *ctx = a->ctx;
+  const int nba = 1 << a->nb_bits;
+  const int grid = nba < ctx->num_sms * 8 ? nba : ctx->num_sms * 8;
+  double *partials = nullptr, *res = nullptr;
+  int rc;
+  if ((rc = dalloc(ctx, &partials, grid)) || (rc = dalloc(ctx, &res, 1))) return rc;
+  k_vec_dot<<<grid, DOT_THREADS, 0, ctx->stream>>>(a->recs, a->count, a->nb_bits, a->capv,
+                                                   a->val_kind, b->recs, b->count, b->nb_bits,
+                                                   b->capv, b->val_kind, partials);
+  k_sum_partials<<<1, 32, 0, ctx->stream>>>(partials, grid, res);
+  rc = rimu_cuda_check(cudaGetLastError(), "k_vec_dot");
+  if (!rc) rc = d2h(ctx, out, res, 1);
+  if (!rc) rc = rimu_cuda_check(cudaStreamSynchronize(ctx->stream), "rimu_vec_dot");
+  dfree(ctx, partials);
+  dfree(ctx, res);
+  return rc;
+}
+
+extern "C" int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind) {
+  if (!dst || !src) return fail_arg("rimu_vec_convert: NULL argument");
+  if (dst == src) return fail_arg("rimu_vec_convert: dst and src must differ");
+  if (val_kind != RIMU_VAL_F64 && val_kind != RIMU_VAL_I64) return fail_arg("rimu_vec_convert: bad val_kind");
+  if (src->val_kind != val_kind && val_kind != RIMU_VAL_F64)
+    return fail_arg("rimu_vec_convert: only Int64 to Float64 converts");
+  int rc;
+  if ((rc = rimu_vec_copy(dst, src))) return rc;
+  if (src->val_kind == val_kind) return RIMU_OK;
+  rimu_ctx *ctx = dst->ctx;
+  const size_t n = ((size_t)1 << dst->nb_bits) * dst->capv;
+  k_convert_i64_f64<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(dst->recs, dst->recs, n);
+  dst->val_kind = RIMU_VAL_F64;
+  return rimu_cuda_check(cudaGetLastError(), "k_convert_i64_f64");
+}

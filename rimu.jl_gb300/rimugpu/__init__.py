@@ -13,9 +13,9 @@ from .styles import (Exact, IsDeterministic, IsDynamicSemistochastic, IsStochast
                      NoCompression, ThresholdCompression, WithReplacement, default_style)
 from .dvec import (FirstOrderTransitionOperator, GPUDVec, GPUWorkingMemory, apply_operator,
                    dot_operator, mul, working_memory)
-from .problem import (DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUpdate, LogUpdate,
-                      LogUpdateAfterTargetWalkers, PMCSimulation, ProjectedEnergy,
-                      ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)
+from .problem import (AllOverlaps, DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUpdate,
+                      LogUpdate, LogUpdateAfterTargetWalkers, NoStats, PMCSimulation,
+                      ProjectedEnergy, ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)
 from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estimator
 from .hv import BasisOperator, eigsolve, hv
 from .batch import BatchedReplicas, solve_batched

@@ -10,7 +10,7 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))   # rimu.jl_gb
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "librimu_gpu.so")
-SOURCES = ["fciqmc.cu", "hv.cu", "capi.cu", "batch.cu"]
+SOURCES = ["fciqmc.cu", "hv.cu", "capi.cu", "batch.cu", "vecops.cu"]
 HEADERS = ["rimu_device.cuh", "rimu_internal.h"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -31,6 +31,7 @@ EXPORTS = [
     "rimu_hv_basis_adjoint_noalloc",
     "rimu_batch_create", "rimu_batch_destroy", "rimu_batch_set_replica", "rimu_batch_set_projector",
     "rimu_batch_set_launch_shape", "rimu_batch_run", "rimu_batch_download", "rimu_batch_info",
+    "rimu_vec_dot", "rimu_vec_convert",
 ]
 
 
@@ -142,6 +143,8 @@ def load(build_if_missing: bool = True):
         "rimu_batch_run": ([vp, P(BatchParams), C.c_uint64, C.c_int, vp], C.c_int),
         "rimu_batch_download": ([vp, C.c_int, u64p, vp, C.c_int64, i64p], C.c_int),
         "rimu_batch_info": ([vp, f64p], C.c_int),
+        "rimu_vec_dot": ([vp, vp, f64p], C.c_int),
+        "rimu_vec_convert": ([vp, vp, C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -147,16 +147,21 @@ class GPUDVec:
         return w
 
     def dot(self, other) -> float:
-        """dot(self, other) for a dict / GPUDVec `other` (small side is looked up)."""
+        """dot(self, other) (abstractdvec.jl:214-230): with a dict `other` its addresses are
+        looked up; with a GPUDVec the product is computed on the device."""
         if isinstance(other, dict):
             keys = np.array([a.key for a in other], dtype=np.uint64)
             mine = self.lookup_keys(keys)
             return float(sum(float(m) * float(o) for m, o in zip(mine, other.values())))
-        if len(other) < len(self):
-            return other.dot(self)
-        k, v = self.download()
-        theirs = other.lookup_keys(k)
-        return float(np.dot(v.astype(float), theirs.astype(float)))
+        out = C.c_double()
+        _lib.check(_lib.load().rimu_vec_dot(self.handle, other.handle, C.byref(out)))
+        return out.value
+
+    def as_float(self) -> "GPUDVec":
+        """A Float64 copy on the device (IsDeterministic style)."""
+        w = GPUDVec(style=IsDeterministic(), address_type=self._addr(0))
+        _lib.check(_lib.load().rimu_vec_convert(w.handle, self.handle, _lib.VAL_F64))
+        return w
 
     def __del__(self):
         try:
@@ -284,12 +289,9 @@ def mul(y: GPUDVec, H, x: GPUDVec, wm: GPUWorkingMemory | None = None) -> GPUDVe
 
 
 def dot_operator(w: GPUDVec, H, v: GPUDVec) -> float:
-    """dot(w, H, v) (abstractdvec.jl:298-324)."""
+    """dot(w, H, v) (abstractdvec.jl:298-324) = <w | H v>: H v by the deterministic step on
+    a Float64 copy of v, then the device dot product; nothing leaves the GPU."""
     tmp = GPUDVec(style=IsDeterministic(), address_type=v._addr(0))
-    src = v
-    if not isinstance(v.style, IsDeterministic):
-        k, vals = v.download()
-        src = GPUDVec(style=IsDeterministic(), address_type=v._addr(0))
-        src.upload(k, vals.astype(np.float64))
+    src = v if isinstance(v.style, IsDeterministic) else v.as_float()
     mul(tmp, H, src)
     return tmp.dot(w)

@@ -138,6 +138,51 @@ class Report:
 
 
 # ----------------------------------------------------------------------------------------
+# Replica strategies (replicastrategy.jl)
+# ----------------------------------------------------------------------------------------
+class NoStats:
+    """NoStats(n_replicas) (replicastrategy.jl:53): replicas without cross statistics."""
+
+    def __init__(self, n_replicas=1):
+        self.n_replicas = n_replicas
+
+    def replica_stats(self, vectors):
+        return (), ()
+
+
+class AllOverlaps:
+    """AllOverlaps(n_replicas=2; operator=nothing, vecnorm=true) (replicastrategy.jl:112-190):
+    for every pair i < j of replicas the overlap c{i}_dot_c{j} = dot(v_i, v_j) and, for each
+    operator k, c{i}_Op{k}_c{j} = dot(v_i, op_k, v_j), all computed on the device."""
+
+    def __init__(self, n_replicas=2, operator=None, vecnorm=True):
+        if not isinstance(n_replicas, int):
+            raise ValueError("n_replicas must be an integer")
+        if operator is None:
+            self.operators = ()
+        elif isinstance(operator, (tuple, list)):
+            self.operators = tuple(operator)
+        else:
+            self.operators = (operator,)
+        self.n_replicas = n_replicas
+        self.vecnorm = vecnorm
+
+    def replica_stats(self, vectors):
+        from .dvec import dot_operator
+        names, values = [], []
+        n = len(vectors)
+        for i in range(n):
+            for j in range(i + 1, n):
+                if self.vecnorm:
+                    names.append(f"c{i + 1}_dot_c{j + 1}")
+                    values.append(vectors[i].dot(vectors[j]))
+                for k, op in enumerate(self.operators):
+                    names.append(f"c{i + 1}_Op{k + 1}_c{j + 1}")
+                    values.append(dot_operator(vectors[i], op, vectors[j]))
+        return tuple(names), tuple(values)
+
+
+# ----------------------------------------------------------------------------------------
 # Problem and simulation
 # ----------------------------------------------------------------------------------------
 class ProjectorMonteCarloProblem:
@@ -148,8 +193,14 @@ class ProjectorMonteCarloProblem:
                  style: StochasticStyle | None = None, time_step=0.01, starting_step=0,
                  last_step=100, wall_time=math.inf, target_walkers=1000, ζ=0.08, ξ=None,
                  shift_strategy=None, reporting_strategy=None, post_step_strategy=(),
-                 max_length=None, random_seed=True, population=10):
+                 max_length=None, random_seed=True, population=10, replica_strategy=None):
         self.hamiltonian = hamiltonian
+        if replica_strategy is None:
+            replica_strategy = NoStats(n_replicas)
+        elif replica_strategy.n_replicas != n_replicas and n_replicas != 1:
+            raise ValueError("n_replicas does not match the replica strategy")
+        n_replicas = replica_strategy.n_replicas
+        self.replica_strategy = replica_strategy
         self.n_replicas = n_replicas
         self.start_at = start_at if start_at is not None else hamiltonian.starting_address()
         self.shift = shift
@@ -269,6 +320,10 @@ class PMCSimulation:
         proceed = True
         for s in self.states:
             proceed &= self._advance(s)
+        if self.step % self.problem.reporting_strategy.reporting_interval == 0:
+            names, values = self.problem.replica_strategy.replica_stats([s.v for s in self.states])
+            for n, val in zip(names, values):
+                self.report.add(n, val)
         self.modified = True
         if not proceed:
             self.aborted = True

@@ -87,7 +87,13 @@ typedef struct {
   uint64_t seed;                 /* random stream seed */
   uint64_t step;                 /* step number (part of every random counter) */
   uint32_t replica;              /* replica id (part of every random key) */
+  int initiator;                 /* RIMU_INIT_*: initiator rule of an InitiatorDVec */
+  double initiator_threshold;    /* initiators are addresses with |value| > threshold */
 } rimu_step_params;
+
+/* Initiator rules (initiators.jl:132-234): NonInitiator, Initiator, SimpleInitiator,
+ * CoherentInitiator.  With a rule, addresses must fit in 63 bits. */
+enum { RIMU_INIT_NONE = 0, RIMU_INIT_INITIATOR = 1, RIMU_INIT_SIMPLE = 2, RIMU_INIT_COHERENT = 3 };
 
 /* Step statistics (step_stats, styles.jl:14-19,94-96,203-208; compression.jl:16) plus the
  * walkernumber_and_length of the new vector (abstractdvec.jl:270) and the ProjectedEnergy

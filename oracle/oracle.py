@@ -48,7 +48,7 @@ class _OParams(C.Structure):
                 ("boost", C.c_double), ("proj_threshold", C.c_double),
                 ("compression", C.c_double), ("rel_threshold", C.c_double),
                 ("abs_threshold", C.c_double), ("seed", C.c_uint64), ("step", C.c_uint32),
-                ("replica", C.c_uint32)]
+                ("replica", C.c_uint32), ("init_rule", C.c_int), ("init_threshold", C.c_double)]
 
 
 class _OStats(C.Structure):
@@ -226,6 +226,9 @@ def diagonal(m: Model, key: int) -> float:
 # ----------------------------------------------------------------------------------------
 # FCIQMC step
 # ----------------------------------------------------------------------------------------
+INIT_NONE, INIT_INITIATOR, INIT_SIMPLE, INIT_COHERENT = 0, 1, 2, 3
+
+
 @dataclass
 class StepParams:
     style: int
@@ -240,6 +243,8 @@ class StepParams:
     rel_threshold: float = 1.0
     abs_threshold: float = float("inf")
     replica: int = 0
+    init_rule: int = 0           # INIT_*: initiator rule (initiators.jl:132-234)
+    init_threshold: float = 1.0
 
     def struct(self) -> _OParams:
         p = _OParams()
@@ -247,6 +252,7 @@ class StepParams:
         p.boost, p.proj_threshold, p.compression = self.boost, self.proj_threshold, self.compression
         p.rel_threshold, p.abs_threshold = self.rel_threshold, self.abs_threshold
         p.seed, p.step, p.replica = self.seed, self.step, self.replica
+        p.init_rule, p.init_threshold = self.init_rule, self.init_threshold
         return p
 
 

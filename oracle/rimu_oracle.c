@@ -323,7 +323,14 @@ typedef struct {
   uint64_t seed;
   uint32_t step;
   uint32_t replica;
+  int init_rule;               /* O_INIT_*: initiator rule of an InitiatorDVec (initiators.jl) */
+  double init_threshold;       /* its threshold: initiators have |value| > threshold */
 } o_params;
+
+/* Initiator rules (initiators.jl:132-234) and the classes of a contribution
+ * (_default_to_initiator_value, initiators.jl:142-157). */
+enum { O_INIT_NONE = 0, O_INIT_INITIATOR = 1, O_INIT_SIMPLE = 2, O_INIT_COHERENT = 3 };
+enum { O_CLS_SAFE = 0, O_CLS_UNSAFE = 1, O_CLS_INITIATOR = 2 };
 
 typedef struct {
   double norm;          /* walkernumber after the step */
@@ -334,7 +341,7 @@ typedef struct {
   int64_t clones, deaths, zombies;   /* IsStochasticInteger only */
 } o_stats;
 
-typedef struct { uint64_t key; int kind; double v; int64_t iv; } o_contrib;
+typedef struct { uint64_t key; int cls; int kind; double v; int64_t iv; } o_contrib;
 
 static uint64_t o_ordered_bits(double v) {
   uint64_t u;
@@ -344,6 +351,7 @@ static uint64_t o_ordered_bits(double v) {
 static int o_cmp_contrib_f(const void *a, const void *b) {
   const o_contrib *x = a, *y = b;
   if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  if (x->cls != y->cls) return x->cls < y->cls ? -1 : 1;
   if (x->kind != y->kind) return x->kind < y->kind ? -1 : 1;
   uint64_t ox = o_ordered_bits(x->v), oy = o_ordered_bits(y->v);
   return ox < oy ? -1 : ox > oy;
@@ -351,19 +359,21 @@ static int o_cmp_contrib_f(const void *a, const void *b) {
 static int o_cmp_contrib_i(const void *a, const void *b) {
   const o_contrib *x = a, *y = b;
   if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  if (x->cls != y->cls) return x->cls < y->cls ? -1 : 1;
   if (x->kind != y->kind) return x->kind < y->kind ? -1 : 1;
   return x->iv < y->iv ? -1 : x->iv > y->iv;
 }
 
 typedef struct { o_contrib *c; int64_t n, cap; int err; } o_buf;
-static void o_push(o_buf *b, uint64_t key, int kind, double v, int64_t iv) {
+static void o_push(o_buf *b, uint64_t key, int cls, int kind, double v, int64_t iv) {
   if (b->n == b->cap) {
     int64_t nc = b->cap ? 2 * b->cap : 1024;
     o_contrib *p = realloc(b->c, nc * sizeof(o_contrib));
     if (!p) { b->err = 1; return; }
     b->c = p; b->cap = nc;
   }
-  b->c[b->n].key = key; b->c[b->n].kind = kind; b->c[b->n].v = v; b->c[b->n].iv = iv;
+  b->c[b->n].key = key; b->c[b->n].cls = cls; b->c[b->n].kind = kind; b->c[b->n].v = v;
+  b->c[b->n].iv = iv;
   b->n++;
 }
 
@@ -454,6 +464,34 @@ static double o_fixed_signed_to_double(__int128 fx) {
   return neg ? -r : r;
 }
 
+/* Value of an address from its field sums by the initiator rule (from_initiator_value,
+ * initiators.jl:138-140, 181-183, 208-214); without a rule every contribution is "safe". */
+static void o_initiator_value(const o_params *p, const double f[3], const int64_t n[3],
+                              double *s, int64_t *si) {
+  const double fs = f[O_CLS_SAFE], fu = f[O_CLS_UNSAFE], fi = f[O_CLS_INITIATOR];
+  const int64_t ns = n[O_CLS_SAFE], nu = n[O_CLS_UNSAFE], ni = n[O_CLS_INITIATOR];
+  switch (p->init_rule) {
+    case O_INIT_INITIATOR:      /* safe + initiator + !iszero(initiator) * unsafe */
+      *s = fs + fi;
+      if (fi != 0.0) *s = *s + fu;
+      *si = ns + ni + (ni != 0 ? nu : 0);
+      return;
+    case O_INIT_SIMPLE:         /* safe + initiator */
+      *s = fs + fi;
+      *si = ns + ni;
+      return;
+    case O_INIT_COHERENT:       /* initiator + safe (+ unsafe if initiator or |unsafe| > threshold) */
+      *s = fi + fs;
+      if (fi != 0.0 || fabs(fu) > p->init_threshold) *s = *s + fu;
+      *si = ni + ns;
+      if (ni != 0 || fabs((double)nu) > p->init_threshold) *si += nu;
+      return;
+    default:
+      *s = fs;
+      *si = ns;
+  }
+}
+
 /* One apply_operator! step (dictvectors.jl:112-140) from `src` into a sorted `dst`.
  * Values are doubles for the float styles and int64 (passed as double-typed storage of
  * the same bits is NOT used: separate arrays) for IsStochasticInteger.
@@ -468,6 +506,14 @@ int o_step(const o_model *h, const o_params *p,
   for (int64_t e = 0; e < n; ++e) {
     uint64_t key = skeys[e];
     double val = is_int ? (double)sivals[e] : svals[e];
+    /* classes of this walker's contributions (_default_to_initiator_value,
+     * initiators.jl:142-157): its diagonal term counts as "initiator" and its spawns as
+     * "safe" when |value| > threshold, else as "safe" and "unsafe" */
+    const int parent_init = fabs(val) > p->init_threshold;
+    const int diag_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
+                                                      : (parent_init ? O_CLS_INITIATOR : O_CLS_SAFE);
+    const int spawn_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
+                                                       : (parent_init ? O_CLS_SAFE : O_CLS_UNSAFE);
     /* ---- diagonal_step! (spawning.jl:73-77) ---- */
     double x = o_t_diag(h, p, key) * val;
     if (is_int) {
@@ -475,7 +521,7 @@ int o_step(const o_model *h, const o_params *p,
       o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
       int64_t res = o_round_int(x, o_u53(r));
       int64_t v = sivals[e];
-      if (res != 0) o_push(&b, key, 0, 0.0, res);
+      if (res != 0) o_push(&b, key, diag_cls, 0, 0.0, res);
       /* clones_deaths_zombies, spawning.jl:79-93 */
       int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
       if (res > v) st->clones += res - v;
@@ -488,7 +534,7 @@ int o_step(const o_model *h, const o_params *p,
         o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
         res = o_project(x, p->proj_threshold, o_u53(r));
       }
-      if (res != 0.0) o_push(&b, key, 0, res, 0);
+      if (res != 0.0) o_push(&b, key, diag_cls, 0, res, 0);
     }
     /* ---- spawn! ---- */
     int noff = o_num_offdiagonals(h, key);
@@ -518,7 +564,7 @@ int o_step(const o_model *h, const o_params *p,
           o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
           y = o_project(y, p->proj_threshold, o_u53(r));
         }
-        if (y != 0.0) { o_push(&b, nk, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
+        if (y != 0.0) { o_push(&b, nk, spawn_cls, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
       }
       continue;
     }
@@ -552,10 +598,10 @@ int o_step(const o_model *h, const o_params *p,
       double y = c * o_t_off(p, hv);
       if (is_int) {
         int64_t k = o_round_int(y, o_u53(r));
-        if (k != 0) { o_push(&b, nk, 1, 0.0, k); st->spawns += (double)(k < 0 ? -k : k); }
+        if (k != 0) { o_push(&b, nk, spawn_cls, 1, 0.0, k); st->spawns += (double)(k < 0 ? -k : k); }
       } else {
         if (p->proj_threshold > 0) y = o_project(y, p->proj_threshold, o_u53(r));
-        if (y != 0.0) { o_push(&b, nk, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
+        if (y != 0.0) { o_push(&b, nk, spawn_cls, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
       }
     }
   }
@@ -573,23 +619,34 @@ int o_step(const o_model *h, const o_params *p,
   if (!ok || !ov || !oi) { free(b.c); free(ok); free(ov); free(oi); return 1; }
   int64_t m = 0;
   for (int64_t i = 0; i < b.n;) {
+    const uint64_t key = b.c[i].key;
+    double fs[3] = {0.0, 0.0, 0.0};
+    int64_t is[3] = {0, 0, 0};
     int64_t j = i;
-    double s = 0.0;
-    int64_t si = 0;
-    int first = 1, exact = 1;
-    __int128 fx = 0;
-    while (j < b.n && b.c[j].key == b.c[i].key) {
-      if (is_int) si += b.c[j].iv;
-      else {
-        s = first ? b.c[j].v : s + b.c[j].v;
-        first = 0;
-        __int128 t;
-        if (exact && o_to_fixed(b.c[j].v, &t)) fx += t; else exact = 0;
+    while (j < b.n && b.c[j].key == key) {       /* one field (class) at a time */
+      const int cls = b.c[j].cls;
+      double s = 0.0;
+      int64_t si = 0;
+      int first = 1, exact = 1;
+      __int128 fx = 0;
+      while (j < b.n && b.c[j].key == key && b.c[j].cls == cls) {
+        if (is_int) si += b.c[j].iv;
+        else {
+          s = first ? b.c[j].v : s + b.c[j].v;
+          first = 0;
+          __int128 t;
+          if (exact && o_to_fixed(b.c[j].v, &t)) fx += t; else exact = 0;
+        }
+        ++j;
       }
-      ++j;
+      if (!is_int && exact) s = o_fixed_signed_to_double(fx);
+      fs[cls] = s;
+      is[cls] = si;
     }
-    if (!is_int && exact) s = o_fixed_signed_to_double(fx);
-    if (is_int ? si != 0 : s != 0.0) { ok[m] = b.c[i].key; ov[m] = s; oi[m] = si; ++m; }
+    double s;
+    int64_t si;
+    o_initiator_value(p, fs, is, &s, &si);
+    if (is_int ? si != 0 : s != 0.0) { ok[m] = key; ov[m] = s; oi[m] = si; ++m; }
     i = j;
   }
   free(b.c);

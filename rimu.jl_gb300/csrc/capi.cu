@@ -662,6 +662,10 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     return bad("rimu_apply_operator: IsStochasticInteger needs Int64 walkers, other styles Float64");
   if (p->style == RIMU_STYLE_INTEGER && (p->proj_threshold != 0 || p->compression != 0))
     return bad("rimu_apply_operator: thresholding not supported for integer walkers");
+  if (p->initiator < RIMU_INIT_NONE || p->initiator > RIMU_INIT_COHERENT)
+    return bad("rimu_apply_operator: unknown initiator rule");
+  if (p->initiator != RIMU_INIT_NONE && m->dm.nbits > 63)
+    return bad("rimu_apply_operator: initiator rules need addresses of at most 63 bits");
   if (!(p->boost > 0)) return bad("rimu_apply_operator: boost must be positive");
   int rc;
   if (p->op == RIMU_OP_TRANSITION && (rc = ensure_aoff(m, p->dt))) return rc;
@@ -727,6 +731,8 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     a.comp_mode = p->compression > 0 ? (p->compression == 1.0 ? 1 : 2) : 0;
     a.boost_one = p->boost == 1.0 && p->rel_spawning_threshold == 1.0;
     a.has_abs_thr = std::isfinite(p->abs_spawning_threshold);
+    a.init_rule = p->initiator;
+    a.init_thr = p->initiator_threshold;
     a.seed = p->seed; a.step = (uint32_t)p->step; a.replica_base = p->replica;
     a.nrep = 1; a.nb_bits = nb_bits;
     a.capv_in = source->capv;

@@ -187,11 +187,15 @@ __device__ __forceinline__ uint32_t step_of(const StepArgs &a) {
   return a.step_dev ? a.step + *a.step_dev : a.step;
 }
 
+// A spawn of a non-initiator parent carries bit 63 of its address (initiator rules only;
+// addresses then fit in 63 bits); the bucket is that of the address itself.
+constexpr uint64_t UNSAFE_BIT = 1ull << 63;
+
 __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout lay, uint64_t nk,
-                                           uint64_t vb) {
+                                           uint64_t vb, uint64_t flag) {
   const uint32_t b = lay.off + bucket_of(nk, lay.bits);
   const uint32_t pos = atomicAdd(&a.scount[b], 1u);
-  if (pos < a.caps) a.spawn[(size_t)b * a.caps + pos] = Rec{nk, vb};
+  if (pos < a.caps) a.spawn[(size_t)b * a.caps + pos] = Rec{nk | flag, vb};
   else atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
 }
 
@@ -209,7 +213,7 @@ __device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key,
 template <int KIND, int STYLE>
 __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout lay, uint32_t step,
                                            uint64_t key, uint64_t vb, double c, int noff,
-                                           int exact, uint32_t j) {
+                                           int exact, uint64_t flag, uint32_t j) {
   const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
     const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
@@ -220,7 +224,7 @@ __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout l
       y = project_threshold(y, a.proj_threshold, u53_of(rr));
     }
     if (is_zero_d(y)) return;
-    emit_spawn(a, r, lay, od.key, dbits(y));
+    emit_spawn(a, r, lay, od.key, dbits(y), flag);
     return;
   }
   const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
@@ -237,11 +241,11 @@ __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout l
   if (STYLE == STYLE_INTEGER) {
     const int64_t k = round_stochastic(y, u53_of(rr));
     if (k == 0) return;
-    emit_spawn(a, r, lay, od.key, (uint64_t)k);
+    emit_spawn(a, r, lay, od.key, (uint64_t)k, flag);
   } else {
     if (a.has_proj) y = project_threshold(y, a.proj_threshold, u53_of(rr));
     if (is_zero_d(y)) return;
-    emit_spawn(a, r, lay, od.key, dbits(y));
+    emit_spawn(a, r, lay, od.key, dbits(y), flag);
   }
 }
 
@@ -255,6 +259,15 @@ __device__ __forceinline__ void flush_spawn_acc(const StepArgs &a, int r, SpawnA
     atomic_add_ll(&st.inexact_steps, ie);
   }
   acc = SpawnAcc{};
+}
+
+// Whether a walker is a non-initiator under the initiator rule (|value| <= threshold,
+// initiators.jl:142-157); always false without a rule.
+template <int STYLE>
+__device__ __forceinline__ int parent_unsafe(const StepArgs &a, uint64_t vb) {
+  if (!a.init_rule) return 0;
+  const double v = STYLE == STYLE_INTEGER ? i2d_exact((int64_t)vb) : bitsd(vb);
+  return !(abs_d(v) > a.init_thr);
 }
 
 __device__ __forceinline__ double dint_of(const DevModel &h, int n) {
@@ -306,7 +319,7 @@ __device__ __forceinline__ uint64_t column_work(const StepArgs &a, uint64_t key,
 
 // Cut a column with more than HEAVY_LIMIT units into chunks for k_spawn_heavy.
 __device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, int noff,
-                           int exact, uint64_t work) {
+                           int exact, int unsafe, uint64_t work) {
   const uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
   const uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
   for (uint64_t k = 0; k < nch; ++k) {
@@ -319,7 +332,7 @@ __device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, i
     ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
     const uint64_t rem = work - k * HEAVY_CHUNK;
     ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
-    ch.rep = (uint32_t)r; ch.pad = 0;
+    ch.rep = (uint32_t)r; ch.unsafe = (uint32_t)unsafe;
     a.heavy[idx + k] = ch;
   }
 }
@@ -388,13 +401,14 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
           }
           acc.attempts += (long long)work;
           if (work > (uint64_t)HEAVY_LIMIT) {
-            push_heavy(a, r, rec, c, noff, exact, work);
+            push_heavy(a, r, rec, c, noff, exact, parent_unsafe<STYLE>(a, rec.val), work);
             work = 0;
           }
           s_key[w][slot] = rec.key;
           s_val[w][slot] = rec.val;
           s_c[w][slot] = c;
-          s_meta[w][slot] = (uint32_t)noff | ((uint32_t)exact << 31);
+          s_meta[w][slot] = (uint32_t)noff | ((uint32_t)exact << 31) |
+                            ((uint32_t)parent_unsafe<STYLE>(a, rec.val) << 30);
           units = (uint32_t)work;
         }
         items[hh] = units;
@@ -418,7 +432,8 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
           if (s_excl[w][lo + st] <= it) lo += st;
         const uint32_t meta = s_meta[w][lo];
         spawn_unit<KIND, STYLE>(a, r, lay, step, s_key[w][lo], s_val[w][lo], s_c[w][lo],
-                                (int)(meta & 0x7fffffffu), (int)(meta >> 31), it - s_excl[w][lo]);
+                                (int)(meta & 0x3fffffffu), (int)(meta >> 31),
+                                ((meta >> 30) & 1u) ? UNSAFE_BIT : 0ull, it - s_excl[w][lo]);
       }
       __syncwarp();
     }
@@ -440,7 +455,7 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
     const RepLayout lay = layout_of(a, (int)ch.rep);
     for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x)
       spawn_unit<KIND, STYLE>(a, (int)ch.rep, lay, step, ch.key, ch.val, ch.c, ch.noff, ch.exact,
-                              ch.j0 + t);
+                              ch.unsafe ? UNSAFE_BIT : 0ull, ch.j0 + t);
   }
 }
 
@@ -468,8 +483,10 @@ constexpr int ANN_THREADS = 256;        // threads of one annihilation CTA
 
 // Shared memory of one annihilation CTA with T table slots and T contribution entries:
 // keys [T] u64, contribution values [T] u64, list heads [T] u32, diagonal-term markers [T]
-// u32, contribution links [T] u32, occupied-slot list [T] u16, compression queue [T] u16.
-__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 32; }
+// u32, contribution links [T] u32, occupied-slot list [T] u16, compression queue [T] u16,
+// contribution classes [T] u8 (initiator rules).
+__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 33; }
+
 
 __device__ __forceinline__ U128 neg128(U128 x) {
   U128 r;
@@ -512,7 +529,7 @@ __device__ __forceinline__ double from_ordered(uint64_t o) {
 // entries; a longer walk means a corrupted list and is cut short.
 __device__ double canonical_sum_list(bool have, double first, uint32_t head, uint32_t skip,
                                      const uint64_t *cval, const uint32_t *cnext, uint32_t n,
-                                     bool *bad) {
+                                     bool *bad, const uint8_t *ccls = nullptr, int cls = 0) {
   double sum = first;
   constexpr int K = 8;
   uint64_t ob[K];
@@ -521,7 +538,7 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, uin
   uint32_t steps = 0;
   for (uint32_t c = head; c != NIL; c = cnext[c]) {
     if (c >= n || ++steps > n) { *bad = true; return sum; }
-    if (c == skip) continue;
+    if (c == skip || (ccls && ccls[c] != cls)) continue;
     if (k < K) ob[k++] = ordered_bits(bitsd(cval[c]));
     else { more = true; break; }
   }
@@ -547,7 +564,7 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, uin
     steps = 0;
     for (uint32_t c = head; c != NIL; c = cnext[c]) {
       if (c >= n || ++steps > n) { *bad = true; return sum; }
-      if (c == skip) continue;
+      if (c == skip || (ccls && ccls[c] != cls)) continue;
       const uint64_t o = ordered_bits(bitsd(cval[c]));
       if (any_last && o <= last) continue;
       if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
@@ -560,6 +577,65 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, uin
   }
   *bad = true;
   return sum;
+}
+
+enum : uint8_t { CLS_SAFE = 0, CLS_UNSAFE = 1, CLS_INITIATOR = 2 };
+
+// Value of an address from the sums of its three contribution classes by the initiator rule
+// (from_initiator_value, initiators.jl:138-140, 181-183, 208-214).
+__device__ __forceinline__ double initiator_value_f(int rule, double thr, double fs, double fu,
+                                                    double fi) {
+  if (rule == RIMU_INIT_INITIATOR) {          // safe + initiator + !iszero(initiator) * unsafe
+    double s = fs + fi;
+    if (!is_zero_d(fi)) s = s + fu;
+    return s;
+  }
+  if (rule == RIMU_INIT_SIMPLE) return fs + fi;
+  double s = fi + fs;                         // CoherentInitiator
+  if (!is_zero_d(fi) || abs_d(fu) > thr) s = s + fu;
+  return s;
+}
+__device__ __forceinline__ int64_t initiator_value_i(int rule, double thr, int64_t ns, int64_t nu,
+                                                     int64_t ni) {
+  if (rule == RIMU_INIT_INITIATOR) return ns + ni + (ni != 0 ? nu : 0);
+  if (rule == RIMU_INIT_SIMPLE) return ns + ni;
+  return ni + ns + ((ni != 0 || abs_d(i2d_exact(nu)) > thr) ? nu : 0);
+}
+
+// Sum of the contributions of one address under an initiator rule: each class summed by the
+// summation rule (the diagonal term, when in that class, first in canonical order), then
+// combined.  Also counts the spawn statistics.
+__device__ double initiator_sum_f(const StepArgs &a, uint32_t head, uint32_t dsrc,
+                                  const uint64_t *cval, const uint32_t *cnext, const uint8_t *ccls,
+                                  uint32_t ncon, AnnAcc &acc, bool *bad) {
+  U128 sum[3] = {{0, 0}, {0, 0}, {0, 0}};
+  bool exact[3] = {true, true, true};
+  int cnt[3] = {0, 0, 0};
+  uint32_t steps = 0;
+  for (uint32_t c = head; c != NIL; c = cnext[c]) {
+    if (c >= ncon || ++steps > ncon) { *bad = true; break; }
+    const uint64_t v = cval[c];
+    const int k = ccls[c] < 3 ? ccls[c] : 0;
+    U128 m;
+    const bool ex = fixed_magnitude(bitsd(v), m);
+    if (c + 1 != dsrc) {
+      acc.records++;
+      acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
+    }
+    exact[k] = exact[k] && ex;
+    sum[k] = add128(sum[k], (v >> 63) ? neg128(m) : m);
+    cnt[k]++;
+  }
+  double f[3];
+  for (int k = 0; k < 3; ++k) {
+    if (cnt[k] == 0) { f[k] = 0.0; continue; }
+    if (exact[k]) { f[k] = signed_fixed_to_double(sum[k]); continue; }
+    const bool dk = dsrc && ccls[dsrc - 1] == k;
+    const double first = dk ? bitsd(cval[dsrc - 1]) : 0.0;
+    f[k] = canonical_sum_list(dk && !is_zero_d(first), first, head, dk ? dsrc - 1 : NIL, cval,
+                              cnext, ncon, bad, ccls, k);
+  }
+  return initiator_value_f(a.init_rule, a.init_thr, f[CLS_SAFE], f[CLS_UNSAFE], f[CLS_INITIATOR]);
 }
 
 // Diagonal step of one walker (diagonal_step!, spawning.jl:73-77), float walkers.
@@ -682,6 +758,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
   uint32_t *cnext = tsrc + T;
   uint16_t *slist = reinterpret_cast<uint16_t *>(cnext + T);
   uint16_t *qlist = slist + T;
+  uint8_t *ccls = reinterpret_cast<uint8_t *>(qlist + T);
   const uint32_t lim = T - ANN_THREADS;   // a warp starts a round of insertions only below this
   const int tbits = 31 - __clz((int)T);
   for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; tsrc[i] = 0; }
@@ -734,9 +811,17 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
         bool add = false, claimed = false, lfail = false, src = false;
         int slot = -1;
         uint64_t vbits = 0;
+        uint8_t cls = CLS_SAFE;
         if (f < need) {
           src = f < nv;
-          const Rec rec = src ? vbase[f] : sp[f - nv];
+          Rec rec = src ? vbase[f] : sp[f - nv];
+          if (a.init_rule) {
+            // classes of the initiator rules (initiators.jl:142-157): a spawn carries its
+            // parent's class in bit 63; a diagonal term is "initiator" for an initiator
+            if (src) cls = parent_unsafe<STYLE>(a, rec.val) ? CLS_SAFE : CLS_INITIATOR;
+            else cls = (rec.key & UNSAFE_BIT) ? CLS_UNSAFE : CLS_SAFE;
+            rec.key &= ~UNSAFE_BIT;
+          }
           if (lvl == 0 || ((uint32_t)(mix64(rec.key) >> 16) & mask) == sel) {
             slot = table_insert(tkey, T, tbits, rec.key, claimed);
             if (slot < 0) {
@@ -768,6 +853,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
         if (add) {
           if (c < T) {
             cval[c] = vbits;
+            ccls[c] = cls;
             cnext[c] = atomicExch(&thead[slot], c);
             if (src) tsrc[slot] = c + 1;
           } else {
@@ -803,13 +889,17 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
             const uint32_t dsrc = tsrc[slot];          // 1 + index of the diagonal term
             uint32_t steps = 0;
             if (STYLE == STYLE_INTEGER) {
-              int64_t iv = 0;
+              int64_t iv = 0, part[3] = {0, 0, 0};
               for (uint32_t c = head; c != NIL; c = cnext[c]) {
                 if (c >= ncon || ++steps > ncon) { bad = true; break; }
                 const int64_t k = (int64_t)cval[c];
                 iv += k;
+                part[ccls[c] < 3 ? ccls[c] : 0] += k;
                 if (c + 1 != dsrc) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
               }
+              if (a.init_rule)
+                iv = initiator_value_i(a.init_rule, a.init_thr, part[CLS_SAFE], part[CLS_UNSAFE],
+                                       part[CLS_INITIATOR]);
               if (iv != 0) {
                 acc.len_before++;
                 keep = true;
@@ -822,7 +912,9 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
               // equals both the exact fixed-point sum and the canonical-order sum.
               double fv;
               const uint32_t c1 = head < ncon ? cnext[head] : NIL;
-              if (head < ncon && (c1 == NIL || (c1 < ncon && cnext[c1] == NIL))) {
+              if (a.init_rule) {
+                fv = initiator_sum_f(a, head, dsrc, cval, cnext, ccls, ncon, acc, &bad);
+              } else if (head < ncon && (c1 == NIL || (c1 < ncon && cnext[c1] == NIL))) {
                 const double y0 = bitsd(cval[head]);
                 if (head + 1 != dsrc) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
                 fv = y0;

@@ -24,7 +24,7 @@ struct __align__(16) HeavyChunk {
   int exact;
   uint32_t j0, cnt;
   uint32_t rep;
-  uint32_t pad;
+  uint32_t unsafe;   // 1: a non-initiator's column (initiator rules)
 };
 
 // Per-replica step accumulators (zeroed before each step).
@@ -56,6 +56,8 @@ struct StepArgs {
   int comp_mode;     // 0: no compression, 1: threshold 1, 2: other threshold
   int boost_one;     // boost == 1 and rel_threshold == 1
   int has_abs_thr;   // abs_threshold finite
+  int init_rule;     // RIMU_INIT_*: initiator rule (0: none)
+  double init_thr;   // initiators have |value| > init_thr
   uint64_t seed;
   uint32_t step;
   uint32_t replica_base;

@@ -19,5 +19,6 @@ from .problem import (AllOverlaps, DoubleLogUpdate, DoubleLogUpdateAfterTargetWa
 from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estimator
 from .hv import BasisOperator, eigsolve, hv
 from .batch import BatchedReplicas, solve_batched
+from .initiators import CoherentInitiator, Initiator, InitiatorRule, NonInitiator, SimpleInitiator
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -53,7 +53,8 @@ class StepParams(C.Structure):
                 ("boost", C.c_double), ("proj_threshold", C.c_double),
                 ("compression", C.c_double), ("rel_spawning_threshold", C.c_double),
                 ("abs_spawning_threshold", C.c_double), ("seed", C.c_uint64),
-                ("step", C.c_uint64), ("replica", C.c_uint32)]
+                ("step", C.c_uint64), ("replica", C.c_uint32), ("initiator", C.c_int),
+                ("initiator_threshold", C.c_double)]
 
 
 class StepStats(C.Structure):

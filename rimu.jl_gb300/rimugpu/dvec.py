@@ -13,6 +13,7 @@ import numpy as np
 
 from . import _lib
 from .addresses import BoseFS
+from .initiators import initiator_rule
 from .styles import IsDeterministic, IsDynamicSemistochastic, StochasticStyle, default_style
 
 
@@ -27,7 +28,7 @@ class GPUDVec:
     ``(addr, val)``, or ``GPUDVec(style=..., address_type=addr)`` for an empty vector."""
 
     def __init__(self, pairs=None, style: StochasticStyle | None = None, address_type=None,
-                 capacity: int = 0):
+                 capacity: int = 0, initiator=None):
         if isinstance(pairs, tuple) and len(pairs) == 2 and not isinstance(pairs[0], tuple):
             pairs = {pairs[0]: pairs[1]}
         pairs = dict(pairs or {})
@@ -36,6 +37,8 @@ class GPUDVec:
             style = default_style(int if issubclass(vt, (int, np.integer)) else float)
         self.style = style
         self.valtype = style.valtype
+        # initiator rule of an InitiatorDVec (initiatordvec.jl): NonInitiator() is a plain DVec
+        self.initiator = initiator_rule(initiator)
         proto = address_type if address_type is not None else (next(iter(pairs)) if pairs else None)
         self.address_type = (type(proto), proto.N, proto.M) if proto is not None else (BoseFS, 0, 0)
         lib = _lib.load()
@@ -139,7 +142,7 @@ class GPUDVec:
 
     def similar(self):
         cls, N, M = self.address_type
-        return GPUDVec(style=self.style, address_type=cls.from_key(0, N, M))
+        return GPUDVec(style=self.style, address_type=cls.from_key(0, N, M), initiator=self.initiator)
 
     def copy(self):
         w = self.similar()
@@ -268,7 +271,10 @@ def apply_operator(wm: GPUWorkingMemory, target: GPUDVec, source: GPUDVec, op, b
         wm.counter += 1
     p.step = int(step) & 0xFFFFFFFF
     p.replica = wm.replica
+    p.initiator = source.initiator.code
+    p.initiator_threshold = source.initiator.threshold
     target.style, target.valtype, target.address_type = source.style, source.valtype, source.address_type
+    target.initiator = source.initiator
     st = _lib.StepStats()
     _lib.check(_lib.load().rimu_apply_operator(ham.handle, wm.handle, target.handle, source.handle,
                                                 C.byref(p), C.byref(st)))

@@ -193,7 +193,8 @@ class ProjectorMonteCarloProblem:
                  style: StochasticStyle | None = None, time_step=0.01, starting_step=0,
                  last_step=100, wall_time=math.inf, target_walkers=1000, ζ=0.08, ξ=None,
                  shift_strategy=None, reporting_strategy=None, post_step_strategy=(),
-                 max_length=None, random_seed=True, population=10, replica_strategy=None):
+                 max_length=None, random_seed=True, population=10, replica_strategy=None,
+                 initiator=False):
         self.hamiltonian = hamiltonian
         if replica_strategy is None:
             replica_strategy = NoStats(n_replicas)
@@ -223,6 +224,8 @@ class ProjectorMonteCarloProblem:
             random_seed = 0
         self.random_seed = int(random_seed) & 0xFFFFFFFFFFFFFFFF
         self.population = population
+        from .initiators import initiator_rule
+        self.initiator = initiator_rule(initiator)
 
 
 class SingleState:
@@ -266,10 +269,10 @@ class PMCSimulation:
         if isinstance(sa, GPUDVec):
             return sa.copy() if copy_vectors else sa
         if isinstance(sa, dict):
-            return GPUDVec(sa, style=problem.style)
+            return GPUDVec(sa, style=problem.style, initiator=problem.initiator)
         val = problem.population
         return GPUDVec({sa: int(val) if problem.style.valtype is int else float(val)},
-                       style=problem.style)
+                       style=problem.style, initiator=problem.initiator)
 
     @staticmethod
     def _initial_shift(H, v: GPUDVec) -> float:

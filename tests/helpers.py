@@ -22,16 +22,19 @@ STYLE_CODE = {R.IsStochasticInteger: O.STYLE_INTEGER, R.IsDeterministic: O.STYLE
               R.IsDynamicSemistochastic: O.STYLE_DSS}
 
 
-def oracle_params(style, dt, shift, seed, step, op=O.OP_TRANSITION, boost=1.0, replica=0):
+def oracle_params(style, dt, shift, seed, step, op=O.OP_TRANSITION, boost=1.0, replica=0,
+                  initiator=None):
     sp = style.params()
+    init = R.NonInitiator() if initiator is None else initiator
     return O.StepParams(STYLE_CODE[type(style)], dt=dt, shift=shift, seed=seed, step=step, op=op,
                         boost=boost, proj_threshold=sp["proj_threshold"],
                         compression=sp["compression"], rel_threshold=sp["rel_spawning_threshold"],
-                        abs_threshold=sp["abs_spawning_threshold"], replica=replica)
+                        abs_threshold=sp["abs_spawning_threshold"], replica=replica,
+                        init_rule=init.code, init_threshold=init.threshold)
 
 
-def gpu_step(h, style, keys, vals, dt, shift, seed, step, boost=1.0, wm=None):
-    src = R.GPUDVec(style=style, address_type=h.address)
+def gpu_step(h, style, keys, vals, dt, shift, seed, step, boost=1.0, wm=None, initiator=None):
+    src = R.GPUDVec(style=style, address_type=h.address, initiator=initiator)
     src.upload(keys, vals)
     dst = src.similar()
     wm = wm or R.GPUWorkingMemory(seed)

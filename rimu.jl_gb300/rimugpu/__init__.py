@@ -20,5 +20,6 @@ from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estim
 from .hv import BasisOperator, eigsolve, hv
 from .batch import BatchedReplicas, solve_batched
 from .initiators import CoherentInitiator, Initiator, InitiatorRule, NonInitiator, SimpleInitiator
+from .rimuio import load_state, save_state
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,59 @@
+"""Checkpoint files in the reference's save_state/load_state format (RimuIO.jl:92-195,
+arrowtypes.jl; the reference's own tests test/RimuIO.jl:98-175): round trips of keys, values
+and metadata, the Arrow schema the reference's reader expects, and the errors for files that
+are not state files.  Host-side only (the files are written from downloaded lists)."""
+import numpy as np
+import pytest
+
+pa = pytest.importorskip("pyarrow")
+
+import rimugpu as R                      # noqa: E402
+from rimugpu import rimuio               # noqa: E402
+
+
+@pytest.mark.parametrize("proto,dtype", [
+    (R.BoseFS([1] * 6), np.uint16),                # 11 bits
+    (R.BoseFS(4, {2: 2}), np.uint8),               # 5 bits
+    (R.BoseFS(20, {10: 10}), np.uint32),           # 29 bits
+    (R.near_uniform(R.BoseFS, 20, 20), np.uint64),  # 39 bits
+    (R.FermiFS([1, 1, 1] + [0] * 13), np.uint16),  # 16 bits
+])
+def test_round_trip_and_schema(tmp_path, proto, dtype):
+    rng = np.random.default_rng(1)
+    B = proto.N + proto.M - 1 if isinstance(proto, R.BoseFS) else proto.M
+    keys = np.unique(rng.integers(0, 2 ** min(B, 62), 500, dtype=np.uint64))
+    for vals in (rng.normal(size=len(keys)), rng.integers(-9, 10, len(keys))):
+        f = tmp_path / "state.arrow"
+        rimuio.save_pairs(f, keys, vals, proto, int=1, float=2.3, complex=1.2 + 3j, string="a string",
+                          bool=True)
+        k, v, p, meta = rimuio.load_pairs(f)
+        assert np.array_equal(k, keys) and np.array_equal(v, vals)
+        assert type(p) is type(proto) and (p.N, p.M) == (proto.N, proto.M)
+        assert meta["int"] == 1 and meta["float"] == 2.3 and meta["complex"] == 1.2 + 3j
+        assert meta["bool"] is True and meta["string"] == "a string"
+        assert meta["RIMU_PACKAGE_VERSION"] == "0.14.0"
+        with pa.memory_map(str(f)) as src:
+            t = pa.ipc.open_file(src).read_all()
+        kf = t.schema.field("key")
+        assert kf.type == pa.list_(pa.from_numpy_dtype(dtype), 1)
+        kind = "BoseFS" if isinstance(proto, R.BoseFS) else "FermiFS"
+        assert kf.metadata[b"ARROW:extension:name"] == f"JuliaLang.Rimu.{kind}.BitString".encode()
+        assert kf.metadata[b"ARROW:extension:metadata"] == f"{proto.N}.{proto.M}.{B}".encode()
+        assert t.schema.field("value").type in (pa.float64(), pa.int64())
+
+
+def test_empty_vector(tmp_path):
+    f = tmp_path / "empty.arrow"
+    rimuio.save_pairs(f, np.zeros(0, dtype=np.uint64), np.zeros(0, dtype=np.int64), R.BoseFS([1, 1, 1]))
+    k, v, _, _ = rimuio.load_pairs(f)
+    assert len(k) == 0 and len(v) == 0
+
+
+def test_files_that_are_not_state_files_are_rejected(tmp_path):
+    f = tmp_path / "bad.arrow"
+    for cols in ({"key": [1, 2, 3], "value": [1, 2, 3], "error": [0, 0, 0]}, {"error": [0, 0, 0]}):
+        t = pa.table(cols)
+        with pa.ipc.new_file(str(f), t.schema) as w:
+            w.write_table(t)
+        with pytest.raises(ValueError):
+            rimuio.load_pairs(f)

@@ -482,10 +482,10 @@ constexpr uint32_t NIL = 0xffffffffu;   // end of a contribution list
 constexpr int ANN_THREADS = 256;        // threads of one annihilation CTA
 
 // Shared memory of one annihilation CTA with T table slots and T contribution entries:
-// keys [T] u64, contribution values [T] u64, list heads [T] u32, diagonal-term markers [T]
-// u32, contribution links [T] u32, occupied-slot list [T] u16, compression queue [T] u16,
-// contribution classes [T] u8 (initiator rules).
-__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 33; }
+// keys [T] u64, contribution values [T] u64, list heads [T] u32, contribution link words
+// [T] u16, occupied-slot list [T] u16, compression queue [T] u16: 26 bytes per slot, so that
+// four CTAs with 2048 slots fit one SM.
+__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 26; }
 
 
 __device__ __forceinline__ U128 neg128(U128 x) {
@@ -523,22 +523,33 @@ __device__ __forceinline__ double from_ordered(uint64_t o) {
   return bitsd((o >> 63) ? (o & 0x7fffffffffffffffull) : ~o);
 }
 
+// Contribution link word (16 bits): the index of the next contribution of the address's list
+// (13 bits; LINK_END after the last), the contribution's class (2 bits, initiator rules) and
+// whether it is the diagonal term of a source walker (1 bit).
+constexpr uint32_t LINK_END = 0x1FFFu;
+__device__ __forceinline__ uint32_t link_next(uint16_t w) {
+  const uint32_t n = w & 0x1FFFu;
+  return n == LINK_END ? NIL : n;
+}
+__device__ __forceinline__ int link_cls(uint16_t w) { return (w >> 13) & 3; }
+__device__ __forceinline__ bool link_diag(uint16_t w) { return (w >> 15) != 0; }
+
 // Canonical-order sum for an address with an inexact contribution: `first` (the diagonal
-// term, when `have`) followed by the spawns of the list starting at `head` (the diagonal
-// term, entry `skip`, left out) in increasing order of value.  Lists hold at most `n`
-// entries; a longer walk means a corrupted list and is cut short.
-__device__ double canonical_sum_list(bool have, double first, uint32_t head, uint32_t skip,
-                                     const uint64_t *cval, const uint32_t *cnext, uint32_t n,
-                                     bool *bad, const uint8_t *ccls = nullptr, int cls = 0) {
+// term, when `have`) followed by the spawns of the list starting at `head` (diagonal terms are
+// skipped; with cls >= 0 only that class counts) in increasing order of value.  Lists hold at
+// most `n` entries; a longer walk means a corrupted list and is cut short.
+__device__ double canonical_sum_list(bool have, double first, uint32_t head, const uint64_t *cval,
+                                     const uint16_t *clink, uint32_t n, bool *bad, int cls = -1) {
   double sum = first;
   constexpr int K = 8;
   uint64_t ob[K];
   int k = 0;
   bool more = false;
   uint32_t steps = 0;
-  for (uint32_t c = head; c != NIL; c = cnext[c]) {
+  for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
     if (c >= n || ++steps > n) { *bad = true; return sum; }
-    if (c == skip || (ccls && ccls[c] != cls)) continue;
+    const uint16_t w = clink[c];
+    if (link_diag(w) || (cls >= 0 && link_cls(w) != cls)) continue;
     if (k < K) ob[k++] = ordered_bits(bitsd(cval[c]));
     else { more = true; break; }
   }
@@ -562,9 +573,10 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, uin
     uint64_t best = ~0ull;
     uint32_t cnt = 0;
     steps = 0;
-    for (uint32_t c = head; c != NIL; c = cnext[c]) {
+    for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
       if (c >= n || ++steps > n) { *bad = true; return sum; }
-      if (c == skip || (ccls && ccls[c] != cls)) continue;
+      const uint16_t w = clink[c];
+      if (link_diag(w) || (cls >= 0 && link_cls(w) != cls)) continue;
       const uint64_t o = ordered_bits(bitsd(cval[c]));
       if (any_last && o <= last) continue;
       if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
@@ -605,20 +617,25 @@ __device__ __forceinline__ int64_t initiator_value_i(int rule, double thr, int64
 // Sum of the contributions of one address under an initiator rule: each class summed by the
 // summation rule (the diagonal term, when in that class, first in canonical order), then
 // combined.  Also counts the spawn statistics.
-__device__ double initiator_sum_f(const StepArgs &a, uint32_t head, uint32_t dsrc,
-                                  const uint64_t *cval, const uint32_t *cnext, const uint8_t *ccls,
-                                  uint32_t ncon, AnnAcc &acc, bool *bad) {
+__device__ double initiator_sum_f(const StepArgs &a, uint32_t head, const uint64_t *cval,
+                                  const uint16_t *clink, uint32_t ncon, AnnAcc &acc, bool *bad) {
   U128 sum[3] = {{0, 0}, {0, 0}, {0, 0}};
   bool exact[3] = {true, true, true};
   int cnt[3] = {0, 0, 0};
+  int dcls = -1;                       // class of the diagonal term, if any
+  double dval = 0.0;
   uint32_t steps = 0;
-  for (uint32_t c = head; c != NIL; c = cnext[c]) {
+  for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
     if (c >= ncon || ++steps > ncon) { *bad = true; break; }
     const uint64_t v = cval[c];
-    const int k = ccls[c] < 3 ? ccls[c] : 0;
+    const uint16_t w = clink[c];
+    const int k = link_cls(w) < 3 ? link_cls(w) : 0;
     U128 m;
     const bool ex = fixed_magnitude(bitsd(v), m);
-    if (c + 1 != dsrc) {
+    if (link_diag(w)) {
+      dcls = k;
+      dval = bitsd(v);
+    } else {
       acc.records++;
       acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
     }
@@ -630,10 +647,9 @@ __device__ double initiator_sum_f(const StepArgs &a, uint32_t head, uint32_t dsr
   for (int k = 0; k < 3; ++k) {
     if (cnt[k] == 0) { f[k] = 0.0; continue; }
     if (exact[k]) { f[k] = signed_fixed_to_double(sum[k]); continue; }
-    const bool dk = dsrc && ccls[dsrc - 1] == k;
-    const double first = dk ? bitsd(cval[dsrc - 1]) : 0.0;
-    f[k] = canonical_sum_list(dk && !is_zero_d(first), first, head, dk ? dsrc - 1 : NIL, cval,
-                              cnext, ncon, bad, ccls, k);
+    const bool dk = dcls == k;
+    f[k] = canonical_sum_list(dk && !is_zero_d(dval), dk ? dval : 0.0, head, cval, clink, ncon,
+                              bad, k);
   }
   return initiator_value_f(a.init_rule, a.init_thr, f[CLS_SAFE], f[CLS_UNSAFE], f[CLS_INITIATOR]);
 }
@@ -744,7 +760,7 @@ __device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t 
 // warps.  A bucket with more contributions than the table holds is processed in passes, each
 // taking the addresses whose hash bits 16.. select it; a pass that still overflows is split.
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int nb_total) {
+__global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
   // per pass parity: occupied slots, contributions, overflow flag, compression queue length
   __shared__ uint32_t s_cnt[2][4];
@@ -754,14 +770,12 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
   uint64_t *tkey = reinterpret_cast<uint64_t *>(smem);
   uint64_t *cval = tkey + T;
   uint32_t *thead = reinterpret_cast<uint32_t *>(cval + T);
-  uint32_t *tsrc = thead + T;
-  uint32_t *cnext = tsrc + T;
-  uint16_t *slist = reinterpret_cast<uint16_t *>(cnext + T);
+  uint16_t *clink = reinterpret_cast<uint16_t *>(thead + T);
+  uint16_t *slist = clink + T;
   uint16_t *qlist = slist + T;
-  uint8_t *ccls = reinterpret_cast<uint8_t *>(qlist + T);
   const uint32_t lim = T - ANN_THREADS;   // a warp starts a round of insertions only below this
   const int tbits = 31 - __clz((int)T);
-  for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; tsrc[i] = 0; }
+  for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; }
   if (tid < 8) s_cnt[tid >> 2][tid & 3] = 0;
   if (tid == 0) s_out = 0;
   __syncthreads();
@@ -853,9 +867,9 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
         if (add) {
           if (c < T) {
             cval[c] = vbits;
-            ccls[c] = cls;
-            cnext[c] = atomicExch(&thead[slot], c);
-            if (src) tsrc[slot] = c + 1;
+            const uint32_t old = atomicExch(&thead[slot], c);
+            clink[c] = (uint16_t)((old == NIL ? LINK_END : old) | ((uint32_t)cls << 13) |
+                                  (src ? 0x8000u : 0u));
           } else {
             lfail = true;
           }
@@ -873,7 +887,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
       if (fail) {
         for (uint32_t i = tid; i < nslots; i += ANN_THREADS) {
           const int slot = slist[i];
-          tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
+          tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
         }
       } else {
         // ---- finalize: exact sum, compression threshold, statistics, output ----
@@ -882,20 +896,21 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
           bool keep = false, queue = false;
           uint64_t key = 0, vb = 0;
           int slot = 0;
+          uint32_t head = NIL;
           if (i < nslots) {
             slot = slist[i];
             key = tkey[slot];
-            const uint32_t head = thead[slot];
-            const uint32_t dsrc = tsrc[slot];          // 1 + index of the diagonal term
+            head = thead[slot];
             uint32_t steps = 0;
             if (STYLE == STYLE_INTEGER) {
               int64_t iv = 0, part[3] = {0, 0, 0};
-              for (uint32_t c = head; c != NIL; c = cnext[c]) {
+              for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
                 if (c >= ncon || ++steps > ncon) { bad = true; break; }
+                const uint16_t lw = clink[c];
                 const int64_t k = (int64_t)cval[c];
                 iv += k;
-                part[ccls[c] < 3 ? ccls[c] : 0] += k;
-                if (c + 1 != dsrc) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
+                part[link_cls(lw) < 3 ? link_cls(lw) : 0] += k;
+                if (!link_diag(lw)) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
               }
               if (a.init_rule)
                 iv = initiator_value_i(a.init_rule, a.init_thr, part[CLS_SAFE], part[CLS_UNSAFE],
@@ -911,27 +926,32 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
               // One or two contributions: a single IEEE addition is correctly rounded, so it
               // equals both the exact fixed-point sum and the canonical-order sum.
               double fv;
-              const uint32_t c1 = head < ncon ? cnext[head] : NIL;
+              const uint16_t w0 = head < ncon ? clink[head] : (uint16_t)LINK_END;
+              const uint32_t c1 = link_next(w0);
               if (a.init_rule) {
-                fv = initiator_sum_f(a, head, dsrc, cval, cnext, ccls, ncon, acc, &bad);
-              } else if (head < ncon && (c1 == NIL || (c1 < ncon && cnext[c1] == NIL))) {
+                fv = initiator_sum_f(a, head, cval, clink, ncon, acc, &bad);
+              } else if (head < ncon && (c1 == NIL || (c1 < ncon && link_next(clink[c1]) == NIL))) {
                 const double y0 = bitsd(cval[head]);
-                if (head + 1 != dsrc) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
+                if (!link_diag(w0)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
                 fv = y0;
                 if (c1 != NIL) {
                   const double y1 = bitsd(cval[c1]);
-                  if (c1 + 1 != dsrc) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
+                  if (!link_diag(clink[c1])) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
                   fv = __dadd_rn(y0, y1);
                 }
               } else {
                 U128 sum{0, 0};
-                bool exact = true;
-                for (uint32_t c = head; c != NIL; c = cnext[c]) {
+                bool exact = true, have_d = false;
+                double first = 0.0;
+                for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
                   if (c >= ncon || ++steps > ncon) { bad = true; break; }
                   const uint64_t v = cval[c];
                   U128 m;
                   const bool ex = fixed_magnitude(bitsd(v), m);
-                  if (c + 1 != dsrc) {
+                  if (link_diag(clink[c])) {
+                    have_d = true;
+                    first = bitsd(v);
+                  } else {
                     acc.records++;
                     acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
                   }
@@ -941,9 +961,8 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
                 if (exact) {
                   fv = signed_fixed_to_double(sum);
                 } else {
-                  const double first = dsrc ? bitsd(cval[dsrc - 1]) : 0.0;
-                  fv = canonical_sum_list(dsrc && !is_zero_d(first), first, head,
-                                          dsrc ? dsrc - 1 : NIL, cval, cnext, ncon, &bad);
+                  fv = canonical_sum_list(have_d && !is_zero_d(first), first, head, cval, clink,
+                                          ncon, &bad);
                 }
               }
               vb = dbits(fv);
@@ -953,7 +972,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
                 if (a.comp_mode == 1) small = abs_lt_one(fv);
                 else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
                 if (small) {
-                  queue = true;
+                  queue = head < ncon;
                 } else {
                   keep = true;
                   account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
@@ -966,13 +985,12 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
           if (STYLE != STYLE_INTEGER) {
             const uint32_t q = warp_append(s_nq, queue);
             if (queue) {
-              // the slot's list head and marker were read above: keep the value there
+              // the list was read above: its head entry keeps the value until the draw
               qlist[q] = (uint16_t)slot;
-              thead[slot] = (uint32_t)vb;
-              tsrc[slot] = (uint32_t)(vb >> 32);
+              cval[head] = vb;
             }
           }
-          if (i < nslots && !queue) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0; }
+          if (i < nslots && !queue) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; }
         }
         if (STYLE != STYLE_INTEGER && a.comp_mode != 0) {
           __syncthreads();
@@ -985,8 +1003,8 @@ __global__ void __launch_bounds__(ANN_THREADS, 3) k_annihilate(StepArgs a, int n
             if (i < nq) {
               const int slot = qlist[i];
               key = tkey[slot];
-              fv = bitsd(((uint64_t)tsrc[slot] << 32) | thead[slot]);
-              tkey[slot] = EMPTY_KEY; thead[slot] = NIL; tsrc[slot] = 0;
+              fv = bitsd(cval[thead[slot]]);
+              tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
               keep = compress_draw<STYLE>(a, r, step, key, fv);
               if (keep) account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
             }
@@ -1139,7 +1157,7 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
   const int cap = ctx->num_sms * 64;
   const int want_s = (nb_total / a.spawn_cb + WARPS - 1) / WARPS;
   const int grid_s = want_s < cap ? want_s : cap;
-  const int cap_a = ctx->num_sms * 3;                 // resident annihilation CTAs
+  const int cap_a = ctx->num_sms * 4;                 // resident annihilation CTAs
   const int grid = nb_total < cap_a ? nb_total : cap_a;
   if (ev) cudaEventRecord(ev[0], st);
   k_spawn<KIND, STYLE><<<grid_s, WARPS * 32, 0, st>>>(a, nb_total);

@@ -470,6 +470,7 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
 struct AnnAcc {
   U128 norm, spawn_fx;
   long long len, len_before, clones, deaths, zombies, spawns_i, records;
+  long long ncomp;                      // survivors of compression draws (|value| = threshold)
 };
 
 // Integer-walker statistics of one pass over a bucket; kept only if the pass completes.
@@ -480,6 +481,7 @@ struct PassAcc {
 constexpr int MAX_SPLIT = 16;           // at most 2^MAX_SPLIT passes over one bucket
 constexpr uint32_t NIL = 0xffffffffu;   // end of a contribution list
 constexpr int ANN_THREADS = 256;        // threads of one annihilation CTA
+constexpr uint32_t PACK_FAIL = 0x80000000u;   // overflow bit of the packed insertion counter
 
 // Shared memory of one annihilation CTA with T table slots and T contribution entries:
 // keys [T] u64, contribution values [T] u64, list heads [T] u32, contribution link words
@@ -688,6 +690,10 @@ __device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, int tbit
 }
 
 __device__ __forceinline__ void flush_ann_acc(const StepArgs &a, int r, AnnAcc &acc) {
+  // each compression survivor adds fixed_of(threshold) to the norm
+  const U128 th = fixed_of(abs_d(a.compression));
+  const uint64_t nc = (uint64_t)acc.ncomp;
+  acc.norm = add128(acc.norm, U128{th.lo * nc, __umul64hi(th.lo, nc) + th.hi * nc});
   const U128 nfx = warp_sum128(acc.norm), sfx = warp_sum128(acc.spawn_fx);
   const long long l = warp_sum(acc.len), lb = warp_sum(acc.len_before);
   const long long cl = warp_sum(acc.clones), de = warp_sum(acc.deaths), zo = warp_sum(acc.zombies);
@@ -729,11 +735,11 @@ __device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t
   return true;
 }
 
-// Statistics and the ProjectedEnergy dot products of a kept address.
+// Statistics and the ProjectedEnergy dot products of a kept address (its |value| in fixed
+// point is added to the norm by the caller).
 template <int STYLE>
-__device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t key, double dv,
-                                             U128 mag, AnnAcc &acc) {
-  acc.norm = add128(acc.norm, mag);
+__device__ __forceinline__ void account_entry(const StepArgs &a, int r, uint64_t key, double dv,
+                                              AnnAcc &acc) {
   acc.len++;
   if (a.nproj == 0) return;
   const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
@@ -749,6 +755,12 @@ __device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t 
     if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
   }
 }
+template <int STYLE>
+__device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t key, double dv,
+                                             U128 mag, AnnAcc &acc) {
+  acc.norm = add128(acc.norm, mag);
+  account_entry<STYLE>(a, r, key, dv, acc);
+}
 
 // One CTA per bucket.  The bucket's contributions -- the source walkers after their
 // diagonal step and the spawns -- are dealt out to all threads: each finds or claims the
@@ -757,12 +769,14 @@ __device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t 
 // its list adding the contributions exactly in 128-bit fixed point, rounds once, applies the
 // compression threshold and appends the survivor to the target slab; addresses below the
 // threshold are queued and drawn together afterwards, so that the random draws run on full
-// warps.  A bucket with more contributions than the table holds is processed in passes, each
-// taking the addresses whose hash bits 16.. select it; a pass that still overflows is split.
+// warps, and float addresses with three or more contributions are finished after them, also
+// by full warps.  A bucket with more contributions than the table holds is processed in
+// passes, each taking the addresses whose hash bits 16.. select it; a pass that still
+// overflows is split.
 template <int KIND, int STYLE>
 __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
-  // per pass parity: occupied slots, contributions, overflow flag, compression queue length
+  // per pass parity: packed insertion counter, compression queue length, second-list length
   __shared__ uint32_t s_cnt[2][4];
   __shared__ uint32_t s_out;            // entries written to the target slab of the bucket
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -779,8 +793,8 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
   if (tid < 8) s_cnt[tid >> 2][tid & 3] = 0;
   if (tid == 0) s_out = 0;
   __syncthreads();
-  // Three barriers per pass: after the insertions, before the compression draws and at the
-  // end.  Each thread clears the slots it finalizes, and the counters of a pass are zeroed
+  // Three barriers per pass: after the insertions, before the addresses with three or more
+  // contributions and the compression draws (float walkers), and at the end.  Each thread clears the slots it finalizes, and the counters of a pass are zeroed
   // during the next pass (they alternate by pass parity).
   int par = 0;
   const uint32_t step = step_of(a);
@@ -811,16 +825,18 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
     uint32_t sel = 0;
     for (;;) {
       const uint32_t mask = (1u << lvl) - 1u;
-      uint32_t *const s_nslots = &s_cnt[par][0], *const s_ncon = &s_cnt[par][1];
-      uint32_t *const s_fail = &s_cnt[par][2], *const s_nq = &s_cnt[par][3];
+      // s_pack: contribution entries (bits 0-15), occupied slots (bits 16-30), overflow (bit 31)
+      uint32_t *const s_pack = &s_cnt[par][0], *const s_nq = &s_cnt[par][1];
+      uint32_t *const s_nslow = &s_cnt[par][2];
       PassAcc pa{};
       // ---- every contribution of this pass onto the list of its address ----
       for (uint32_t f0 = (uint32_t)w * 32; f0 < need; f0 += ANN_THREADS) {
-        const uint32_t filled = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_nslots, 0);
-        const uint32_t used = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_ncon, 0);
-        const uint32_t failed = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_fail, 0);
-        if (failed) break;
-        if (filled > lim || used > lim) { if (lane == 0) atomicExch(s_fail, 1u); break; }
+        const uint32_t pk = __shfl_sync(0xffffffffu, *(volatile uint32_t *)s_pack, 0);
+        if (pk >> 31) break;
+        if ((pk & 0xffffu) > lim || ((pk >> 16) & 0x7fffu) > lim) {
+          if (lane == 0) atomicOr(s_pack, PACK_FAIL);
+          break;
+        }
         const uint32_t f = f0 + lane;
         bool add = false, claimed = false, lfail = false, src = false;
         int slot = -1;
@@ -863,8 +879,16 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             }
           }
         }
-        const uint32_t c = warp_append(s_ncon, add);
+        // one shared-memory atomic reserves the warp's contribution and occupied-slot entries
+        const uint32_t madd = __ballot_sync(0xffffffffu, add);
+        const uint32_t mcl = __ballot_sync(0xffffffffu, claimed);
+        uint32_t base = 0;
+        if (lane == 0 && (madd | mcl))
+          base = atomicAdd(s_pack, (uint32_t)__popc(madd) | ((uint32_t)__popc(mcl) << 16));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const uint32_t lt = lanemask_lt();
         if (add) {
+          const uint32_t c = (base & 0xffffu) + (uint32_t)__popc(madd & lt);
           if (c < T) {
             cval[c] = vbits;
             const uint32_t old = atomicExch(&thead[slot], c);
@@ -874,14 +898,17 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             lfail = true;
           }
         }
-        const uint32_t pos = warp_append(s_nslots, claimed);
-        if (claimed && pos < T) slist[pos] = (uint16_t)slot;
-        if (__any_sync(0xffffffffu, lfail)) { if (lane == 0) atomicExch(s_fail, 1u); break; }
+        if (claimed) {
+          const uint32_t pos = ((base >> 16) & 0x7fffu) + (uint32_t)__popc(mcl & lt);
+          if (pos < T) slist[pos] = (uint16_t)slot;
+        }
+        if (__any_sync(0xffffffffu, lfail)) { if (lane == 0) atomicOr(s_pack, PACK_FAIL); break; }
       }
       __syncthreads();
-      const bool fail = *s_fail != 0;
-      const uint32_t nslots = *s_nslots < T ? *s_nslots : T;
-      const uint32_t ncon = *s_ncon < T ? *s_ncon : T;
+      const uint32_t pk = *s_pack;
+      const bool fail = (pk >> 31) != 0;
+      const uint32_t nslots = ((pk >> 16) & 0x7fffu) < T ? ((pk >> 16) & 0x7fffu) : T;
+      const uint32_t ncon = (pk & 0xffffu) < T ? (pk & 0xffffu) : T;
       // the other parity's counters were last read before the previous pass ended
       if (tid < 4) s_cnt[par ^ 1][tid] = 0;
       if (fail) {
@@ -891,9 +918,12 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
         }
       } else {
         // ---- finalize: exact sum, compression threshold, statistics, output ----
+        // Float addresses with one or two contributions are finished here; the others (and
+        // every address under an initiator rule) go to a second list, finished by full warps
+        // after the next barrier, so that the short common case does not wait for them.
         for (uint32_t i0 = (uint32_t)w * 32; i0 < nslots; i0 += ANN_THREADS) {
           const uint32_t i = i0 + lane;
-          bool keep = false, queue = false;
+          bool keep = false, queue = false, slow = false;
           uint64_t key = 0, vb = 0;
           int slot = 0;
           uint32_t head = NIL;
@@ -901,8 +931,8 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             slot = slist[i];
             key = tkey[slot];
             head = thead[slot];
-            uint32_t steps = 0;
             if (STYLE == STYLE_INTEGER) {
+              uint32_t steps = 0;
               int64_t iv = 0, part[3] = {0, 0, 0};
               for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
                 if (c >= ncon || ++steps > ncon) { bad = true; break; }
@@ -923,26 +953,72 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
                 account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, mag}, acc);
               }
             } else {
-              // One or two contributions: a single IEEE addition is correctly rounded, so it
-              // equals both the exact fixed-point sum and the canonical-order sum.
-              double fv;
               const uint16_t w0 = head < ncon ? clink[head] : (uint16_t)LINK_END;
               const uint32_t c1 = link_next(w0);
-              if (a.init_rule) {
-                fv = initiator_sum_f(a, head, cval, clink, ncon, acc, &bad);
-              } else if (head < ncon && (c1 == NIL || (c1 < ncon && link_next(clink[c1]) == NIL))) {
+              if (!a.init_rule && head < ncon && (c1 == NIL || (c1 < ncon && link_next(clink[c1]) == NIL))) {
+                // One or two contributions: a single IEEE addition is correctly rounded, so
+                // it equals both the exact fixed-point sum and the canonical-order sum.
                 const double y0 = bitsd(cval[head]);
                 if (!link_diag(w0)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
-                fv = y0;
+                double fv = y0;
                 if (c1 != NIL) {
                   const double y1 = bitsd(cval[c1]);
                   if (!link_diag(clink[c1])) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
                   fv = __dadd_rn(y0, y1);
                 }
+                vb = dbits(fv);
+                if (!is_zero_d(fv)) {
+                  acc.len_before++;
+                  bool small = false;
+                  if (a.comp_mode == 1) small = abs_lt_one(fv);
+                  else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
+                  if (small) {
+                    queue = true;
+                  } else {
+                    keep = true;
+                    account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+                  }
+                }
+              } else {
+                slow = true;
+              }
+            }
+          }
+          const uint32_t pos = warp_append(&s_out, keep);
+          if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+          if (STYLE != STYLE_INTEGER) {
+            // compression queue from the bottom of qlist, second list from the top
+            const uint32_t q = warp_append(s_nq, queue);
+            if (queue) {
+              qlist[q] = (uint16_t)slot;
+              cval[head] = vb;          // the list was read above: its head keeps the value
+            }
+            const uint32_t sl = warp_append(s_nslow, slow);
+            if (slow) qlist[T - 1 - sl] = (uint16_t)slot;
+          }
+          if (i < nslots && !queue && !slow) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; }
+        }
+        if (STYLE != STYLE_INTEGER) {
+          __syncthreads();
+          const uint32_t nq = *s_nq, nslow = *s_nslow;
+          // ---- addresses with three or more contributions ----
+          for (uint32_t i0 = (uint32_t)w * 32; i0 < nslow; i0 += ANN_THREADS) {
+            const uint32_t i = i0 + lane;
+            bool keep = false;
+            uint64_t key = 0, vb = 0;
+            if (i < nslow && nq + i < T) {
+              const int slot = qlist[T - 1 - i];
+              key = tkey[slot];
+              const uint32_t head = thead[slot];
+              tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
+              double fv;
+              if (a.init_rule) {
+                fv = initiator_sum_f(a, head, cval, clink, ncon, acc, &bad);
               } else {
                 U128 sum{0, 0};
                 bool exact = true, have_d = false;
                 double first = 0.0;
+                uint32_t steps = 0;
                 for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
                   if (c >= ncon || ++steps > ncon) { bad = true; break; }
                   const uint64_t v = cval[c];
@@ -965,36 +1041,25 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
                                           ncon, &bad);
                 }
               }
-              vb = dbits(fv);
               if (!is_zero_d(fv)) {
                 acc.len_before++;
                 bool small = false;
                 if (a.comp_mode == 1) small = abs_lt_one(fv);
                 else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
                 if (small) {
-                  queue = head < ncon;
+                  keep = compress_draw<STYLE>(a, r, step, key, fv);
+                  if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
                 } else {
                   keep = true;
                   account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
                 }
               }
+              vb = dbits(fv);
             }
+            const uint32_t pos = warp_append(&s_out, keep);
+            if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
           }
-          const uint32_t pos = warp_append(&s_out, keep);
-          if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
-          if (STYLE != STYLE_INTEGER) {
-            const uint32_t q = warp_append(s_nq, queue);
-            if (queue) {
-              // the list was read above: its head entry keeps the value until the draw
-              qlist[q] = (uint16_t)slot;
-              cval[head] = vb;
-            }
-          }
-          if (i < nslots && !queue) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; }
-        }
-        if (STYLE != STYLE_INTEGER && a.comp_mode != 0) {
-          __syncthreads();
-          const uint32_t nq = *s_nq;
+          // ---- compression draws of the queued addresses, on full warps ----
           for (uint32_t i0 = (uint32_t)w * 32; i0 < nq; i0 += ANN_THREADS) {
             const uint32_t i = i0 + lane;
             bool keep = false;
@@ -1006,7 +1071,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
               fv = bitsd(cval[thead[slot]]);
               tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
               keep = compress_draw<STYLE>(a, r, step, key, fv);
-              if (keep) account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+              if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
             }
             const uint32_t pos = warp_append(&s_out, keep);
             if (keep && pos < a.capv) vout[pos] = Rec{key, dbits(fv)};

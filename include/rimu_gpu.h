@@ -58,19 +58,33 @@ typedef struct rimu_wm rimu_wm;
 
 /* Hamiltonian description.  Addresses are single-chunk bit strings of at most 64 bits
  * (BoseFS: n_particles + n_modes - 1 bits; FermiFS: n_modes bits), with the chunk layout of
- * src/BitStringAddresses/bitstring.jl:464-472 (bosons) and 713-723 (fermions). */
+ * src/BitStringAddresses/bitstring.jl:464-472 (bosons) and 713-723 (fermions).
+ *
+ * Two-component addresses (CompositeFS of two components, multicomponent.jl:10-30, and its
+ * alias FermiFS2C, :87-103): n_components = 2, each component a BoseFS or FermiFS with the
+ * same n_modes, both in one 64-bit key: component 1 in the high bits, component 2 in the low
+ * comp_bits(2) bits, so that unsigned key order is the reference's order of the component
+ * tuple (multicomponent.jl:79).  The two widths must add up to at most 64 bits.  Supported
+ * for HubbardRealSpace (CompositeFS of BoseFS/FermiFS components, HubbardRealSpace.jl:18-61,
+ * 100-107, 344-391) and HubbardMom1D (FermiFS2C, HubbardMom1D.jl:141-205). */
 typedef struct {
   int kind;                 /* RIMU_MODEL_* */
   int fermion;              /* 1: FermiFS addresses (RIMU_MODEL_REALSPACE only) */
-  int n_particles;
-  int n_modes;
+  int n_particles;          /* all components together */
+  int n_modes;              /* per component */
   double u;                 /* interaction (HubbardRealSpace: u[1,1]) */
   double t;                 /* hopping */
   int ndim;                 /* HubbardRealSpace CubicGrid dimensions (1..3) */
   int dims[3];
   int periodic[3];          /* 1: PeriodicBoundaries, 0: HardwallBoundaries per dimension */
-  const double *potential;  /* HubbardRealSpace trap energy per site (n_modes) or NULL */
+  const double *potential;  /* HubbardRealSpace trap energy per site (n_modes; with two
+                               components 2 * n_modes, component 1 first) or NULL */
   const double *dispersion; /* HubbardMom1D kinetic energies h.kes (n_modes), required */
+  int n_components;         /* 0 or 1: one component; 2: two components */
+  int comp_fermion[2];      /* per component: 1 FermiFS, 0 BoseFS */
+  int comp_particles[2];    /* particles per component */
+  double comp_t[2];         /* HubbardRealSpace hopping t[c] */
+  double comp_u[3];         /* HubbardRealSpace interaction u[1,1], u[1,2] = u[2,1], u[2,2] */
 } rimu_model_desc;
 
 /* Parameters of one projector step (apply_operator!, src/Interfaces/dictvectors.jl:112). */

@@ -40,7 +40,9 @@ class _OModel(C.Structure):
     _fields_ = [("kind", C.c_int), ("fermion", C.c_int), ("N", C.c_int), ("M", C.c_int),
                 ("u", C.c_double), ("t", C.c_double), ("ndim", C.c_int),
                 ("dims", C.c_int * 3), ("periodic", C.c_int * 3),
-                ("pot", C.POINTER(C.c_double)), ("kes", C.POINTER(C.c_double))]
+                ("pot", C.POINTER(C.c_double)), ("kes", C.POINTER(C.c_double)),
+                ("ncomp", C.c_int), ("cferm", C.c_int * 2), ("cN", C.c_int * 2),
+                ("ct", C.c_double * 2), ("cu", C.c_double * 3)]
 
 
 class _OParams(C.Structure):
@@ -116,6 +118,11 @@ class Model:
     periodic: tuple = ()
     pot: np.ndarray | None = None
     kes: np.ndarray | None = None
+    # two components (CompositeFS / FermiFS2C): per-component fermion flags, particle numbers,
+    # HubbardRealSpace hoppings and the interactions (u11, u12, u22)
+    comps: tuple = ()
+    ct: tuple = (1.0, 1.0)
+    cu: tuple = (0.0, 0.0, 0.0)
     _keep: list = field(default_factory=list, repr=False)
 
     def struct(self) -> _OModel:
@@ -136,10 +143,22 @@ class Model:
             arr = np.ascontiguousarray(self.kes, dtype=np.float64)
             self._keep.append(arr)
             m.kes = _p(arr, C.c_double)
+        m.ncomp = 2 if self.comps else 1
+        for c, (ferm, n) in enumerate(self.comps):
+            m.cferm[c], m.cN[c] = int(ferm), int(n)
+        m.ct[0], m.ct[1] = (float(x) for x in self.ct)
+        for i in range(3):
+            m.cu[i] = float(self.cu[i])
         return m
+
+    def comp_bits(self, c: int) -> int:
+        ferm, n = self.comps[c]
+        return self.M if ferm else n + self.M - 1
 
     @property
     def nbits(self) -> int:
+        if self.comps:
+            return self.comp_bits(0) + self.comp_bits(1)
         return self.M if self.fermion else self.N + self.M - 1
 
 
@@ -164,6 +183,24 @@ def realspace(N, dims, u=1.0, t=1.0, periodic=None, fermion=False, pot=None):
 
 def mom1d(N, M, u=1.0, t=1.0):
     return Model(MOM1D, N, M, u, t, kes=mom1d_kes(M, t))
+
+
+def realspace2(comps, dims, t=(1.0, 1.0), u=((1.0, 1.0), (1.0, 1.0)), periodic=None, pot=None):
+    """HubbardRealSpace with a two-component CompositeFS: `comps` = ((fermion, N), (fermion,
+    N)) for components 1 and 2; `u` the symmetric 2x2 interaction matrix; `pot` (2, M) or None."""
+    M = int(np.prod(dims))
+    periodic = periodic if periodic is not None else tuple(True for _ in dims)
+    u = np.asarray(u, dtype=float)
+    p = None if pot is None else np.ascontiguousarray(np.ravel(np.asarray(pot, dtype=float)))
+    N = sum(n for _, n in comps)
+    return Model(REALSPACE, N, M, 0.0, 0.0, False, tuple(dims), tuple(periodic), p,
+                 comps=tuple((bool(f), int(n)) for f, n in comps), ct=tuple(t),
+                 cu=(u[0, 0], u[0, 1], u[1, 1]))
+
+
+def mom1d_2c(N1, N2, M, u=1.0, t=1.0):
+    """HubbardMom1D with a FermiFS2C address of N1 and N2 fermions in M modes."""
+    return Model(MOM1D, N1 + N2, M, u, t, kes=mom1d_kes(M, t), comps=((True, N1), (True, N2)))
 
 
 # ----------------------------------------------------------------------------------------
@@ -286,12 +323,21 @@ def step(m: Model, prm: StepParams, keys, vals):
 # ----------------------------------------------------------------------------------------
 # Full-basis products and exact diagonalisation
 # ----------------------------------------------------------------------------------------
-def basis(m: Model) -> np.ndarray:
-    B, w = m.nbits, m.N
+def _fixed_weight(B, w):
     n = lib().o_enumerate_fixed_weight(B, w, None, 0)
     out = np.zeros(n, dtype=np.uint64)
     lib().o_enumerate_fixed_weight(B, w, _p(out, C.c_uint64), n)
     return out
+
+
+def basis(m: Model) -> np.ndarray:
+    """All addresses with the model's particle numbers, in increasing order (build_basis,
+    basis_fock.jl:12-36); for two components the product of the component bases."""
+    if m.comps:
+        b0 = _fixed_weight(m.comp_bits(0), m.comps[0][1])
+        b1 = _fixed_weight(m.comp_bits(1), m.comps[1][1])
+        return ((b0[:, None] << np.uint64(m.comp_bits(1))) | b1[None, :]).ravel()
+    return _fixed_weight(m.nbits, m.N)
 
 
 def hv_basis(m: Model, keys, v):

@@ -14,6 +14,12 @@
  *                                                 279-338; geometry.jl:127-139,161-181,232-235
  *   - HubbardMom1D (BoseFS)                       src/Hamiltonians/HubbardMom1D.jl:49-65,131-194;
  *                                                 excitations.jl:26-80,126-137
+ *   - two-component addresses (CompositeFS of     src/BitStringAddresses/multicomponent.jl:10-103
+ *     two components, FermiFS2C) with
+ *     HubbardRealSpace                            src/Hamiltonians/HubbardRealSpace.jl:18-61,
+ *                                                 90-107,284-287,344-391
+ *     and HubbardMom1D (FermiFS2C)                src/Hamiltonians/HubbardMom1D.jl:141-205;
+ *                                                 excitations.jl:82-119,172-180
  *   - FirstOrderTransitionOperator                src/fciqmc.jl:78-112
  *   - the stochastic styles                       src/StochasticStyles/styles.jl:11-25,94-105,
  *                                                 175-214; spawning.jl:9-93,174-182,232-243,
@@ -125,14 +131,38 @@ typedef struct {
   int ndim;          /* HubbardRealSpace geometry */
   int dims[3];
   int periodic[3];
-  const double *pot; /* HubbardRealSpace trap energy per site, or NULL */
+  const double *pot; /* HubbardRealSpace trap energy per site (two components: 2M, component
+                        1 first), or NULL */
   const double *kes; /* HubbardMom1D dispersion per mode */
+  /* Two components: the key holds component 1 in its high bits and component 2 in the low
+   * cbits[1] bits; the ONR of such an address is component 1's M modes then component 2's. */
+  int ncomp;         /* 1 or 2 */
+  int cferm[2];      /* FermiFS (1) or BoseFS (0) per component */
+  int cN[2];         /* particles per component */
+  double ct[2];      /* HubbardRealSpace t per component */
+  double cu[3];      /* HubbardRealSpace u[1,1], u[1,2], u[2,2] */
 } o_model;
 
+static int o_comp_bits(const o_model *h, int c) {
+  return h->cferm[c] ? h->M : h->cN[c] + h->M - 1;
+}
 static void o_to_onr(const o_model *h, uint64_t key, int *onr) {
+  if (h->ncomp == 2) {
+    int b1 = o_comp_bits(h, 1);
+    uint64_t k0 = b1 >= 64 ? 0 : key >> b1, k1 = b1 >= 64 ? key : key & (((uint64_t)1 << b1) - 1);
+    if (h->cferm[0]) o_fermi_to_onr(k0, h->M, onr); else o_bose_to_onr(k0, h->M, onr);
+    if (h->cferm[1]) o_fermi_to_onr(k1, h->M, onr + h->M); else o_bose_to_onr(k1, h->M, onr + h->M);
+    return;
+  }
   if (h->fermion) o_fermi_to_onr(key, h->M, onr); else o_bose_to_onr(key, h->M, onr);
 }
 static uint64_t o_from_onr(const o_model *h, const int *onr) {
+  if (h->ncomp == 2) {
+    uint64_t k0 = h->cferm[0] ? o_fermi_from_onr(onr, h->M) : o_bose_from_onr(onr, h->M);
+    uint64_t k1 = h->cferm[1] ? o_fermi_from_onr(onr + h->M, h->M) : o_bose_from_onr(onr + h->M, h->M);
+    int b1 = o_comp_bits(h, 1);
+    return (b1 >= 64 ? 0 : k0 << b1) | k1;
+  }
   return h->fermion ? o_fermi_from_onr(onr, h->M) : o_bose_from_onr(onr, h->M);
 }
 static int o_num_occupied(const int *onr, int M) {
@@ -165,8 +195,13 @@ static int o_neighbor_site(const o_model *h, int mode, int chosen) {
 }
 
 int o_num_offdiagonals(const o_model *h, uint64_t key) {
-  int onr[O_MAXM];
+  int onr[2 * O_MAXM];
   o_to_onr(h, key, onr);
+  if (h->ncomp == 2) {
+    if (h->kind == O_MOM1D) return h->cN[0] * h->cN[1] * (h->M - 1);   /* HubbardMom1D.jl:141-144 */
+    /* each component's hops (HubbardRealSpace.jl:316-321, 366-371) */
+    return (o_num_occupied(onr, h->M) + o_num_occupied(onr + h->M, h->M)) * 2 * h->ndim;
+  }
   int s = o_num_occupied(onr, h->M);
   if (h->kind == O_REAL1D) return 2 * s;                        /* HubbardReal1D.jl:51-53 */
   if (h->kind == O_REALSPACE) return s * 2 * h->ndim;           /* HubbardRealSpace.jl:316-321 */
@@ -190,12 +225,69 @@ static int o_fermi_hop(int *onr, int src, int dst) {
 /* Hamiltonian matrix element of offdiagonal `chosen` (1-based) of column `key`:
  * returns the new address and H_{new,key}; *prod receives the integer under the square
  * root of the element (0 for an illegal move). */
+/* One component's HubbardRealSpace hop on its ONR (HubbardRealSpace.jl:325-338): returns the
+ * matrix element -t * excitation value and the product under the square root; onr updated. */
+static double o_realspace_hop(const o_model *h, int *onr, int fermion, double t, int chosen,
+                              long *prod) {
+  int M = h->M, nb = 2 * h->ndim;
+  int particle = (chosen - 1) / nb + 1, neigh = (chosen - 1) % nb + 1;
+  int src = o_find_occupied(onr, M, particle);
+  int dst = o_neighbor_site(h, src, neigh);
+  *prod = 0;
+  if (dst < 0) return 0.0;
+  if (fermion) {
+    int sgn = o_fermi_hop(onr, src, dst);
+    if (!sgn) return 0.0;
+    *prod = 1;
+    return -t * (double)sgn;
+  }
+  int value = onr[src] * (onr[dst] + 1);   /* bose_excitation_value, fockaddress.jl:559-567 */
+  *prod = value;
+  onr[src] -= 1;
+  onr[dst] += 1;
+  return -t * sqrt((double)value);
+}
+
 void o_get_offdiagonal_p(const o_model *h, uint64_t key, int chosen, uint64_t *nkey,
                          double *val, long *prod) {
-  int onr[O_MAXM];
+  int onr[2 * O_MAXM];
   *prod = 0;
   o_to_onr(h, key, onr);
   int M = h->M;
+  if (h->ncomp == 2 && h->kind == O_REALSPACE) {
+    /* component 1's hops, then component 2's (HubbardRealSpace.jl:344-391) */
+    int n0 = o_num_occupied(onr, M) * 2 * h->ndim;
+    int c = chosen <= n0 ? 0 : 1;
+    double v = o_realspace_hop(h, onr + c * M, h->cferm[c], h->ct[c], c ? chosen - n0 : chosen, prod);
+    if (*prod == 0) { *nkey = key; *val = 0.0; return; }
+    *nkey = o_from_onr(h, onr);
+    *val = v;
+    return;
+  }
+  if (h->ncomp == 2) {
+    /* FermiFS2C: momentum_transfer_excitation of two components, fold=true
+     * (excitations.jl:82-119); element u/M * (val_a * val_b) (HubbardMom1D.jl:196-205) */
+    int *oa = onr, *ob = onr + M;
+    int nbn = h->cN[1];
+    int src_a, rem, dst_a, src_b;
+    src_a = (chosen - 1) / ((M - 1) * nbn) + 1;          /* fldmod1(chosen, (M-1)*N_b) */
+    rem = (chosen - 1) % ((M - 1) * nbn) + 1;
+    dst_a = (rem - 1) / nbn + 1;                          /* fldmod1(rem, N_b) */
+    src_b = (rem - 1) % nbn + 1;
+    int sa = o_find_occupied(oa, M, src_a) + 1, sb = o_find_occupied(ob, M, src_b) + 1;
+    if (dst_a >= sa) dst_a += 1;
+    int mom = dst_a - sa;
+    int dst_b = sb - mom;
+    dst_a = ((dst_a - 1) % M + M) % M + 1;                /* mod1 */
+    dst_b = ((dst_b - 1) % M + M) % M + 1;
+    int ga = o_fermi_hop(oa, sa - 1, dst_a - 1);
+    int gb = ga ? o_fermi_hop(ob, sb - 1, dst_b - 1) : 0;
+    if (!ga || !gb) { *nkey = key; *val = 0.0; return; }
+    *nkey = o_from_onr(h, onr);
+    *prod = 4;
+    *val = h->u / M * ((double)ga * (double)gb);
+    return;
+  }
   if (h->kind == O_REAL1D) {
     /* hopnextneighbour restated on the ONR, as in test/BitStringAddresses.jl:251-267. */
     int site = (chosen + 1) / 2;
@@ -275,10 +367,49 @@ void o_get_offdiagonal(const o_model *h, uint64_t key, int chosen, uint64_t *nke
   o_get_offdiagonal_p(h, key, chosen, nkey, val, &prod);
 }
 
+/* external_potential of one component (HubbardRealSpace.jl:90-97). */
+static double o_potential(const int *onr, int M, const double *pot) {
+  double pe = 0.0;
+  for (int i = 0; i < M; ++i) if (onr[i]) pe += onr[i] * pot[i];
+  return pe;
+}
+
 double o_diagonal(const o_model *h, uint64_t key) {
-  int onr[O_MAXM];
+  int onr[2 * O_MAXM];
   o_to_onr(h, key, onr);
   int M = h->M;
+  if (h->ncomp == 2 && h->kind == O_MOM1D) {
+    /* dot(kes, map_a) + dot(kes, map_b) + u/2M * 2 n_a n_b (HubbardMom1D.jl:182-187) */
+    double ka = 0.0, kb = 0.0;
+    long na = 0, nb = 0;
+    for (int i = 0; i < M; ++i) if (onr[i]) { ka += h->kes[i] * 1; ++na; }
+    for (int i = 0; i < M; ++i) if (onr[M + i]) { kb += h->kes[i] * 1; ++nb; }
+    return ka + kb + h->u / (2 * M) * (double)(2 * na * nb);
+  }
+  if (h->ncomp == 2) {
+    /* _interactions of two components: (self_1 + (u12 * dot + 0)) + ((self_2 + 0) + 0.0),
+     * local_interaction of a FermiFS being 0 (HubbardRealSpace.jl:18-61); then the trap,
+     * (0.0 + pot_1) + pot_2 (:100-107); diagonal = int + pot (:284-287). */
+    double in = 0.0;
+    if (h->cu[0] != 0.0 || h->cu[1] != 0.0 || h->cu[2] != 0.0) {
+      double self[2];
+      for (int c = 0; c < 2; ++c) {
+        long bhi = 0;
+        for (int i = 0; i < M; ++i) bhi += (long)onr[c * M + i] * (onr[c * M + i] - 1);
+        self[c] = h->cferm[c] ? 0.0 : h->cu[c == 0 ? 0 : 2] * (double)bhi / 2;
+      }
+      long dot = 0;
+      for (int i = 0; i < M; ++i) dot += (long)onr[i] * onr[M + i];
+      double row = h->cu[1] * (double)dot + 0.0;
+      in = (self[0] + row) + (self[1] + 0.0);
+    }
+    double pe = 0.0;
+    if (h->pot) {
+      pe += o_potential(onr, M, h->pot);
+      pe += o_potential(onr + M, M, h->pot + M);
+    }
+    return in + pe;
+  }
   if (h->kind == O_REAL1D) {
     long bhi = 0;
     for (int i = 0; i < M; ++i) bhi += (long)onr[i] * (onr[i] - 1);
@@ -717,7 +848,7 @@ int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, co
   int64_t missing = o_hv_basis(h, keys, D, gw, gv);
   double su = 0.0, st = 0.0;
   for (int64_t i = 0; i < D; ++i) {
-    int onr[O_MAXM];
+    int onr[2 * O_MAXM];
     o_to_onr(h, keys[i], onr);
     long bhi = 0;
     for (int k = 0; k < h->M; ++k) bhi += (long)onr[k] * (onr[k] - 1);

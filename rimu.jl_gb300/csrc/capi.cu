@@ -100,11 +100,31 @@ int rimu_ctx_synchronize(rimu_ctx *ctx) {
 // ---------------------------------------------------------------------------------------------
 // Helpers
 // ---------------------------------------------------------------------------------------------
+static bool two_components(const rimu_model_desc &d) { return d.n_components == 2; }
+
+// Largest occupation product under the square root of an offdiagonal element (one table
+// block; with two HubbardRealSpace components, of either component).
 static int model_max_prod(const rimu_model_desc &d) {
   int N = d.n_particles;
-  if (d.kind == RIMU_MODEL_MOM1D) return (N + 1) * (N + 1) * (N + 1) * (N + 1);
+  if (d.kind == RIMU_MODEL_MOM1D) return two_components(d) ? 4 : (N + 1) * (N + 1) * (N + 1) * (N + 1);
+  if (two_components(d)) {
+    int p = 1;
+    for (int c = 0; c < 2; ++c)
+      if (!d.comp_fermion[c]) p = std::max(p, d.comp_particles[c] * (d.comp_particles[c] + 1));
+    return p;
+  }
   if (d.fermion) return 1;
   return N * (N + 1);
+}
+
+// Hamiltonian offdiagonal magnitude for occupation product p in table block c: -t sqrt(p)
+// (HubbardReal1D.jl:59-62, HubbardRealSpace.jl:336, per component t[c]) or u/(2M) sqrt(p)
+// (HubbardMom1D.jl:189-194; FermiFS2C's u/M is p = 4).
+static double hoff_value(const rimu_model_desc &d, int c, int p) {
+  const double s = std::sqrt((double)p);
+  if (d.kind == RIMU_MODEL_MOM1D) return d.u / (2 * d.n_modes) * s;
+  const double t = two_components(d) ? d.comp_t[c] : d.t;
+  return -t * s;
 }
 
 static int64_t binomial_u(int n, int k, bool *ovf) {
@@ -135,7 +155,26 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
   if (d->kind < 1 || d->kind > 3) return bad("rimu_model_create: unknown model kind");
   if (d->n_particles < 0 || d->n_modes < 1 || d->n_modes > 64)
     return bad("rimu_model_create: need 1 <= n_modes <= 64");
+  if (d->n_components < 0 || d->n_components > 2)
+    return bad("rimu_model_create: n_components must be 0, 1 or 2");
+  const bool two = two_components(*d);
   int nbits = d->fermion ? d->n_modes : d->n_particles + d->n_modes - 1;
+  int cbits[2] = {0, 0};
+  if (two) {
+    if (d->kind == RIMU_MODEL_REAL1D)
+      return bad("rimu_model_create: HubbardReal1D takes a single-component BoseFS");
+    if (d->kind == RIMU_MODEL_MOM1D && !(d->comp_fermion[0] && d->comp_fermion[1]))
+      return bad("rimu_model_create: HubbardMom1D takes two components only as FermiFS2C");
+    for (int c = 0; c < 2; ++c) {
+      if (d->comp_particles[c] < 0) return bad("rimu_model_create: negative particle number");
+      if (d->comp_fermion[c] && d->comp_particles[c] > d->n_modes)
+        return bad("rimu_model_create: too many fermions in a component");
+      cbits[c] = d->comp_fermion[c] ? d->n_modes : d->comp_particles[c] + d->n_modes - 1;
+    }
+    if (d->comp_particles[0] + d->comp_particles[1] != d->n_particles)
+      return bad("rimu_model_create: n_particles must be the sum over the components");
+    nbits = cbits[0] + cbits[1];
+  }
   if (nbits > 64) return bad("rimu_model_create: address does not fit 64 bits");
   if (d->fermion && d->kind != RIMU_MODEL_REALSPACE)
     return bad("rimu_model_create: FermiFS is supported with HubbardRealSpace only");
@@ -160,8 +199,17 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
   m->desc.potential = nullptr;
   m->desc.dispersion = nullptr;
   DevModel &h = m->dm;
-  h.kind = d->kind; h.fermion = d->fermion; h.N = d->n_particles; h.M = d->n_modes;
+  h.kind = d->kind; h.fermion = two ? 0 : d->fermion; h.N = d->n_particles; h.M = d->n_modes;
   h.nbits = nbits; h.u = d->u; h.t = d->t;
+  h.ncomp = two ? 2 : 1;
+  for (int c = 0; c < 2; ++c) {
+    h.cferm[c] = two ? (d->comp_fermion[c] != 0) : 0;
+    h.cN[c] = two ? d->comp_particles[c] : 0;
+    h.cbits[c] = cbits[c];
+    h.ct[c] = two ? d->comp_t[c] : d->t;
+  }
+  for (int i = 0; i < 3; ++i) h.cu[i] = two ? d->comp_u[i] : 0.0;
+  h.u_nonzero = two && (d->comp_u[0] != 0.0 || d->comp_u[1] != 0.0 || d->comp_u[2] != 0.0);
   h.ndim = ndim;
   for (int i = 0; i < 3; ++i) {
     h.dims[i] = d->kind == RIMU_MODEL_REALSPACE ? (i < ndim ? d->dims[i] : 1) : (i == 0 ? d->n_modes : 1);
@@ -174,7 +222,8 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     h.kes = m->d_kes;
   }
   if (d->kind == RIMU_MODEL_REALSPACE && d->potential) {
-    if ((rc = dalloc(ctx, &m->d_pot, M)) || (rc = h2d(ctx, m->d_pot, d->potential, M))) goto fail;
+    const int np = two ? 2 * M : M;    // with two components: component 1's sites first
+    if ((rc = dalloc(ctx, &m->d_pot, np)) || (rc = h2d(ctx, m->d_pot, d->potential, np))) goto fail;
     h.pot = m->d_pot;
   }
   {
@@ -188,29 +237,34 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     h.recip = m->d_recip;
     h.dint = m->d_recip + nr;
     h.recip_len = nr;
-    // Hamiltonian offdiagonal magnitudes: -t sqrt(p) (HubbardReal1D.jl:59-62,
-    // HubbardRealSpace.jl:336) or u/(2M) sqrt(p) (HubbardMom1D.jl:189-194)
-    int pmax = model_max_prod(*d);
-    m->aoff_len = pmax + 1;
-    std::vector<double> hoff(pmax + 1);
-    for (int p = 0; p <= pmax; ++p) {
-      double s = std::sqrt((double)p);
-      hoff[p] = d->kind == RIMU_MODEL_MOM1D ? d->u / (2 * M) * s : -d->t * s;
-    }
-    if ((rc = dalloc(ctx, &m->d_hoff, pmax + 1)) || (rc = h2d(ctx, m->d_hoff, hoff.data(), pmax + 1)))
+    // Hamiltonian offdiagonal magnitudes by occupation product, one block per component
+    // with its own t for two HubbardRealSpace components
+    const int pmax = model_max_prod(*d);
+    const int blocks = (two && d->kind == RIMU_MODEL_REALSPACE) ? 2 : 1;
+    const int len = blocks * (pmax + 1);
+    m->aoff_len = len;
+    h.cstride = blocks == 2 ? pmax + 1 : 0;
+    std::vector<double> hoff(len);
+    for (int c = 0; c < blocks; ++c)
+      for (int p = 0; p <= pmax; ++p) hoff[c * (pmax + 1) + p] = hoff_value(*d, c, p);
+    if ((rc = dalloc(ctx, &m->d_hoff, len)) || (rc = h2d(ctx, m->d_hoff, hoff.data(), len)))
       goto fail;
-    if ((rc = dalloc(ctx, &m->d_aoff, pmax + 1))) goto fail;
+    if ((rc = dalloc(ctx, &m->d_aoff, len))) goto fail;
     h.hoff = m->d_hoff;
     h.aoff = m->d_aoff;
-    h.aoff_len = pmax + 1;
+    h.aoff_len = len;
     m->aoff_dt = std::nan("");
-    bool table_diag = d->kind == RIMU_MODEL_REAL1D ||
-                      (d->kind == RIMU_MODEL_REALSPACE && !d->potential);
+    bool table_diag = !two && (d->kind == RIMU_MODEL_REAL1D ||
+                               (d->kind == RIMU_MODEL_REALSPACE && !d->potential));
     m->ndiag = table_diag ? (d->fermion ? 1 : N * (N - 1) + 1) : 0;
     // max offdiagonals of a column (capacity planning)
-    if (d->kind == RIMU_MODEL_MOM1D) {
+    if (d->kind == RIMU_MODEL_MOM1D && two) {
+      m->max_offdiag = d->comp_particles[0] * d->comp_particles[1] * (M - 1);
+    } else if (d->kind == RIMU_MODEL_MOM1D) {
       int s = std::min(N, M);
       m->max_offdiag = s * (s - 1) * (M - 2) + s * (M - 1);
+    } else if (two) {
+      m->max_offdiag = (std::min(d->comp_particles[0], M) + std::min(d->comp_particles[1], M)) * 2 * ndim;
     } else {
       int s = std::min(N, M);
       m->max_offdiag = s * 2 * ndim;
@@ -254,13 +308,9 @@ extern "C" int rimu_model_destroy(rimu_model *m) {
 int ensure_aoff(rimu_model *m, double dt) {
   if (m->aoff_dt == dt) return RIMU_OK;
   const rimu_model_desc &d = m->desc;
-  int n = m->aoff_len, M = d.n_modes;
+  const int n = m->aoff_len, stride = m->dm.cstride ? m->dm.cstride : n;
   std::vector<double> a(n);
-  for (int p = 0; p < n; ++p) {
-    double s = std::sqrt((double)p);
-    double hv = d.kind == RIMU_MODEL_MOM1D ? d.u / (2 * M) * s : -d.t * s;
-    a[p] = -hv * dt;
-  }
+  for (int i = 0; i < n; ++i) a[i] = -hoff_value(d, i / stride, i % stride) * dt;
   int rc = h2d(m->ctx, m->d_aoff, a.data(), n);
   if (rc) return rc;
   RIMU_CUDA(cudaStreamSynchronize(m->ctx->stream));
@@ -285,6 +335,7 @@ extern "C" int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t 
 
 static int host_num_offdiagonals(const rimu_model *m, uint64_t key) {
   const DevModel &h = m->dm;
+  if (h.kind == MODEL_MOM1D && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
   if (h.kind == MODEL_MOM1D) {
     MomMap mm;
     mom_map(key, mm);
@@ -832,6 +883,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
 static int basis_dim(const rimu_model *m, int64_t *dim) {
   bool ovf = false;
   int B = m->dm.nbits, w = m->dm.N;
+  if (m->dm.ncomp == 2) { g_err = "basis: two-component addresses are not supported"; return RIMU_ERR_BADARG; }
   if (B > 63) { g_err = "basis: address wider than 63 bits"; return RIMU_ERR_BADARG; }
   *dim = binomial_u(B, w, &ovf);
   if (ovf) { g_err = "basis: dimension does not fit int64"; return RIMU_ERR_BADARG; }

@@ -31,6 +31,8 @@ namespace rimu {
 template <int KIND>
 __device__ __forceinline__ int column_noff(const DevModel &h, uint64_t key) {
   if (KIND == MODEL_MOM1D) {
+    // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144)
+    if (h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
     MomMap m;
     mom_map(key, m);
     return num_offdiagonals_mom(h, m);
@@ -42,6 +44,7 @@ template <int KIND>
 __device__ __forceinline__ Offdiag column_offdiag(const DevModel &h, uint64_t key, int chosen) {
   if (KIND == MODEL_REAL1D) return real1d_offdiag(h, key, chosen);
   if (KIND == MODEL_REALSPACE) return realspace_offdiag(h, key, chosen);
+  if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
   MomMap m;
   mom_map(key, m);
   return mom1d_offdiag(h, key, m, chosen);
@@ -60,9 +63,63 @@ __device__ __forceinline__ int bose_interaction(uint64_t key) {
   return acc;
 }
 
+// external_potential of one component chunk: sum over occupied modes, in mode order, of
+// n * pot[mode] (HubbardRealSpace.jl:90-97)
+__device__ __forceinline__ double component_potential(uint64_t ck, int fermion, const double *pot) {
+  double pe = 0.0;
+  uint64_t x = ck;
+  if (fermion) {
+    while (x) { int b = ctz64(x); pe += 1.0 * pot[b]; x &= x - 1; }
+    return pe;
+  }
+  int mode = 1;
+  while (x) {
+    int z = ctz64(x);
+    x = shr64(x, z); mode += z;
+    int n = ctz64(~x);
+    pe += (double)n * pot[mode - 1];
+    x = shr64(x, n);
+  }
+  return pe;
+}
+
+// dot(h.kes, OccupiedModeMap(f)) of a FermiFS chunk (fockaddress.jl:316-322)
+__device__ __forceinline__ double fermi_kinetic(uint64_t ck, const double *kes) {
+  double kin = 0.0;
+  uint64_t x = ck;
+  while (x) { int b = ctz64(x); kin += kes[b] * 1.0; x &= x - 1; }
+  return kin;
+}
+
 // Hamiltonian diagonal computed per address (HubbardRealSpace with trap, HubbardMom1D).
 template <int KIND>
 __device__ double model_diagonal(const DevModel &h, uint64_t key) {
+  if (KIND == MODEL_MOM1D && h.ncomp == 2) {
+    // FermiFS2C: dot(kes, map_a) + dot(kes, map_b) + u/(2M) * 2 n_a n_b
+    // (HubbardMom1D.jl:168-171, 182-187; excitations.jl:172-180)
+    const uint64_t ka = component_of(h, key, 0), kb = component_of(h, key, 1);
+    const long long nab = 2LL * popc64(ka) * popc64(kb);
+    return fermi_kinetic(ka, h.kes) + fermi_kinetic(kb, h.kes) + h.u / (2 * h.M) * (double)nab;
+  }
+  if (KIND == MODEL_REALSPACE && h.ncomp == 2) {
+    // local_interaction of the two components with the u matrix, then the trap
+    // (HubbardRealSpace.jl:18-61, 100-107, 284-287).  _interactions evaluates
+    // (self_1 + (u12 * dot + 0)) + ((self_2 + 0) + 0.0); the "+ 0.0" terms keep its signed zeros.
+    const uint64_t k0 = component_of(h, key, 0), k1 = component_of(h, key, 1);
+    double in = 0.0;
+    if (h.u_nonzero) {
+      const double s0 = h.cferm[0] ? 0.0 : h.cu[0] * (double)bose_interaction(k0) / 2;
+      const double row = h.cu[1] * (double)component_overlap(h, k0, k1) + 0.0;
+      const double s1 = (h.cferm[1] ? 0.0 : h.cu[2] * (double)bose_interaction(k1) / 2) + 0.0;
+      in = (s0 + row) + s1;
+    }
+    double pe = 0.0;
+    if (h.pot) {
+      pe += component_potential(k0, h.cferm[0], h.pot);
+      pe += component_potential(k1, h.cferm[1], h.pot + h.M);
+    }
+    return in + pe;
+  }
   if (KIND == MODEL_MOM1D) {
     // dot(h.kes, map) + u/(2M) * momentum_transfer_diagonal(map)  (HubbardMom1D.jl:174-177)
     uint64_t x = key;
@@ -88,23 +145,7 @@ __device__ double model_diagonal(const DevModel &h, uint64_t key) {
   // HubbardRealSpace one component (HubbardRealSpace.jl:284-293)
   double in = 0.0;
   if (!h.fermion && h.u != 0.0) in = h.u * (double)bose_interaction(key) / 2;
-  double pe = 0.0;
-  if (h.pot) {
-    if (h.fermion) {
-      uint64_t x = key;
-      while (x) { int b = ctz64(x); pe += 1.0 * h.pot[b]; x &= x - 1; }
-    } else {
-      uint64_t x = key;
-      int mode = 1;
-      while (x) {
-        int z = ctz64(x);
-        x = shr64(x, z); mode += z;
-        int n = ctz64(~x);
-        pe += (double)n * h.pot[mode - 1];
-        x = shr64(x, n);
-      }
-    }
-  }
+  const double pe = h.pot ? component_potential(key, h.fermion, h.pot) : 0.0;
   return in + pe;
 }
 

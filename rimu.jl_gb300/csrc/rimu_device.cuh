@@ -44,6 +44,16 @@ struct DevModel {
   const double *recip;   // recip[n] = 1.0 / n for n < recip_len
   int recip_len;
   const double *dint;    // dint[n] = (double)n for n < recip_len
+  // Two-component addresses (CompositeFS, FermiFS2C): component 1 in the high bits
+  // [cbits[1], cbits[1] + cbits[0]) of the key, component 2 in the low cbits[1] bits.
+  int ncomp;             // 1 or 2
+  int cferm[2];          // per component: FermiFS (1) or BoseFS (0)
+  int cN[2];             // particles per component
+  int cbits[2];          // bits per component
+  double ct[2];          // HubbardRealSpace hopping t[c]
+  double cu[3];          // HubbardRealSpace u[1,1], u[1,2], u[2,2]
+  int u_nonzero;         // HubbardRealSpace: some interaction is nonzero
+  int cstride;           // offdiagonal-table offset of component 2 (HubbardRealSpace)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -361,6 +371,11 @@ RIMU_HD uint64_t bose_move(uint64_t c, int from, int to) {
 struct Offdiag { uint64_t key; int prod; int sign; };
 
 RIMU_HD int num_offdiagonals_real(const DevModel &h, uint64_t key) {
+  if (h.ncomp == 2) {   // component 1 in the high bits, component 2 in the low cbits[1]
+    const uint64_t k0 = shr64(key, h.cbits[1]), k1 = key & lowmask(h.cbits[1]);
+    return ((h.cferm[0] ? popc64(k0) : bose_num_occupied(k0)) +
+            (h.cferm[1] ? popc64(k1) : bose_num_occupied(k1))) * 2 * h.ndim;
+  }
   int s = h.fermion ? popc64(key) : bose_num_occupied(key);
   return h.kind == MODEL_REAL1D ? 2 * s : s * 2 * h.ndim;
 }
@@ -465,25 +480,37 @@ RIMU_HD int neighbor_site(const DevModel &h, int mode, int chosen) {
   return site + 1;
 }
 
-// HubbardRealSpace one-component offdiagonal (HubbardRealSpace.jl:325-338).
-RIMU_HD Offdiag realspace_offdiag(const DevModel &h, uint64_t key, int chosen) {
+// Fermionic single excitation a+_dst a_src on one FermiFS chunk (1-based modes; src occupied):
+// false when dst is occupied; else the new chunk and the sign (-1)^(occupied modes below src,
+// then below dst after the removal) (fermi_excitation, bitstring.jl:746-791).
+RIMU_HD bool fermi_move(uint64_t key, int src, int dst, uint64_t &out, int &sign) {
+  if ((key >> (dst - 1)) & 1) return false;
+  int count = popc64(key & lowmask(src - 1));
+  const uint64_t k1 = key ^ (1ull << (src - 1));
+  count += popc64(k1 & lowmask(dst - 1));
+  out = k1 | (1ull << (dst - 1));
+  sign = (count & 1) ? -1 : 1;
+  return true;
+}
+
+// HubbardRealSpace offdiagonal `chosen` of one component's chunk (HubbardRealSpace.jl:325-338).
+RIMU_HD Offdiag realspace_hop(const DevModel &h, uint64_t key, int chosen, bool fermion) {
   int nb = 2 * h.ndim;
   int particle = (chosen - 1) / nb + 1, neigh = (chosen - 1) % nb + 1;
   Offdiag r{key, 0, 1};
-  if (h.fermion) {
+  if (fermion) {
     // particle-th set bit
     uint64_t x = key;
     for (int i = 1; i < particle; ++i) x &= x - 1;
     int src = ctz64(x) + 1;
     int dst = neighbor_site(h, src, neigh);
     if (dst == 0) return r;
-    if ((key >> (dst - 1)) & 1) return r;       // Pauli blocked
-    int count = popc64(key & lowmask(src - 1));
-    uint64_t k1 = key ^ (1ull << (src - 1));
-    count += popc64(k1 & lowmask(dst - 1));
-    r.key = k1 | (1ull << (dst - 1));
+    uint64_t nk;
+    int sign;
+    if (!fermi_move(key, src, dst, nk, sign)) return r;   // Pauli blocked
+    r.key = nk;
     r.prod = 1;
-    r.sign = (count & 1) ? -1 : 1;
+    r.sign = sign;
     return r;
   }
   ModeIdx src = bose_find_occupied(key, particle, nullptr);
@@ -492,6 +519,87 @@ RIMU_HD Offdiag realspace_offdiag(const DevModel &h, uint64_t key, int chosen) {
   ModeIdx dst = bose_find_mode(key, dst_mode);
   r.key = bose_move(key, src.offset, dst.offset);
   r.prod = src.occ * (dst.occ + 1);
+  return r;
+}
+
+// ---- two-component addresses -------------------------------------------------------------
+RIMU_HD uint64_t component_of(const DevModel &h, uint64_t key, int c) {
+  return c == 0 ? shr64(key, h.cbits[1]) : (key & lowmask(h.cbits[1]));
+}
+RIMU_HD uint64_t with_component(const DevModel &h, uint64_t key, int c, uint64_t ck) {
+  const uint64_t lo = lowmask(h.cbits[1]);
+  return c == 0 ? ((key & lo) | shl64(ck, h.cbits[1])) : ((key & ~lo) | ck);
+}
+RIMU_HD int component_occupied(uint64_t ck, int fermion) {
+  return fermion ? popc64(ck) : bose_num_occupied(ck);
+}
+// Occupation number of every mode of one component chunk (0-based modes < M).
+RIMU_HD void component_occupations(uint64_t ck, int fermion, int M, uint8_t *occ) {
+  for (int i = 0; i < M; ++i) occ[i] = 0;
+  uint64_t x = ck;
+  if (fermion) {
+    while (x) { occ[ctz64(x)] = 1; x &= x - 1; }
+    return;
+  }
+  int mode = 0;
+  while (x) {
+    const int z = ctz64(x);
+    x = shr64(x, z); mode += z;
+    const int n = ctz64(~x);
+    if (mode < M) occ[mode] = (uint8_t)n;
+    x = shr64(x, n);
+  }
+}
+// sum_i n_{a,i} n_{b,i} (dot of occupied modes, fockaddress.jl:692-717; two FermiFS chunks:
+// the popcount of their intersection, bitstring.jl:833-838)
+RIMU_HD int component_overlap(const DevModel &h, uint64_t a, uint64_t b) {
+  if (h.cferm[0] && h.cferm[1]) return popc64(a & b);
+  uint8_t oa[MAX_MODES], ob[MAX_MODES];
+  component_occupations(a, h.cferm[0], h.M, oa);
+  component_occupations(b, h.cferm[1], h.M, ob);
+  int acc = 0;
+  for (int i = 0; i < h.M; ++i) acc += (int)oa[i] * (int)ob[i];
+  return acc;
+}
+
+// HubbardRealSpace offdiagonal: one component, or component 1's hops followed by component
+// 2's (HubbardRealSpaceOffdiagonals, HubbardRealSpace.jl:344-391), each with its own t
+// (table block c).
+RIMU_HD Offdiag realspace_offdiag(const DevModel &h, uint64_t key, int chosen) {
+  if (h.ncomp != 2) return realspace_hop(h, key, chosen, h.fermion != 0);
+  const uint64_t k0 = component_of(h, key, 0);
+  const int n0 = component_occupied(k0, h.cferm[0]) * 2 * h.ndim;
+  const int c = chosen <= n0 ? 0 : 1;
+  Offdiag r = realspace_hop(h, c ? component_of(h, key, 1) : k0, c ? chosen - n0 : chosen,
+                            h.cferm[c] != 0);
+  if (r.prod == 0) { r.key = key; return r; }
+  r.key = with_component(h, key, c, r.key);
+  r.prod += c * h.cstride;
+  return r;
+}
+
+// HubbardMom1D with FermiFS2C: momentum_transfer_excitation of two components with fold=true
+// (excitations.jl:82-119) and element u/M * (sign_a * sign_b) (HubbardMom1D.jl:196-205).  The
+// magnitude u/M = u/(2M) * sqrt(4) is entry 4 of the u/(2M) sqrt(p) table (exact: scaling by 2).
+RIMU_HD Offdiag mom2c_offdiag(const DevModel &h, uint64_t key, int chosen) {
+  const int M = h.M, nb = h.cN[1];
+  const uint64_t ka = component_of(h, key, 0), kb = component_of(h, key, 1);
+  const int per_a = (M - 1) * nb;
+  const int src_a = (chosen - 1) / per_a + 1, rem = (chosen - 1) % per_a + 1;
+  int dst_a = (rem - 1) / nb + 1;
+  const int src_b = (rem - 1) % nb + 1;
+  Offdiag r{key, 0, 1};
+  if (src_a > popc64(ka) || src_b > popc64(kb)) return r;
+  const int sa = select_bit(ka, src_a - 1) + 1, sb = select_bit(kb, src_b - 1) + 1;
+  if (dst_a >= sa) dst_a += 1;               // skip the source mode
+  const int mom = dst_a - sa;
+  const int dst_b = ((sb - mom - 1) % M + M) % M + 1;
+  uint64_t na, nbk;
+  int ga, gb;
+  if (!fermi_move(ka, sa, dst_a, na, ga) || !fermi_move(kb, sb, dst_b, nbk, gb)) return r;
+  r.key = shl64(na, h.cbits[1]) | nbk;
+  r.prod = 4;
+  r.sign = ga * gb;
   return r;
 }
 

@@ -5,7 +5,7 @@ StochasticStyle traits, HubbardReal1D / HubbardRealSpace / HubbardMom1D, BoseFS 
 over the C ABI of librimu_gpu (include/rimu_gpu.h).  All compute runs in the CUDA library.
 """
 from ._lib import RimuError, load as load_library, library_path
-from .addresses import BoseFS, FermiFS, near_uniform, near_uniform_onr
+from .addresses import BoseFS, CompositeFS, FermiFS, FermiFS2C, near_uniform, near_uniform_onr
 from .hamiltonians import (CubicGrid, HardwallBoundaries, HubbardMom1D, HubbardReal1D,
                            HubbardRealSpace, LadderBoundaries, PeriodicBoundaries,
                            continuum_dispersion, hubbard_dispersion)

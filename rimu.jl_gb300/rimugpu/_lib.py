@@ -45,7 +45,10 @@ class ModelDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("fermion", C.c_int), ("n_particles", C.c_int),
                 ("n_modes", C.c_int), ("u", C.c_double), ("t", C.c_double), ("ndim", C.c_int),
                 ("dims", C.c_int * 3), ("periodic", C.c_int * 3),
-                ("potential", C.POINTER(C.c_double)), ("dispersion", C.POINTER(C.c_double))]
+                ("potential", C.POINTER(C.c_double)), ("dispersion", C.POINTER(C.c_double)),
+                ("n_components", C.c_int), ("comp_fermion", C.c_int * 2),
+                ("comp_particles", C.c_int * 2), ("comp_t", C.c_double * 2),
+                ("comp_u", C.c_double * 3)]
 
 
 class StepParams(C.Structure):

@@ -6,6 +6,9 @@ are the raw chunk values the device kernels operate on:
   n_i ones followed by a zero separator (src/BitStringAddresses/bitstring.jl:464-472,
   511-520); FermiFS{N,M}: mode k <-> bit k-1 (bitstring.jl:713-723).
 Ordering of addresses is the unsigned integer order of the key (bitstring.jl:317-324).
+CompositeFS of two components (multicomponent.jl:10-30; FermiFS2C, :87-103) puts component 1
+in the high bits and component 2 in the low bits of one key, so key order is the order of the
+component tuple (multicomponent.jl:79).
 """
 from __future__ import annotations
 
@@ -69,6 +72,10 @@ class BoseFS:
     def nbits(self) -> int:
         return self.N + self.M - 1
 
+    def with_key(self, key: int) -> "BoseFS":
+        """The address of this type (same N, M) with chunk `key`."""
+        return BoseFS.from_key(key, self.N, self.M)
+
     def onr(self) -> tuple:
         return _bose_onr(self.key, self.M)
 
@@ -123,6 +130,9 @@ class FermiFS:
     def nbits(self) -> int:
         return self.M
 
+    def with_key(self, key: int) -> "FermiFS":
+        return FermiFS.from_key(key, self.N, self.M)
+
     def onr(self) -> tuple:
         return tuple((self.key >> k) & 1 for k in range(self.M))
 
@@ -153,3 +163,86 @@ def near_uniform(kind, N: int, M: int):
     if kind is FermiFS:
         return FermiFS([1] * N + [0] * (M - N))
     return BoseFS(near_uniform_onr(N, M))
+
+
+@total_ordering
+class CompositeFS:
+    """CompositeFS(a, b) of two single-component addresses with the same number of modes
+    (multicomponent.jl:10-30).  One 64-bit key: component 1 in the high bits, component 2 in
+    the low ``b.nbits`` bits."""
+
+    __slots__ = ("components", "N", "M", "key")
+    fermion = False
+
+    def __init__(self, *components):
+        if len(components) != 2:
+            raise ValueError("CompositeFS with two components is supported")
+        a, b = components
+        if not all(isinstance(c, (BoseFS, FermiFS)) for c in components):
+            raise TypeError("CompositeFS components must be BoseFS or FermiFS")
+        if a.M != b.M:
+            raise ValueError("all addresses must have the same number of modes")
+        if a.nbits + b.nbits > 64:
+            raise ValueError("CompositeFS wider than 64 bits is not supported")
+        self.components = (a, b)
+        self.N, self.M = a.N + b.N, a.M
+        self.key = (a.key << b.nbits) | b.key
+
+    @property
+    def nbits(self) -> int:
+        return self.components[0].nbits + self.components[1].nbits
+
+    def with_key(self, key: int) -> "CompositeFS":
+        a, b = self.components
+        key = int(key)
+        c = CompositeFS.__new__(CompositeFS)
+        c.components = (a.with_key(key >> b.nbits), b.with_key(key & ((1 << b.nbits) - 1)))
+        c.N, c.M, c.key = self.N, self.M, key
+        return c
+
+    def onr(self) -> tuple:
+        return tuple(c.onr() for c in self.components)
+
+    def num_occupied_modes(self) -> int:
+        return sum(c.num_occupied_modes() for c in self.components)
+
+    def __eq__(self, o):
+        return (isinstance(o, CompositeFS) and self.key == o.key and
+                all(type(x) is type(y) and x.N == y.N and x.M == y.M
+                    for x, y in zip(self.components, o.components)))
+
+    def __lt__(self, o):
+        return self.key < o.key
+
+    def __hash__(self):
+        return hash(("C",) + tuple((type(c).__name__, c.N, c.M) for c in self.components) +
+                    (self.key,))
+
+    def __repr__(self):
+        return f"CompositeFS({self.components[0]!r}, {self.components[1]!r})"
+
+
+def FermiFS2C(*args):
+    """FermiFS2C(f1, f2), FermiFS2C(onr_a, onr_b) or FermiFS2C(M, pairs) with pairs
+    `mode => 1` (first component) or `mode => -1` (second), as a dict or a list of
+    (mode, +-1) (multicomponent.jl:87-103)."""
+    if len(args) == 2 and isinstance(args[0], FermiFS) and isinstance(args[1], FermiFS):
+        return CompositeFS(args[0], args[1])
+    if len(args) == 2 and isinstance(args[0], int):
+        M, pairs = args
+        items = list(pairs.items()) if isinstance(pairs, dict) else list(pairs)
+        up, dn = [0] * M, [0] * M
+        for mode, occ in items:
+            if occ > 0:
+                up[mode - 1] = occ
+            elif occ < 0:
+                dn[mode - 1] = -occ
+        return CompositeFS(FermiFS(up), FermiFS(dn))
+    if len(args) == 2:
+        return CompositeFS(FermiFS(args[0]), FermiFS(args[1]))
+    raise TypeError("FermiFS2C(f1, f2), FermiFS2C(onr_a, onr_b) or FermiFS2C(M, pairs)")
+
+
+def is_fermi2c(address) -> bool:
+    return (isinstance(address, CompositeFS) and
+            all(isinstance(c, FermiFS) for c in address.components))

@@ -40,7 +40,9 @@ class GPUDVec:
         # initiator rule of an InitiatorDVec (initiatordvec.jl): NonInitiator() is a plain DVec
         self.initiator = initiator_rule(initiator)
         proto = address_type if address_type is not None else (next(iter(pairs)) if pairs else None)
-        self.address_type = (type(proto), proto.N, proto.M) if proto is not None else (BoseFS, 0, 0)
+        # an address of the vector's type (its key is irrelevant): makes addresses from keys
+        self._proto = proto.with_key(0) if proto is not None else BoseFS.from_key(0, 0, 0)
+        self.address_type = (type(self._proto), self._proto.N, self._proto.M)
         lib = _lib.load()
         self._ctx = _lib.default_context()
         h = C.c_void_p()
@@ -90,8 +92,7 @@ class GPUDVec:
         return n.value
 
     def _addr(self, key):
-        cls, N, M = self.address_type
-        return cls.from_key(int(key), N, M)
+        return self._proto.with_key(int(key))
 
     def pairs(self):
         k, v = self.sorted_arrays()
@@ -141,8 +142,7 @@ class GPUDVec:
     zerovector_ = empty
 
     def similar(self):
-        cls, N, M = self.address_type
-        return GPUDVec(style=self.style, address_type=cls.from_key(0, N, M), initiator=self.initiator)
+        return GPUDVec(style=self.style, address_type=self._proto, initiator=self.initiator)
 
     def copy(self):
         w = self.similar()
@@ -274,6 +274,7 @@ def apply_operator(wm: GPUWorkingMemory, target: GPUDVec, source: GPUDVec, op, b
     p.initiator = source.initiator.code
     p.initiator_threshold = source.initiator.threshold
     target.style, target.valtype, target.address_type = source.style, source.valtype, source.address_type
+    target._proto = source._proto
     target.initiator = source.initiator
     st = _lib.StepStats()
     _lib.check(_lib.load().rimu_apply_operator(ham.handle, wm.handle, target.handle, source.handle,

@@ -1,7 +1,8 @@
 """Hamiltonians: the AbstractHamiltonian interface on device-side model handles.
 
-HubbardReal1D (src/Hamiltonians/HubbardReal1D.jl), HubbardRealSpace with one component
-(HubbardRealSpace.jl, geometry.jl) and HubbardMom1D with BoseFS (HubbardMom1D.jl).  Matrix
+HubbardReal1D (src/Hamiltonians/HubbardReal1D.jl), HubbardRealSpace with one component or a
+two-component CompositeFS (HubbardRealSpace.jl, geometry.jl) and HubbardMom1D with BoseFS or
+FermiFS2C (HubbardMom1D.jl).  Matrix
 elements are evaluated by librimu_gpu; this module only holds parameters and converts.
 """
 from __future__ import annotations
@@ -12,7 +13,7 @@ import math
 import numpy as np
 
 from . import _lib
-from .addresses import BoseFS, FermiFS
+from .addresses import BoseFS, CompositeFS, FermiFS, is_fermi2c
 
 
 class CubicGrid:
@@ -106,7 +107,7 @@ class AbstractHamiltonian:
         return self.address.M
 
     def _addr(self, key):
-        return type(self.address).from_key(key, self.N, self.M)
+        return self.address.with_key(key)
 
     def diagonal_element(self, address) -> float:
         out = np.zeros(1)
@@ -181,52 +182,95 @@ class HubbardReal1D(AbstractHamiltonian):
         return f"HubbardReal1D({self.address}; u={self.u}, t={self.t})"
 
 
+def _trap_potential(dims, vrow):
+    """Trap energy per site for one component: sum_d v[d] * x_d^2 with x_d centred on the
+    grid (HubbardRealSpace.jl:214-226; sites in linear order, first dimension fastest)."""
+    ranges = [[-(Md // 2) + i for i in range(Md)] for Md in dims]
+    pot = []
+    for lin in range(int(np.prod(dims))):
+        rem, acc = lin, None
+        for d, Md in enumerate(dims):
+            x = ranges[d][rem % Md]
+            rem //= Md
+            term = vrow[d] * (x ** 2)
+            acc = term if acc is None else acc + term
+        pot.append(acc)
+    return np.array(pot, dtype=np.float64)
+
+
 class HubbardRealSpace(AbstractHamiltonian):
-    """HubbardRealSpace(address; geometry, t, u, v) with one component
-    (HubbardRealSpace.jl:182-231).  `t` and `u` may be scalars or 1-element sequences; `v`
-    (trap strengths per dimension) gives the potential of HubbardRealSpace.jl:214-226."""
+    """HubbardRealSpace(address; geometry, t, u, v) (HubbardRealSpace.jl:182-231) with a
+    BoseFS/FermiFS address or a CompositeFS of two components.  One component: `t` and `u`
+    scalars or 1-element sequences.  Two components: `t` of length 2, `u` a symmetric 2x2
+    matrix (defaults all ones), `v` a 2 x D matrix of trap strengths."""
     kind = _lib.MODEL_REALSPACE
 
-    def __init__(self, address, geometry: CubicGrid | None = None, t=(1.0,), u=((1.0,),), v=None):
-        if not isinstance(address, (BoseFS, FermiFS)):
-            raise TypeError("HubbardRealSpace needs a single-component BoseFS or FermiFS")
+    def __init__(self, address, geometry: CubicGrid | None = None, t=None, u=None, v=None):
+        if not isinstance(address, (BoseFS, FermiFS, CompositeFS)):
+            raise TypeError("HubbardRealSpace needs a BoseFS, FermiFS or CompositeFS address")
         super().__init__(address)
         self.geometry = geometry if geometry is not None else PeriodicBoundaries(address.M)
         if len(self.geometry) != address.M:
             raise ValueError("`geometry` does not have the correct number of sites")
-        self.t = float(np.ravel(t)[0])
-        self.u = float(np.ravel(u)[0])
-        self.v = None if v is None or not np.any(v) else np.ravel(np.asarray(v, dtype=float))
+        D = len(self.geometry.dims)
+        self.ncomp = 2 if isinstance(address, CompositeFS) else 1
+        C_ = self.ncomp
+        tv = np.ravel(np.asarray(1.0 if t is None else t, dtype=float))
+        um = np.asarray(1.0 if u is None else u, dtype=float)
+        if C_ == 1:
+            self.t = float(tv[0])
+            self.u = float(np.ravel(um)[0])
+            self.v = None if v is None or not np.any(v) else np.ravel(np.asarray(v, dtype=float))
+            self.potential = None if self.v is None else _trap_potential(self.geometry.dims, self.v)
+            return
+        if t is not None and tv.size != 2:
+            raise ValueError("`t` must be a vector of length 2")
+        self.t = tuple(float(x) for x in (tv if tv.size == 2 else np.ones(2)))
+        if u is not None and um.size != 4:
+            raise ValueError("`u` must be a 2 × 2 matrix")
+        um = um.reshape(2, 2) if um.size == 4 else np.ones((2, 2))
+        if um[0, 1] != um[1, 0]:
+            raise ValueError("`u` must be symmetric")
+        self.u = um
+        vm = None if v is None else np.asarray(v, dtype=float)
+        if vm is not None and vm.size != 2 * D:
+            raise ValueError(f"`v` must be a 2 × {D} matrix")
+        self.v = None if vm is None or not np.any(vm) else vm.reshape(2, D)
         self.potential = None
         if self.v is not None:
-            dims = self.geometry.dims
-            ranges = [[-(Md // 2) + i for i in range(Md)] for Md in dims]
-            pot = []
-            for lin in range(address.M):
-                rem, acc = lin, None
-                for d, Md in enumerate(dims):
-                    x = ranges[d][rem % Md]
-                    rem //= Md
-                    term = self.v[d] * (x ** 2)
-                    acc = term if acc is None else acc + term
-                pot.append(acc)
-            self.potential = np.array(pot, dtype=np.float64)
+            self.potential = np.concatenate([_trap_potential(self.geometry.dims, self.v[c])
+                                             for c in range(2)])
 
     def _desc(self):
         d = _lib.ModelDesc()
         d.kind, d.n_particles, d.n_modes = self.kind, self.N, self.M
-        d.fermion = 1 if isinstance(self.address, FermiFS) else 0
-        d.u, d.t = self.u, self.t
         g = self.geometry
         d.ndim = len(g.dims)
         for i in range(3):
             d.dims[i] = g.dims[i] if i < len(g.dims) else 1
             d.periodic[i] = int(g.fold[i]) if i < len(g.dims) else 1
+        if self.ncomp == 1:
+            d.fermion = 1 if isinstance(self.address, FermiFS) else 0
+            d.u, d.t = self.u, self.t
+        else:
+            d.fermion = 0
+            d.n_components = 2
+            d.u, d.t = float(self.u[0, 0]), self.t[0]
+            for c, comp in enumerate(self.address.components):
+                d.comp_fermion[c] = 1 if isinstance(comp, FermiFS) else 0
+                d.comp_particles[c] = comp.N
+                d.comp_t[c] = self.t[c]
+            d.comp_u[0], d.comp_u[1], d.comp_u[2] = self.u[0, 0], self.u[0, 1], self.u[1, 1]
         if self.potential is not None:
             arr = np.ascontiguousarray(self.potential)
             self._keep.append(arr)
             d.potential = arr.ctypes.data_as(C.POINTER(C.c_double))
         return d
+
+    def dimension(self) -> int:
+        if self.ncomp == 1:
+            return super().dimension()
+        return math.prod(_component_dimension(c) for c in self.address.components)
 
     def with_params(self, u=None, t=None):
         return HubbardRealSpace(self.address, self.geometry, self.t if t is None else t,
@@ -236,14 +280,19 @@ class HubbardRealSpace(AbstractHamiltonian):
         return f"HubbardRealSpace({self.address}; geometry={self.geometry}, t={self.t}, u={self.u})"
 
 
+def _component_dimension(c) -> int:
+    """number_conserving_dimension of one component: C(N+M-1, N) or C(M, N)."""
+    return math.comb(c.M, c.N) if isinstance(c, FermiFS) else math.comb(c.N + c.M - 1, c.N)
+
+
 class HubbardMom1D(AbstractHamiltonian):
-    """HubbardMom1D(address; u=1.0, t=1.0, dispersion=hubbard_dispersion) with BoseFS
-    (HubbardMom1D.jl:49-65)."""
+    """HubbardMom1D(address; u=1.0, t=1.0, dispersion=hubbard_dispersion) with a BoseFS or a
+    FermiFS2C address (HubbardMom1D.jl:49-65, 141-205)."""
     kind = _lib.MODEL_MOM1D
 
-    def __init__(self, address: BoseFS, u=1.0, t=1.0, dispersion=hubbard_dispersion):
-        if not isinstance(address, BoseFS):
-            raise TypeError("HubbardMom1D is supported with BoseFS addresses")
+    def __init__(self, address, u=1.0, t=1.0, dispersion=hubbard_dispersion):
+        if not (isinstance(address, BoseFS) or is_fermi2c(address)):
+            raise TypeError("HubbardMom1D is supported with BoseFS and FermiFS2C addresses")
         super().__init__(address)
         self.u, self.t = float(u), float(t)
         M = address.M
@@ -257,10 +306,20 @@ class HubbardMom1D(AbstractHamiltonian):
         d.kind, d.fermion, d.n_particles, d.n_modes = self.kind, 0, self.N, self.M
         d.u, d.t, d.ndim = self.u, self.t, 1
         d.dims[0], d.periodic[0] = self.M, 1
+        if isinstance(self.address, CompositeFS):
+            d.n_components = 2
+            for c, comp in enumerate(self.address.components):
+                d.comp_fermion[c] = 1
+                d.comp_particles[c] = comp.N
         arr = np.ascontiguousarray(self.kes)
         self._keep.append(arr)
         d.dispersion = arr.ctypes.data_as(C.POINTER(C.c_double))
         return d
+
+    def dimension(self) -> int:
+        if isinstance(self.address, CompositeFS):
+            return math.prod(_component_dimension(c) for c in self.address.components)
+        return super().dimension()
 
     def __repr__(self):
         return f"HubbardMom1D({self.address}; u={self.u}, t={self.t})"

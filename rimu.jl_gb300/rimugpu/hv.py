@@ -12,6 +12,7 @@ import math
 import numpy as np
 
 from . import _lib
+from .addresses import CompositeFS
 
 
 def _torch():
@@ -24,6 +25,8 @@ class BasisOperator:
     ``op(v)`` returns H v for a float64 CUDA tensor v of length ``op.dim``."""
 
     def __init__(self, hamiltonian):
+        if isinstance(hamiltonian.address, CompositeFS):
+            raise TypeError("the full-basis H·v enumerates one-component BoseFS/FermiFS bases")
         self.hamiltonian = hamiltonian
         self.dim = hamiltonian.dimension()
 

@@ -128,8 +128,7 @@ def save_state(filename, vector, **metadata):
     """save_state(filename, vector; kwargs...) (RimuIO.jl:92-110): the walker list of a
     GPUDVec with the keyword arguments as metadata."""
     keys, vals = vector.sorted_arrays()
-    cls, N, M = vector.address_type
-    save_pairs(filename, keys, vals, cls.from_key(0, N, M), **metadata)
+    save_pairs(filename, keys, vals, vector._addr(0), **metadata)
 
 
 def load_state(filename, style=None, **kwargs):

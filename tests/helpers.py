@@ -1,5 +1,7 @@
 """Shared helpers for the GPU parity tests: build matching oracle models, run one step on
 both sides with the same seed/step, compare exactly."""
+import math
+
 import numpy as np
 
 import oracle as O
@@ -10,10 +12,18 @@ def oracle_model(h):
     if isinstance(h, R.HubbardReal1D):
         return O.real1d(h.N, h.M, h.u, h.t)
     if isinstance(h, R.HubbardMom1D):
-        m = O.mom1d(h.N, h.M, h.u, h.t)
+        if isinstance(h.address, R.CompositeFS):
+            a, b = h.address.components
+            m = O.mom1d_2c(a.N, b.N, h.M, h.u, h.t)
+        else:
+            m = O.mom1d(h.N, h.M, h.u, h.t)
         m.kes = np.array(h.kes)
         return m
     g = h.geometry
+    if isinstance(h.address, R.CompositeFS):
+        comps = tuple((isinstance(c, R.FermiFS), c.N) for c in h.address.components)
+        pot = None if h.potential is None else np.asarray(h.potential).reshape(2, h.M)
+        return O.realspace2(comps, g.dims, t=h.t, u=h.u, periodic=g.fold, pot=pot)
     return O.realspace(h.N, g.dims, u=h.u, t=h.t, periodic=g.fold,
                        fermion=isinstance(h.address, R.FermiFS), pot=h.potential)
 
@@ -61,3 +71,26 @@ def assert_same_step(gpu, ora, style):
             float(np.max(np.abs(gv - ov) / np.maximum(np.abs(ov), 1e-300)))
     for k in STAT_KEYS:
         assert gs[k] == os_[k], (k, gs[k], os_[k])
+
+
+def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=None, seed=0x5EED):
+    """`steps` steps from `start` on the GPU and in the oracle, compared after every step;
+    with `target`, DoubleLogUpdate on the (identical) norm."""
+    m = oracle_model(h)
+    keys = np.array([a.key for a in start], dtype=np.uint64)
+    vals = np.array(list(start.values()), dtype=np.int64 if style.valtype is int else np.float64)
+    S = h.diagonal_element(next(iter(start))) if shift is None else shift
+    pnorm = float(np.abs(vals).sum())
+    wm = R.GPUWorkingMemory(seed)
+    for step in range(1, steps + 1):
+        g = gpu_step(h, style, keys, vals, dt, S, seed, step, boost=boost, wm=wm)
+        o = O.step(m, oracle_params(style, dt, S, seed, step, boost=boost), keys, vals)
+        assert_same_step(g, o, style)
+        keys, vals = o[0], o[1]
+        if len(keys) == 0:
+            break
+        if target is not None:   # DoubleLogUpdate on the (identical) norm
+            tn = o[2]["norm"]
+            S -= 0.08 ** 2 / 4 / dt * math.log(tn / target) + 0.08 / dt * math.log(tn / pnorm)
+            pnorm = tn
+    return keys, vals

@@ -2,39 +2,16 @@
 addresses, same amplitudes (identical bits, including Float64), same statistics, for the
 three styles on the three models, plus the edge cases the step has (empty vectors, heavy
 columns, capacity growth, boost, thresholds)."""
-import math
-
 import numpy as np
 import pytest
 
 import oracle as O
 import rimugpu as R
-from helpers import assert_same_step, gpu_step, oracle_model, oracle_params
+from helpers import assert_same_step, gpu_step, oracle_model, oracle_params, run_trajectory
 
 pytestmark = pytest.mark.gpu
 
 SEED = 0x5EED
-
-
-def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=None):
-    m = oracle_model(h)
-    keys = np.array([a.key for a in start], dtype=np.uint64)
-    vals = np.array(list(start.values()), dtype=np.int64 if style.valtype is int else np.float64)
-    S = h.diagonal_element(next(iter(start))) if shift is None else shift
-    pnorm = float(np.abs(vals).sum())
-    wm = R.GPUWorkingMemory(SEED)
-    for step in range(1, steps + 1):
-        g = gpu_step(h, style, keys, vals, dt, S, SEED, step, boost=boost, wm=wm)
-        o = O.step(m, oracle_params(style, dt, S, SEED, step, boost=boost), keys, vals)
-        assert_same_step(g, o, style)
-        keys, vals = o[0], o[1]
-        if len(keys) == 0:
-            break
-        if target is not None:   # DoubleLogUpdate on the (identical) norm
-            tn = o[2]["norm"]
-            S -= 0.08 ** 2 / 4 / dt * math.log(tn / target) + 0.08 / dt * math.log(tn / pnorm)
-            pnorm = tn
-    return keys, vals
 
 
 B66 = R.BoseFS(1, 1, 1, 1, 1, 1)

@@ -1,0 +1,106 @@
+"""Two-component addresses in the oracle, pinned against the reference's own known answers,
+and the host-side CompositeFS / FermiFS2C address classes.
+
+Known answers (test/Hamiltonians.jl):
+  * "1D Fermions" (:365-385): two non-interacting fermion components on 6 sites with t = 1, 2
+    have E0 = -3 + -6; a repulsive inter-component u raises it, an attractive one lowers it;
+  * "1D Bosons (2-component)" (:327-362): one particle in the second component gives the same
+    energy as a boson or a fermion, and with the components swapped;
+  * "1D trap" (:397-411): the same with a trap potential per component.
+Independent of the reference's numbers: HubbardMom1D with FermiFS2C is the Fourier transform of
+the two-component real-space Hubbard model, so on the momentum block of the start address the
+two exact ground-state energies coincide.  The two oracle models are written from different
+reference files (HubbardMom1D.jl / excitations.jl and HubbardRealSpace.jl)."""
+import numpy as np
+import pytest
+
+import oracle as O
+import rimugpu as R
+
+
+def test_noninteracting_fermion_components_add_up():
+    m = O.realspace2(((True, 4), (True, 2)), (6,), t=(1.0, 2.0), u=((0, 0), (0, 0)))
+    assert O.ground_energy(m) == pytest.approx(-3 + -6, rel=1e-12)
+
+
+def test_inter_component_interaction_raises_and_lowers_the_energy():
+    rep = O.realspace2(((True, 4), (True, 2)), (6,), t=(1.0, 2.0), u=((0, 1), (1, 0)))
+    att = O.realspace2(((True, 4), (True, 2)), (6,), t=(1.0, 2.0), u=((0, -1), (-1, 0)))
+    assert O.ground_energy(rep) > -9
+    assert O.ground_energy(att) < -9
+
+
+@pytest.mark.parametrize("trap", [False, True])
+def test_single_particle_component_is_bose_or_fermi_in_either_order(trap):
+    v2 = ((0.0,), (0.0,))
+    cases = [(((False, 3), (False, 1)), (1, 4), ((2, 3), (3, 0)), ((1.0,), (4.0,))),
+             (((False, 3), (True, 1)), (1, 4), ((2, 3), (3, 0)), ((1.0,), (4.0,))),
+             (((False, 1), (False, 3)), (4, 1), ((0, 3), (3, 2)), ((4.0,), (1.0,))),
+             (((True, 1), (False, 3)), (4, 1), ((0, 3), (3, 2)), ((4.0,), (1.0,)))]
+    if trap:   # the reference's trap case keeps t = (1, 1)
+        cases = [(c, (1, 1), u, v) for c, _, u, v in cases]
+    energies = []
+    for comps, t, u, v in cases:
+        pot = None
+        if trap:
+            # HubbardRealSpace.jl:214-226 on 6 periodic sites: x in -3..2, pot = v x^2
+            x = np.arange(6) - 3
+            pot = np.array([v[0][0] * x ** 2, v[1][0] * x ** 2], dtype=float)
+        energies.append(O.ground_energy(O.realspace2(comps, (6,), t=t, u=u, pot=pot)))
+    assert np.allclose(energies, energies[0], rtol=1e-12)
+
+
+@pytest.mark.parametrize("M,up,dn,u", [
+    (5, (0, 0, 1, 0, 0), (0, 0, 1, 0, 0), 2.0),
+    (6, (0, 1, 1, 1, 0, 0), (0, 1, 1, 1, 0, 0), 3.0),
+    (6, (0, 1, 1, 1, 0, 0), (0, 1, 1, 1, 0, 0), -2.0),
+    (7, (0, 0, 1, 1, 1, 0, 0), (0, 0, 1, 1, 1, 0, 0), 4.0),
+])
+def test_fermi2c_momentum_space_equals_real_space(M, up, dn, u):
+    n1, n2 = sum(up), sum(dn)
+    key = (O.fermi_key(up) << M) | O.fermi_key(dn)
+    em = O.ground_energy(O.mom1d_2c(n1, n2, M, u=u, t=1.0), start=key)
+    er = O.ground_energy(O.realspace2(((True, n1), (True, n2)), (M,), t=(1.0, 1.0),
+                                      u=((0, u), (u, 0))))
+    assert em == pytest.approx(er, abs=1e-10)
+
+
+def test_fermi2c_offdiagonal_count_and_hermiticity():
+    m = O.mom1d_2c(2, 3, 6, u=1.5)
+    keys = O.basis(m)
+    for k in keys[::7]:
+        assert O.num_offdiagonals(m, int(k)) == 2 * 3 * 5        # HubbardMom1D.jl:141-144
+    H = O.sparse_matrix(m, keys)
+    assert abs(H - H.T).max() < 1e-14
+
+
+def test_composite_realspace_is_hermitian_with_hardwall_and_trap():
+    pot = np.array([[0.5, 0.0, 0.5, 1.0, 0.25, 0.0], [0.0, 2.0, 0.0, 1.0, 0.0, 3.0]])
+    m = O.realspace2(((False, 2), (True, 2)), (2, 3), t=(1.0, 0.5), u=((1.5, 2.0), (2.0, 0.0)),
+                     periodic=(False, True), pot=pot)
+    H = O.sparse_matrix(m)
+    assert H.shape[0] == 21 * 15
+    assert abs(H - H.T).max() < 1e-14
+
+
+def test_composite_key_order_is_component_tuple_order():
+    """isless(a, b) = isless(a.components, b.components) (multicomponent.jl:79)."""
+    a = R.CompositeFS(R.FermiFS((1, 1, 0, 0, 0, 0)), R.BoseFS((5, 0, 0, 0, 0, 0)))
+    b = R.CompositeFS(R.FermiFS((0, 1, 1, 0, 0, 0)), R.BoseFS((1, 1, 1, 1, 1, 0)))
+    c = R.CompositeFS(R.FermiFS((0, 1, 1, 0, 0, 0)), R.BoseFS((0, 0, 0, 0, 0, 5)))
+    assert (a < b) == ((a.components[0].key, a.components[1].key) <
+                       (b.components[0].key, b.components[1].key))
+    assert sorted([b, c, a]) == sorted([b, c, a], key=lambda x: tuple(y.key for y in x.components))
+    assert a.with_key(a.key) == a and a.with_key(b.key).components == b.components
+    assert a.N == 7 and a.M == 6 and a.onr() == ((1, 1, 0, 0, 0, 0), (5, 0, 0, 0, 0, 0))
+    with pytest.raises(ValueError):
+        R.CompositeFS(R.BoseFS((1, 1)), R.BoseFS((1, 1, 1)))
+
+
+def test_fermi2c_constructors_agree():
+    """The three forms of the FermiFS2C docstring (multicomponent.jl:87-113)."""
+    f1 = R.FermiFS2C(R.FermiFS(1, 0, 0), R.FermiFS(0, 1, 1))
+    f2 = R.FermiFS2C((1, 0, 0), (0, 1, 1))
+    f3 = R.FermiFS2C(3, [(1, 1), (2, -1), (3, -1)])
+    assert f1 == f2 == f3
+    assert R.FermiFS2C(3, {1: 1}).N == 1 and R.FermiFS2C(3, {1: -1}).N == 1

@@ -56,9 +56,14 @@ typedef struct rimu_model rimu_model;
 typedef struct rimu_vec rimu_vec;
 typedef struct rimu_wm rimu_wm;
 
-/* Hamiltonian description.  Addresses are single-chunk bit strings of at most 64 bits
- * (BoseFS: n_particles + n_modes - 1 bits; FermiFS: n_modes bits), with the chunk layout of
- * src/BitStringAddresses/bitstring.jl:464-472 (bosons) and 713-723 (fermions).
+/* Hamiltonian description.  Addresses are bit strings (BoseFS: n_particles + n_modes - 1
+ * bits; FermiFS: n_modes bits) with the layout of src/BitStringAddresses/bitstring.jl:464-472
+ * (bosons) and 713-723 (fermions).  Up to 64 bits an address is one uint64_t.  HubbardReal1D
+ * and one-component HubbardRealSpace also take addresses of 65-128 bits (the reference's
+ * two-chunk BitString, bitstring.jl:6-18): wherever such an address crosses this interface it
+ * is a pair of uint64_t, (lo, hi), bit k of the address being bit k of lo for k < 64 and bit
+ * k - 64 of hi otherwise; key arrays then hold 2 words per address.  Walker lists for them
+ * are created with rimu_vec_create_kw(..., key_words = 2, ...).
  *
  * Two-component addresses (CompositeFS of two components, multicomponent.jl:10-30, and its
  * alias FermiFS2C, :87-103): n_components = 2, each component a BoseFS or FermiFS with the
@@ -144,18 +149,30 @@ int rimu_ctx_synchronize(rimu_ctx *ctx);
  * (HubbardReal1D.jl:26, HubbardRealSpace.jl:182, HubbardMom1D.jl:49). */
 int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *desc, rimu_model **out);
 int rimu_model_destroy(rimu_model *m);
-/* diagonal_element (Interfaces/hamiltonians.jl:241) for n host addresses. */
+/* diagonal_element (Interfaces/hamiltonians.jl:241) for n host addresses (2n words for a
+ * model with addresses wider than 64 bits). */
 int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t n, double *out);
 /* num_offdiagonals / offdiagonals (Interfaces/hamiltonians.jl:263,309): all offdiagonal
  * (address, element) pairs of one column, in the reference's order; illegal hard-wall moves
  * give (address, 0.0) as in HubbardRealSpace.jl:331-332. */
 int rimu_model_num_offdiagonals(rimu_model *m, uint64_t key, int *out);
+/* The same with the address as (lo, hi) and, for wide models, keys as 2 words each. */
+int rimu_model_num_offdiagonals_w(rimu_model *m, const uint64_t *key2, int *out);
+int rimu_model_offdiagonals_w(rimu_model *m, const uint64_t *key2, uint64_t *keys2, double *vals,
+                              int cap, int *n);
 int rimu_model_offdiagonals(rimu_model *m, uint64_t key, uint64_t *keys, double *vals, int cap,
                             int *n);
 
 /* Device-resident walker list: stands behind DVec / PDVec (src/DictVectors/dvec.jl,
  * pdvec.jl) as an AbstractDVec (Interfaces/dictvectors.jl:40). */
 int rimu_vec_create(rimu_ctx *ctx, int val_kind, int64_t capacity_hint, rimu_vec **out);
+/* A walker list with key_words = 1 (addresses of at most 64 bits) or 2 (65-128 bits; its key
+ * arrays in upload, download and lookup hold (lo, hi) pairs).  Two-word lists step with
+ * rimu_apply_operator (without initiator rules or projectors); dot products, conversions and
+ * batched runs take one-word lists. */
+int rimu_vec_create_kw(rimu_ctx *ctx, int val_kind, int key_words, int64_t capacity_hint,
+                       rimu_vec **out);
+int rimu_vec_key_words(const rimu_vec *v, int *key_words);
 int rimu_vec_destroy(rimu_vec *v);
 /* Replace the contents with n (address, value) pairs from host memory; addresses must be
  * distinct.  vals points to double (RIMU_VAL_F64) or int64_t (RIMU_VAL_I64). */

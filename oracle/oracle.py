@@ -96,6 +96,13 @@ def lib():
         _lib.o_enumerate_fixed_weight.restype = C.c_int64
         _lib.o_connected_basis.argtypes = [P(_OModel), C.c_uint64, u64p, C.c_int64]
         _lib.o_connected_basis.restype = C.c_int64
+        # addresses of up to 128 bits as (lo, hi) word pairs
+        _lib.o_num_offdiagonals_w.argtypes = [P(_OModel), C.c_uint64, C.c_uint64]
+        _lib.o_get_offdiagonal_w.argtypes = [P(_OModel), C.c_uint64, C.c_uint64, C.c_int, u64p, f64p]
+        _lib.o_diagonal_w.argtypes = [P(_OModel), C.c_uint64, C.c_uint64]
+        _lib.o_diagonal_w.restype = C.c_double
+        _lib.o_step_w.argtypes = [P(_OModel), P(_OParams), u64p, f64p, i64p, C.c_int64,
+                                  P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
     return _lib
 
 
@@ -207,8 +214,25 @@ def mom1d_2c(N1, N2, M, u=1.0, t=1.0):
 # Address helpers
 # ----------------------------------------------------------------------------------------
 def bose_key(onr) -> int:
+    if sum(onr) + len(onr) - 1 > 64:     # two chunks: the same encoding on a Python int
+        key = 0
+        for n in reversed(list(onr)):
+            key = (key << (n + 1)) | ((1 << n) - 1)
+        return key
     a = np.ascontiguousarray(onr, dtype=np.int32)
     return int(lib().o_bose_from_onr(_p(a, C.c_int), len(a)))
+
+
+_M64 = (1 << 64) - 1
+
+
+def _wide(m: "Model") -> bool:
+    return m.nbits > 64
+
+
+def _split(key: int):
+    key = int(key)
+    return C.c_uint64(key & _M64), C.c_uint64(key >> 64)
 
 
 def bose_onr(key: int, M: int) -> list:
@@ -241,13 +265,22 @@ def draw(seed, purpose, replica, step, addr, j):
 # ----------------------------------------------------------------------------------------
 def num_offdiagonals(m: Model, key: int) -> int:
     s = m.struct()
+    if _wide(m):
+        return lib().o_num_offdiagonals_w(C.byref(s), *_split(key))
     return lib().o_num_offdiagonals(C.byref(s), C.c_uint64(key))
 
 
 def offdiagonals(m: Model, key: int):
     s = m.struct()
-    n = lib().o_num_offdiagonals(C.byref(s), C.c_uint64(key))
     out = []
+    if _wide(m):
+        n = lib().o_num_offdiagonals_w(C.byref(s), *_split(key))
+        for c in range(1, n + 1):
+            nk, hv = (C.c_uint64 * 2)(), C.c_double()
+            lib().o_get_offdiagonal_w(C.byref(s), *_split(key), c, nk, C.byref(hv))
+            out.append((int(nk[0]) | (int(nk[1]) << 64), float(hv.value)))
+        return out
+    n = lib().o_num_offdiagonals(C.byref(s), C.c_uint64(key))
     for c in range(1, n + 1):
         nk, hv = C.c_uint64(), C.c_double()
         lib().o_get_offdiagonal(C.byref(s), C.c_uint64(key), c, C.byref(nk), C.byref(hv))
@@ -257,6 +290,8 @@ def offdiagonals(m: Model, key: int):
 
 def diagonal(m: Model, key: int) -> float:
     s = m.struct()
+    if _wide(m):
+        return float(lib().o_diagonal_w(C.byref(s), *_split(key)))
     return float(lib().o_diagonal(C.byref(s), C.c_uint64(key)))
 
 
@@ -294,7 +329,10 @@ class StepParams:
 
 
 def step(m: Model, prm: StepParams, keys, vals):
-    """One projector step; returns (sorted keys, values, stats dict)."""
+    """One projector step; returns (sorted keys, values, stats dict).  Addresses wider than 64
+    bits are Python ints in and out (object arrays)."""
+    if _wide(m):
+        return _step_wide(m, prm, keys, vals)
     keys = np.ascontiguousarray(keys, dtype=np.uint64)
     n = len(keys)
     is_int = prm.style == STYLE_INTEGER
@@ -314,6 +352,36 @@ def step(m: Model, prm: StepParams, keys, vals):
         v = np.ctypeslib.as_array(oi, shape=(on.value,)).copy() if on.value else np.zeros(0, np.int64)
     else:
         v = np.ctypeslib.as_array(ov, shape=(on.value,)).copy() if on.value else np.zeros(0)
+    for p in (ok, ov, oi):
+        lib().o_free(C.cast(p, C.c_void_p))
+    stats = {f: getattr(st, f) for f, _ in _OStats._fields_}
+    return k, v, stats
+
+
+def _step_wide(m: Model, prm: StepParams, keys, vals):
+    n = len(keys)
+    k2 = np.zeros(2 * max(n, 1), dtype=np.uint64)
+    for i, k in enumerate(keys):
+        k2[2 * i], k2[2 * i + 1] = int(k) & _M64, int(k) >> 64
+    is_int = prm.style == STYLE_INTEGER
+    fv = np.ascontiguousarray(vals if not is_int else np.zeros(n), dtype=np.float64)
+    iv = np.ascontiguousarray(vals if is_int else np.zeros(n), dtype=np.int64)
+    ok, ov, oi = C.POINTER(C.c_uint64)(), C.POINTER(C.c_double)(), C.POINTER(C.c_int64)()
+    on = C.c_int64()
+    st = _OStats()
+    ms, ps = m.struct(), prm.struct()
+    rc = lib().o_step_w(C.byref(ms), C.byref(ps), _p(k2, C.c_uint64), _p(fv, C.c_double),
+                        _p(iv, C.c_int64), n, C.byref(ok), C.byref(ov), C.byref(oi),
+                        C.byref(on), C.byref(st))
+    if rc != 0:
+        raise MemoryError("oracle step failed")
+    nn = on.value
+    w = np.ctypeslib.as_array(ok, shape=(2 * nn,)).copy() if nn else np.zeros(0, np.uint64)
+    k = np.array([int(w[2 * i]) | (int(w[2 * i + 1]) << 64) for i in range(nn)], dtype=object)
+    if is_int:
+        v = np.ctypeslib.as_array(oi, shape=(nn,)).copy() if nn else np.zeros(0, np.int64)
+    else:
+        v = np.ctypeslib.as_array(ov, shape=(nn,)).copy() if nn else np.zeros(0)
     for p in (ok, ov, oi):
         lib().o_free(C.cast(p, C.c_void_p))
     stats = {f: getattr(st, f) for f, _ in _OStats._fields_}

@@ -46,7 +46,16 @@
 #include <string.h>
 #include <math.h>
 
-#define O_MAXM 64
+#define O_MAXM 128
+
+/* Addresses are handled as 128-bit integers: a single 64-bit chunk has hi = 0, a two-chunk
+ * address (65-128 bits, bitstring.jl:6-18) keeps the same bit positions across both words.
+ * The exported 64-bit entry points convert; the *_w entry points take (lo, hi) word pairs. */
+typedef unsigned __int128 okey;
+#define OKEY_ONE ((okey)1)
+static okey o_key_of(uint64_t lo, uint64_t hi) { return ((okey)hi << 64) | lo; }
+static uint64_t o_lo(okey k) { return (uint64_t)k; }
+static uint64_t o_hi(okey k) { return (uint64_t)(k >> 64); }
 
 /* ------------------------------------------------------------------------------------ */
 /* Philox4x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2, 3", SC'11). */
@@ -75,6 +84,20 @@ void o_draw(uint64_t seed, uint32_t purpose, uint32_t replica, uint32_t step, ui
   uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32) ^ (purpose << 28) ^ replica};
   o_philox4x32_10(ctr, key, out);
 }
+/* murmur3 fmix64 finalizer (mix64 of the device code); mix64(0) = 0. */
+static uint64_t o_mix64(uint64_t x) {
+  x ^= x >> 33; x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+/* The 64-bit word that stands for an address in random-number counters: the chunk itself for
+ * addresses of at most 64 bits, lo ^ mix64(hi) for two chunks. */
+static uint64_t o_key_word(okey k) { return o_lo(k) ^ o_mix64(o_hi(k)); }
+static void o_draw_k(uint64_t seed, uint32_t purpose, uint32_t replica, uint32_t step, okey addr,
+                     uint32_t j, uint32_t out[4]) {
+  o_draw(seed, purpose, replica, step, o_key_word(addr), j, out);
+}
 static inline uint64_t o_u53(const uint32_t r[4]) {
   return ((uint64_t)r[1] << 21) | (uint64_t)(r[2] >> 11);
 }
@@ -88,35 +111,39 @@ static inline int o_bernoulli(uint64_t u53, double p) {
 /* ------------------------------------------------------------------------------------ */
 /* from_bose_onr, single chunk: bitstring.jl:464-472.  Mode 1 sits at the low end; each
  * mode contributes n_i ones followed by one zero (the last mode has no trailing zero). */
-uint64_t o_bose_from_onr(const int *onr, int M) {
-  uint64_t result = 0;
+static okey o_bose_from_onr_k(const int *onr, int M) {
+  okey result = 0;
   for (int i = M - 1; i >= 0; --i) {
-    uint64_t n = (uint64_t)onr[i];
-    result = (n + 1 >= 64) ? 0 : (result << (n + 1));
-    result |= (n >= 64) ? ~0ull : (((uint64_t)1 << n) - 1);
+    int n = onr[i];
+    result = (n + 1 >= 128) ? 0 : (result << (n + 1));
+    result |= (n >= 128) ? ~(okey)0 : ((OKEY_ONE << n) - 1);
   }
   return result;
 }
-/* to_bose_onr, single chunk: bitstring.jl:511-520. */
-void o_bose_to_onr(uint64_t key, int M, int *onr) {
+/* to_bose_onr, one 128-bit word: bitstring.jl:511-520. */
+static void o_bose_to_onr_k(okey key, int M, int *onr) {
   for (int i = 0; i < M; ++i) onr[i] = 0;
   for (int mode = 0; mode < M; ++mode) {
     int b = 0;
-    while (b < 64 && ((key >> b) & 1)) ++b;
+    while (b < 128 && ((key >> b) & 1)) ++b;
     onr[mode] = b;
-    key = (b + 1 >= 64) ? 0 : key >> (b + 1);
+    key = (b + 1 >= 128) ? 0 : key >> (b + 1);
     if (key == 0) break;
   }
 }
 /* from_fermi_onr: bitstring.jl:713-723 (mode k <-> bit k-1). */
-uint64_t o_fermi_from_onr(const int *onr, int M) {
-  uint64_t r = 0;
-  for (int k = 0; k < M; ++k) if (onr[k]) r |= (uint64_t)1 << k;
+static okey o_fermi_from_onr_k(const int *onr, int M) {
+  okey r = 0;
+  for (int k = 0; k < M; ++k) if (onr[k]) r |= OKEY_ONE << k;
   return r;
 }
-void o_fermi_to_onr(uint64_t key, int M, int *onr) {
+static void o_fermi_to_onr_k(okey key, int M, int *onr) {
   for (int k = 0; k < M; ++k) onr[k] = (int)((key >> k) & 1);
 }
+uint64_t o_bose_from_onr(const int *onr, int M) { return o_lo(o_bose_from_onr_k(onr, M)); }
+void o_bose_to_onr(uint64_t key, int M, int *onr) { o_bose_to_onr_k(key, M, onr); }
+uint64_t o_fermi_from_onr(const int *onr, int M) { return o_lo(o_fermi_from_onr_k(onr, M)); }
+void o_fermi_to_onr(uint64_t key, int M, int *onr) { o_fermi_to_onr_k(key, M, onr); }
 
 /* ------------------------------------------------------------------------------------ */
 /* Models                                                                                */
@@ -146,24 +173,23 @@ typedef struct {
 static int o_comp_bits(const o_model *h, int c) {
   return h->cferm[c] ? h->M : h->cN[c] + h->M - 1;
 }
-static void o_to_onr(const o_model *h, uint64_t key, int *onr) {
+static void o_to_onr(const o_model *h, okey key, int *onr) {
   if (h->ncomp == 2) {
     int b1 = o_comp_bits(h, 1);
-    uint64_t k0 = b1 >= 64 ? 0 : key >> b1, k1 = b1 >= 64 ? key : key & (((uint64_t)1 << b1) - 1);
-    if (h->cferm[0]) o_fermi_to_onr(k0, h->M, onr); else o_bose_to_onr(k0, h->M, onr);
-    if (h->cferm[1]) o_fermi_to_onr(k1, h->M, onr + h->M); else o_bose_to_onr(k1, h->M, onr + h->M);
+    okey k0 = key >> b1, k1 = key & ((OKEY_ONE << b1) - 1);
+    if (h->cferm[0]) o_fermi_to_onr_k(k0, h->M, onr); else o_bose_to_onr_k(k0, h->M, onr);
+    if (h->cferm[1]) o_fermi_to_onr_k(k1, h->M, onr + h->M); else o_bose_to_onr_k(k1, h->M, onr + h->M);
     return;
   }
-  if (h->fermion) o_fermi_to_onr(key, h->M, onr); else o_bose_to_onr(key, h->M, onr);
+  if (h->fermion) o_fermi_to_onr_k(key, h->M, onr); else o_bose_to_onr_k(key, h->M, onr);
 }
-static uint64_t o_from_onr(const o_model *h, const int *onr) {
+static okey o_from_onr(const o_model *h, const int *onr) {
   if (h->ncomp == 2) {
-    uint64_t k0 = h->cferm[0] ? o_fermi_from_onr(onr, h->M) : o_bose_from_onr(onr, h->M);
-    uint64_t k1 = h->cferm[1] ? o_fermi_from_onr(onr + h->M, h->M) : o_bose_from_onr(onr + h->M, h->M);
-    int b1 = o_comp_bits(h, 1);
-    return (b1 >= 64 ? 0 : k0 << b1) | k1;
+    okey k0 = h->cferm[0] ? o_fermi_from_onr_k(onr, h->M) : o_bose_from_onr_k(onr, h->M);
+    okey k1 = h->cferm[1] ? o_fermi_from_onr_k(onr + h->M, h->M) : o_bose_from_onr_k(onr + h->M, h->M);
+    return (k0 << o_comp_bits(h, 1)) | k1;
   }
-  return h->fermion ? o_fermi_from_onr(onr, h->M) : o_bose_from_onr(onr, h->M);
+  return h->fermion ? o_fermi_from_onr_k(onr, h->M) : o_bose_from_onr_k(onr, h->M);
 }
 static int o_num_occupied(const int *onr, int M) {
   int c = 0;
@@ -194,7 +220,7 @@ static int o_neighbor_site(const o_model *h, int mode, int chosen) {
   return site;
 }
 
-int o_num_offdiagonals(const o_model *h, uint64_t key) {
+static int o_noff(const o_model *h, okey key) {
   int onr[2 * O_MAXM];
   o_to_onr(h, key, onr);
   if (h->ncomp == 2) {
@@ -248,8 +274,8 @@ static double o_realspace_hop(const o_model *h, int *onr, int fermion, double t,
   return -t * sqrt((double)value);
 }
 
-void o_get_offdiagonal_p(const o_model *h, uint64_t key, int chosen, uint64_t *nkey,
-                         double *val, long *prod) {
+static void o_offdiag_k(const o_model *h, okey key, int chosen, okey *nkey, double *val,
+                        long *prod) {
   int onr[2 * O_MAXM];
   *prod = 0;
   o_to_onr(h, key, onr);
@@ -362,9 +388,28 @@ void o_get_offdiagonal_p(const o_model *h, uint64_t key, int chosen, uint64_t *n
   *val = h->u / (2 * M) * sqrt((double)value);
 }
 
+int o_num_offdiagonals(const o_model *h, uint64_t key) { return o_noff(h, key); }
+void o_get_offdiagonal_p(const o_model *h, uint64_t key, int chosen, uint64_t *nkey,
+                         double *val, long *prod) {
+  okey nk;
+  o_offdiag_k(h, key, chosen, &nk, val, prod);
+  *nkey = o_lo(nk);
+}
 void o_get_offdiagonal(const o_model *h, uint64_t key, int chosen, uint64_t *nkey, double *val) {
   long prod;
   o_get_offdiagonal_p(h, key, chosen, nkey, val, &prod);
+}
+/* Two-word forms: keys as (lo, hi). */
+int o_num_offdiagonals_w(const o_model *h, uint64_t lo, uint64_t hi) {
+  return o_noff(h, o_key_of(lo, hi));
+}
+void o_get_offdiagonal_w(const o_model *h, uint64_t lo, uint64_t hi, int chosen, uint64_t *nkey2,
+                         double *val) {
+  okey nk;
+  long prod;
+  o_offdiag_k(h, o_key_of(lo, hi), chosen, &nk, val, &prod);
+  nkey2[0] = o_lo(nk);
+  nkey2[1] = o_hi(nk);
 }
 
 /* external_potential of one component (HubbardRealSpace.jl:90-97). */
@@ -374,7 +419,11 @@ static double o_potential(const int *onr, int M, const double *pot) {
   return pe;
 }
 
-double o_diagonal(const o_model *h, uint64_t key) {
+static double o_diag_k(const o_model *h, okey key);
+double o_diagonal(const o_model *h, uint64_t key) { return o_diag_k(h, key); }
+double o_diagonal_w(const o_model *h, uint64_t lo, uint64_t hi) { return o_diag_k(h, o_key_of(lo, hi)); }
+
+static double o_diag_k(const o_model *h, okey key) {
   int onr[2 * O_MAXM];
   o_to_onr(h, key, onr);
   int M = h->M;
@@ -472,7 +521,7 @@ typedef struct {
   int64_t clones, deaths, zombies;   /* IsStochasticInteger only */
 } o_stats;
 
-typedef struct { uint64_t key; int cls; int kind; double v; int64_t iv; } o_contrib;
+typedef struct { okey key; int cls; int kind; double v; int64_t iv; } o_contrib;
 
 static uint64_t o_ordered_bits(double v) {
   uint64_t u;
@@ -496,7 +545,7 @@ static int o_cmp_contrib_i(const void *a, const void *b) {
 }
 
 typedef struct { o_contrib *c; int64_t n, cap; int err; } o_buf;
-static void o_push(o_buf *b, uint64_t key, int cls, int kind, double v, int64_t iv) {
+static void o_push(o_buf *b, okey key, int cls, int kind, double v, int64_t iv) {
   if (b->n == b->cap) {
     int64_t nc = b->cap ? 2 * b->cap : 1024;
     o_contrib *p = realloc(b->c, nc * sizeof(o_contrib));
@@ -509,8 +558,8 @@ static void o_push(o_buf *b, uint64_t key, int cls, int kind, double v, int64_t 
 }
 
 /* Transition operator elements (fciqmc.jl:93-112). */
-static double o_t_diag(const o_model *h, const o_params *p, uint64_t key) {
-  double d = o_diagonal(h, key);
+static double o_t_diag(const o_model *h, const o_params *p, okey key) {
+  double d = o_diag_k(h, key);
   return p->op == O_OP_HAMILTONIAN ? d : 1 - p->dt * (d - p->shift);
 }
 static double o_t_off(const o_params *p, double hval) {
@@ -627,15 +676,15 @@ static void o_initiator_value(const o_params *p, const double f[3], const int64_
  * Values are doubles for the float styles and int64 (passed as double-typed storage of
  * the same bits is NOT used: separate arrays) for IsStochasticInteger.
  * Returns 0 on success, nonzero on allocation failure.  *dst arrays are malloc'd. */
-int o_step(const o_model *h, const o_params *p,
-           const uint64_t *skeys, const double *svals, const int64_t *sivals, int64_t n,
-           uint64_t **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
+static int o_step_k(const o_model *h, const o_params *p,
+                    const okey *skeys, const double *svals, const int64_t *sivals, int64_t n,
+                    okey **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
   memset(st, 0, sizeof(*st));
   o_buf b = {0};
   int is_int = p->style == O_STYLE_INTEGER;
   o_u128 spawn_acc = 0;
   for (int64_t e = 0; e < n; ++e) {
-    uint64_t key = skeys[e];
+    okey key = skeys[e];
     double val = is_int ? (double)sivals[e] : svals[e];
     /* classes of this walker's contributions (_default_to_initiator_value,
      * initiators.jl:142-157): its diagonal term counts as "initiator" and its spawns as
@@ -649,7 +698,7 @@ int o_step(const o_model *h, const o_params *p,
     double x = o_t_diag(h, p, key) * val;
     if (is_int) {
       uint32_t r[4];
-      o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+      o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
       int64_t res = o_round_int(x, o_u53(r));
       int64_t v = sivals[e];
       if (res != 0) o_push(&b, key, diag_cls, 0, 0.0, res);
@@ -662,13 +711,13 @@ int o_step(const o_model *h, const o_params *p,
       double res = x;
       if (p->proj_threshold > 0) {
         uint32_t r[4];
-        o_draw(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+        o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
         res = o_project(x, p->proj_threshold, o_u53(r));
       }
       if (res != 0.0) o_push(&b, key, diag_cls, 0, res, 0);
     }
     /* ---- spawn! ---- */
-    int noff = o_num_offdiagonals(h, key);
+    int noff = o_noff(h, key);
     int exact = 0;
     if (p->style == O_STYLE_DETERMINISTIC) {
       exact = 1;                       /* apply_column! returns (1,), styles.jl:101-105 */
@@ -687,12 +736,12 @@ int o_step(const o_model *h, const o_params *p,
       /* Exact, spawning.jl:174-182: deposit val * mat_elem for every offdiagonal. */
       st->spawn_attempts += noff;
       for (int c = 1; c <= noff; ++c) {
-        uint64_t nk; double hv;
-        o_get_offdiagonal(h, key, c, &nk, &hv);
+        okey nk; double hv; long prod;
+        o_offdiag_k(h, key, c, &nk, &hv, &prod);
         double y = val * o_t_off(p, hv);
         if (p->proj_threshold > 0 && p->style == O_STYLE_DSS) {
           uint32_t r[4];
-          o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
+          o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
           y = o_project(y, p->proj_threshold, o_u53(r));
         }
         if (y != 0.0) { o_push(&b, nk, spawn_cls, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
@@ -717,15 +766,15 @@ int o_step(const o_model *h, const o_params *p,
       uint32_t r[4];
       uint32_t word;
       if (grouped) {
-        o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(j >> 2), r);
+        o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(j >> 2), r);
         word = r[j & 3];
       } else {
-        o_draw(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
+        o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
         word = r[0];
       }
       int chosen = (int)(((uint64_t)word * (uint64_t)noff) >> 32) + 1;
-      uint64_t nk; double hv;
-      o_get_offdiagonal(h, key, chosen, &nk, &hv);
+      okey nk; double hv; long prod;
+      o_offdiag_k(h, key, chosen, &nk, &hv, &prod);
       double y = c * o_t_off(p, hv);
       if (is_int) {
         int64_t k = o_round_int(y, o_u53(r));
@@ -744,13 +793,13 @@ int o_step(const o_model *h, const o_params *p,
    * double (ties to even); otherwise the contributions are added in canonical order, the
    * diagonal term first and then the spawns in increasing numerical order. */
   qsort(b.c, (size_t)b.n, sizeof(o_contrib), is_int ? o_cmp_contrib_i : o_cmp_contrib_f);
-  uint64_t *ok = malloc((size_t)(b.n ? b.n : 1) * 8);
+  okey *ok = malloc((size_t)(b.n ? b.n : 1) * sizeof(okey));
   double *ov = malloc((size_t)(b.n ? b.n : 1) * 8);
   int64_t *oi = malloc((size_t)(b.n ? b.n : 1) * 8);
   if (!ok || !ov || !oi) { free(b.c); free(ok); free(ov); free(oi); return 1; }
   int64_t m = 0;
   for (int64_t i = 0; i < b.n;) {
-    const uint64_t key = b.c[i].key;
+    const okey key = b.c[i].key;
     double fs[3] = {0.0, 0.0, 0.0};
     int64_t is[3] = {0, 0, 0};
     int64_t j = i;
@@ -790,7 +839,7 @@ int o_step(const o_model *h, const o_params *p,
       double prob = (p->compression == 1.0) ? fabs(w) : fabs(w) / p->compression;
       if (prob < 1) {
         uint32_t r[4];
-        o_draw(p->seed, O_PURPOSE_COMPRESS, p->replica, p->step, ok[i], 0, r);
+        o_draw_k(p->seed, O_PURPOSE_COMPRESS, p->replica, p->step, ok[i], 0, r);
         w = o_bernoulli(o_u53(r), prob) ? (w < 0 ? -p->compression : p->compression) : 0.0;
       }
       if (w != 0.0) { ok[q] = ok[i]; ov[q] = w; oi[q] = 0; ++q; }
@@ -806,6 +855,44 @@ int o_step(const o_model *h, const o_params *p,
 }
 
 void o_free(void *p) { free(p); }
+
+/* One step with 64-bit addresses (single chunk). */
+int o_step(const o_model *h, const o_params *p,
+           const uint64_t *skeys, const double *svals, const int64_t *sivals, int64_t n,
+           uint64_t **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
+  okey *sk = malloc((size_t)(n ? n : 1) * sizeof(okey));
+  if (!sk) return 1;
+  for (int64_t i = 0; i < n; ++i) sk[i] = skeys[i];
+  okey *ok;
+  int rc = o_step_k(h, p, sk, svals, sivals, n, &ok, ovals, oivals, on, st);
+  free(sk);
+  if (rc) return rc;
+  uint64_t *out = malloc((size_t)(*on ? *on : 1) * 8);
+  if (!out) { free(ok); free(*ovals); free(*oivals); return 1; }
+  for (int64_t i = 0; i < *on; ++i) out[i] = o_lo(ok[i]);
+  free(ok);
+  *okeys = out;
+  return 0;
+}
+
+/* One step with addresses of up to 128 bits as (lo, hi) word pairs (2n words in and out). */
+int o_step_w(const o_model *h, const o_params *p,
+             const uint64_t *skeys2, const double *svals, const int64_t *sivals, int64_t n,
+             uint64_t **okeys2, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
+  okey *sk = malloc((size_t)(n ? n : 1) * sizeof(okey));
+  if (!sk) return 1;
+  for (int64_t i = 0; i < n; ++i) sk[i] = o_key_of(skeys2[2 * i], skeys2[2 * i + 1]);
+  okey *ok;
+  int rc = o_step_k(h, p, sk, svals, sivals, n, &ok, ovals, oivals, on, st);
+  free(sk);
+  if (rc) return rc;
+  uint64_t *out = malloc((size_t)(*on ? 2 * *on : 2) * 8);
+  if (!out) { free(ok); free(*ovals); free(*oivals); return 1; }
+  for (int64_t i = 0; i < *on; ++i) { out[2 * i] = o_lo(ok[i]); out[2 * i + 1] = o_hi(ok[i]); }
+  free(ok);
+  *okeys2 = out;
+  return 0;
+}
 
 /* ------------------------------------------------------------------------------------ */
 /* Matrix-free product on the full sorted basis (abstractdvec.jl:275-284 in pull form).  */

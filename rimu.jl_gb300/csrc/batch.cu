@@ -163,7 +163,7 @@ static int regrid(rimu_batch *b, const std::vector<int> &nbits, uint32_t ncapv) 
         rc = rimu_launch_rebucket(ctx, b->recs[b->cur] + (size_t)b->off[r] * b->capv,
                                   b->cnt[b->cur] + b->off[r], b->bits[r], b->capv,
                                   nr[0] + (size_t)noff[r] * ncapv, nc[0] + noff[r], nbits[r], ncapv,
-                                  flag);
+                                  flag, 1);
     } else {
       for (int r = 0; r < b->nrep && !rc; ++r) {
         const int64_t n = (int64_t)b->hkeys[r].size();
@@ -172,7 +172,7 @@ static int regrid(rimu_batch *b, const std::vector<int> &nbits, uint32_t ncapv) 
         if (!(rc = dalloc(ctx, &dk, n)) && !(rc = dalloc(ctx, &dv, n)) &&
             !(rc = h2d(ctx, dk, b->hkeys[r].data(), n)) && !(rc = h2d(ctx, dv, b->hvals[r].data(), n)))
           rc = rimu_launch_bucketize(ctx, dk, dv, n, nbits[r], ncapv,
-                                     nr[0] + (size_t)noff[r] * ncapv, nc[0] + noff[r], flag);
+                                     nr[0] + (size_t)noff[r] * ncapv, nc[0] + noff[r], flag, 1);
         dfree(ctx, dk);
         dfree(ctx, dv);
       }
@@ -378,6 +378,7 @@ static int enqueue_step(rimu_batch *b, const rimu_batch_params *p, int j) {
   a.capv = b->capv;
   a.caps = b->caps;
   a.tsize = b->T;
+  a.kw = 1;
   a.spawn_cb = b->spawn_cb;
   a.v_in = b->recs[src];
   a.cnt_in = b->cnt[src];
@@ -551,6 +552,7 @@ extern "C" int rimu_batch_set_replica(rimu_batch *b, int replica, rimu_model *m,
   if (replica < 0 || replica >= b->nrep) return fail_arg("rimu_batch_set_replica: replica out of range");
   if (m->ctx->device != b->ctx->device) return fail_arg("rimu_batch_set_replica: model on another device");
   if (!(target_walkers > 0)) return fail_arg("rimu_batch_set_replica: target_walkers must be positive");
+  if (m->dm.nbits > 64) return fail_arg("rimu_batch_set_replica: batched runs take addresses of at most 64 bits");
   for (int r = 0; r < b->nrep; ++r) {
     const rimu_model *o = b->models[r];
     if (!o || r == replica) continue;
@@ -790,7 +792,7 @@ extern "C" int rimu_batch_download(rimu_batch *b, int replica, uint64_t *keys, v
   if ((rc = dalloc(ctx, &doff, nb)) || (rc = dalloc(ctx, &dk, tot)) || (rc = dalloc(ctx, &dv, tot))) return rc;
   if (!(rc = h2d(ctx, doff, offs.data(), nb)) &&
       !(rc = rimu_launch_compact(ctx, b->recs[b->cur] + (size_t)o * b->capv, b->cnt[b->cur] + o, nb,
-                                 b->capv, doff, dk, dv)) &&
+                                 b->capv, doff, dk, dv, 1)) &&
       !(rc = d2h(ctx, keys, dk, tot)))
     rc = d2h(ctx, (uint64_t *)vals, dv, tot);
   dfree(ctx, doff);

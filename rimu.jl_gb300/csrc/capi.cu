@@ -153,8 +153,8 @@ extern "C" int rimu_model_destroy(rimu_model *m);
 extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_model **out) {
   if (!ctx || !d || !out) return bad("rimu_model_create: NULL argument");
   if (d->kind < 1 || d->kind > 3) return bad("rimu_model_create: unknown model kind");
-  if (d->n_particles < 0 || d->n_modes < 1 || d->n_modes > 64)
-    return bad("rimu_model_create: need 1 <= n_modes <= 64");
+  if (d->n_particles < 0 || d->n_modes < 1 || d->n_modes > 128)
+    return bad("rimu_model_create: need 1 <= n_modes <= 128");
   if (d->n_components < 0 || d->n_components > 2)
     return bad("rimu_model_create: n_components must be 0, 1 or 2");
   const bool two = two_components(*d);
@@ -175,7 +175,10 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
       return bad("rimu_model_create: n_particles must be the sum over the components");
     nbits = cbits[0] + cbits[1];
   }
-  if (nbits > 64) return bad("rimu_model_create: address does not fit 64 bits");
+  if (nbits > 128) return bad("rimu_model_create: address does not fit 128 bits");
+  if ((nbits > 64 || d->n_modes > 64) && (two || d->kind == RIMU_MODEL_MOM1D))
+    return bad("rimu_model_create: addresses wider than 64 bits need HubbardReal1D or "
+               "one-component HubbardRealSpace");
   if (d->fermion && d->kind != RIMU_MODEL_REALSPACE)
     return bad("rimu_model_create: FermiFS is supported with HubbardRealSpace only");
   if (d->fermion && d->n_particles > d->n_modes) return bad("rimu_model_create: too many fermions");
@@ -325,16 +328,18 @@ extern "C" int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t 
   uint64_t *dk = nullptr;
   double *dv = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, &dk, n)) || (rc = dalloc(ctx, &dv, n))) return rc;
-  if ((rc = h2d(ctx, dk, keys, n)) || (rc = rimu_launch_diagonal(ctx, m->dm, dk, n, dv)) ||
+  const int kw = m->dm.nbits > 64 ? 2 : 1;   // wide addresses come as (lo, hi) pairs
+  if ((rc = dalloc(ctx, &dk, n * kw)) || (rc = dalloc(ctx, &dv, n))) return rc;
+  if ((rc = h2d(ctx, dk, keys, n * kw)) || (rc = rimu_launch_diagonal(ctx, m->dm, dk, n, dv)) ||
       (rc = d2h(ctx, out, dv, n))) { dfree(ctx, dk); dfree(ctx, dv); return rc; }
   dfree(ctx, dk); dfree(ctx, dv);
   RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
   return RIMU_OK;
 }
 
-static int host_num_offdiagonals(const rimu_model *m, uint64_t key) {
+static int host_num_offdiagonals(const rimu_model *m, uint64_t key, uint64_t key_hi = 0) {
   const DevModel &h = m->dm;
+  if (h.nbits > 64) return num_offdiagonals_real(h, k128(key, key_hi));
   if (h.kind == MODEL_MOM1D && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
   if (h.kind == MODEL_MOM1D) {
     MomMap mm;
@@ -346,29 +351,49 @@ static int host_num_offdiagonals(const rimu_model *m, uint64_t key) {
 
 extern "C" int rimu_model_num_offdiagonals(rimu_model *m, uint64_t key, int *out) {
   if (!m || !out) return bad("rimu_model_num_offdiagonals: NULL argument");
+  if (m->dm.nbits > 64) return bad("rimu_model_num_offdiagonals: use the _w form for wide addresses");
   *out = host_num_offdiagonals(m, key);
   return RIMU_OK;
 }
 
-extern "C" int rimu_model_offdiagonals(rimu_model *m, uint64_t key, uint64_t *keys,
-                                       double *vals, int cap, int *n) {
+extern "C" int rimu_model_num_offdiagonals_w(rimu_model *m, const uint64_t *key2, int *out) {
+  if (!m || !key2 || !out) return bad("rimu_model_num_offdiagonals_w: NULL argument");
+  *out = host_num_offdiagonals(m, key2[0], m->dm.nbits > 64 ? key2[1] : 0);
+  return RIMU_OK;
+}
+
+static int model_offdiagonals(rimu_model *m, uint64_t key, uint64_t key_hi, uint64_t *keys,
+                              double *vals, int cap, int *n) {
   if (!m || !n) return bad("rimu_model_offdiagonals: NULL argument");
-  int noff = host_num_offdiagonals(m, key);
+  int noff = host_num_offdiagonals(m, key, key_hi);
   *n = noff;
   if (noff == 0) return RIMU_OK;
   if (cap < noff || !keys || !vals) return bad("rimu_model_offdiagonals: buffer too small");
   rimu_ctx *ctx = m->ctx;
+  const int kw = m->dm.nbits > 64 ? 2 : 1;
   uint64_t *dk = nullptr;
   double *dv = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, &dk, noff)) || (rc = dalloc(ctx, &dv, noff))) return rc;
-  rc = rimu_launch_offdiagonals(ctx, m->dm, key, noff, dk, dv);
-  if (!rc) rc = d2h(ctx, keys, dk, noff);
+  if ((rc = dalloc(ctx, &dk, noff * kw)) || (rc = dalloc(ctx, &dv, noff))) return rc;
+  rc = rimu_launch_offdiagonals(ctx, m->dm, key, key_hi, noff, dk, dv);
+  if (!rc) rc = d2h(ctx, keys, dk, noff * kw);
   if (!rc) rc = d2h(ctx, vals, dv, noff);
   dfree(ctx, dk); dfree(ctx, dv);
   if (rc) return rc;
   RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
   return RIMU_OK;
+}
+
+extern "C" int rimu_model_offdiagonals(rimu_model *m, uint64_t key, uint64_t *keys,
+                                       double *vals, int cap, int *n) {
+  if (m && m->dm.nbits > 64) return bad("rimu_model_offdiagonals: use the _w form for wide addresses");
+  return model_offdiagonals(m, key, 0, keys, vals, cap, n);
+}
+
+extern "C" int rimu_model_offdiagonals_w(rimu_model *m, const uint64_t *key2, uint64_t *keys2,
+                                         double *vals, int cap, int *n) {
+  if (!m || !key2) return bad("rimu_model_offdiagonals_w: NULL argument");
+  return model_offdiagonals(m, key2[0], m->dm.nbits > 64 ? key2[1] : 0, keys2, vals, cap, n);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -383,7 +408,7 @@ static int vec_alloc(rimu_vec *v, int nb_bits, uint32_t capv) {
   vec_free(v);
   size_t nb = (size_t)1 << nb_bits;
   int rc;
-  if ((rc = dalloc(v->ctx, &v->recs, nb * capv)) || (rc = dalloc(v->ctx, &v->count, nb))) return rc;
+  if ((rc = dalloc(v->ctx, &v->recs, nb * capv * v->kw)) || (rc = dalloc(v->ctx, &v->count, nb))) return rc;
   RIMU_CUDA(cudaMemsetAsync(v->count, 0, nb * sizeof(uint32_t), v->ctx->stream));
   v->nb_bits = nb_bits;
   v->capv = capv;
@@ -396,16 +421,29 @@ static uint32_t capv_for(int64_t n, int nb_bits) {
   return round_up(c, 32);
 }
 
-extern "C" int rimu_vec_create(rimu_ctx *ctx, int val_kind, int64_t capacity_hint, rimu_vec **out) {
+extern "C" int rimu_vec_create_kw(rimu_ctx *ctx, int val_kind, int key_words,
+                                  int64_t capacity_hint, rimu_vec **out) {
   if (!ctx || !out) return bad("rimu_vec_create: NULL argument");
   if (val_kind != RIMU_VAL_F64 && val_kind != RIMU_VAL_I64) return bad("rimu_vec_create: bad val_kind");
+  if (key_words != 1 && key_words != 2) return bad("rimu_vec_create: key_words must be 1 or 2");
   rimu_vec *v = new rimu_vec();
   v->ctx = ctx;
   v->val_kind = val_kind;
+  v->kw = key_words;
   int nb_bits = ceil_log2(std::max<int64_t>(1, capacity_hint / 256));
   int rc = vec_alloc(v, nb_bits, capv_for(capacity_hint, nb_bits));
   if (rc) { delete v; return rc; }
   *out = v;
+  return RIMU_OK;
+}
+
+extern "C" int rimu_vec_create(rimu_ctx *ctx, int val_kind, int64_t capacity_hint, rimu_vec **out) {
+  return rimu_vec_create_kw(ctx, val_kind, 1, capacity_hint, out);
+}
+
+extern "C" int rimu_vec_key_words(const rimu_vec *v, int *key_words) {
+  if (!v || !key_words) return bad("rimu_vec_key_words: NULL argument");
+  *key_words = v->kw;
   return RIMU_OK;
 }
 
@@ -433,8 +471,9 @@ extern "C" int rimu_vec_upload(rimu_vec *v, const uint64_t *keys, const void *va
   uint64_t *dk = nullptr, *dv = nullptr;
   unsigned int *flag = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, &dk, n)) || (rc = dalloc(ctx, &dv, n)) || (rc = dalloc(ctx, &flag, 1))) return rc;
-  if ((rc = h2d(ctx, dk, keys, n)) || (rc = h2d(ctx, dv, (const uint64_t *)vals, n))) goto done;
+  const int kw = v->kw;
+  if ((rc = dalloc(ctx, &dk, n * kw)) || (rc = dalloc(ctx, &dv, n)) || (rc = dalloc(ctx, &flag, 1))) return rc;
+  if ((rc = h2d(ctx, dk, keys, n * kw)) || (rc = h2d(ctx, dv, (const uint64_t *)vals, n))) goto done;
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (nb_bits != v->nb_bits || capv != v->capv) {
       if ((rc = vec_alloc(v, nb_bits, capv))) goto done;
@@ -443,7 +482,7 @@ extern "C" int rimu_vec_upload(rimu_vec *v, const uint64_t *keys, const void *va
     }
     unsigned int hflag = 0;
     RIMU_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
-    if ((rc = rimu_launch_bucketize(ctx, dk, dv, n, nb_bits, capv, v->recs, v->count, flag))) goto done;
+    if ((rc = rimu_launch_bucketize(ctx, dk, dv, n, nb_bits, capv, v->recs, v->count, flag, kw))) goto done;
     if ((rc = d2h(ctx, &hflag, flag, 1))) goto done;
     RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
     if (!hflag) {
@@ -479,7 +518,7 @@ extern "C" int rimu_vec_walkernumber_and_length(rimu_vec *v, double *norm, int64
   int rc;
   if ((rc = dalloc(ctx, &acc, 3))) return rc;
   RIMU_CUDA(cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), ctx->stream));
-  rc = rimu_launch_norm(ctx, v->recs, v->count, 1 << v->nb_bits, v->capv, v->val_kind, acc);
+  rc = rimu_launch_norm(ctx, v->recs, v->count, 1 << v->nb_bits, v->capv, v->val_kind, acc, v->kw);
   if (!rc) rc = d2h(ctx, h, acc, 3);
   dfree(ctx, acc);
   if (rc) return rc;
@@ -506,10 +545,10 @@ extern "C" int rimu_vec_download(rimu_vec *v, uint64_t *keys, void *vals, int64_
   if (tot == 0) return RIMU_OK;
   if ((int64_t)tot > cap || !keys || !vals) return bad("rimu_vec_download: buffer too small");
   uint64_t *doff = nullptr, *dk = nullptr, *dv = nullptr;
-  if ((rc = dalloc(ctx, &doff, nb)) || (rc = dalloc(ctx, &dk, tot)) || (rc = dalloc(ctx, &dv, tot))) return rc;
+  if ((rc = dalloc(ctx, &doff, nb)) || (rc = dalloc(ctx, &dk, tot * v->kw)) || (rc = dalloc(ctx, &dv, tot))) return rc;
   if (!(rc = h2d(ctx, doff, off.data(), nb)) &&
-      !(rc = rimu_launch_compact(ctx, v->recs, v->count, nb, v->capv, doff, dk, dv)) &&
-      !(rc = d2h(ctx, keys, dk, tot)))
+      !(rc = rimu_launch_compact(ctx, v->recs, v->count, nb, v->capv, doff, dk, dv, v->kw)) &&
+      !(rc = d2h(ctx, keys, dk, tot * v->kw)))
     rc = d2h(ctx, (uint64_t *)vals, dv, tot);
   dfree(ctx, doff); dfree(ctx, dk); dfree(ctx, dv);
   if (rc) return rc;
@@ -524,9 +563,9 @@ extern "C" int rimu_vec_lookup(rimu_vec *v, const uint64_t *keys, int64_t n, voi
   uint64_t *dk = nullptr, *dv = nullptr;
   int *df = nullptr;
   int rc;
-  if ((rc = dalloc(ctx, &dk, n)) || (rc = dalloc(ctx, &dv, n)) || (rc = dalloc(ctx, &df, n))) return rc;
-  if (!(rc = h2d(ctx, dk, keys, n)) &&
-      !(rc = rimu_launch_lookup(ctx, v->recs, v->count, v->nb_bits, v->capv, dk, n, dv, df)))
+  if ((rc = dalloc(ctx, &dk, n * v->kw)) || (rc = dalloc(ctx, &dv, n)) || (rc = dalloc(ctx, &df, n))) return rc;
+  if (!(rc = h2d(ctx, dk, keys, n * v->kw)) &&
+      !(rc = rimu_launch_lookup(ctx, v->recs, v->count, v->nb_bits, v->capv, dk, n, dv, df, v->kw)))
     rc = d2h(ctx, (uint64_t *)vals, dv, n);
   dfree(ctx, dk); dfree(ctx, dv); dfree(ctx, df);
   if (rc) return rc;
@@ -538,10 +577,12 @@ extern "C" int rimu_vec_copy(rimu_vec *dst, const rimu_vec *src) {
   if (!dst || !src) return bad("rimu_vec_copy: NULL argument");
   if (dst == src) return RIMU_OK;
   int rc;
-  if (dst->nb_bits != src->nb_bits || dst->capv != src->capv)
+  if (dst->nb_bits != src->nb_bits || dst->capv != src->capv || dst->kw != src->kw) {
+    dst->kw = src->kw;
     if ((rc = vec_alloc(dst, src->nb_bits, src->capv))) return rc;
+  }
   size_t nb = (size_t)1 << src->nb_bits;
-  RIMU_CUDA(cudaMemcpyAsync(dst->recs, src->recs, nb * src->capv * sizeof(Rec),
+  RIMU_CUDA(cudaMemcpyAsync(dst->recs, src->recs, nb * src->capv * sizeof(Rec) * src->kw,
                             cudaMemcpyDeviceToDevice, src->ctx->stream));
   RIMU_CUDA(cudaMemcpyAsync(dst->count, src->count, nb * sizeof(uint32_t),
                             cudaMemcpyDeviceToDevice, src->ctx->stream));
@@ -564,10 +605,10 @@ static int vec_regrid(rimu_vec *v, int nb_bits, uint32_t capv) {
     Rec *nr = nullptr;
     uint32_t *nc = nullptr;
     size_t nb = (size_t)1 << nb_bits;
-    if ((rc = dalloc(ctx, &nr, nb * capv)) || (rc = dalloc(ctx, &nc, nb)) || (rc = dalloc(ctx, &flag, 1))) return rc;
+    if ((rc = dalloc(ctx, &nr, nb * capv * v->kw)) || (rc = dalloc(ctx, &nc, nb)) || (rc = dalloc(ctx, &flag, 1))) return rc;
     RIMU_CUDA(cudaMemsetAsync(nc, 0, nb * sizeof(uint32_t), ctx->stream));
     RIMU_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
-    if ((rc = rimu_launch_rebucket(ctx, old, oldc, old_bits, old_capv, nr, nc, nb_bits, capv, flag))) return rc;
+    if ((rc = rimu_launch_rebucket(ctx, old, oldc, old_bits, old_capv, nr, nc, nb_bits, capv, flag, v->kw))) return rc;
     unsigned int hflag = 0;
     if ((rc = d2h(ctx, &hflag, flag, 1))) return rc;
     RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -666,13 +707,15 @@ extern "C" int rimu_wm_set_projector(rimu_wm *w, const uint64_t *keys, const dou
   return RIMU_OK;
 }
 
-static int wm_ensure(rimu_wm *w, int nb_total, uint32_t caps, uint32_t heavy_cap, int ndiag) {
+static int wm_ensure(rimu_wm *w, int nb_total, uint32_t caps, uint32_t heavy_cap, int ndiag,
+                     int kw) {
   rimu_ctx *ctx = w->ctx;
   int rc;
-  if (w->nb_total != nb_total || w->caps != caps) {
+  if (w->nb_total != nb_total || w->caps != caps || w->kw != kw) {
     dfree(ctx, w->spawn);
     dfree(ctx, w->scount);
-    if ((rc = dalloc(ctx, &w->spawn, (size_t)nb_total * caps)) || (rc = dalloc(ctx, &w->scount, nb_total))) return rc;
+    if ((rc = dalloc(ctx, &w->spawn, (size_t)nb_total * caps * kw)) || (rc = dalloc(ctx, &w->scount, nb_total))) return rc;
+    w->kw = kw;
     RIMU_CUDA(cudaMemsetAsync(w->scount, 0, (size_t)nb_total * sizeof(uint32_t), ctx->stream));
     w->nb_total = nb_total;
     w->caps = caps;
@@ -718,6 +761,17 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   if (p->initiator != RIMU_INIT_NONE && m->dm.nbits > 63)
     return bad("rimu_apply_operator: initiator rules need addresses of at most 63 bits");
   if (!(p->boost > 0)) return bad("rimu_apply_operator: boost must be positive");
+  {
+    const int need_kw = m->dm.nbits > 64 ? 2 : 1;
+    if (source->kw != need_kw)
+      return bad("rimu_apply_operator: the vector's address width does not match the model's");
+    if (need_kw == 2 && (p->initiator != RIMU_INIT_NONE || w->nproj != 0))
+      return bad("rimu_apply_operator: initiator rules and projectors need addresses of at most 64 bits");
+    if (target->kw != need_kw) {
+      target->kw = need_kw;
+      target->nb_bits = -1;                   // forces a new allocation below
+    }
+  }
   int rc;
   if (p->op == RIMU_OP_TRANSITION && (rc = ensure_aoff(m, p->dt))) return rc;
 
@@ -762,7 +816,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
       if ((rc = vec_alloc(target, nb_bits, capv))) return rc;
     }
     target->val_kind = source->val_kind;
-    if ((rc = wm_ensure(w, (int)nb, caps, heavy_cap, ndiag))) return rc;
+    if ((rc = wm_ensure(w, (int)nb, caps, heavy_cap, ndiag, source->kw))) return rc;
     RIMU_CUDA(cudaMemsetAsync(w->stats, 0, sizeof(DevStats), ctx->stream));
     RIMU_CUDA(cudaMemsetAsync(w->heavy_count, 0, sizeof(uint32_t), ctx->stream));
     if (w->nproj) {
@@ -799,6 +853,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     int cb = 1;
     while (cb < 32 && (double)cb * mu_v < 256.0 && cb < (int)nb) cb <<= 1;
     a.spawn_cb = cb;
+    a.kw = source->kw;
     a.v_in = source->recs; a.cnt_in = source->count;
     a.v_out = target->recs; a.cnt_out = target->count;
     a.spawn = w->spawn; a.scount = w->scount;
@@ -848,7 +903,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     w->t_ms[3] += 1;
     // algorithmic bytes: spawn reads the source and writes the spawns; annihilation reads
     // spawns and source and writes the target (16-byte records)
-    const double r = (double)sizeof(Rec);
+    const double r = (double)sizeof(Rec) * source->kw;   // record bytes
     w->bytes[0] += r * ((double)source->len + (double)st.spawn_records);
     w->bytes[1] += r * ((double)st.spawn_records + (double)source->len + (double)st.len);
     w->bytes[2] += 1;

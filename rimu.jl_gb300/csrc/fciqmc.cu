@@ -28,9 +28,9 @@ namespace rimu {
 // ------------------------------------------------------------------------------------------
 // Model dispatch
 // ------------------------------------------------------------------------------------------
-template <int KIND>
-__device__ __forceinline__ int column_noff(const DevModel &h, uint64_t key) {
-  if (KIND == MODEL_MOM1D) {
+template <int KIND, class K>
+__device__ __forceinline__ int column_noff(const DevModel &h, K key) {
+  if constexpr (KIND == MODEL_MOM1D) {
     // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144)
     if (h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
     MomMap m;
@@ -40,45 +40,51 @@ __device__ __forceinline__ int column_noff(const DevModel &h, uint64_t key) {
   return num_offdiagonals_real(h, key);
 }
 
-template <int KIND>
-__device__ __forceinline__ Offdiag column_offdiag(const DevModel &h, uint64_t key, int chosen) {
-  if (KIND == MODEL_REAL1D) return real1d_offdiag(h, key, chosen);
-  if (KIND == MODEL_REALSPACE) return realspace_offdiag(h, key, chosen);
-  if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
-  MomMap m;
-  mom_map(key, m);
-  return mom1d_offdiag(h, key, m, chosen);
+template <int KIND, class K>
+__device__ __forceinline__ OffdiagT<K> column_offdiag(const DevModel &h, K key, int chosen) {
+  if constexpr (KIND == MODEL_REAL1D) {
+    return real1d_offdiag(h, key, chosen);
+  } else if constexpr (KIND == MODEL_REALSPACE) {
+    return realspace_offdiag(h, key, chosen);
+  } else {
+    if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
+    MomMap m;
+    mom_map(key, m);
+    return mom1d_offdiag(h, key, m, chosen);
+  }
 }
 
 // sum_i n_i (n_i - 1) of a BoseFS key (bose_hubbard_interaction, bosefs.jl:415-428)
-__device__ __forceinline__ int bose_interaction(uint64_t key) {
-  uint64_t x = key;
+template <class K>
+__device__ __forceinline__ int bose_interaction(K key) {
+  K x = key;
   int acc = 0;
-  while (x) {
-    x = shr64(x, ctz64(x));
-    int n = ctz64(~x);
+  while (!kzero(x)) {
+    x = kshr(x, kctz(x));
+    int n = kctz(~x);
     acc += n * (n - 1);
-    x = shr64(x, n);
+    x = kshr(x, n);
   }
   return acc;
 }
 
 // external_potential of one component chunk: sum over occupied modes, in mode order, of
 // n * pot[mode] (HubbardRealSpace.jl:90-97)
-__device__ __forceinline__ double component_potential(uint64_t ck, int fermion, const double *pot) {
+template <class K>
+__device__ __forceinline__ double component_potential(K ck, int fermion, const double *pot) {
   double pe = 0.0;
-  uint64_t x = ck;
+  K x = ck;
   if (fermion) {
-    while (x) { int b = ctz64(x); pe += 1.0 * pot[b]; x &= x - 1; }
+    while (!kzero(x)) { int b = kctz(x); pe += 1.0 * pot[b]; x = kclear_lowest(x); }
     return pe;
   }
   int mode = 1;
-  while (x) {
-    int z = ctz64(x);
-    x = shr64(x, z); mode += z;
-    int n = ctz64(~x);
+  while (!kzero(x)) {
+    int z = kctz(x);
+    x = kshr(x, z); mode += z;
+    int n = kctz(~x);
     pe += (double)n * pot[mode - 1];
-    x = shr64(x, n);
+    x = kshr(x, n);
   }
   return pe;
 }
@@ -93,7 +99,24 @@ __device__ __forceinline__ double fermi_kinetic(uint64_t ck, const double *kes) 
 
 // Hamiltonian diagonal computed per address (HubbardRealSpace with trap, HubbardMom1D).
 template <int KIND>
-__device__ double model_diagonal(const DevModel &h, uint64_t key) {
+__device__ double model_diagonal64(const DevModel &h, uint64_t key);
+
+template <int KIND, class K>
+__device__ double model_diagonal(const DevModel &h, K key) {
+  if constexpr (KT<K>::BITS == 64) return model_diagonal64<KIND>(h, key);
+  else if constexpr (KIND == MODEL_REAL1D) return h.u * (double)bose_interaction(key) / 2;
+  else {
+    // HubbardRealSpace one component (HubbardRealSpace.jl:284-293)
+    double in = 0.0;
+    if (!h.fermion && h.u != 0.0) in = h.u * (double)bose_interaction(key) / 2;
+    const double pe = h.pot ? component_potential(key, h.fermion, h.pot) : 0.0;
+    return in + pe;
+  }
+}
+
+// The same for 64-bit addresses, with the momentum-space and two-component models.
+template <int KIND>
+__device__ double model_diagonal64(const DevModel &h, uint64_t key) {
   if (KIND == MODEL_MOM1D && h.ncomp == 2) {
     // FermiFS2C: dot(kes, map_a) + dot(kes, map_b) + u/(2M) * 2 n_a n_b
     // (HubbardMom1D.jl:168-171, 182-187; excitations.jl:172-180)
@@ -150,8 +173,8 @@ __device__ double model_diagonal(const DevModel &h, uint64_t key) {
 }
 
 // Diagonal element of the applied operator for replica r.
-template <int KIND>
-__device__ __forceinline__ double op_diagonal(const StepArgs &a, int r, uint64_t key) {
+template <int KIND, class K>
+__device__ __forceinline__ double op_diagonal(const StepArgs &a, int r, K key) {
   if (a.dtab) {
     int I = a.h.fermion ? 0 : bose_interaction_fast(key);
     return a.dtab[(size_t)r * a.ndiag + I];
@@ -161,7 +184,8 @@ __device__ __forceinline__ double op_diagonal(const StepArgs &a, int r, uint64_t
 }
 
 // Offdiagonal element of the applied operator: -H_{new,key} dt (fciqmc.jl:109-112) or H.
-__device__ __forceinline__ double op_offdiag(const StepArgs &a, const Offdiag &od) {
+template <class K>
+__device__ __forceinline__ double op_offdiag(const StepArgs &a, const OffdiagT<K> &od) {
   const double *tab = a.op == OP_TRANSITION ? a.h.aoff : a.h.hoff;
   double v = tab[od.prod];
   return od.sign < 0 ? -v : v;
@@ -232,18 +256,24 @@ __device__ __forceinline__ uint32_t step_of(const StepArgs &a) {
 // addresses then fit in 63 bits); the bucket is that of the address itself.
 constexpr uint64_t UNSAFE_BIT = 1ull << 63;
 
-__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout lay, uint64_t nk,
+template <class K>
+__device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout lay, K nk,
                                            uint64_t vb, uint64_t flag) {
   const uint32_t b = lay.off + bucket_of(nk, lay.bits);
   const uint32_t pos = atomicAdd(&a.scount[b], 1u);
-  if (pos < a.caps) a.spawn[(size_t)b * a.caps + pos] = Rec{nk | flag, vb};
-  else atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
+  if (pos < a.caps) {
+    RecT<K> *sp = static_cast<RecT<K> *>(a.spawn);
+    if constexpr (KT<K>::BITS == 64) sp[(size_t)b * a.caps + pos] = RecT<K>{nk | flag, vb};
+    else sp[(size_t)b * a.caps + pos] = RecT<K>{nk, vb};   // no initiator rules: flag is 0
+  } else {
+    atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
+  }
 }
 
-template <int KIND>
-__device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key, int chosen) {
-  if (KIND == MODEL_REAL1D) return real1d_offdiag_fast(key, h.nbits, chosen);
-  return column_offdiag<KIND>(h, key, chosen);
+template <int KIND, class K>
+__device__ __forceinline__ OffdiagT<K> step_offdiag(const DevModel &h, K key, int chosen) {
+  if constexpr (KIND == MODEL_REAL1D) return real1d_offdiag_fast(key, h.nbits, chosen);
+  else return column_offdiag<KIND>(h, key, chosen);
 }
 
 // Unit j of one column.  Exact columns deposit val * T_{new,key} for offdiagonal j+1
@@ -251,17 +281,17 @@ __device__ __forceinline__ Offdiag step_offdiag(const DevModel &h, uint64_t key,
 // c * T_{new,key} (spawning.jl:232-243).  With float walkers and no on-the-fly projection an
 // attempt needs 32 random bits: attempt j takes word j % 4 of Philox block j / 4 (each lane
 // evaluates the block of its own attempt; under SIMT this costs no extra issue slots).
-template <int KIND, int STYLE>
+template <int KIND, int STYLE, class K>
 __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout lay, uint32_t step,
-                                           uint64_t key, uint64_t vb, double c, int noff,
+                                           K key, uint64_t vb, double c, int noff,
                                            int exact, uint64_t flag, uint32_t j) {
   const uint32_t rep = a.replica_base + (uint32_t)r;
   if (exact) {
-    const Offdiag od = step_offdiag<KIND>(a.h, key, (int)j + 1);
+    const OffdiagT<K> od = step_offdiag<KIND>(a.h, key, (int)j + 1);
     if (od.prod == 0) return;
     double y = bitsd(vb) * op_offdiag(a, od);
     if (STYLE == STYLE_DSS && a.has_proj) {
-      const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, key, j);
+      const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, kword(key), j);
       y = project_threshold(y, a.proj_threshold, u53_of(rr));
     }
     if (is_zero_d(y)) return;
@@ -269,14 +299,14 @@ __device__ __forceinline__ void spawn_unit(const StepArgs &a, int r, RepLayout l
     return;
   }
   const bool grouped = STYLE != STYLE_INTEGER && !a.has_proj;
-  const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, key, grouped ? j >> 2 : j);
+  const U4 rr = draw(a.seed, PURPOSE_SPAWN, rep, step, kword(key), grouped ? j >> 2 : j);
   uint32_t word = rr.x;
   if (grouped) {
     const uint32_t q = j & 3;
     word = q == 0 ? rr.x : q == 1 ? rr.y : q == 2 ? rr.z : rr.w;
   }
   const int chosen = (int)uniform_index(word, (uint32_t)noff) + 1;
-  const Offdiag od = step_offdiag<KIND>(a.h, key, chosen);
+  const OffdiagT<K> od = step_offdiag<KIND>(a.h, key, chosen);
   if (od.prod == 0) return;
   double y = c * op_offdiag(a, od);
   if (STYLE == STYLE_INTEGER) {
@@ -318,8 +348,8 @@ __device__ __forceinline__ double dint_of(const DevModel &h, int n) {
 // Work of one column: units (offdiagonals if exact, attempts otherwise) and the spawn
 // coefficient c, without FP64 compares (DynamicSemistochastic, spawning.jl:364-378;
 // WithReplacement attempts, spawning.jl:234-235).
-template <int KIND, int STYLE>
-__device__ __forceinline__ uint64_t column_work(const StepArgs &a, uint64_t key, uint64_t vb,
+template <int KIND, int STYLE, class K>
+__device__ __forceinline__ uint64_t column_work(const StepArgs &a, K key, uint64_t vb,
                                                 int &noff, int &exact, double &c,
                                                 SpawnAcc &acc) {
   noff = column_noff<KIND>(a.h, key);
@@ -359,7 +389,8 @@ __device__ __forceinline__ uint64_t column_work(const StepArgs &a, uint64_t key,
 }
 
 // Cut a column with more than HEAVY_LIMIT units into chunks for k_spawn_heavy.
-__device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, int noff,
+template <class K>
+__device__ void push_heavy(const StepArgs &a, int r, const RecT<K> &rec, double c, int noff,
                            int exact, int unsafe, uint64_t work) {
   const uint64_t nch = (work + HEAVY_CHUNK - 1) / HEAVY_CHUNK;
   const uint32_t idx = atomicAdd(a.heavy_count, (uint32_t)nch);
@@ -369,7 +400,8 @@ __device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, i
       break;
     }
     HeavyChunk ch;
-    ch.key = rec.key; ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
+    ch.key = KT<K>::lo(rec.key); ch.key_hi = KT<K>::hi(rec.key);
+    ch.val = rec.val; ch.c = c; ch.noff = noff; ch.exact = exact;
     ch.j0 = (uint32_t)(k * HEAVY_CHUNK);
     const uint64_t rem = work - k * HEAVY_CHUNK;
     ch.cnt = (uint32_t)(rem < (uint64_t)HEAVY_CHUNK ? rem : HEAVY_CHUNK);
@@ -383,10 +415,10 @@ __device__ void push_heavy(const StepArgs &a, int r, const Rec &rec, double c, i
 // time: every lane evaluates the columns of two walkers, then the batch's units (spawn
 // attempts, or offdiagonals of exact columns) are dealt out one per lane by an exclusive scan
 // and a binary search.
-template <int KIND, int STYLE>
+template <int KIND, int STYLE, class K>
 __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_total) {
   __shared__ uint32_t s_bpre[WARPS][CHUNK_BUCKETS + 1];
-  __shared__ uint64_t s_key[WARPS][BATCH];
+  __shared__ K s_key[WARPS][BATCH];
   __shared__ uint64_t s_val[WARPS][BATCH];
   __shared__ double s_c[WARPS][BATCH];
   __shared__ uint32_t s_excl[WARPS][BATCH];
@@ -432,7 +464,8 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
 #pragma unroll
           for (int st = 16; st >= 1; st >>= 1)
             if (bi + st < cb && s_bpre[w][bi + st] <= f) bi += st;
-          const Rec rec = a.v_in[(size_t)(b0 + bi) * a.capv_in + (f - s_bpre[w][bi])];
+          const RecT<K> rec = static_cast<const RecT<K> *>(a.v_in)[(size_t)(b0 + bi) * a.capv_in +
+                                                                  (f - s_bpre[w][bi])];
           int noff, exact;
           double c;
           uint64_t work = column_work<KIND, STYLE>(a, rec.key, rec.val, noff, exact, c, acc);
@@ -482,7 +515,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_spawn(StepArgs a, int nb_tota
   if (cur_r >= 0) flush_spawn_acc(a, cur_r, acc);
 }
 
-template <int KIND, int STYLE>
+template <int KIND, int STYLE, class K>
 __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
   const uint32_t step = step_of(a);
   uint32_t nch = *a.heavy_count;
@@ -495,8 +528,8 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
     }
     const RepLayout lay = layout_of(a, (int)ch.rep);
     for (uint32_t t = threadIdx.x; t < ch.cnt; t += blockDim.x)
-      spawn_unit<KIND, STYLE>(a, (int)ch.rep, lay, step, ch.key, ch.val, ch.c, ch.noff, ch.exact,
-                              ch.unsafe ? UNSAFE_BIT : 0ull, ch.j0 + t);
+      spawn_unit<KIND, STYLE>(a, (int)ch.rep, lay, step, KT<K>::make(ch.key, ch.key_hi), ch.val,
+                              ch.c, ch.noff, ch.exact, ch.unsafe ? UNSAFE_BIT : 0ull, ch.j0 + t);
   }
 }
 
@@ -528,7 +561,9 @@ constexpr uint32_t PACK_FAIL = 0x80000000u;   // overflow bit of the packed inse
 // keys [T] u64, contribution values [T] u64, list heads [T] u32, contribution link words
 // [T] u16, occupied-slot list [T] u16, compression queue [T] u16: 26 bytes per slot, so that
 // four CTAs with 2048 slots fit one SM.
-__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * 26; }
+// With two-word addresses the keys take 16 bytes: 34 bytes per slot.
+template <class K = uint64_t>
+__host__ __device__ inline size_t ann_smem(uint32_t T) { return (size_t)T * (sizeof(K) + 18); }
 
 
 __device__ __forceinline__ U128 neg128(U128 x) {
@@ -698,12 +733,12 @@ __device__ double initiator_sum_f(const StepArgs &a, uint32_t head, const uint64
 }
 
 // Diagonal step of one walker (diagonal_step!, spawning.jl:73-77), float walkers.
-template <int KIND>
+template <int KIND, class K>
 __device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t rep, uint32_t step,
-                                             const Rec &rec) {
+                                             const RecT<K> &rec) {
   double res = op_diagonal<KIND>(a, r, rec.key) * bitsd(rec.val);
   if (a.has_proj) {
-    const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
+    const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, kword(rec.key), 0);
     res = project_threshold(res, a.proj_threshold, u53_of(rr));
   }
   return res;
@@ -711,6 +746,20 @@ __device__ __forceinline__ double diag_float(const StepArgs &a, int r, uint32_t 
 
 // Slot of `key` in the table, claimed if the key is new; -1 if the table is full.  Probing
 // starts at the top bits of a multiplicative hash of the key.
+__device__ __forceinline__ int table_insert(Key128 *tkey, uint32_t T, int tbits, Key128 key,
+                                            bool &claimed) {
+  // two-word keys: every probe is a 16-byte compare-and-swap (no torn reads of a slot)
+  uint32_t sl = (uint32_t)((kword(key) * 0x9E3779B97F4A7C15ull) >> (64 - tbits));
+  claimed = false;
+  const Key128 empty = KT<Key128>::empty();
+  for (uint32_t p = 0; p < T; ++p) {
+    const Key128 old = atomicCAS(&tkey[sl], empty, key);
+    if (old == empty) { claimed = true; return (int)sl; }
+    if (old == key) return (int)sl;
+    sl = (sl + 1) & (T - 1);
+  }
+  return -1;
+}
 __device__ __forceinline__ int table_insert(uint64_t *tkey, uint32_t T, int tbits, uint64_t key,
                                             bool &claimed) {
   uint32_t sl = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - tbits));
@@ -766,11 +815,11 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *count, bool flag) {
 
 // Compression draw (compression.jl:28-42) for an address whose |value| is below the
 // threshold: kept at +-threshold with probability |value| / threshold.
-template <int STYLE>
-__device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t step, uint64_t key,
+template <int STYLE, class K>
+__device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t step, K key,
                                               double &fv) {
   const double prob = a.comp_mode == 1 ? abs_d(fv) : abs_d(fv) / a.compression;
-  const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, step, key, 0);
+  const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, step, kword(key), 0);
   if (!bernoulli53(u53_of(rr), prob)) return false;
   fv = signed_like(a.compression, fv);
   return true;
@@ -778,26 +827,28 @@ __device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t
 
 // Statistics and the ProjectedEnergy dot products of a kept address (its |value| in fixed
 // point is added to the norm by the caller).
-template <int STYLE>
-__device__ __forceinline__ void account_entry(const StepArgs &a, int r, uint64_t key, double dv,
+template <int STYLE, class K>
+__device__ __forceinline__ void account_entry(const StepArgs &a, int r, K key, double dv,
                                               AnnAcc &acc) {
   acc.len++;
-  if (a.nproj == 0) return;
-  const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
-  int lo = 0, hi = a.nproj - 1;
-  while (lo <= hi) {
-    const int mid = (lo + hi) >> 1;
-    if (pk[mid] == key) {
-      const size_t o = (size_t)r * a.nproj + mid;
-      a.proj_out_v[o] = a.proj_v[o] * dv;
-      a.proj_out_h[o] = a.proj_h[o] * dv;
-      break;
+  if constexpr (KT<K>::BITS == 64) {   // projectors hold 64-bit addresses
+    if (a.nproj == 0) return;
+    const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
+    int lo = 0, hi = a.nproj - 1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      if (pk[mid] == key) {
+        const size_t o = (size_t)r * a.nproj + mid;
+        a.proj_out_v[o] = a.proj_v[o] * dv;
+        a.proj_out_h[o] = a.proj_h[o] * dv;
+        break;
+      }
+      if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
     }
-    if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
   }
 }
-template <int STYLE>
-__device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t key, double dv,
+template <int STYLE, class K>
+__device__ __forceinline__ void account_kept(const StepArgs &a, int r, K key, double dv,
                                              U128 mag, AnnAcc &acc) {
   acc.norm = add128(acc.norm, mag);
   account_entry<STYLE>(a, r, key, dv, acc);
@@ -814,7 +865,7 @@ __device__ __forceinline__ void account_kept(const StepArgs &a, int r, uint64_t 
 // by full warps.  A bucket with more contributions than the table holds is processed in
 // passes, each taking the addresses whose hash bits 16.. select it; a pass that still
 // overflows is split.
-template <int KIND, int STYLE>
+template <int KIND, int STYLE, class K>
 __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
   // per pass parity: packed insertion counter, compression queue length, second-list length
@@ -822,15 +873,16 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
   __shared__ uint32_t s_out;            // entries written to the target slab of the bucket
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const uint32_t T = a.tsize;
-  uint64_t *tkey = reinterpret_cast<uint64_t *>(smem);
-  uint64_t *cval = tkey + T;
+  K *tkey = reinterpret_cast<K *>(smem);
+  uint64_t *cval = reinterpret_cast<uint64_t *>(tkey + T);
   uint32_t *thead = reinterpret_cast<uint32_t *>(cval + T);
   uint16_t *clink = reinterpret_cast<uint16_t *>(thead + T);
   uint16_t *slist = clink + T;
   uint16_t *qlist = slist + T;
   const uint32_t lim = T - ANN_THREADS;   // a warp starts a round of insertions only below this
   const int tbits = 31 - __clz((int)T);
-  for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY_KEY; thead[i] = NIL; }
+  const K EMPTY = KT<K>::empty();
+  for (uint32_t i = tid; i < T; i += ANN_THREADS) { tkey[i] = EMPTY; thead[i] = NIL; }
   if (tid < 8) s_cnt[tid >> 2][tid & 3] = 0;
   if (tid == 0) s_out = 0;
   __syncthreads();
@@ -853,9 +905,9 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
     const uint32_t ns = nsp < a.caps ? nsp : a.caps;
     const uint32_t nv0 = a.cnt_in[gb];
     const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
-    const Rec *sp = a.spawn + (size_t)gb * a.caps;
-    const Rec *vbase = a.v_in + (size_t)gb * a.capv_in;
-    Rec *vout = a.v_out + (size_t)gb * a.capv;
+    const RecT<K> *sp = static_cast<const RecT<K> *>(a.spawn) + (size_t)gb * a.caps;
+    const RecT<K> *vbase = static_cast<const RecT<K> *>(a.v_in) + (size_t)gb * a.capv_in;
+    RecT<K> *vout = static_cast<RecT<K> *>(a.v_out) + (size_t)gb * a.capv;
     const uint32_t need = nv + ns;   // contributions: also an upper bound on the addresses
     int lvl0 = 0;
     if (need > lim) {
@@ -885,15 +937,15 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
         uint8_t cls = CLS_SAFE;
         if (f < need) {
           src = f < nv;
-          Rec rec = src ? vbase[f] : sp[f - nv];
-          if (a.init_rule) {
+          RecT<K> rec = src ? vbase[f] : sp[f - nv];
+          if constexpr (KT<K>::BITS == 64) if (a.init_rule) {
             // classes of the initiator rules (initiators.jl:142-157): a spawn carries its
             // parent's class in bit 63; a diagonal term is "initiator" for an initiator
             if (src) cls = parent_unsafe<STYLE>(a, rec.val) ? CLS_SAFE : CLS_INITIATOR;
             else cls = (rec.key & UNSAFE_BIT) ? CLS_UNSAFE : CLS_SAFE;
             rec.key &= ~UNSAFE_BIT;
           }
-          if (lvl == 0 || ((uint32_t)(mix64(rec.key) >> 16) & mask) == sel) {
+          if (lvl == 0 || ((uint32_t)(mix64(kword(rec.key)) >> 16) & mask) == sel) {
             slot = table_insert(tkey, T, tbits, rec.key, claimed);
             if (slot < 0) {
               lfail = true;
@@ -905,7 +957,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
                 if (STYLE == STYLE_INTEGER) {
                   const int64_t v = (int64_t)rec.val;
                   const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
-                  const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
+                  const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, kword(rec.key), 0);
                   const int64_t res = round_stochastic(x, u53_of(rr));
                   // clones_deaths_zombies (spawning.jl:79-93)
                   const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
@@ -955,7 +1007,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
       if (fail) {
         for (uint32_t i = tid; i < nslots; i += ANN_THREADS) {
           const int slot = slist[i];
-          tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
+          tkey[slot] = EMPTY; thead[slot] = NIL;
         }
       } else {
         // ---- finalize: exact sum, compression threshold, statistics, output ----
@@ -965,7 +1017,8 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
         for (uint32_t i0 = (uint32_t)w * 32; i0 < nslots; i0 += ANN_THREADS) {
           const uint32_t i = i0 + lane;
           bool keep = false, queue = false, slow = false;
-          uint64_t key = 0, vb = 0;
+          K key = KT<K>::from(0);
+          uint64_t vb = 0;
           int slot = 0;
           uint32_t head = NIL;
           if (i < nslots) {
@@ -1026,7 +1079,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             }
           }
           const uint32_t pos = warp_append(&s_out, keep);
-          if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+          if (keep && pos < a.capv) vout[pos] = RecT<K>{key, vb};
           if (STYLE != STYLE_INTEGER) {
             // compression queue from the bottom of qlist, second list from the top
             const uint32_t q = warp_append(s_nq, queue);
@@ -1037,7 +1090,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             const uint32_t sl = warp_append(s_nslow, slow);
             if (slow) qlist[T - 1 - sl] = (uint16_t)slot;
           }
-          if (i < nslots && !queue && !slow) { tkey[slot] = EMPTY_KEY; thead[slot] = NIL; }
+          if (i < nslots && !queue && !slow) { tkey[slot] = EMPTY; thead[slot] = NIL; }
         }
         if (STYLE != STYLE_INTEGER) {
           __syncthreads();
@@ -1046,12 +1099,13 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
           for (uint32_t i0 = (uint32_t)w * 32; i0 < nslow; i0 += ANN_THREADS) {
             const uint32_t i = i0 + lane;
             bool keep = false;
-            uint64_t key = 0, vb = 0;
+            K key = KT<K>::from(0);
+            uint64_t vb = 0;
             if (i < nslow && nq + i < T) {
               const int slot = qlist[T - 1 - i];
               key = tkey[slot];
               const uint32_t head = thead[slot];
-              tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
+              tkey[slot] = EMPTY; thead[slot] = NIL;
               double fv;
               if (a.init_rule) {
                 fv = initiator_sum_f(a, head, cval, clink, ncon, acc, &bad);
@@ -1098,24 +1152,24 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
               vb = dbits(fv);
             }
             const uint32_t pos = warp_append(&s_out, keep);
-            if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+            if (keep && pos < a.capv) vout[pos] = RecT<K>{key, vb};
           }
           // ---- compression draws of the queued addresses, on full warps ----
           for (uint32_t i0 = (uint32_t)w * 32; i0 < nq; i0 += ANN_THREADS) {
             const uint32_t i = i0 + lane;
             bool keep = false;
-            uint64_t key = 0;
+            K key = KT<K>::from(0);
             double fv = 0.0;
             if (i < nq) {
               const int slot = qlist[i];
               key = tkey[slot];
               fv = bitsd(cval[thead[slot]]);
-              tkey[slot] = EMPTY_KEY; thead[slot] = NIL;
+              tkey[slot] = EMPTY; thead[slot] = NIL;
               keep = compress_draw<STYLE>(a, r, step, key, fv);
               if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
             }
             const uint32_t pos = warp_append(&s_out, keep);
-            if (keep && pos < a.capv) vout[pos] = Rec{key, dbits(fv)};
+            if (keep && pos < a.capv) vout[pos] = RecT<K>{key, dbits(fv)};
           }
         }
         acc.clones += pa.clones; acc.deaths += pa.deaths; acc.zombies += pa.zombies;
@@ -1163,24 +1217,28 @@ __global__ void k_diag_table(DevModel h, int op, double dt, const double *shift,
   dtab[i] = op == OP_TRANSITION ? 1 - dt * (d - shift[r]) : d;
 }
 
-__global__ void k_bucketize(const uint64_t *keys, const uint64_t *vals, int64_t n, int nb_bits,
-                            uint32_t capv, Rec *recs, uint32_t *count, unsigned int *flag) {
+// Walker-list kernels, on Rec (one-word addresses) or Rec2 (two-word addresses, K = Key128,
+// host key arrays of (lo, hi) pairs).
+template <class K>
+__global__ void k_bucketize(const K *keys, const uint64_t *vals, int64_t n, int nb_bits,
+                            uint32_t capv, RecT<K> *recs, uint32_t *count, unsigned int *flag) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint64_t k = keys[i];
+  const K k = keys[i];
   uint32_t b = bucket_of(k, nb_bits);
   uint32_t pos = atomicAdd(&count[b], 1u);
-  if (pos < capv) recs[(size_t)b * capv + pos] = Rec{k, vals[i]};
+  if (pos < capv) recs[(size_t)b * capv + pos] = RecT<K>{k, vals[i]};
   else atomicOr(flag, (unsigned)FLAG_V_OVERFLOW);
 }
 
-__global__ void k_rebucket(const Rec *old_recs, const uint32_t *old_count, int old_nb,
-                           uint32_t old_capv, Rec *recs, uint32_t *count, int nb_bits,
+template <class K>
+__global__ void k_rebucket(const RecT<K> *old_recs, const uint32_t *old_count, int old_nb,
+                           uint32_t old_capv, RecT<K> *recs, uint32_t *count, int nb_bits,
                            uint32_t capv, unsigned int *flag) {
   for (int gb = blockIdx.x; gb < old_nb; gb += gridDim.x) {
     uint32_t n = old_count[gb];
     for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-      Rec rec = old_recs[(size_t)gb * old_capv + e];
+      RecT<K> rec = old_recs[(size_t)gb * old_capv + e];
       uint32_t b = bucket_of(rec.key, nb_bits);
       uint32_t pos = atomicAdd(&count[b], 1u);
       if (pos < capv) recs[(size_t)b * capv + pos] = rec;
@@ -1189,28 +1247,30 @@ __global__ void k_rebucket(const Rec *old_recs, const uint32_t *old_count, int o
   }
 }
 
-__global__ void k_compact(const Rec *recs, const uint32_t *count, int nb, uint32_t capv,
-                          const uint64_t *offsets, uint64_t *keys, uint64_t *vals) {
+template <class K>
+__global__ void k_compact(const RecT<K> *recs, const uint32_t *count, int nb, uint32_t capv,
+                          const uint64_t *offsets, K *keys, uint64_t *vals) {
   for (int gb = blockIdx.x; gb < nb; gb += gridDim.x) {
     uint32_t n = count[gb];
     uint64_t o = offsets[gb];
     for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-      Rec rec = recs[(size_t)gb * capv + e];
+      RecT<K> rec = recs[(size_t)gb * capv + e];
       keys[o + e] = rec.key;
       vals[o + e] = rec.val;
     }
   }
 }
 
-__global__ void k_norm(const Rec *recs, const uint32_t *count, int nb, uint32_t capv,
+template <class K>
+__global__ void k_norm(const RecT<K> *recs, const uint32_t *count, int nb, uint32_t capv,
                        int val_kind, unsigned long long *acc3) {
   U128 fx{0, 0};
   long long len = 0;
   for (int gb = blockIdx.x; gb < nb; gb += gridDim.x) {
     uint32_t n = count[gb];
     for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-      Rec rec = recs[(size_t)gb * capv + e];
-      double v = val_kind == RIMU_VAL_I64 ? (double)(int64_t)rec.val : bitsd(rec.val);
+      const uint64_t val = recs[(size_t)gb * capv + e].val;
+      double v = val_kind == RIMU_VAL_I64 ? (double)(int64_t)val : bitsd(val);
       fx = add128(fx, fixed_of(fabs(v)));
       len++;
     }
@@ -1223,14 +1283,15 @@ __global__ void k_norm(const Rec *recs, const uint32_t *count, int nb, uint32_t 
   }
 }
 
-__global__ void k_lookup(const Rec *recs, const uint32_t *count, int nb_bits, uint32_t capv,
-                         const uint64_t *keys, int64_t n, uint64_t *vals, int *found) {
+template <class K>
+__global__ void k_lookup(const RecT<K> *recs, const uint32_t *count, int nb_bits, uint32_t capv,
+                         const K *keys, int64_t n, uint64_t *vals, int *found) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint64_t k = keys[i];
+  const K k = keys[i];
   uint32_t b = bucket_of(k, nb_bits);
   uint32_t c = count[b];
-  const Rec *base = recs + (size_t)b * capv;
+  const RecT<K> *base = recs + (size_t)b * capv;
   vals[i] = 0;
   found[i] = 0;
   for (uint32_t e = 0; e < c; ++e) {
@@ -1238,17 +1299,17 @@ __global__ void k_lookup(const Rec *recs, const uint32_t *count, int nb_bits, ui
   }
 }
 
-template <int KIND>
-__global__ void k_diagonal(DevModel h, const uint64_t *keys, int64_t n, double *out) {
+template <int KIND, class K>
+__global__ void k_diagonal(DevModel h, const K *keys, int64_t n, double *out) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) out[i] = model_diagonal<KIND>(h, keys[i]);
 }
 
-template <int KIND>
-__global__ void k_offdiagonals(DevModel h, uint64_t key, int noff, uint64_t *keys, double *vals) {
+template <int KIND, class K>
+__global__ void k_offdiagonals(DevModel h, K key, int noff, K *keys, double *vals) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= noff) return;
-  Offdiag od = column_offdiag<KIND>(h, key, c + 1);
+  OffdiagT<K> od = column_offdiag<KIND>(h, key, c + 1);
   keys[c] = od.key;
   double v = od.prod == 0 ? 0.0 : h.hoff[od.prod];
   vals[c] = od.sign < 0 ? -v : v;
@@ -1257,7 +1318,7 @@ __global__ void k_offdiagonals(DevModel h, uint64_t key, int noff, uint64_t *key
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-template <int KIND, int STYLE>
+template <int KIND, int STYLE, class K>
 static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
   const int cap = ctx->num_sms * 64;
@@ -1266,28 +1327,28 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
   const int cap_a = ctx->num_sms * 4;                 // resident annihilation CTAs
   const int grid = nb_total < cap_a ? nb_total : cap_a;
   if (ev) cudaEventRecord(ev[0], st);
-  k_spawn<KIND, STYLE><<<grid_s, WARPS * 32, 0, st>>>(a, nb_total);
+  k_spawn<KIND, STYLE, K><<<grid_s, WARPS * 32, 0, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[1], st);
-  k_spawn_heavy<KIND, STYLE><<<ctx->num_sms * 4, 256, 0, st>>>(a);
+  k_spawn_heavy<KIND, STYLE, K><<<ctx->num_sms * 4, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  const size_t smem = ann_smem(a.tsize);
+  const size_t smem = ann_smem<K>(a.tsize);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_annihilate<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_annihilate<KIND, STYLE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
     attr_set = true;
   }
-  k_annihilate<KIND, STYLE><<<grid, ANN_THREADS, smem, st>>>(a, nb_total);
+  k_annihilate<KIND, STYLE, K><<<grid, ANN_THREADS, smem, st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[3], st);
   return rimu_cuda_check(cudaGetLastError(), "step kernels");
 }
 
-template <int KIND>
+template <int KIND, class K>
 static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
   switch (a.style) {
-    case STYLE_INTEGER: return launch_step_t<KIND, STYLE_INTEGER>(ctx, a, nb_total, ev);
-    case STYLE_DETERMINISTIC: return launch_step_t<KIND, STYLE_DETERMINISTIC>(ctx, a, nb_total, ev);
-    default: return launch_step_t<KIND, STYLE_DSS>(ctx, a, nb_total, ev);
+    case STYLE_INTEGER: return launch_step_t<KIND, STYLE_INTEGER, K>(ctx, a, nb_total, ev);
+    case STYLE_DETERMINISTIC: return launch_step_t<KIND, STYLE_DETERMINISTIC, K>(ctx, a, nb_total, ev);
+    default: return launch_step_t<KIND, STYLE_DSS, K>(ctx, a, nb_total, ev);
   }
 }
 
@@ -1296,53 +1357,86 @@ static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
 using namespace rimu;
 
 int rimu_launch_step(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
+  if (a.kw == 2) {   // two-word addresses: HubbardReal1D and one-component HubbardRealSpace
+    switch (a.h.kind) {
+      case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D, Key128>(ctx, a, nb_total, ev);
+      case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE, Key128>(ctx, a, nb_total, ev);
+      default: rimu_set_error("two-word addresses: model not supported"); return RIMU_ERR_BADARG;
+    }
+  }
   switch (a.h.kind) {
-    case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D>(ctx, a, nb_total, ev);
-    case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE>(ctx, a, nb_total, ev);
-    default: return launch_step_k<MODEL_MOM1D>(ctx, a, nb_total, ev);
+    case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D, uint64_t>(ctx, a, nb_total, ev);
+    case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE, uint64_t>(ctx, a, nb_total, ev);
+    default: return launch_step_k<MODEL_MOM1D, uint64_t>(ctx, a, nb_total, ev);
   }
 }
 
 int rimu_launch_bucketize(rimu_ctx *ctx, const uint64_t *keys, const uint64_t *vals, int64_t n,
-                          int nb_bits, uint32_t capv, Rec *recs, uint32_t *count,
-                          unsigned int *flag) {
+                          int nb_bits, uint32_t capv, void *recs, uint32_t *count,
+                          unsigned int *flag, int kw) {
   if (n == 0) return 0;
-  int64_t blocks = (n + 255) / 256;
-  k_bucketize<<<(unsigned)blocks, 256, 0, ctx->stream>>>(keys, vals, n, nb_bits, capv, recs,
-                                                         count, flag);
+  unsigned blocks = (unsigned)((n + 255) / 256);
+  if (kw == 2)
+    k_bucketize<<<blocks, 256, 0, ctx->stream>>>(reinterpret_cast<const Key128 *>(keys), vals, n,
+                                                 nb_bits, capv, static_cast<Rec2 *>(recs), count, flag);
+  else
+    k_bucketize<<<blocks, 256, 0, ctx->stream>>>(keys, vals, n, nb_bits, capv,
+                                                 static_cast<Rec *>(recs), count, flag);
   return rimu_cuda_check(cudaGetLastError(), "k_bucketize");
 }
 
-int rimu_launch_rebucket(rimu_ctx *ctx, const Rec *old_recs, const uint32_t *old_count,
-                         int old_nb_bits, uint32_t old_capv, Rec *recs, uint32_t *count,
-                         int nb_bits, uint32_t capv, unsigned int *flag) {
+int rimu_launch_rebucket(rimu_ctx *ctx, const void *old_recs, const uint32_t *old_count,
+                         int old_nb_bits, uint32_t old_capv, void *recs, uint32_t *count,
+                         int nb_bits, uint32_t capv, unsigned int *flag, int kw) {
   int old_nb = 1 << old_nb_bits;
   int grid = old_nb < 65536 ? old_nb : 65536;
-  k_rebucket<<<grid, 256, 0, ctx->stream>>>(old_recs, old_count, old_nb, old_capv, recs, count,
-                                            nb_bits, capv, flag);
+  if (kw == 2)
+    k_rebucket<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec2 *>(old_recs), old_count, old_nb,
+                                              old_capv, static_cast<Rec2 *>(recs), count, nb_bits,
+                                              capv, flag);
+  else
+    k_rebucket<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec *>(old_recs), old_count, old_nb,
+                                              old_capv, static_cast<Rec *>(recs), count, nb_bits,
+                                              capv, flag);
   return rimu_cuda_check(cudaGetLastError(), "k_rebucket");
 }
 
-int rimu_launch_compact(rimu_ctx *ctx, const Rec *recs, const uint32_t *count, int nb,
-                        uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals) {
+int rimu_launch_compact(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
+                        uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals,
+                        int kw) {
   int grid = nb < 65536 ? nb : 65536;
-  k_compact<<<grid, 256, 0, ctx->stream>>>(recs, count, nb, capv, offsets, keys, vals);
+  if (kw == 2)
+    k_compact<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec2 *>(recs), count, nb, capv,
+                                             offsets, reinterpret_cast<Key128 *>(keys), vals);
+  else
+    k_compact<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec *>(recs), count, nb, capv,
+                                             offsets, keys, vals);
   return rimu_cuda_check(cudaGetLastError(), "k_compact");
 }
 
-int rimu_launch_norm(rimu_ctx *ctx, const Rec *recs, const uint32_t *count, int nb,
-                     uint32_t capv, int val_kind, unsigned long long *acc3) {
+int rimu_launch_norm(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
+                     uint32_t capv, int val_kind, unsigned long long *acc3, int kw) {
   int grid = nb < ctx->num_sms * 8 ? nb : ctx->num_sms * 8;
-  k_norm<<<grid, 256, 0, ctx->stream>>>(recs, count, nb, capv, val_kind, acc3);
+  if (kw == 2)
+    k_norm<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec2 *>(recs), count, nb, capv,
+                                          val_kind, acc3);
+  else
+    k_norm<<<grid, 256, 0, ctx->stream>>>(static_cast<const Rec *>(recs), count, nb, capv,
+                                          val_kind, acc3);
   return rimu_cuda_check(cudaGetLastError(), "k_norm");
 }
 
-int rimu_launch_lookup(rimu_ctx *ctx, const Rec *recs, const uint32_t *count, int nb_bits,
+int rimu_launch_lookup(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb_bits,
                        uint32_t capv, const uint64_t *keys, int64_t n, uint64_t *vals,
-                       int *found) {
+                       int *found, int kw) {
   if (n == 0) return 0;
-  k_lookup<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(recs, count, nb_bits, capv,
-                                                                 keys, n, vals, found);
+  const unsigned g = (unsigned)((n + 127) / 128);
+  if (kw == 2)
+    k_lookup<<<g, 128, 0, ctx->stream>>>(static_cast<const Rec2 *>(recs), count, nb_bits, capv,
+                                         reinterpret_cast<const Key128 *>(keys), n, vals, found);
+  else
+    k_lookup<<<g, 128, 0, ctx->stream>>>(static_cast<const Rec *>(recs), count, nb_bits, capv,
+                                         keys, n, vals, found);
   return rimu_cuda_check(cudaGetLastError(), "k_lookup");
 }
 
@@ -1353,10 +1447,18 @@ int rimu_launch_diag_table(rimu_ctx *ctx, const DevModel &h, int op, double dt,
   return rimu_cuda_check(cudaGetLastError(), "k_diag_table");
 }
 
+// Diagonal elements of n addresses; with an address wider than 64 bits (h.nbits > 64) the
+// keys are (lo, hi) pairs, 2n words.
 int rimu_launch_diagonal(rimu_ctx *ctx, const DevModel &h, const uint64_t *keys, int64_t n,
                          double *out) {
   if (n == 0) return 0;
   unsigned g = (unsigned)((n + 255) / 256);
+  if (h.nbits > 64) {
+    const Key128 *k2 = reinterpret_cast<const Key128 *>(keys);
+    if (h.kind == MODEL_REAL1D) k_diagonal<MODEL_REAL1D><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
+    else k_diagonal<MODEL_REALSPACE><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
+    return rimu_cuda_check(cudaGetLastError(), "k_diagonal");
+  }
   switch (h.kind) {
     case MODEL_REAL1D: k_diagonal<MODEL_REAL1D><<<g, 256, 0, ctx->stream>>>(h, keys, n, out); break;
     case MODEL_REALSPACE: k_diagonal<MODEL_REALSPACE><<<g, 256, 0, ctx->stream>>>(h, keys, n, out); break;
@@ -1365,10 +1467,20 @@ int rimu_launch_diagonal(rimu_ctx *ctx, const DevModel &h, const uint64_t *keys,
   return rimu_cuda_check(cudaGetLastError(), "k_diagonal");
 }
 
-int rimu_launch_offdiagonals(rimu_ctx *ctx, const DevModel &h, uint64_t key, int noff,
-                             uint64_t *keys, double *vals) {
+// All offdiagonals of the column of address (key_lo, key_hi); keys out as one word each, or
+// as (lo, hi) pairs when h.nbits > 64.
+int rimu_launch_offdiagonals(rimu_ctx *ctx, const DevModel &h, uint64_t key_lo, uint64_t key_hi,
+                             int noff, uint64_t *keys, double *vals) {
   if (noff == 0) return 0;
   unsigned g = (unsigned)((noff + 127) / 128);
+  if (h.nbits > 64) {
+    const Key128 key = k128(key_lo, key_hi);
+    Key128 *k2 = reinterpret_cast<Key128 *>(keys);
+    if (h.kind == MODEL_REAL1D) k_offdiagonals<MODEL_REAL1D><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
+    else k_offdiagonals<MODEL_REALSPACE><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
+    return rimu_cuda_check(cudaGetLastError(), "k_offdiagonals");
+  }
+  const uint64_t key = key_lo;
   switch (h.kind) {
     case MODEL_REAL1D: k_offdiagonals<MODEL_REAL1D><<<g, 128, 0, ctx->stream>>>(h, key, noff, keys, vals); break;
     case MODEL_REALSPACE: k_offdiagonals<MODEL_REALSPACE><<<g, 128, 0, ctx->stream>>>(h, key, noff, keys, vals); break;

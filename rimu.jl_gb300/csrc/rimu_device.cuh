@@ -96,6 +96,80 @@ RIMU_HD uint32_t bucket_of(uint64_t key, int nb_bits) {
 }
 
 // ------------------------------------------------------------------------------------------
+// Address words.  An address of at most 64 bits is one uint64_t; a two-chunk address (65-128
+// bits, bitstring.jl:6-18) is a Key128 with the same bit positions across both words.  The
+// generic helpers below let the BoseFS/FermiFS operations be written once for both.
+// ------------------------------------------------------------------------------------------
+struct __align__(16) Key128 { uint64_t lo, hi; };
+RIMU_HD Key128 k128(uint64_t lo, uint64_t hi) { Key128 k; k.lo = lo; k.hi = hi; return k; }
+RIMU_HD bool operator==(Key128 a, Key128 b) { return a.lo == b.lo && a.hi == b.hi; }
+RIMU_HD bool operator!=(Key128 a, Key128 b) { return a.lo != b.lo || a.hi != b.hi; }
+RIMU_HD bool operator<(Key128 a, Key128 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+RIMU_HD Key128 operator&(Key128 a, Key128 b) { return k128(a.lo & b.lo, a.hi & b.hi); }
+RIMU_HD Key128 operator|(Key128 a, Key128 b) { return k128(a.lo | b.lo, a.hi | b.hi); }
+RIMU_HD Key128 operator^(Key128 a, Key128 b) { return k128(a.lo ^ b.lo, a.hi ^ b.hi); }
+RIMU_HD Key128 operator~(Key128 a) { return k128(~a.lo, ~a.hi); }
+
+// shifts by any s >= 0 (0 beyond the width)
+RIMU_HD uint64_t kshl(uint64_t a, int s) { return shl64(a, s); }
+RIMU_HD uint64_t kshr(uint64_t a, int s) { return shr64(a, s); }
+RIMU_HD Key128 kshl(Key128 a, int s) {
+  if (s <= 0) return a;
+  if (s >= 128) return k128(0, 0);
+  if (s >= 64) return k128(0, a.lo << (s - 64));
+  return k128(a.lo << s, (a.hi << s) | (a.lo >> (64 - s)));
+}
+RIMU_HD Key128 kshr(Key128 a, int s) {
+  if (s <= 0) return a;
+  if (s >= 128) return k128(0, 0);
+  if (s >= 64) return k128(a.hi >> (s - 64), 0);
+  return k128((a.lo >> s) | (a.hi << (64 - s)), a.hi >> s);
+}
+RIMU_HD int kctz(uint64_t x) { return ctz64(x); }
+RIMU_HD int kctz(Key128 x) { return x.lo ? ctz64(x.lo) : 64 + ctz64(x.hi); }
+RIMU_HD int kpopc(uint64_t x) { return popc64(x); }
+RIMU_HD int kpopc(Key128 x) { return popc64(x.lo) + popc64(x.hi); }
+RIMU_HD int kclz(uint64_t x) { return clz64_hd(x); }
+RIMU_HD int kclz(Key128 x) { return x.hi ? clz64_hd(x.hi) : 64 + clz64_hd(x.lo); }
+RIMU_HD bool kzero(uint64_t x) { return x == 0; }
+RIMU_HD bool kzero(Key128 x) { return (x.lo | x.hi) == 0; }
+RIMU_HD bool ktest(uint64_t x, int b) { return ((x >> b) & 1) != 0; }
+RIMU_HD bool ktest(Key128 x, int b) { return b < 64 ? ((x.lo >> b) & 1) != 0 : ((x.hi >> (b - 64)) & 1) != 0; }
+RIMU_HD uint64_t kclear_lowest(uint64_t x) { return x & (x - 1); }
+RIMU_HD Key128 kclear_lowest(Key128 x) {
+  return x.lo ? k128(x.lo & (x.lo - 1), x.hi) : k128(0, x.hi & (x.hi - 1));
+}
+// The 64-bit word that stands for an address in hashes and random-number counters: the
+// address itself up to 64 bits, lo ^ mix64(hi) for two words (mix64(0) = 0).
+RIMU_HD uint64_t kword(uint64_t k) { return k; }
+RIMU_HD uint64_t kword(Key128 k) { return k.lo ^ mix64(k.hi); }
+RIMU_HD uint32_t bucket_of(Key128 key, int nb_bits) { return bucket_of(kword(key), nb_bits); }
+
+template <class K> struct KT;
+template <> struct KT<uint64_t> {
+  static constexpr int BITS = 64;
+  RIMU_HD static uint64_t make(uint64_t lo, uint64_t) { return lo; }
+  RIMU_HD static uint64_t lo(uint64_t k) { return k; }
+  RIMU_HD static uint64_t hi(uint64_t) { return 0; }
+  RIMU_HD static uint64_t mask(int n) { return lowmask(n); }            // low n bits
+  RIMU_HD static uint64_t bit(int i) { return 1ull << i; }
+  RIMU_HD static uint64_t from(uint64_t v) { return v; }
+  RIMU_HD static uint64_t empty() { return ~0ull; }
+};
+template <> struct KT<Key128> {
+  static constexpr int BITS = 128;
+  RIMU_HD static Key128 make(uint64_t lo, uint64_t hi) { return k128(lo, hi); }
+  RIMU_HD static uint64_t lo(Key128 k) { return k.lo; }
+  RIMU_HD static uint64_t hi(Key128 k) { return k.hi; }
+  RIMU_HD static Key128 mask(int n) {
+    return n >= 128 ? k128(~0ull, ~0ull) : (n >= 64 ? k128(~0ull, lowmask(n - 64)) : k128(lowmask(n), 0));
+  }
+  RIMU_HD static Key128 bit(int i) { return i < 64 ? k128(1ull << i, 0) : k128(0, 1ull << (i - 64)); }
+  RIMU_HD static Key128 from(uint64_t v) { return k128(v, 0); }
+  RIMU_HD static Key128 empty() { return k128(~0ull, ~0ull); }
+};
+
+// ------------------------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11).  Counter (draw, step, address lo, address hi), key (seed lo, seed hi ^ purpose ^
 // replica): a draw depends only on what it is for, never on the thread that makes it.
@@ -306,58 +380,64 @@ RIMU_HD double fixed_to_double(U128 x) {
 struct ModeIdx { int occ, mode, offset; };
 
 // k-th occupied mode (1-based).  Also reports the previous occupied mode (mode 0 if none).
-RIMU_HD ModeIdx bose_find_occupied(uint64_t key, int k, ModeIdx *prev) {
-  uint64_t x = key;
+template <class K>
+RIMU_HD ModeIdx bose_find_occupied(K key, int k, ModeIdx *prev) {
+  K x = key;
   int mode = 1, bit = 0;
   ModeIdx p{0, 0, 0};
-  while (x) {
-    int z = ctz64(x);
-    x = shr64(x, z); mode += z; bit += z;
-    int n = ctz64(~x);
+  while (!kzero(x)) {
+    int z = kctz(x);
+    x = kshr(x, z); mode += z; bit += z;
+    int n = kctz(~x);
     ModeIdx cur{n, mode, bit};
     if (--k == 0) { if (prev) *prev = p; return cur; }
     p = cur;
-    x = shr64(x, n); bit += n;
+    x = kshr(x, n); bit += n;
   }
   if (prev) *prev = p;
   return ModeIdx{0, 0, 0};
 }
 
 // find_mode (bosefs.jl:188-203): occupation and offset of a given 1-based mode.
-RIMU_HD ModeIdx bose_find_mode(uint64_t key, int mode_wanted) {
-  uint64_t x = key;
+template <class K>
+RIMU_HD ModeIdx bose_find_mode(K key, int mode_wanted) {
+  K x = key;
   int mode = 1, bit = 0, last_occ = 0, last_mode = 0, last_off = 0;
-  while (x) {
-    int z = ctz64(x);
-    x = shr64(x, z); mode += z; bit += z;
-    int n = ctz64(~x);
+  while (!kzero(x)) {
+    int z = kctz(x);
+    x = kshr(x, z); mode += z; bit += z;
+    int n = kctz(~x);
     int dist = mode_wanted - mode;
     if (dist == 0) return ModeIdx{n, mode_wanted, bit};
     if (dist < 0) return ModeIdx{0, mode_wanted, bit + dist};
     last_occ = n; last_mode = mode; last_off = bit;
-    x = shr64(x, n); bit += n;
+    x = kshr(x, n); bit += n;
   }
   return ModeIdx{0, mode_wanted, last_off + last_occ + mode_wanted - last_mode};
 }
 
-RIMU_HD int bose_num_occupied(uint64_t key) {
+template <class K>
+RIMU_HD int bose_num_occupied(K key) {
   // number of runs of ones
-  return popc64(key & ~(key << 1));
+  return kpopc(key & ~kshl(key, 1));
 }
 
 // partial_left_shift / partial_right_shift (bitstring.jl:342-375) on one 64-bit chunk.
-RIMU_HD uint64_t partial_left_shift(uint64_t c, int i, int j) {
-  uint64_t mask = shl64(lowmask(j - i + 1), i);
-  uint64_t shifted = ((c & mask) << 1) & mask;
-  return shifted | (c & ~mask) | (1ull << i);
+template <class K>
+RIMU_HD K partial_left_shift(K c, int i, int j) {
+  const K mask = kshl(KT<K>::mask(j - i + 1), i);
+  const K shifted = kshl(c & mask, 1) & mask;
+  return shifted | (c & ~mask) | KT<K>::bit(i);
 }
-RIMU_HD uint64_t partial_right_shift(uint64_t c, int i, int j) {
-  uint64_t mask = shl64(lowmask(j - i + 1), i);
-  uint64_t shifted = ((c & mask) >> 1) & mask;
-  return shifted | (c & ~mask) | (1ull << j);
+template <class K>
+RIMU_HD K partial_right_shift(K c, int i, int j) {
+  const K mask = kshl(KT<K>::mask(j - i + 1), i);
+  const K shifted = kshr(c & mask, 1) & mask;
+  return shifted | (c & ~mask) | KT<K>::bit(j);
 }
 // bose_move_particle (bitstring.jl:559-567): move one boson between bit offsets.
-RIMU_HD uint64_t bose_move(uint64_t c, int from, int to) {
+template <class K>
+RIMU_HD K bose_move(K c, int from, int to) {
   if (to == from) return c;
   if (to < from) return partial_left_shift(c, to, from);
   return partial_right_shift(c, from, to - 1);
@@ -368,47 +448,52 @@ RIMU_HD uint64_t bose_move(uint64_t c, int from, int to) {
 // square root is the magnitude (index into the aoff/hoff tables), plus a sign.  prod == 0
 // marks an illegal move (value 0.0, address unchanged).
 // ------------------------------------------------------------------------------------------
-struct Offdiag { uint64_t key; int prod; int sign; };
+template <class K> struct OffdiagT { K key; int prod; int sign; };
+using Offdiag = OffdiagT<uint64_t>;
 
-RIMU_HD int num_offdiagonals_real(const DevModel &h, uint64_t key) {
-  if (h.ncomp == 2) {   // component 1 in the high bits, component 2 in the low cbits[1]
-    const uint64_t k0 = shr64(key, h.cbits[1]), k1 = key & lowmask(h.cbits[1]);
-    return ((h.cferm[0] ? popc64(k0) : bose_num_occupied(k0)) +
-            (h.cferm[1] ? popc64(k1) : bose_num_occupied(k1))) * 2 * h.ndim;
+template <class K>
+RIMU_HD int num_offdiagonals_real(const DevModel &h, K key) {
+  if constexpr (KT<K>::BITS == 64) {
+    if (h.ncomp == 2) {   // component 1 in the high bits, component 2 in the low cbits[1]
+      const uint64_t k0 = shr64(key, h.cbits[1]), k1 = key & lowmask(h.cbits[1]);
+      return ((h.cferm[0] ? popc64(k0) : bose_num_occupied(k0)) +
+              (h.cferm[1] ? popc64(k1) : bose_num_occupied(k1))) * 2 * h.ndim;
+    }
   }
-  int s = h.fermion ? popc64(key) : bose_num_occupied(key);
+  int s = h.fermion ? kpopc(key) : bose_num_occupied(key);
   return h.kind == MODEL_REAL1D ? 2 * s : s * 2 * h.ndim;
 }
 
 // HubbardReal1D.get_offdiagonal via hopnextneighbour (bosefs.jl:297-345).
-RIMU_HD Offdiag real1d_offdiag(const DevModel &h, uint64_t key, int chosen) {
+template <class K>
+RIMU_HD OffdiagT<K> real1d_offdiag(const DevModel &h, K key, int chosen) {
   int site = (chosen + 1) >> 1;
   ModeIdx prev;
   ModeIdx cur = bose_find_occupied(key, site, &prev);
   int M = h.M, B = h.nbits;
-  Offdiag r;
+  OffdiagT<K> r;
   r.sign = 1;
   if (chosen & 1) {   // hop right
     if (cur.mode == M) {
-      r.key = ((key << 1) | 1ull) & lowmask(B);
-      r.prod = cur.occ * (ctz64(~key) + 1);
+      r.key = (kshl(key, 1) | KT<K>::from(1)) & KT<K>::mask(B);
+      r.prod = cur.occ * (kctz(~key) + 1);
     } else {
       int after = cur.offset + cur.occ;          // separator after the site
-      int next = ctz64(~shr64(key, after + 1));  // occupation of mode+1
-      r.key = key ^ (3ull << (after - 1));
+      int next = kctz(~kshr(key, after + 1));    // occupation of mode+1
+      r.key = key ^ kshl(KT<K>::from(3), after - 1);
       r.prod = cur.occ * (next + 1);
     }
   } else {            // hop left
     if (cur.mode == 1) {
-      uint64_t nk = (key >> 1) | (1ull << (B - 1));
+      K nk = kshr(key, 1) | KT<K>::bit(B - 1);
       // leading ones of nk within B bits = occupation of mode M after the hop
       int lead = 0;
-      for (int b = B - 1; b >= 0 && ((nk >> b) & 1); --b) ++lead;
+      for (int b = B - 1; b >= 0 && ktest(nk, b); --b) ++lead;
       r.key = nk;
-      r.prod = ctz64(~key) * lead;
+      r.prod = kctz(~key) * lead;
     } else {
       int prev_occ = (prev.mode == cur.mode - 1) ? prev.occ : 0;
-      r.key = key ^ (3ull << (cur.offset - 1));
+      r.key = key ^ kshl(KT<K>::from(3), cur.offset - 1);
       r.prod = cur.occ * (prev_occ + 1);
     }
   }
@@ -417,48 +502,52 @@ RIMU_HD Offdiag real1d_offdiag(const DevModel &h, uint64_t key, int chosen) {
 
 // sum_i n_i (n_i - 1) of a BoseFS word: each run of n ones contributes n(n-1), and
 // sum over runs of C(n, 2) = sum_{d >= 1} popcount(bits starting d+1 consecutive ones).
-RIMU_HD int bose_interaction_fast(uint64_t x) {
+template <class K>
+RIMU_HD int bose_interaction_fast(K x) {
   int acc = 0;
-  uint64_t y = x & (x >> 1);
-  while (y) { acc += popc64(y); y &= y >> 1; }
+  K y = x & kshr(x, 1);
+  while (!kzero(y)) { acc += kpopc(y); y = y & kshr(y, 1); }
   return 2 * acc;
 }
 
 // Position of the k-th (0-based) set bit.
-RIMU_HD int select_bit(uint64_t x, int k) {
-  for (int i = 0; i < k; ++i) x &= x - 1;
-  return ctz64(x);
+template <class K>
+RIMU_HD int select_bit(K x, int k) {
+  for (int i = 0; i < k; ++i) x = kclear_lowest(x);
+  return kctz(x);
 }
 
 // HubbardReal1D offdiagonal with word operations only: the site-th occupied mode starts at
 // the site-th run start (bits that are set and whose lower neighbour is not); same results
 // as hopnextneighbour (bosefs.jl:297-345).
-RIMU_HD Offdiag real1d_offdiag_fast(uint64_t key, int B, int chosen) {
+template <class K>
+RIMU_HD OffdiagT<K> real1d_offdiag_fast(K key, int B, int chosen) {
+  constexpr int W = KT<K>::BITS;
   const int site = (chosen + 1) >> 1;
-  const uint64_t starts = key & ~(key << 1);
+  const K starts = key & ~kshl(key, 1);
   const int start = select_bit(starts, site - 1);
-  const int n = ctz64(~shr64(key, start));
+  const int n = kctz(~kshr(key, start));
   const int end = start + n;                 // separator after the mode, or B for mode M
-  Offdiag r;
+  OffdiagT<K> r;
   r.sign = 1;
   if (chosen & 1) {                          // hop right
     if (end == B) {                          // from mode M to mode 1 (periodic wrap)
-      r.key = ((key << 1) | 1ull) & lowmask(B);
-      r.prod = n * (ctz64(~key) + 1);
+      r.key = (kshl(key, 1) | KT<K>::from(1)) & KT<K>::mask(B);
+      r.prod = n * (kctz(~key) + 1);
     } else {
-      const int next = ctz64(~shr64(key, end + 1));
-      r.key = key ^ (3ull << (end - 1));
+      const int next = kctz(~kshr(key, end + 1));
+      r.key = key ^ kshl(KT<K>::from(3), end - 1);
       r.prod = n * (next + 1);
     }
   } else {                                   // hop left
     if (start == 0) {                        // from mode 1 to mode M
-      const uint64_t nk = (key >> 1) | (1ull << (B - 1));
-      const int lead = clz64_hd(~(nk << (64 - B)));
+      const K nk = kshr(key, 1) | KT<K>::bit(B - 1);
+      const int lead = kclz(~kshl(nk, W - B));
       r.key = nk;
       r.prod = n * lead;
     } else {
-      const int prev = start >= 2 ? clz64_hd(~(key << (65 - start))) : 0;
-      r.key = key ^ (3ull << (start - 1));
+      const int prev = start >= 2 ? kclz(~kshl(key, W + 1 - start)) : 0;
+      r.key = key ^ kshl(KT<K>::from(3), start - 1);
       r.prod = n * (prev + 1);
     }
   }
@@ -483,29 +572,31 @@ RIMU_HD int neighbor_site(const DevModel &h, int mode, int chosen) {
 // Fermionic single excitation a+_dst a_src on one FermiFS chunk (1-based modes; src occupied):
 // false when dst is occupied; else the new chunk and the sign (-1)^(occupied modes below src,
 // then below dst after the removal) (fermi_excitation, bitstring.jl:746-791).
-RIMU_HD bool fermi_move(uint64_t key, int src, int dst, uint64_t &out, int &sign) {
-  if ((key >> (dst - 1)) & 1) return false;
-  int count = popc64(key & lowmask(src - 1));
-  const uint64_t k1 = key ^ (1ull << (src - 1));
-  count += popc64(k1 & lowmask(dst - 1));
-  out = k1 | (1ull << (dst - 1));
+template <class K>
+RIMU_HD bool fermi_move(K key, int src, int dst, K &out, int &sign) {
+  if (ktest(key, dst - 1)) return false;
+  int count = kpopc(key & KT<K>::mask(src - 1));
+  const K k1 = key ^ KT<K>::bit(src - 1);
+  count += kpopc(k1 & KT<K>::mask(dst - 1));
+  out = k1 | KT<K>::bit(dst - 1);
   sign = (count & 1) ? -1 : 1;
   return true;
 }
 
 // HubbardRealSpace offdiagonal `chosen` of one component's chunk (HubbardRealSpace.jl:325-338).
-RIMU_HD Offdiag realspace_hop(const DevModel &h, uint64_t key, int chosen, bool fermion) {
+template <class K>
+RIMU_HD OffdiagT<K> realspace_hop(const DevModel &h, K key, int chosen, bool fermion) {
   int nb = 2 * h.ndim;
   int particle = (chosen - 1) / nb + 1, neigh = (chosen - 1) % nb + 1;
-  Offdiag r{key, 0, 1};
+  OffdiagT<K> r{key, 0, 1};
   if (fermion) {
     // particle-th set bit
-    uint64_t x = key;
-    for (int i = 1; i < particle; ++i) x &= x - 1;
-    int src = ctz64(x) + 1;
+    K x = key;
+    for (int i = 1; i < particle; ++i) x = kclear_lowest(x);
+    int src = kctz(x) + 1;
     int dst = neighbor_site(h, src, neigh);
     if (dst == 0) return r;
-    uint64_t nk;
+    K nk;
     int sign;
     if (!fermi_move(key, src, dst, nk, sign)) return r;   // Pauli blocked
     r.key = nk;
@@ -565,17 +656,22 @@ RIMU_HD int component_overlap(const DevModel &h, uint64_t a, uint64_t b) {
 // HubbardRealSpace offdiagonal: one component, or component 1's hops followed by component
 // 2's (HubbardRealSpaceOffdiagonals, HubbardRealSpace.jl:344-391), each with its own t
 // (table block c).
-RIMU_HD Offdiag realspace_offdiag(const DevModel &h, uint64_t key, int chosen) {
-  if (h.ncomp != 2) return realspace_hop(h, key, chosen, h.fermion != 0);
-  const uint64_t k0 = component_of(h, key, 0);
-  const int n0 = component_occupied(k0, h.cferm[0]) * 2 * h.ndim;
-  const int c = chosen <= n0 ? 0 : 1;
-  Offdiag r = realspace_hop(h, c ? component_of(h, key, 1) : k0, c ? chosen - n0 : chosen,
-                            h.cferm[c] != 0);
-  if (r.prod == 0) { r.key = key; return r; }
-  r.key = with_component(h, key, c, r.key);
-  r.prod += c * h.cstride;
-  return r;
+template <class K>
+RIMU_HD OffdiagT<K> realspace_offdiag(const DevModel &h, K key, int chosen) {
+  if constexpr (KT<K>::BITS == 64) {
+    if (h.ncomp == 2) {
+      const uint64_t k0 = component_of(h, key, 0);
+      const int n0 = component_occupied(k0, h.cferm[0]) * 2 * h.ndim;
+      const int c = chosen <= n0 ? 0 : 1;
+      Offdiag r = realspace_hop(h, c ? component_of(h, key, 1) : k0, c ? chosen - n0 : chosen,
+                                h.cferm[c] != 0);
+      if (r.prod == 0) { r.key = key; return r; }
+      r.key = with_component(h, key, c, r.key);
+      r.prod += c * h.cstride;
+      return r;
+    }
+  }
+  return realspace_hop(h, key, chosen, h.fermion != 0);
 }
 
 // HubbardMom1D with FermiFS2C: momentum_transfer_excitation of two components with fold=true

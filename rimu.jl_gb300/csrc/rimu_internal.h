@@ -9,15 +9,19 @@
 
 namespace rimu {
 
-// One walker: an address and its amplitude (double or int64 bit pattern).
-struct __align__(16) Rec { uint64_t key; uint64_t val; };
+// One walker: an address and its amplitude (double or int64 bit pattern).  16 bytes for
+// addresses of up to 64 bits, 32 bytes (16-byte aligned) for two-word addresses.
+template <class K> struct __align__(16) RecT { K key; uint64_t val; };
+using Rec = RecT<uint64_t>;
+using Rec2 = RecT<Key128>;
 
 // A heavy column is split into chunks of at most HEAVY_CHUNK spawn attempts.
 constexpr int HEAVY_CHUNK = 2048;
 constexpr int HEAVY_LIMIT = 1024;   // columns with more work than this go to the heavy list
 
 struct __align__(16) HeavyChunk {
-  uint64_t key;
+  uint64_t key;      // address (low word)
+  uint64_t key_hi;   // high word of a two-word address, else 0
   uint64_t val;      // amplitude bits
   double c;          // spawn coefficient
   int noff;
@@ -71,11 +75,12 @@ struct StepArgs {
   const uint32_t *rep_off;    // [nrep + 1]
   const int *rep_bits;        // [nrep]
   const uint32_t *step_dev;   // when non-null, *step_dev is added to `step` (device counter)
-  const Rec *v_in;
+  int kw;                     // address words: 1 (Rec records) or 2 (Rec2 records)
+  const void *v_in;
   const uint32_t *cnt_in;
-  Rec *v_out;
+  void *v_out;
   uint32_t *cnt_out;
-  Rec *spawn;
+  void *spawn;
   uint32_t *scount;
   HeavyChunk *heavy;
   uint32_t heavy_cap;
@@ -119,6 +124,7 @@ struct rimu_vec {
   int val_kind = RIMU_VAL_F64;
   int nb_bits = 0;
   uint32_t capv = 0;
+  int kw = 1;               // address words: records are Rec (1) or Rec2 (2, two Rec units)
   rimu::Rec *recs = nullptr;
   uint32_t *count = nullptr;
   int64_t len = 0;          // length after the last operation that changed it
@@ -141,6 +147,7 @@ struct rimu_wm {
   int dtab_n = 0;
   double *d_shift = nullptr;
   int64_t last_spawns = -1;
+  int kw = 1;                           // address words of the spawn slabs
   int keys_per_bucket = 1024;           // expected contributions per bucket (launch shape)
   int table_slots = 0;                  // annihilation table slots per CTA (0: automatic)
   // projector
@@ -199,22 +206,25 @@ int ensure_aoff(rimu_model *m, double dt);
 // after k_annihilate on the context stream.
 int rimu_launch_step(rimu_ctx *ctx, const rimu::StepArgs &a, int nb_total,
                      cudaEvent_t *ev = nullptr);
+// Walker-list launchers; kw = address words (1: Rec records, 2: Rec2 records and (lo, hi) key
+// pairs in the host-side key arrays).
 int rimu_launch_bucketize(rimu_ctx *ctx, const uint64_t *keys, const uint64_t *vals, int64_t n,
-                          int nb_bits, uint32_t capv, rimu::Rec *recs, uint32_t *count,
-                          unsigned int *flag);
-int rimu_launch_rebucket(rimu_ctx *ctx, const rimu::Rec *old_recs, const uint32_t *old_count,
-                         int old_nb_bits, uint32_t old_capv, rimu::Rec *recs, uint32_t *count,
-                         int nb_bits, uint32_t capv, unsigned int *flag);
-int rimu_launch_compact(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb,
-                        uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals);
-int rimu_launch_norm(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb,
-                     uint32_t capv, int val_kind, unsigned long long *acc3);
-int rimu_launch_lookup(rimu_ctx *ctx, const rimu::Rec *recs, const uint32_t *count, int nb_bits,
+                          int nb_bits, uint32_t capv, void *recs, uint32_t *count,
+                          unsigned int *flag, int kw);
+int rimu_launch_rebucket(rimu_ctx *ctx, const void *old_recs, const uint32_t *old_count,
+                         int old_nb_bits, uint32_t old_capv, void *recs, uint32_t *count,
+                         int nb_bits, uint32_t capv, unsigned int *flag, int kw);
+int rimu_launch_compact(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
+                        uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals,
+                        int kw);
+int rimu_launch_norm(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
+                     uint32_t capv, int val_kind, unsigned long long *acc3, int kw);
+int rimu_launch_lookup(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb_bits,
                        uint32_t capv, const uint64_t *keys, int64_t n, uint64_t *vals,
-                       int *found);
+                       int *found, int kw);
 int rimu_launch_diag_table(rimu_ctx *ctx, const rimu::DevModel &h, int op, double dt,
                            const double *shift, int nrep, int ndiag, double *dtab);
 int rimu_launch_diagonal(rimu_ctx *ctx, const rimu::DevModel &h, const uint64_t *keys,
                          int64_t n, double *out);
-int rimu_launch_offdiagonals(rimu_ctx *ctx, const rimu::DevModel &h, uint64_t key, int noff,
-                             uint64_t *keys, double *vals);
+int rimu_launch_offdiagonals(rimu_ctx *ctx, const rimu::DevModel &h, uint64_t key_lo,
+                             uint64_t key_hi, int noff, uint64_t *keys, double *vals);

@@ -104,6 +104,7 @@ int fail_arg(const std::string &msg) {
 extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
   if (!a || !b || !out) return fail_arg("rimu_vec_dot: NULL argument");
   if (a->ctx != b->ctx) return fail_arg("rimu_vec_dot: vectors of different contexts");
+  if (a->kw != 1 || b->kw != 1) return fail_arg("rimu_vec_dot: addresses of at most 64 bits only");
   if (a->nb_bits > b->nb_bits) std::swap(a, b);
   rimu_ctx *ctx = a->ctx;
   const int nba = 1 << a->nb_bits;
@@ -126,6 +127,7 @@ extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
 extern "C" int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind) {
   if (!dst || !src) return fail_arg("rimu_vec_convert: NULL argument");
   if (dst == src) return fail_arg("rimu_vec_convert: dst and src must differ");
+  if (src->kw != 1) return fail_arg("rimu_vec_convert: addresses of at most 64 bits only");
   if (val_kind != RIMU_VAL_F64 && val_kind != RIMU_VAL_I64) return fail_arg("rimu_vec_convert: bad val_kind");
   if (src->val_kind != val_kind && val_kind != RIMU_VAL_F64)
     return fail_arg("rimu_vec_convert: only Int64 to Float64 converts");

@@ -21,7 +21,8 @@ OP_TRANSITION, OP_HAMILTONIAN = 0, 1
 EXPORTS = [
     "rimu_version", "rimu_last_error", "rimu_ctx_create", "rimu_ctx_destroy",
     "rimu_ctx_synchronize", "rimu_model_create", "rimu_model_destroy", "rimu_model_diagonal",
-    "rimu_model_num_offdiagonals", "rimu_model_offdiagonals", "rimu_vec_create",
+    "rimu_model_num_offdiagonals", "rimu_model_offdiagonals", "rimu_model_num_offdiagonals_w",
+    "rimu_model_offdiagonals_w", "rimu_vec_create", "rimu_vec_create_kw", "rimu_vec_key_words",
     "rimu_vec_destroy", "rimu_vec_upload", "rimu_vec_download", "rimu_vec_length",
     "rimu_vec_walkernumber_and_length", "rimu_vec_lookup", "rimu_vec_copy", "rimu_vec_empty",
     "rimu_wm_create", "rimu_wm_destroy", "rimu_wm_set_projector", "rimu_wm_set_timing",
@@ -117,6 +118,10 @@ def load(build_if_missing: bool = True):
         "rimu_model_num_offdiagonals": ([vp, C.c_uint64, P(C.c_int)], C.c_int),
         "rimu_model_offdiagonals": ([vp, C.c_uint64, u64p, f64p, C.c_int, P(C.c_int)], C.c_int),
         "rimu_vec_create": ([vp, C.c_int, C.c_int64, P(vp)], C.c_int),
+        "rimu_vec_create_kw": ([vp, C.c_int, C.c_int, C.c_int64, P(vp)], C.c_int),
+        "rimu_vec_key_words": ([vp, P(C.c_int)], C.c_int),
+        "rimu_model_num_offdiagonals_w": ([vp, u64p, P(C.c_int)], C.c_int),
+        "rimu_model_offdiagonals_w": ([vp, u64p, u64p, f64p, C.c_int, P(C.c_int)], C.c_int),
         "rimu_vec_destroy": ([vp], C.c_int),
         "rimu_vec_upload": ([vp, u64p, vp, C.c_int64], C.c_int),
         "rimu_vec_download": ([vp, u64p, vp, C.c_int64, i64p], C.c_int),

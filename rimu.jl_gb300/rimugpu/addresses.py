@@ -58,8 +58,8 @@ class BoseFS:
             raise ValueError("invalid ONR: negative occupation")
         self.N = int(sum(onr))
         self.M = len(onr)
-        if self.N + self.M - 1 > 64:
-            raise ValueError("BoseFS wider than 64 bits is not supported")
+        if self.N + self.M - 1 > 128:
+            raise ValueError("BoseFS wider than 128 bits is not supported")
         self.key = _bose_key(onr)
 
     @classmethod
@@ -116,8 +116,8 @@ class FermiFS:
             raise ValueError("invalid fermionic ONR")
         self.N = int(sum(onr))
         self.M = len(onr)
-        if self.M > 64:
-            raise ValueError("FermiFS wider than 64 bits is not supported")
+        if self.M > 128:
+            raise ValueError("FermiFS wider than 128 bits is not supported")
         self.key = sum(1 << k for k, n in enumerate(onr) if n)
 
     @classmethod

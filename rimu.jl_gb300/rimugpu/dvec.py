@@ -17,6 +17,28 @@ from .initiators import initiator_rule
 from .styles import IsDeterministic, IsDynamicSemistochastic, StochasticStyle, default_style
 
 
+_M64 = (1 << 64) - 1
+
+
+def pack_keys(keys, kw: int) -> np.ndarray:
+    """Addresses as the C ABI takes them: uint64 words, (lo, hi) pairs when kw == 2."""
+    if kw == 1:
+        return np.ascontiguousarray(keys, dtype=np.uint64)
+    out = np.zeros(2 * len(keys), dtype=np.uint64)
+    for i, k in enumerate(keys):
+        k = int(k)
+        out[2 * i], out[2 * i + 1] = k & _M64, k >> 64
+    return out
+
+
+def unpack_keys(words: np.ndarray, kw: int) -> np.ndarray:
+    """Inverse of pack_keys: uint64 keys, or Python ints (object array) when kw == 2."""
+    if kw == 1:
+        return words
+    return np.array([int(words[2 * i]) | (int(words[2 * i + 1]) << 64)
+                     for i in range(len(words) // 2)], dtype=object)
+
+
 def _u64p(a):
     return a.ctypes.data_as(C.POINTER(C.c_uint64))
 
@@ -43,11 +65,14 @@ class GPUDVec:
         # an address of the vector's type (its key is irrelevant): makes addresses from keys
         self._proto = proto.with_key(0) if proto is not None else BoseFS.from_key(0, 0, 0)
         self.address_type = (type(self._proto), self._proto.N, self._proto.M)
+        # addresses wider than 64 bits (two BitString chunks) use two-word walker records
+        self.kw = 2 if self._proto.nbits > 64 else 1
         lib = _lib.load()
         self._ctx = _lib.default_context()
         h = C.c_void_p()
         vk = _lib.VAL_I64 if self.valtype is int else _lib.VAL_F64
-        _lib.check(lib.rimu_vec_create(self._ctx.handle, vk, max(capacity, len(pairs)), C.byref(h)))
+        _lib.check(lib.rimu_vec_create_kw(self._ctx.handle, vk, self.kw, max(capacity, len(pairs)),
+                                          C.byref(h)))
         self.handle = h
         if pairs:
             self.set_pairs(pairs)
@@ -57,10 +82,11 @@ class GPUDVec:
         return np.ascontiguousarray(vals, dtype=np.int64 if self.valtype is int else np.float64)
 
     def upload(self, keys, vals):
-        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        n = len(keys)
+        words = pack_keys(keys, self.kw)
         vals = self._np_vals(vals)
-        _lib.check(_lib.load().rimu_vec_upload(self.handle, _u64p(keys), vals.ctypes.data_as(C.c_void_p),
-                                                len(keys)))
+        _lib.check(_lib.load().rimu_vec_upload(self.handle, _u64p(words), vals.ctypes.data_as(C.c_void_p),
+                                                n))
 
     def set_pairs(self, pairs: dict):
         keys = [a.key for a in pairs]
@@ -73,12 +99,12 @@ class GPUDVec:
         n = C.c_int64()
         _lib.check(lib.rimu_vec_length(self.handle, C.byref(n)))
         cap = max(n.value, 1)
-        keys = np.zeros(cap, dtype=np.uint64)
+        words = np.zeros(cap * self.kw, dtype=np.uint64)
         vals = np.zeros(cap, dtype=np.int64 if self.valtype is int else np.float64)
         got = C.c_int64()
-        _lib.check(lib.rimu_vec_download(self.handle, _u64p(keys), vals.ctypes.data_as(C.c_void_p),
+        _lib.check(lib.rimu_vec_download(self.handle, _u64p(words), vals.ctypes.data_as(C.c_void_p),
                                           cap, C.byref(got)))
-        return keys[:got.value], vals[:got.value]
+        return unpack_keys(words[:got.value * self.kw], self.kw), vals[:got.value]
 
     def sorted_arrays(self):
         k, v = self.download()
@@ -108,17 +134,14 @@ class GPUDVec:
         return dict(self.pairs())
 
     def __getitem__(self, addr):
-        keys = np.array([addr.key], dtype=np.uint64)
-        out = np.zeros(1, dtype=np.int64 if self.valtype is int else np.float64)
-        _lib.check(_lib.load().rimu_vec_lookup(self.handle, _u64p(keys), 1,
-                                                out.ctypes.data_as(C.c_void_p)))
-        return self.valtype(out[0])
+        return self.valtype(self.lookup_keys([addr.key])[0])
 
     def lookup_keys(self, keys):
-        keys = np.ascontiguousarray(keys, dtype=np.uint64)
-        out = np.zeros(len(keys), dtype=np.int64 if self.valtype is int else np.float64)
-        if len(keys):
-            _lib.check(_lib.load().rimu_vec_lookup(self.handle, _u64p(keys), len(keys),
+        n = len(keys)
+        words = pack_keys(keys, self.kw)
+        out = np.zeros(n, dtype=np.int64 if self.valtype is int else np.float64)
+        if n:
+            _lib.check(_lib.load().rimu_vec_lookup(self.handle, _u64p(words), n,
                                                     out.ctypes.data_as(C.c_void_p)))
         return out
 
@@ -274,7 +297,7 @@ def apply_operator(wm: GPUWorkingMemory, target: GPUDVec, source: GPUDVec, op, b
     p.initiator = source.initiator.code
     p.initiator_threshold = source.initiator.threshold
     target.style, target.valtype, target.address_type = source.style, source.valtype, source.address_type
-    target._proto = source._proto
+    target._proto, target.kw = source._proto, source.kw
     target.initiator = source.initiator
     st = _lib.StepStats()
     _lib.check(_lib.load().rimu_apply_operator(ham.handle, wm.handle, target.handle, source.handle,

@@ -13,6 +13,7 @@ import math
 import numpy as np
 
 from . import _lib
+from .dvec import pack_keys, unpack_keys
 from .addresses import BoseFS, CompositeFS, FermiFS, is_fermi2c
 
 
@@ -109,40 +110,45 @@ class AbstractHamiltonian:
     def _addr(self, key):
         return self.address.with_key(key)
 
+    @property
+    def key_words(self) -> int:
+        """1 for addresses of at most 64 bits, 2 for two-chunk addresses (65-128 bits)."""
+        return 2 if self.address.nbits > 64 else 1
+
     def diagonal_element(self, address) -> float:
-        out = np.zeros(1)
-        keys = np.array([address.key], dtype=np.uint64)
-        _lib.check(_lib.load().rimu_model_diagonal(
-            self.handle, keys.ctypes.data_as(C.POINTER(C.c_uint64)), 1,
-            out.ctypes.data_as(C.POINTER(C.c_double))))
-        return float(out[0])
+        return float(self.diagonal_elements([address.key])[0])
 
     def diagonal_elements(self, keys) -> np.ndarray:
-        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        words = pack_keys(keys, self.key_words)
         out = np.zeros(len(keys))
         _lib.check(_lib.load().rimu_model_diagonal(
-            self.handle, keys.ctypes.data_as(C.POINTER(C.c_uint64)), len(keys),
+            self.handle, words.ctypes.data_as(C.POINTER(C.c_uint64)), len(keys),
             out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
     def num_offdiagonals(self, address) -> int:
         n = C.c_int()
-        _lib.check(_lib.load().rimu_model_num_offdiagonals(self.handle, C.c_uint64(address.key),
-                                                          C.byref(n)))
+        k2 = pack_keys([address.key], 2)
+        _lib.check(_lib.load().rimu_model_num_offdiagonals_w(
+            self.handle, k2.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(n)))
         return n.value
 
     def offdiagonal_keys(self, key: int):
-        """(keys, values) of all offdiagonals of column `key`, in the reference's order."""
+        """(keys, values) of all offdiagonals of column `key`, in the reference's order
+        (keys as Python ints for addresses wider than 64 bits)."""
         lib = _lib.load()
         n = C.c_int()
-        _lib.check(lib.rimu_model_num_offdiagonals(self.handle, C.c_uint64(key), C.byref(n)))
-        ks = np.zeros(max(n.value, 1), dtype=np.uint64)
+        k2 = pack_keys([key], 2)
+        kp = k2.ctypes.data_as(C.POINTER(C.c_uint64))
+        _lib.check(lib.rimu_model_num_offdiagonals_w(self.handle, kp, C.byref(n)))
+        kw = self.key_words
+        ks = np.zeros(max(n.value, 1) * kw, dtype=np.uint64)
         vs = np.zeros(max(n.value, 1))
         got = C.c_int()
-        _lib.check(lib.rimu_model_offdiagonals(
-            self.handle, C.c_uint64(key), ks.ctypes.data_as(C.POINTER(C.c_uint64)),
-            vs.ctypes.data_as(C.POINTER(C.c_double)), len(ks), C.byref(got)))
-        return ks[:got.value], vs[:got.value]
+        _lib.check(lib.rimu_model_offdiagonals_w(
+            self.handle, kp, ks.ctypes.data_as(C.POINTER(C.c_uint64)),
+            vs.ctypes.data_as(C.POINTER(C.c_double)), max(n.value, 1), C.byref(got)))
+        return unpack_keys(ks[:got.value * kw], kw), vs[:got.value]
 
     def offdiagonals(self, address):
         """offdiagonals(H, address): list of (address, matrix element)."""

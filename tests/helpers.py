@@ -77,7 +77,8 @@ def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=Non
     """`steps` steps from `start` on the GPU and in the oracle, compared after every step;
     with `target`, DoubleLogUpdate on the (identical) norm."""
     m = oracle_model(h)
-    keys = np.array([a.key for a in start], dtype=np.uint64)
+    wide = h.address.nbits > 64     # two-chunk addresses travel as Python ints
+    keys = np.array([a.key for a in start], dtype=object if wide else np.uint64)
     vals = np.array(list(start.values()), dtype=np.int64 if style.valtype is int else np.float64)
     S = h.diagonal_element(next(iter(start))) if shift is None else shift
     pnorm = float(np.abs(vals).sum())

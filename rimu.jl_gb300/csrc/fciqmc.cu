@@ -187,8 +187,8 @@ __device__ __forceinline__ double op_diagonal(const StepArgs &a, int r, K key) {
 template <class K>
 __device__ __forceinline__ double op_offdiag(const StepArgs &a, const OffdiagT<K> &od) {
   const double *tab = a.op == OP_TRANSITION ? a.h.aoff : a.h.hoff;
-  double v = tab[od.prod];
-  return od.sign < 0 ? -v : v;
+  // the sign by flipping the sign bit (an integer operation; the same value as -v)
+  return bitsd(dbits(tab[od.prod]) ^ ((uint64_t)(od.sign < 0) << 63));
 }
 
 // ------------------------------------------------------------------------------------------
@@ -344,6 +344,11 @@ __device__ __forceinline__ int parent_unsafe(const StepArgs &a, uint64_t vb) {
 __device__ __forceinline__ double dint_of(const DevModel &h, int n) {
   return n < h.recip_len ? h.dint[n] : (double)n;
 }
+// 1/n from the host table (the division only beyond it)
+__device__ __forceinline__ double recip_of(const DevModel &h, uint64_t n) {
+  if (n < (uint64_t)h.recip_len) return h.recip[n];
+  return 1.0 / (double)n;
+}
 
 // Work of one column: units (offdiagonals if exact, attempts otherwise) and the spawn
 // coefficient c, without FP64 compares (DynamicSemistochastic, spawning.jl:364-378;
@@ -361,15 +366,28 @@ __device__ __forceinline__ uint64_t column_work(const StepArgs &a, K key, uint64
     acc.exact_n++;
   } else if (STYLE == STYLE_DSS) {
     const double val = bitsd(vb);
-    const double amount = a.boost_one ? abs_d(val) : a.boost * abs_d(val) * a.rel_threshold;
-    if (!a.has_abs_thr || a.abs_threshold >= (double)noff) exact = floor_abs(amount) >= (int64_t)noff;
-    else exact = amount >= a.abs_threshold;
-    if (exact) acc.exact_n++; else acc.inexact_n++;
-    if (!exact) {
-      natt = (uint64_t)floor_abs(a.boost_one ? val : abs_d(val) * a.boost);
-      if (natt < 1) natt = 1;
-      const double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
-      c = (natt == 1 ? val : val * rc) * dint_of(a.h, noff);
+    if (a.boost_one && !a.has_abs_thr) {
+      // boost 1, rel_threshold 1, no absolute threshold: the amount is |val| and the column is
+      // exact when floor(|val|) >= noff; only the spawn coefficient takes FP64 multiplies
+      const int64_t fl = floor_abs(val);
+      exact = fl >= (int64_t)noff;
+      if (exact) acc.exact_n++; else acc.inexact_n++;
+      if (!exact) {
+        natt = fl < 1 ? 1 : (uint64_t)fl;
+        double t = val;
+        if (natt != 1) t = val * recip_of(a.h, natt);
+        c = t * dint_of(a.h, noff);
+      }
+    } else {
+      const double amount = a.boost_one ? abs_d(val) : a.boost * abs_d(val) * a.rel_threshold;
+      if (!a.has_abs_thr || a.abs_threshold >= (double)noff) exact = floor_abs(amount) >= (int64_t)noff;
+      else exact = amount >= a.abs_threshold;
+      if (exact) acc.exact_n++; else acc.inexact_n++;
+      if (!exact) {
+        natt = (uint64_t)floor_abs(a.boost_one ? val : abs_d(val) * a.boost);
+        if (natt < 1) natt = 1;
+        c = (natt == 1 ? val : val * recip_of(a.h, natt)) * dint_of(a.h, noff);
+      }
     }
   } else {  // IsStochasticInteger
     const int64_t iv = (int64_t)vb;
@@ -381,8 +399,7 @@ __device__ __forceinline__ uint64_t column_work(const StepArgs &a, K key, uint64
     } else {
       natt = (uint64_t)floor_abs(i2d_exact(iv) * a.boost);
       if (natt < 1) natt = 1;
-      const double rc = natt < (uint64_t)a.h.recip_len ? a.h.recip[natt] : 1.0 / (double)natt;
-      c = (i2d_exact(iv) * rc) * dint_of(a.h, noff);
+      c = (i2d_exact(iv) * recip_of(a.h, natt)) * dint_of(a.h, noff);
     }
   }
   return noff == 0 ? 0 : (exact ? (uint64_t)noff : natt);

@@ -77,6 +77,14 @@ int rimu_ctx_create(int device, void *stream, rimu_ctx **out) {
   // example a torch tensor initialised on it) is ordered with the library's kernels.
   c->stream = (cudaStream_t)stream;
   c->own_stream = false;
+  // Keep freed stream-ordered allocations in the device's pool instead of returning them to
+  // the system at every synchronization: steps, uploads and downloads reallocate buffers of
+  // gigabytes, and mapping them again costs milliseconds each time.  rimu_ctx_destroy trims it.
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   *out = c;
   return RIMU_OK;
 }
@@ -84,6 +92,8 @@ int rimu_ctx_create(int device, void *stream, rimu_ctx **out) {
 int rimu_ctx_destroy(rimu_ctx *ctx) {
   if (!ctx) return RIMU_OK;
   cudaStreamSynchronize(ctx->stream);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return RIMU_OK;
@@ -415,6 +425,10 @@ static int vec_alloc(rimu_vec *v, int nb_bits, uint32_t capv) {
   return RIMU_OK;
 }
 
+// Walkers per bucket when a list is sized from its length alone (upload, creation): a step
+// with about as many spawns as walkers then sees about 1024 contributions per bucket.
+static constexpr int64_t kWalkersPerBucket = 512;
+
 static uint32_t capv_for(int64_t n, int nb_bits) {
   double mu = (double)n / (double)(1ull << nb_bits);
   uint64_t c = (uint64_t)(1.25 * mu + 8.0 * std::sqrt(mu) + 64.0);
@@ -430,7 +444,7 @@ extern "C" int rimu_vec_create_kw(rimu_ctx *ctx, int val_kind, int key_words,
   v->ctx = ctx;
   v->val_kind = val_kind;
   v->kw = key_words;
-  int nb_bits = ceil_log2(std::max<int64_t>(1, capacity_hint / 256));
+  int nb_bits = ceil_log2(std::max<int64_t>(1, capacity_hint / kWalkersPerBucket));
   int rc = vec_alloc(v, nb_bits, capv_for(capacity_hint, nb_bits));
   if (rc) { delete v; return rc; }
   *out = v;
@@ -466,7 +480,7 @@ extern "C" int rimu_vec_empty(rimu_vec *v) {
 extern "C" int rimu_vec_upload(rimu_vec *v, const uint64_t *keys, const void *vals, int64_t n) {
   if (!v || (n > 0 && (!keys || !vals))) return bad("rimu_vec_upload: NULL argument");
   rimu_ctx *ctx = v->ctx;
-  int nb_bits = std::max(v->nb_bits, ceil_log2(std::max<int64_t>(1, n / 256)));
+  int nb_bits = std::max(v->nb_bits, ceil_log2(std::max<int64_t>(1, n / kWalkersPerBucket)));
   uint32_t capv = std::max(v->capv, capv_for(n, nb_bits));
   uint64_t *dk = nullptr, *dv = nullptr;
   unsigned int *flag = nullptr;
@@ -782,10 +796,14 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   int64_t S_est;
   if (w->last_spawns >= 0) S_est = (int64_t)(1.3 * (double)w->last_spawns) + 256;
   else if (p->style == RIMU_STYLE_DETERMINISTIC) S_est = L * (int64_t)m->max_offdiag + 256;
-  else S_est = (int64_t)(norm * p->boost) + L * 4 + 256;
+  // about one spawn per attempt, and max(floor(|v| boost), 1) attempts per walker; an
+  // underestimate only costs a re-run of this first step with larger slabs
+  else S_est = std::max<int64_t>((int64_t)(norm * p->boost), L) + 256;
   const double kKeys = (double)w->keys_per_bucket;
   int need_bits = ceil_log2((uint64_t)((double)(L + S_est) / kKeys) + 1);
-  int nb_bits = std::max(source->nb_bits, need_bits);
+  // A source with more than twice the buckets the step needs (a list uploaded or grown for a
+  // larger load) is re-bucketed once to need_bits; otherwise buckets only grow.
+  int nb_bits = source->nb_bits > need_bits + 1 ? need_bits : std::max(source->nb_bits, need_bits);
   uint32_t caps = 0, capv = 0;
   uint32_t heavy_cap = 0;
   int retries = 0;

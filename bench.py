@@ -37,8 +37,8 @@ WORKLOAD = "HubbardReal1D M=N=20 u=4 t=1, IsDynamicSemistochastic(threshold=1), 
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one k_spawn plus one
 # k_annihilate launch per algorithmic byte (16-byte records read and written), measured at an
-# equilibrated norm of 3e7: (409.9 + 422.7 + 838.1 + 354.9) MB / (830 + 1211) MB.
-TRAFFIC_PER_ALGORITHMIC_BYTE = (409.9 + 422.7 + 838.1 + 354.9) / (830.0 + 1211.0)
+# equilibrated norm of 3e7: (409.8 + 421.6 + 838.1 + 355.5) MB / (830 + 1211) MB.
+TRAFFIC_PER_ALGORITHMIC_BYTE = (409.8 + 421.6 + 838.1 + 355.5) / (830.0 + 1211.0)
 
 
 def peaks():

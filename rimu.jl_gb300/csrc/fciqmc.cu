@@ -3,7 +3,8 @@
 // Layout in HBM.  A walker list is 2^nb_bits buckets per replica; bucket b holds the walkers
 // whose address hashes (top nb_bits of mix64) to b, as 16-byte (address, amplitude) records
 // in a fixed-capacity slab [b * capv, b * capv + count[b]).  The spawn buffer uses the same
-// buckets with slabs of capacity caps.
+// buckets with slabs of capacity caps.  Every kernel is a template on the address type: one
+// 64-bit word, or a Key128 (two words, 32-byte records) for addresses of 65-128 bits.
 //
 // One step (apply_operator!, src/Interfaces/dictvectors.jl:112-140):
 //   k_spawn      each warp lays the walkers of 32 consecutive buckets out as one list,
@@ -551,7 +552,7 @@ __global__ void __launch_bounds__(256) k_spawn_heavy(StepArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Annihilation: one warp per bucket, exact fixed-point sums in a shared-memory table
+// Annihilation: one CTA per bucket, exact sums from per-address lists in a shared-memory table
 // ------------------------------------------------------------------------------------------
 // Summation rule (the oracle states the same): when every contribution to an address is a
 // multiple of 2^-64 below 2^48 in magnitude, the address gets the exact sum rounded once to

@@ -38,6 +38,17 @@ __device__ __forceinline__ uint64_t unrank(uint64_t r, int B, int w, const uint6
   return key;
 }
 
+// The next larger word with the same number of set bits (Gosper's hack): row r + 1 of the
+// basis from row r, since the basis is in increasing numeric order.
+__device__ __forceinline__ uint64_t next_combination(uint64_t x) {
+  const uint64_t c = x & (~x + 1);           // lowest set bit
+  const uint64_t r = x + c;
+  return r | (((x ^ r) >> 2) >> ctz64(x));
+}
+
+// Rows per thread: a thread unranks the first row of its run and steps to the next ones.
+constexpr int HV_ROWS = 4;
+
 __device__ __forceinline__ uint64_t rank_of(uint64_t key, int w, const uint64_t *tab) {
   uint64_t r = 0;
   int i = 1;
@@ -207,17 +218,22 @@ __global__ void __launch_bounds__(HB) k_hv(DevModel h, const uint64_t *binom, in
   extern __shared__ uint64_t s_tab[];
   load_binom(s_tab, binom, ntab);
   const int B = h.nbits, wt = h.N;
-  for (int64_t row = blockIdx.x * (int64_t)HB + threadIdx.x; row < dim;
-       row += (int64_t)gridDim.x * HB) {
-    uint64_t key = unrank((uint64_t)row, B, wt, s_tab);
-    double acc;
-    if (KIND == MODEL_REAL1D) {
-      double k;
-      real1d_row<false>(h, s_tab, (uint64_t)row, dim, key, v, nullptr, dtabH, nullptr, acc, k);
-    } else {
-      acc = generic_row<KIND>(h, s_tab, (uint64_t)row, dim, key, v, hv_diag<KIND>(h, key));
+  for (int64_t row0 = (blockIdx.x * (int64_t)HB + threadIdx.x) * HV_ROWS; row0 < dim;
+       row0 += (int64_t)gridDim.x * HB * HV_ROWS) {
+    uint64_t key = unrank((uint64_t)row0, B, wt, s_tab);
+    for (int k = 0; k < HV_ROWS; ++k) {
+      const int64_t row = row0 + k;
+      if (row >= dim) break;
+      if (k) key = next_combination(key);
+      double acc;
+      if (KIND == MODEL_REAL1D) {
+        double kk;
+        real1d_row<false>(h, s_tab, (uint64_t)row, dim, key, v, nullptr, dtabH, nullptr, acc, kk);
+      } else {
+        acc = generic_row<KIND>(h, s_tab, (uint64_t)row, dim, key, v, hv_diag<KIND>(h, key));
+      }
+      w[row] = acc;
     }
-    w[row] = acc;
   }
 }
 
@@ -237,9 +253,13 @@ __global__ void __launch_bounds__(HB) k_hv_adjoint(DevModel h, const uint64_t *b
   load_binom(s_tab, binom, ntab);
   const int B = h.nbits, wt = h.N;
   double su = 0.0, st = 0.0;
-  for (int64_t row = blockIdx.x * (int64_t)HB + threadIdx.x; row < dim;
-       row += (int64_t)gridDim.x * HB) {
-    uint64_t key = unrank((uint64_t)row, B, wt, s_tab);
+  for (int64_t row0 = (blockIdx.x * (int64_t)HB + threadIdx.x) * HV_ROWS; row0 < dim;
+       row0 += (int64_t)gridDim.x * HB * HV_ROWS) {
+  uint64_t key = unrank((uint64_t)row0, B, wt, s_tab);
+  for (int kr = 0; kr < HV_ROWS; ++kr) {
+    const int64_t row = row0 + kr;
+    if (row >= dim) break;
+    if (kr) key = next_combination(key);
     double acc, kv;
     if (KIND == MODEL_REAL1D) {
       real1d_row<true>(h, s_tab, (uint64_t)row, dim, key, gw, v, dtabH, dhdt, acc, kv);
@@ -261,6 +281,7 @@ __global__ void __launch_bounds__(HB) k_hv_adjoint(DevModel h, const uint64_t *b
     const double g = gw[row];
     su += g * ((double)bose_interaction_hv(key) / 2 * v[row]);
     st += g * kv;
+  }
   }
   for (int o = 16; o > 0; o >>= 1) {
     su += __shfl_down_sync(0xffffffffu, su, o);
@@ -297,7 +318,7 @@ __global__ void k_reduce_partials(const double *partial, int nblocks, double *ou
 using namespace rimu;
 
 int rimu_hv_grid(rimu_ctx *ctx, int64_t dim) {
-  int64_t want = (dim + HB - 1) / HB;
+  int64_t want = (dim + (int64_t)HB * HV_ROWS - 1) / ((int64_t)HB * HV_ROWS);
   int64_t cap = (int64_t)ctx->num_sms * 8;
   return (int)(want < cap ? (want < 1 ? 1 : want) : cap);
 }
@@ -476,7 +497,7 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
   h.hoff = s->hoff;
   h.aoff = s->hoff;
   h.aoff_len = nprod;
-  int64_t want = (dim + HB - 1) / HB;
+  int64_t want = (dim + (int64_t)HB * HV_ROWS - 1) / ((int64_t)HB * HV_ROWS);
   int64_t cap = (int64_t)g_noalloc_sms[dev] * 8;
   if (cap > NOALLOC_MAX_BLOCKS) cap = NOALLOC_MAX_BLOCKS;
   int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);

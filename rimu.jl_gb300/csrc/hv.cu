@@ -106,7 +106,8 @@ __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *ta
         int q = bit + n - 1;
         int next = ctz64(~shr64(key, bit + n + 1));
         prod = n * (next + 1);
-        int idx = popc64(key & lowmask(q + 1));
+        // ones in bits [0, q]: the bosons of modes 1..mode (bit - (mode - 1) before this one)
+        int idx = bit - mode + 1 + n;
         j = row + C(tab, w, q, idx - 1);
       }
       if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }
@@ -126,7 +127,7 @@ __device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *ta
       } else {
         int po = (prev_mode == mode - 1) ? prev_occ : 0;
         prod = n * (po + 1);
-        int idx = popc64(key & lowmask(bit + 1));
+        int idx = bit - mode + 2;                // ones in bits [0, bit]
         j = row - C(tab, w, bit - 1, idx - 1);
       }
       if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }

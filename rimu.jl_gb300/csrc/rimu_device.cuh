@@ -510,11 +510,26 @@ RIMU_HD int bose_interaction_fast(K x) {
   return 2 * acc;
 }
 
-// Position of the k-th (0-based) set bit.
-template <class K>
-RIMU_HD int select_bit(K x, int k) {
-  for (int i = 0; i < k; ++i) x = kclear_lowest(x);
-  return kctz(x);
+// Position of the k-th (0-based) set bit (k < number of set bits): a binary search on
+// popcounts of halves, constant time and without divergent loops.
+RIMU_HD int select_bit(uint64_t x, int k) {
+  int pos = 0;
+  int c = popc64(x & 0xffffffffull);
+  if (k >= c) { k -= c; x >>= 32; pos = 32; }
+  uint32_t y = (uint32_t)x;
+  c = popc64(y & 0xffffu);
+  if (k >= c) { k -= c; y >>= 16; pos += 16; }
+  c = popc64(y & 0xffu);
+  if (k >= c) { k -= c; y >>= 8; pos += 8; }
+  c = popc64(y & 0xfu);
+  if (k >= c) { k -= c; y >>= 4; pos += 4; }
+  c = popc64(y & 0x3u);
+  if (k >= c) { k -= c; y >>= 2; pos += 2; }
+  return pos + (k >= (int)(y & 1u) ? 1 : 0);
+}
+RIMU_HD int select_bit(Key128 x, int k) {
+  const int c = popc64(x.lo);
+  return k < c ? select_bit(x.lo, k) : 64 + select_bit(x.hi, k - c);
 }
 
 // HubbardReal1D offdiagonal with word operations only: the site-th occupied mode starts at

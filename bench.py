@@ -442,7 +442,9 @@ def bench_hv(R, torch, peak):
     h = R.HubbardReal1D(R.BoseFS([1] * 14), u=4.0, t=1.0)
     op = R.BasisOperator(h)
     D = op.dim
-    nnz_off = 2 * 14 * 9657700          # 2 M C(26,13): offdiagonal nonzeros of HubbardReal1D(14,14)
+    # offdiagonal nonzeros of HubbardReal1D(14,14): two hops per occupied site, and
+    # C(N+M-2, N-1) = C(26,13) basis states have a given site occupied: 2 M C(26,13)
+    nnz_off = 2 * 14 * math.comb(26, 13)
     nnz = D + nnz_off
     g = torch.Generator(device="cuda").manual_seed(3)
     v = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)

@@ -929,18 +929,23 @@ int64_t o_hv_basis(const o_model *h, const uint64_t *keys, int64_t D, const doub
 }
 
 /* Adjoint of w = H(u, t) v for HubbardReal1D / one-component bosonic HubbardRealSpace
- * without trap: gv = H^T gw, gu = <gw, dH/du v>, gt = <gw, dH/dt v>. */
+ * without trap.  H = D(u) + t K with the hopping part K_ij = -sqrt(prod_ij) symmetric, so
+ *   gv = H^T gw = D gw + t (K gw),
+ *   gu = <gw, dH/du v> = sum_i gw_i (I_i / 2) v_i      (I_i = sum_k n_k (n_k - 1)),
+ *   gt = <gw, dH/dt v> = <gw, K v> = <v, K gw>,
+ * and one pass over the rows with one gather of gw per nonzero gives all three: the hop sum
+ * k_i = (K gw)_i of row i in offdiagonal order (fused multiply-adds from 0), then
+ * gv_i = fma(t, k_i, d_i gw_i), gu += gw_i ((I_i / 2) v_i) and gt += v_i k_i (fused). */
 int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, const double *v,
                            const double *gw, double *gv, double *gu, double *gt) {
-  int64_t missing = o_hv_basis(h, keys, D, gw, gv);
+  int64_t missing = 0;
   double su = 0.0, st = 0.0;
   for (int64_t i = 0; i < D; ++i) {
     int onr[2 * O_MAXM];
     o_to_onr(h, keys[i], onr);
     long bhi = 0;
     for (int k = 0; k < h->M; ++k) bhi += (long)onr[k] * (onr[k] - 1);
-    su += gw[i] * ((double)bhi / 2 * v[i]);
-    double kv = 0.0;
+    double kg = 0.0;
     int noff = o_num_offdiagonals(h, keys[i]);
     for (int c = 1; c <= noff; ++c) {
       uint64_t nk; double hv; long prod;
@@ -948,9 +953,11 @@ int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, co
       if (hv == 0.0) continue;
       int64_t j = o_bsearch(keys, D, nk);
       if (j < 0) { ++missing; continue; }
-      kv = fma(-sqrt((double)prod), v[j], kv);   /* dH_{ji}/dt = -sqrt(prod) */
+      kg = fma(-sqrt((double)prod), gw[j], kg);   /* K_ij = dH_ij/dt = -sqrt(prod) */
     }
-    st += gw[i] * kv;
+    gv[i] = fma(h->t, kg, o_diagonal(h, keys[i]) * gw[i]);
+    su = fma(gw[i], (double)bhi / 2 * v[i], su);
+    st = fma(v[i], kg, st);
   }
   *gu = su;
   *gt = st;

@@ -19,41 +19,62 @@ namespace rimu {
 constexpr int HB = 256;
 constexpr int MAXB = 64;
 
-struct Binom {
-  const uint64_t *c;   // c[p * (w + 1) + i] = C(p, i), p in [0, B], i in [0, w]
-  int w;
+// Word operations of the H*v kernels on a W-bit address word.  Addresses of at most 32 bits
+// (the full-basis workloads: HubbardReal1D M = N = 14 has 27) run on 32-bit words and 32-bit
+// ranks, where a shift or a bit count is one instruction instead of two; wider addresses
+// run on 64-bit words.  Both give the same ranks, products and therefore the same sums.
+template <class W> struct HW;
+template <> struct HW<uint32_t> {
+  static constexpr int BITS = 32;
+  __device__ static __forceinline__ int ctz(uint32_t x) { return x ? __ffs((int)x) - 1 : 32; }
+  __device__ static __forceinline__ int popc(uint32_t x) { return __popc(x); }
+  __device__ static __forceinline__ uint32_t shr(uint32_t x, int s) { return s >= 32 ? 0u : x >> s; }
+  __device__ static __forceinline__ uint32_t low(int n) { return n >= 32 ? ~0u : ((1u << n) - 1u); }
+};
+template <> struct HW<uint64_t> {
+  static constexpr int BITS = 64;
+  __device__ static __forceinline__ int ctz(uint64_t x) { return ctz64(x); }
+  __device__ static __forceinline__ int popc(uint64_t x) { return __popcll(x); }
+  __device__ static __forceinline__ uint64_t shr(uint64_t x, int s) { return shr64(x, s); }
+  __device__ static __forceinline__ uint64_t low(int n) { return lowmask(n); }
 };
 
-__device__ __forceinline__ uint64_t C(const uint64_t *tab, int w, int p, int i) {
+// Binomial table c[p * (w + 1) + i] = C(p, i), p in [0, B], i in [0, w], staged in shared
+// memory as W words (every C(p, i) with p <= 32 fits 32 bits).
+template <class W>
+__device__ __forceinline__ W C(const W *tab, int w, int p, int i) {
   return tab[p * (w + 1) + i];
 }
 
-__device__ __forceinline__ uint64_t unrank(uint64_t r, int B, int w, const uint64_t *tab) {
-  uint64_t key = 0;
+template <class W>
+__device__ __forceinline__ W unrank(uint64_t r64, int B, int w, const W *tab) {
+  W r = (W)r64, key = 0;
   int i = w;
   for (int p = B - 1; p >= 0 && i > 0; --p) {
-    uint64_t c = C(tab, w, p, i);
-    if (c <= r) { key |= 1ull << p; r -= c; --i; }
+    const W c = C(tab, w, p, i);
+    if (c <= r) { key |= (W)1 << p; r -= c; --i; }
   }
   return key;
 }
 
 // The next larger word with the same number of set bits (Gosper's hack): row r + 1 of the
 // basis from row r, since the basis is in increasing numeric order.
-__device__ __forceinline__ uint64_t next_combination(uint64_t x) {
-  const uint64_t c = x & (~x + 1);           // lowest set bit
-  const uint64_t r = x + c;
-  return r | (((x ^ r) >> 2) >> ctz64(x));
+template <class W>
+__device__ __forceinline__ W next_combination(W x) {
+  const W c = x & (~x + 1);           // lowest set bit
+  const W r = x + c;
+  return r | (((x ^ r) >> 2) >> HW<W>::ctz(x));
 }
 
 // Rows per thread: a thread unranks the first row of its run and steps to the next ones.
 constexpr int HV_ROWS = 4;
 
-__device__ __forceinline__ uint64_t rank_of(uint64_t key, int w, const uint64_t *tab) {
-  uint64_t r = 0;
+template <class W>
+__device__ __forceinline__ W rank_of(W key, int w, const W *tab) {
+  W r = 0;
   int i = 1;
   while (key) {
-    int p = ctz64(key);
+    const int p = HW<W>::ctz(key);
     r += C(tab, w, p, i);
     ++i;
     key &= key - 1;
@@ -61,82 +82,78 @@ __device__ __forceinline__ uint64_t rank_of(uint64_t key, int w, const uint64_t 
   return r;
 }
 
-__device__ __forceinline__ int bose_interaction_hv(uint64_t key) {
-  uint64_t x = key;
+// sum_i n_i (n_i - 1) of a BoseFS word (bose_hubbard_interaction, bosefs.jl:415-428): a run
+// of n ones holds n - d windows of d + 1 ones, so sum_{d >= 1} popcount(windows of d + 1
+// ones) = sum_i n_i (n_i - 1) / 2.
+template <class W>
+__device__ __forceinline__ int bose_interaction_hv(W key) {
   int acc = 0;
-  while (x) {
-    x = shr64(x, ctz64(x));
-    int n = ctz64(~x);
-    acc += n * (n - 1);
-    x = shr64(x, n);
-  }
-  return acc;
+  W y = key & (key >> 1);
+  while (y) { acc += HW<W>::popc(y); y &= y >> 1; }
+  return 2 * acc;
 }
 
-// One HubbardReal1D row: w = d v + sum fma(H, v_j), optionally also k = sum fma(-sqrt p, x_j)
-// for the hopping derivative (second vector x).
+// One HubbardReal1D row in the reference's offdiagonal order: acc = fma(coef[p_j], v_j, acc)
+// from the given start, with coef = H's hopping elements -t sqrt(p) and start d v_row for
+// H v, or coef = -sqrt(p) and start 0 for the hopping part alone (the adjoint).
 // A rank outside the basis can only come from an inconsistent address; the gather is
 // skipped and the row marked NaN so that callers see it.
 #define RIMU_GATHER_GUARD(j) if ((j) >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); continue; }
 
-template <bool ADJ>
-__device__ __forceinline__ void real1d_row(const DevModel &h, const uint64_t *tab, uint64_t row,
-                                           int64_t dim,
-                                           uint64_t key, const double *__restrict__ v,
-                                           const double *__restrict__ x, const double *dtabH,
-                                           const double *dhdt, double &acc, double &kacc) {
+template <class W>
+__device__ __forceinline__ double real1d_row(const DevModel &h, const W *tab, W row, W dim, W key,
+                                             const double *coef, const double *__restrict__ v,
+                                             double acc) {
+  using O = HW<W>;
   const int B = h.nbits, M = h.M, w = h.N;
-  acc = dtabH[bose_interaction_hv(key)] * v[row];
-  kacc = 0.0;
-  uint64_t y = key;
+  W y = key;
   int mode = 1, bit = 0, prev_mode = 0, prev_occ = 0;
   while (y) {
-    int z = ctz64(y);
-    y = shr64(y, z); mode += z; bit += z;
-    const int n = ctz64(~y);
+    const int z = O::ctz(y);          // < BITS: y is not zero
+    y >>= z; mode += z; bit += z;
+    const int n = O::ctz(~y);         // run length, below BITS (M >= 2 leaves a zero)
     // right hop (odd chosen)
     {
-      uint64_t j;
+      W j;
       int prod;
       if (mode == M) {
-        uint64_t nk = ((key << 1) | 1ull) & lowmask(B);
-        prod = n * (ctz64(~key) + 1);
+        const W nk = ((key << 1) | (W)1) & O::low(B);
+        prod = n * (O::ctz(~key) + 1);
         j = rank_of(nk, w, tab);
       } else {
-        int q = bit + n - 1;
-        int next = ctz64(~shr64(key, bit + n + 1));
+        const int q = bit + n - 1;
+        const int next = O::ctz(~O::shr(key, bit + n + 1));
         prod = n * (next + 1);
         // ones in bits [0, q]: the bosons of modes 1..mode (bit - (mode - 1) before this one)
-        int idx = bit - mode + 1 + n;
+        const int idx = bit - mode + 1 + n;
         j = row + C(tab, w, q, idx - 1);
       }
-      if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }
-      acc = fma(h.hoff[prod], v[j], acc);
-      if (ADJ) kacc = fma(dhdt[prod], x[j], kacc);
+      if (j >= dim) return __longlong_as_double(0x7ff8000000000000ll);
+      acc = fma(coef[prod], v[j], acc);
     }
     // left hop (even chosen)
     {
-      uint64_t j;
+      W j;
       int prod;
       if (mode == 1) {
-        uint64_t nk = (key >> 1) | (1ull << (B - 1));
-        int lead = 0;
+        const W nk = (key >> 1) | ((W)1 << (B - 1));
+        int lead = 0;                             // ones at the top of the B-bit word nk
         for (int b = B - 1; b >= 0 && ((nk >> b) & 1); --b) ++lead;
-        prod = ctz64(~key) * lead;
+        prod = O::ctz(~key) * lead;
         j = rank_of(nk, w, tab);
       } else {
-        int po = (prev_mode == mode - 1) ? prev_occ : 0;
+        const int po = (prev_mode == mode - 1) ? prev_occ : 0;
         prod = n * (po + 1);
-        int idx = bit - mode + 2;                // ones in bits [0, bit]
+        const int idx = bit - mode + 2;          // ones in bits [0, bit]
         j = row - C(tab, w, bit - 1, idx - 1);
       }
-      if (j >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); break; }
-      acc = fma(h.hoff[prod], v[j], acc);
-      if (ADJ) kacc = fma(dhdt[prod], x[j], kacc);
+      if (j >= dim) return __longlong_as_double(0x7ff8000000000000ll);
+      acc = fma(coef[prod], v[j], acc);
     }
     prev_mode = mode; prev_occ = n;
-    y = shr64(y, n); bit += n;
+    y >>= n; bit += n;
   }
+  return acc;
 }
 
 template <int KIND>
@@ -207,29 +224,33 @@ __device__ double hv_diag(const DevModel &h, uint64_t key) {
   return in + pe;
 }
 
-__device__ __forceinline__ void load_binom(uint64_t *s_tab, const uint64_t *g_tab, int n) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s_tab[i] = g_tab[i];
+// Binomial table into shared memory as W words.
+template <class W>
+__device__ __forceinline__ void load_binom(W *s_tab, const uint64_t *g_tab, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s_tab[i] = (W)g_tab[i];
   __syncthreads();
 }
 
-template <int KIND>
+template <int KIND, class W>
 __global__ void __launch_bounds__(HB) k_hv(DevModel h, const uint64_t *binom, int ntab,
                                            const double *__restrict__ v, double *__restrict__ w,
                                            int64_t dim, const double *dtabH) {
-  extern __shared__ uint64_t s_tab[];
+  static_assert(KIND == MODEL_REAL1D || sizeof(W) == 8, "32-bit words: HubbardReal1D only");
+  extern __shared__ __align__(16) unsigned char hv_smem[];
+  W *s_tab = reinterpret_cast<W *>(hv_smem);
   load_binom(s_tab, binom, ntab);
   const int B = h.nbits, wt = h.N;
   for (int64_t row0 = (blockIdx.x * (int64_t)HB + threadIdx.x) * HV_ROWS; row0 < dim;
        row0 += (int64_t)gridDim.x * HB * HV_ROWS) {
-    uint64_t key = unrank((uint64_t)row0, B, wt, s_tab);
+    W key = unrank<W>((uint64_t)row0, B, wt, s_tab);
     for (int k = 0; k < HV_ROWS; ++k) {
       const int64_t row = row0 + k;
       if (row >= dim) break;
       if (k) key = next_combination(key);
       double acc;
-      if (KIND == MODEL_REAL1D) {
-        double kk;
-        real1d_row<false>(h, s_tab, (uint64_t)row, dim, key, v, nullptr, dtabH, nullptr, acc, kk);
+      if constexpr (KIND == MODEL_REAL1D) {
+        acc = real1d_row<W>(h, s_tab, (W)row, (W)dim, key, h.hoff, v,
+                            dtabH[bose_interaction_hv(key)] * v[row]);
       } else {
         acc = generic_row<KIND>(h, s_tab, (uint64_t)row, dim, key, v, hv_diag<KIND>(h, key));
       }
@@ -238,51 +259,55 @@ __global__ void __launch_bounds__(HB) k_hv(DevModel h, const uint64_t *binom, in
   }
 }
 
-// Adjoint: gv = H gw (H symmetric), and per-block partial sums of
-//   gu = sum_r gw_r * ((I_r / 2) * v_r)       (dH/du = sum_i n_i (n_i - 1) / 2)
-//   gt = sum_r gw_r * (sum_j (-sqrt p_rj) v_j) (dH/dt = hopping part / t)
-// written to partial[2 * blockIdx.x + {0, 1}].
-template <int KIND>
+// Adjoint of w = H(u, t) v with H = D(u) + t K, K the hopping part (K_ij = -sqrt p_ij,
+// symmetric): per row the hop sum k_r = (K gw)_r, one gather of gw per nonzero, gives
+//   gv_r = (H gw)_r = fma(t, k_r, d_r gw_r)
+// and the per-block partial sums, written to partial[2 * blockIdx.x + {0, 1}], of
+//   gu = sum_r gw_r ((I_r / 2) v_r)   (dH/du = sum_i n_i (n_i - 1) / 2)
+//   gt = sum_r v_r k_r                (<gw, K v> = <v, K gw>; dH/dt = K).
+template <int KIND, class W>
 __global__ void __launch_bounds__(HB) k_hv_adjoint(DevModel h, const uint64_t *binom, int ntab,
                                                    const double *__restrict__ v,
                                                    const double *__restrict__ gw,
                                                    double *__restrict__ gv, int64_t dim,
                                                    const double *dtabH, const double *dhdt,
                                                    double *partial) {
-  extern __shared__ uint64_t s_tab[];
+  static_assert(KIND == MODEL_REAL1D || sizeof(W) == 8, "32-bit words: HubbardReal1D only");
+  extern __shared__ __align__(16) unsigned char hv_smem[];
+  W *s_tab = reinterpret_cast<W *>(hv_smem);
   __shared__ double s_red[2][HB / 32];
   load_binom(s_tab, binom, ntab);
   const int B = h.nbits, wt = h.N;
   double su = 0.0, st = 0.0;
   for (int64_t row0 = (blockIdx.x * (int64_t)HB + threadIdx.x) * HV_ROWS; row0 < dim;
        row0 += (int64_t)gridDim.x * HB * HV_ROWS) {
-  uint64_t key = unrank((uint64_t)row0, B, wt, s_tab);
-  for (int kr = 0; kr < HV_ROWS; ++kr) {
-    const int64_t row = row0 + kr;
-    if (row >= dim) break;
-    if (kr) key = next_combination(key);
-    double acc, kv;
-    if (KIND == MODEL_REAL1D) {
-      real1d_row<true>(h, s_tab, (uint64_t)row, dim, key, gw, v, dtabH, dhdt, acc, kv);
-    } else {
-      // bosonic one-component HubbardRealSpace without trap
-      acc = dtabH[bose_interaction_hv(key)] * gw[row];
-      kv = 0.0;
-      int noff = num_offdiagonals_real(h, key);
-      for (int c = 1; c <= noff; ++c) {
-        Offdiag od = realspace_offdiag(h, key, c);
-        if (od.prod == 0) continue;
-        uint64_t j = rank_of(od.key, wt, s_tab);
-        RIMU_GATHER_GUARD(j);
-        acc = fma(h.hoff[od.prod], gw[j], acc);
-        kv = fma(dhdt[od.prod], v[j], kv);
+    W key = unrank<W>((uint64_t)row0, B, wt, s_tab);
+    for (int kr = 0; kr < HV_ROWS; ++kr) {
+      const int64_t row = row0 + kr;
+      if (row >= dim) break;
+      if (kr) key = next_combination(key);
+      const int I = bose_interaction_hv(key);
+      double kg;
+      if constexpr (KIND == MODEL_REAL1D) {
+        kg = real1d_row<W>(h, s_tab, (W)row, (W)dim, key, dhdt, gw, 0.0);
+      } else {
+        // bosonic one-component HubbardRealSpace without trap
+        double acc = 0.0;
+        int noff = num_offdiagonals_real(h, key);
+        for (int c = 1; c <= noff; ++c) {
+          Offdiag od = realspace_offdiag(h, key, c);
+          if (od.prod == 0) continue;
+          uint64_t j = rank_of(od.key, wt, s_tab);
+          RIMU_GATHER_GUARD(j);
+          acc = fma(dhdt[od.prod], gw[j], acc);
+        }
+        kg = acc;
       }
+      const double g = gw[row], x = v[row];
+      gv[row] = fma(h.t, kg, dtabH[I] * g);
+      su = fma(g, (double)I / 2 * x, su);
+      st = fma(x, kg, st);
     }
-    gv[row] = acc;
-    const double g = gw[row];
-    su += g * ((double)bose_interaction_hv(key) / 2 * v[row]);
-    st += g * kv;
-  }
   }
   for (int o = 16; o > 0; o >>= 1) {
     su += __shfl_down_sync(0xffffffffu, su, o);
@@ -324,28 +349,48 @@ int rimu_hv_grid(rimu_ctx *ctx, int64_t dim) {
   return (int)(want < cap ? (want < 1 ? 1 : want) : cap);
 }
 
+// HubbardReal1D addresses of at most 32 bits run on 32-bit words: every rank is below
+// C(32, 16) < 2^32.
+static bool narrow_words(const DevModel &h) { return h.kind == MODEL_REAL1D && h.nbits <= 32; }
+
 int rimu_launch_hv(rimu_ctx *ctx, const DevModel &h, const uint64_t *binom, int ntab,
                    const double *v, double *w, int64_t dim, const double *dtabH) {
   int grid = rimu_hv_grid(ctx, dim);
-  size_t smem = (size_t)ntab * 8;
+  const size_t smem = (size_t)ntab * 8;
+  if (narrow_words(h)) {
+    k_hv<MODEL_REAL1D, uint32_t><<<grid, HB, (size_t)ntab * 4, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH);
+    return rimu_cuda_check(cudaGetLastError(), "k_hv");
+  }
   switch (h.kind) {
-    case MODEL_REAL1D: k_hv<MODEL_REAL1D><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
-    case MODEL_REALSPACE: k_hv<MODEL_REALSPACE><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
-    default: k_hv<MODEL_MOM1D><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
+    case MODEL_REAL1D: k_hv<MODEL_REAL1D, uint64_t><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
+    case MODEL_REALSPACE: k_hv<MODEL_REALSPACE, uint64_t><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
+    default: k_hv<MODEL_MOM1D, uint64_t><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, w, dim, dtabH); break;
   }
   return rimu_cuda_check(cudaGetLastError(), "k_hv");
+}
+
+// The adjoint kernel and the fixed-order reduction of its block partials, on `st`.
+static void launch_adjoint(const DevModel &h, const uint64_t *binom, int ntab, const double *v,
+                           const double *gw, double *gv, int64_t dim, const double *dtabH,
+                           const double *dhdt, double *partial, int grid, double *out2,
+                           cudaStream_t st) {
+  if (narrow_words(h))
+    k_hv_adjoint<MODEL_REAL1D, uint32_t><<<grid, HB, (size_t)ntab * 4, st>>>(
+        h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial);
+  else if (h.kind == MODEL_REAL1D)
+    k_hv_adjoint<MODEL_REAL1D, uint64_t><<<grid, HB, (size_t)ntab * 8, st>>>(
+        h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial);
+  else
+    k_hv_adjoint<MODEL_REALSPACE, uint64_t><<<grid, HB, (size_t)ntab * 8, st>>>(
+        h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial);
+  k_reduce_partials<<<1, 32, 0, st>>>(partial, grid, out2);
 }
 
 int rimu_launch_hv_adjoint(rimu_ctx *ctx, const DevModel &h, const uint64_t *binom, int ntab,
                            const double *v, const double *gw, double *gv, int64_t dim,
                            const double *dtabH, const double *dhdt, double *partial,
                            int grid, double *out2) {
-  size_t smem = (size_t)ntab * 8;
-  if (h.kind == MODEL_REAL1D)
-    k_hv_adjoint<MODEL_REAL1D><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial);
-  else
-    k_hv_adjoint<MODEL_REALSPACE><<<grid, HB, smem, ctx->stream>>>(h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial);
-  k_reduce_partials<<<1, 32, 0, ctx->stream>>>(partial, grid, out2);
+  launch_adjoint(h, binom, ntab, v, gw, gv, dim, dtabH, dhdt, partial, grid, out2, ctx->stream);
   return rimu_cuda_check(cudaGetLastError(), "k_hv_adjoint");
 }
 
@@ -502,14 +547,8 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
   int64_t cap = (int64_t)g_noalloc_sms[dev] * 8;
   if (cap > NOALLOC_MAX_BLOCKS) cap = NOALLOC_MAX_BLOCKS;
   int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);
-  size_t smem = (size_t)nbinom * 8;
-  if (d->kind == RIMU_MODEL_REAL1D)
-    k_hv_adjoint<MODEL_REAL1D><<<grid, HB, smem, st>>>(h, s->binom, nbinom, v, gw, gv, dim,
-                                                       s->dtabH, s->dhdt, s->partial);
-  else
-    k_hv_adjoint<MODEL_REALSPACE><<<grid, HB, smem, st>>>(h, s->binom, nbinom, v, gw, gv, dim,
-                                                          s->dtabH, s->dhdt, s->partial);
-  k_reduce_partials<<<1, 32, 0, st>>>(s->partial, grid, s->out2);
+  launch_adjoint(h, s->binom, nbinom, v, gw, gv, dim, s->dtabH, s->dhdt, s->partial, grid,
+                 s->out2, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return rimu_cuda_check(e, "k_hv_adjoint (no-alloc)");
   double out[2];

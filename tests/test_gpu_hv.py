@@ -22,7 +22,12 @@ HV_MODELS = [
     R.HubbardRealSpace(R.BoseFS([1, 0, 2, 0, 1, 0]), R.HardwallBoundaries(2, 3), u=[[1.0]], t=[1.2]),
     R.HubbardRealSpace(R.FermiFS([1, 1, 1] + [0] * 13), R.PeriodicBoundaries(4, 4), u=[[0.0]]),
     R.HubbardMom1D(R.BoseFS([0, 1, 3, 1, 0, 0]), u=2.0),
+    # the widths where the kernels change word size: 32-bit addresses (M=30, N=3) run on
+    # 32-bit words, 33-bit addresses (M=31, N=3) on 64-bit words
+    R.HubbardReal1D(R.BoseFS([1, 0, 1] + [0] * 26 + [1]), u=1.5, t=0.8),
+    R.HubbardReal1D(R.BoseFS([1, 0, 1] + [0] * 27 + [1]), u=1.5, t=0.8),
 ]
+ADJOINT_MODELS = HV_MODELS[:4] + HV_MODELS[6:]
 
 
 @pytest.mark.parametrize("h", HV_MODELS, ids=repr)
@@ -38,7 +43,7 @@ def test_hv_basis_bit_exact(h):
     assert np.array_equal(w.view(np.uint64), want.view(np.uint64))
 
 
-@pytest.mark.parametrize("h", HV_MODELS[:4], ids=repr)
+@pytest.mark.parametrize("h", ADJOINT_MODELS, ids=repr)
 def test_adjoint_matches_oracle(h):
     m = oracle_model(h)
     keys = O.basis(m)

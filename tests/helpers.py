@@ -95,3 +95,39 @@ def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=Non
             S -= 0.08 ** 2 / 4 / dt * math.log(tn / target) + 0.08 / dt * math.log(tn / pnorm)
             pnorm = tn
     return keys, vals
+
+
+def oracle_solve(m, style, start_key, population, steps, dt, target, seed, zeta=0.08):
+    """The host loop of solve (pmc_simulation.jl:265-310; advance!, fciqmc.jl:126-181) run on
+    the oracle's step: one start address with `population` walkers, the initial shift its
+    diagonal element, DoubleLogUpdate (shiftstrategy.jl:174-181) after every step and a
+    ProjectedEnergy onto the start address (poststepstrategy.jl:82-121).  Same step numbers,
+    seed and shift arithmetic as the package's solve, so it is the CPU run of the same
+    trajectory.  Returns the report columns shift, vproj and hproj."""
+    basis = O.basis(m)
+    H = O.sparse_matrix(m, basis).tocsc()
+    ia = int(np.searchsorted(basis, np.uint64(start_key)))
+    assert basis[ia] == start_key
+    col = H[:, ia]                      # H P for the projector P = |start>
+    hp_keys, hp_vals = basis[col.indices], col.data
+    integer = style.valtype is int
+    keys = np.array([start_key], dtype=np.uint64)
+    vals = np.array([population], dtype=np.int64 if integer else np.float64)
+    S, pnorm = float(H[ia, ia]), float(abs(population))
+    xi = zeta ** 2 / 4
+    out = {"shift": [], "vproj": [], "hproj": []}
+    for step in range(1, steps + 1):
+        keys, vals, st = O.step(m, oracle_params(style, dt, S, seed, step), keys, vals)
+        tn = st["norm"]
+        if len(keys):
+            S -= xi / dt * math.log(tn / target) + zeta / dt * math.log(tn / pnorm)
+            pnorm = tn
+        out["shift"].append(S)
+        pos = np.minimum(np.searchsorted(keys, hp_keys), max(len(keys) - 1, 0))
+        hit = (keys[pos] == hp_keys) if len(keys) else np.zeros(len(hp_keys), bool)
+        out["hproj"].append(float(np.sum(hp_vals[hit] * vals[pos[hit]])))
+        j = np.searchsorted(keys, np.uint64(start_key))
+        out["vproj"].append(float(vals[j]) if j < len(keys) and keys[j] == start_key else 0.0)
+        if len(keys) == 0:
+            break
+    return out

@@ -10,21 +10,29 @@ pytestmark = pytest.mark.gpu
 
 
 def test_c1_integer_walkers_shift_brackets_exact_energy():
-    """HubbardReal1D M=N=6, u=6: shift and projected energy agree with E0 = -4.0215
-    (test/KrylovKit.jl:15) within 3 blocking errors."""
+    """HubbardReal1D M=N=6, u=6, IsStochasticInteger, 1 000 target walkers, dt = 1e-3, 20 000
+    steps.  The GPU run's shift series equals the oracle's CPU run of the same trajectory
+    exactly, and shift and projected energy lie within 2 blocking errors of E0 = -4.0215
+    (test/KrylovKit.jl:15) and of the CPU run's estimates."""
+    from helpers import oracle_solve
     addr = R.BoseFS([1] * 6)
     H = R.HubbardReal1D(addr, u=6.0, t=1.0)
     p = R.ProjectorMonteCarloProblem(H, style=R.IsStochasticInteger(), target_walkers=1000,
-                                     time_step=1e-3, last_step=12000, random_seed=1234,
+                                     time_step=1e-3, last_step=20000, random_seed=1234,
                                      post_step_strategy=R.ProjectedEnergy(H, (addr, 1.0)))
     sim = R.solve(p)
     assert sim.success
     df = sim.df
+    cpu = oracle_solve(O.real1d(6, 6, 6.0, 1.0), R.IsStochasticInteger(), addr.key, 10, 20000,
+                       1e-3, 1000, 1234)
+    assert np.array_equal(np.asarray(df["shift"], dtype=float), np.asarray(cpu["shift"]))
     E0 = O.ground_energy(O.real1d(6, 6, 6.0))
     r = R.shift_estimator(df, skip=3000)
-    assert abs(r.mean - E0) < max(3 * r.err, 0.02), (r.mean, r.err)
+    assert abs(r.mean - E0) < 2 * r.err, (r.mean, r.err)
     pe, pe_err = R.projected_energy(df, skip=3000)
-    assert abs(pe - E0) < max(3 * pe_err, 0.02), (pe, pe_err)
+    assert abs(pe - E0) < 2 * pe_err, (pe, pe_err)
+    pc, _ = R.projected_energy(cpu, skip=3000)
+    assert abs(pe - pc) < 2 * pe_err, (pe, pc, pe_err)
 
 
 def test_dss_shift_brackets_exact_energy():

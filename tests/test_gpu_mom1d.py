@@ -47,6 +47,11 @@ def test_small_mom1d_fifty_deterministic_steps_match_oracle():
 
 
 def test_mom1d_integer_walkers_shift_brackets_exact_energy():
+    """HubbardMom1D M=10, N=5 (all bosons in k = 0), u=6, IsStochasticInteger, 2 000 target
+    walkers, dt = 5e-4, 20 000 steps.  The GPU run's shift series equals the oracle's CPU run
+    of the same trajectory exactly, and shift and projected energy lie within 2 blocking
+    errors of the exact energy of the k = 0 sector."""
+    from helpers import oracle_solve
     M, N, u = 10, 5, 6.0
     addr = k0_address(M, N)
     h = R.HubbardMom1D(addr, u=u, t=1.0)
@@ -54,8 +59,14 @@ def test_mom1d_integer_walkers_shift_brackets_exact_energy():
     p = R.ProjectorMonteCarloProblem(h, style=R.IsStochasticInteger(), target_walkers=2000,
                                      time_step=5e-4, last_step=20000, random_seed=2024,
                                      population=100,
-                                     shift_strategy=R.DoubleLogUpdate(2000, 0.05, 0.05 ** 2 / 4))
+                                     shift_strategy=R.DoubleLogUpdate(2000, 0.05, 0.05 ** 2 / 4),
+                                     post_step_strategy=R.ProjectedEnergy(h, (addr, 1.0)))
     sim = R.solve(p)
     assert sim.success, sim.message
+    cpu = oracle_solve(O.mom1d(N, M, u, 1.0), R.IsStochasticInteger(), addr.key, 100, 20000,
+                       5e-4, 2000, 2024, zeta=0.05)
+    assert np.array_equal(np.asarray(sim.df["shift"], dtype=float), np.asarray(cpu["shift"]))
     r = R.shift_estimator(sim.df, skip=5000)
-    assert abs(r.mean - E0) < max(3 * r.err, 0.05), (r.mean, r.err, E0)
+    assert abs(r.mean - E0) < 2 * r.err, (r.mean, r.err, E0)
+    pe, pe_err = R.projected_energy(sim.df, skip=5000)
+    assert abs(pe - E0) < 2 * pe_err, (pe, pe_err, E0)

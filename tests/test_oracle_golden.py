@@ -148,3 +148,39 @@ def test_oracle_adjoint_matches_finite_differences():
     fu = (gw @ O.hv_basis(O.real1d(N, M, u + h, t), keys, v) - gw @ O.hv_basis(O.real1d(N, M, u - h, t), keys, v)) / (2 * h)
     ft = (gw @ O.hv_basis(O.real1d(N, M, u, t + h), keys, v) - gw @ O.hv_basis(O.real1d(N, M, u, t - h), keys, v)) / (2 * h)
     assert gu == pytest.approx(fu, rel=1e-7) and gt == pytest.approx(ft, rel=1e-7)
+
+
+def test_oracle_c1_energies_within_two_blocking_errors():
+    """The small plain configuration run through the oracle: HubbardReal1D M=N=6, u=6, t=1,
+    IsStochasticInteger, 1 000 target walkers, dt = 1e-3, 20 000 steps, seed 1234.  Shift and
+    projected energy (blocking analysis, first 3 000 steps skipped) lie within 2 blocking
+    errors of the exact energy, which is the reference's E0 = -4.0215 (test/KrylovKit.jl:6-15)."""
+    import rimugpu as R
+    from helpers import oracle_solve
+    m = O.real1d(6, 6, 6.0, 1.0)
+    E0 = O.ground_energy(m)
+    assert E0 == pytest.approx(-4.0215, abs=1e-4)
+    df = oracle_solve(m, R.IsStochasticInteger(), R.BoseFS([1] * 6).key, 10, 20000, 1e-3, 1000, 1234)
+    assert len(df["shift"]) == 20000
+    r = R.shift_estimator(df, skip=3000)
+    pe, pe_err = R.projected_energy(df, skip=3000)
+    assert abs(r.mean - E0) < 2 * r.err, (r.mean, r.err)
+    assert abs(pe - E0) < 2 * pe_err, (pe, pe_err)
+
+
+def test_oracle_mom1d_energies_within_two_blocking_errors():
+    """HubbardMom1D M=10, N=5 with all bosons in k = 0 (mode M/2, HubbardMom1D.jl:55-61),
+    u=6, IsStochasticInteger, 2 000 target walkers, dt = 5e-4, 20 000 steps through the
+    oracle: shift and projected energy within 2 blocking errors of the exact energy of the
+    k = 0 sector."""
+    import rimugpu as R
+    from helpers import oracle_solve
+    M, N = 10, 5
+    addr = R.BoseFS(M, {M // 2: N})
+    m = O.mom1d(N, M, 6.0, 1.0)
+    E0 = O.ground_energy(m, start=addr.key)
+    df = oracle_solve(m, R.IsStochasticInteger(), addr.key, 100, 20000, 5e-4, 2000, 2024, zeta=0.05)
+    r = R.shift_estimator(df, skip=5000)
+    pe, pe_err = R.projected_energy(df, skip=5000)
+    assert abs(r.mean - E0) < 2 * r.err, (r.mean, r.err)
+    assert abs(pe - E0) < 2 * pe_err, (pe, pe_err)

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 import rimugpu
 from rimugpu import _lib
 
@@ -66,3 +68,38 @@ def test_blocking_analysis_on_correlated_series():
     x = np.convolve(rng.normal(size=2 ** 14 + 63), np.ones(64) / 64, mode="valid")
     r = rimugpu.blocking_analysis(x)
     assert r.k > 1 and r.err > np.std(x) / np.sqrt(len(x))
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of the ABI structs have the size and field offsets of the C
+    declarations in include/rimu_gpu.h (compiled with the host C compiler)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from rimugpu import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    pairs = [("rimu_model_desc", _lib.ModelDesc), ("rimu_step_params", _lib.StepParams),
+             ("rimu_step_stats", _lib.StepStats), ("rimu_batch_params", _lib.BatchParams),
+             ("rimu_batch_stats", _lib.BatchStats)]
+    lines = ['#include <stdio.h>', '#include "rimu_gpu.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-o", str(exe)], check=True,
+                   capture_output=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        name, field, val = ln.split()
+        got[(name, field)] = int(val)
+    for cname, py in pairs:
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)

@@ -184,3 +184,23 @@ def test_oracle_mom1d_energies_within_two_blocking_errors():
     pe, pe_err = R.projected_energy(df, skip=5000)
     assert abs(r.mean - E0) < 2 * r.err, (r.mean, r.err)
     assert abs(pe - E0) < 2 * pe_err, (pe, pe_err)
+
+
+@pytest.mark.parametrize("periodic", [(True, True), (False, False)], ids=["periodic", "hardwall"])
+def test_oracle_adjoint_realspace_matches_sparse_matrix_and_finite_differences(periodic):
+    """The single-pass adjoint on one-component bosonic HubbardRealSpace (2x3 lattice, N=4):
+    gv = H^T gw, and the u and t gradients against central finite differences of <gw, H v>."""
+    N, dims, u, t = 4, (2, 3), 1.5, 0.7
+    def model(uu, tt):
+        return O.realspace(N, dims, u=uu, t=tt, periodic=periodic)
+    m = model(u, t)
+    keys = O.basis(m)
+    rng = np.random.default_rng(7)
+    v, gw = rng.normal(size=len(keys)), rng.normal(size=len(keys))
+    gv, gu, gt = O.hv_basis_adjoint(m, keys, v, gw)
+    assert np.allclose(gv, O.sparse_matrix(m, keys).T @ gw, rtol=1e-13, atol=1e-13)
+    h = 1e-5
+    def f(uu, tt):
+        return gw @ O.hv_basis(model(uu, tt), keys, v)
+    assert gu == pytest.approx((f(u + h, t) - f(u - h, t)) / (2 * h), rel=1e-7)
+    assert gt == pytest.approx((f(u, t + h) - f(u, t - h)) / (2 * h), rel=1e-7)

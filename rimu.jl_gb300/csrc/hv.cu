@@ -96,8 +96,9 @@ __device__ __forceinline__ int bose_interaction_hv(W key) {
 // One HubbardReal1D row in the reference's offdiagonal order: acc = fma(coef[p_j], v_j, acc)
 // from the given start, with coef = H's hopping elements -t sqrt(p) and start d v_row for
 // H v, or coef = -sqrt(p) and start 0 for the hopping part alone (the adjoint).
-// A rank outside the basis can only come from an inconsistent address; the gather is
-// skipped and the row marked NaN so that callers see it.
+// A rank outside the basis can only come from an inconsistent address: the gather is skipped
+// and the row's result is NaN so that callers see it (real1d_row returns NaN; the generic
+// rows below use RIMU_GATHER_GUARD).
 #define RIMU_GATHER_GUARD(j) if ((j) >= (uint64_t)dim) { acc = __longlong_as_double(0x7ff8000000000000ll); continue; }
 
 template <class W>

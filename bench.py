@@ -516,9 +516,9 @@ def run_reference(args, ws, rank, local):
         pn = tn
     procs = os.cpu_count() or 1
     vals_per_step = []
-    for _ in range(args.warmup):
-        pass
     per = max(args.cpu_seconds / max(args.steps, 1), 1.0)
+    for _ in range(args.warmup):          # untimed: same sample, results discarded
+        cpu_baseline(keys, vals, S, per, procs)
     t_all = time.time()
     for _ in range(args.steps):
         thr, _ = cpu_baseline(keys, vals, S, per, procs)

@@ -1,0 +1,82 @@
+"""The oracle's stochastic primitives against the reference's own statistical tests
+(test/StochasticStyles.jl:187-275): sampled spawning averages to exact spawning, and threshold
+compression leaves a vector unchanged on average.  CPU only: this pins the checker's random
+parts before it is trusted for GPU parity."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+
+def _sums(outputs):
+    """Sum of several sparse vectors given as (keys, values) pairs, as {key: value}."""
+    keys = np.concatenate([k for k, _ in outputs])
+    vals = np.concatenate([np.asarray(v, dtype=float) for _, v in outputs])
+    uniq, inv = np.unique(keys, return_inverse=True)
+    return dict(zip(uniq.tolist(), np.bincount(inv, weights=vals).tolist()))
+
+
+# the reference's two (Hamiltonian, address) cases, test/StochasticStyles.jl:196-199
+SPAWN_CASES = [
+    ("mom1d", O.mom1d(5, 6, u=6.0), [0, 0, 0, 3, 1, 1]),
+    ("real1d", O.real1d(10, 7, u=1.0), [5, 0, 0, 5, 0, 0, 0]),
+]
+
+
+@pytest.mark.parametrize("style", [O.STYLE_DSS, O.STYLE_INTEGER], ids=["dss", "integer"])
+@pytest.mark.parametrize("name,m,onr", SPAWN_CASES, ids=[c[0] for c in SPAWN_CASES])
+def test_sampled_spawns_average_to_exact_spawns(name, m, onr, style):
+    """10 000 columns of one address with random values in [0, 1.2 n_offdiag): the summed
+    sampled steps (WithReplacement attempts, exact columns where DynamicSemistochastic switches
+    to them; integer walkers rounded stochastically) agree with the summed exact steps within
+    10 % on every address, the reference's bound for these strategies."""
+    key = O.bose_key(onr)
+    noff = O.num_offdiagonals(m, key)
+    rng = np.random.default_rng(11)
+    sampled, exact = [], []
+    for i in range(10000):
+        val = rng.random() * noff * 1.2
+        if style == O.STYLE_INTEGER:
+            val = float(max(1, round(val)))
+            src = np.array([int(val)], dtype=np.int64)
+        else:
+            src = np.array([val])
+        k, v, _ = O.step(m, O.StepParams(style, dt=0.1, seed=77, step=i + 1), [key], src)
+        sampled.append((k, v))
+        k, v, _ = O.step(m, O.StepParams(O.STYLE_DETERMINISTIC, dt=0.1, step=i + 1), [key],
+                         np.array([val]))
+        exact.append((k, v))
+    s, e = _sums(sampled), _sums(exact)
+    assert 1 < len(e) <= noff + 1     # the address and its distinct offdiagonal targets
+    for a, want in e.items():
+        assert s.get(a, 0.0) == pytest.approx(want, rel=0.1), a
+
+
+@pytest.mark.parametrize("threshold", [1.0, 2.0])
+def test_threshold_compression_preserves_the_vector_on_average(threshold):
+    """ThresholdCompression(1) and (2) applied 1 000 times to a normalised vector of
+    HubbardMom1D(BoseFS(0,0,0,10,0,0,0)) (test/StochasticStyles.jl:240-275): every compressed
+    vector is shorter, the source is unchanged, and the average has the source's walker number
+    and unit overlap with it within 10 %.  A step with dt = 0 is the compression alone (the
+    transition operator is the identity and every spawn is zero)."""
+    import scipy.sparse.linalg as sla
+    m = O.mom1d(10, 7)
+    start = O.bose_key([0, 0, 0, 10, 0, 0, 0])
+    keys = O.connected_basis(m, start)
+    _, vecs = sla.eigsh(O.sparse_matrix(m, keys), k=1, which="SA")
+    dv = vecs[:, 0] / np.linalg.norm(vecs[:, 0])
+    keep = dv != 0.0
+    keys, dv = np.ascontiguousarray(keys[keep]), np.ascontiguousarray(dv[keep])
+    before = dv.copy()
+    outs = []
+    for i in range(1000):
+        k, v, _ = O.step(m, O.StepParams(O.STYLE_DSS, dt=0.0, seed=5, step=i + 1,
+                                         compression=threshold), keys, dv)
+        assert len(k) < len(keys)
+        outs.append((k, v / 1000))
+    assert np.array_equal(dv, before)
+    avg = _sums(outs)
+    pos = {int(a): i for i, a in enumerate(keys.tolist())}
+    overlap = sum(val * dv[pos[a]] for a, val in avg.items())
+    assert sum(abs(x) for x in avg.values()) == pytest.approx(np.abs(dv).sum(), rel=0.1)
+    assert overlap == pytest.approx(1.0, rel=0.1)

@@ -204,3 +204,30 @@ def test_oracle_adjoint_realspace_matches_sparse_matrix_and_finite_differences(p
         return gw @ O.hv_basis(model(uu, tt), keys, v)
     assert gu == pytest.approx((f(u + h, t) - f(u - h, t)) / (2 * h), rel=1e-7)
     assert gt == pytest.approx((f(u, t + h) - f(u, t - h)) / (2 * h), rel=1e-7)
+
+
+def test_oracle_momentum_transfer_excitations():
+    """momentum_transfer_excitation with fold=true, the periodic form HubbardMom1D uses
+    (test/Hamiltonians.jl:97-152), through the oracle's HubbardMom1D offdiagonals, whose values
+    are (u/2M) * onproduct, or (u/M) * onproduct for FermiFS2C (HubbardMom1D.jl:189-205)."""
+    u = 2.0
+    m = O.mom1d(2, 4, u=u)
+    # BoseFS((0,1,1,0)): all four excitations reach (1,0,0,1) with onproduct 1
+    offs = O.offdiagonals(m, O.bose_key([0, 1, 1, 0]))
+    assert len(offs) == 4
+    for k, v in offs:
+        assert k == O.bose_key([1, 0, 0, 1]) and v == pytest.approx(u / 8)
+    # BoseFS((1,1,0,0)): onproduct 1 for all four
+    offs = O.offdiagonals(m, O.bose_key([1, 1, 0, 0]))
+    assert len(offs) == 4 and all(v == pytest.approx(u / 8) for _, v in offs)
+    # BoseFS((0,3,0)): both excitations reach (1,1,1) with onproduct sqrt(6)
+    offs = O.offdiagonals(O.mom1d(3, 3, u=u), O.bose_key([0, 3, 0]))
+    assert len(offs) == 2
+    for k, v in offs:
+        assert k == O.bose_key([1, 1, 1]) and v == pytest.approx(u / 6 * math.sqrt(6))
+    # FermiFS2C pairs: onproduct 1 for each of the three excitations
+    M = 4
+    for a, b in (([0, 0, 1, 0], [0, 1, 0, 0]), ([1, 0, 0, 0], [0, 1, 0, 0])):
+        key = (O.fermi_key(a) << M) | O.fermi_key(b)
+        offs = O.offdiagonals(O.mom1d_2c(1, 1, M, u=u), key)
+        assert len(offs) == 3 and all(v == pytest.approx(u / M) for _, v in offs)

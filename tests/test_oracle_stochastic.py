@@ -80,3 +80,28 @@ def test_threshold_compression_preserves_the_vector_on_average(threshold):
     overlap = sum(val * dv[pos[a]] for a, val in avg.items())
     assert sum(abs(x) for x in avg.values()) == pytest.approx(np.abs(dv).sum(), rel=0.1)
     assert overlap == pytest.approx(1.0, rel=0.1)
+
+
+def test_style_comparison_on_the_reference_model():
+    """The reference's style comparison (test/lomc.jl:543-605) for the styles of this path:
+    HubbardReal1D(BoseFS{5,5}(1,1,1,1,1)), one walker to start, DoubleLogUpdate(zeta=0.05,
+    xi=zeta^2/4, target 100), dt = 0.01, 2 500 steps.  Every style's shift (steps 500 on)
+    lies within 3 of its errors of E0 = -8.280991746582686, and the stochastic-integer error
+    exceeds the dynamic-semistochastic one."""
+    import rimugpu as R
+    from rimugpu.stats import mean_and_se
+    from helpers import oracle_solve
+    m = O.real1d(5, 5, 1.0, 1.0)
+    E0 = -8.280991746582686
+    assert O.ground_energy(m) == pytest.approx(E0, abs=1e-12)
+    key = R.BoseFS([1] * 5).key
+    est = {}
+    for name, style, pop in (("st", R.IsStochasticInteger(), 1),
+                             ("dy", R.IsDynamicSemistochastic(), 1.0),
+                             ("de", R.IsDeterministic(), 1.0),
+                             ("dp", R.IsDeterministic(R.ThresholdCompression()), 1.0)):
+        df = oracle_solve(m, style, key, pop, 2500, 0.01, 100, 1234, zeta=0.05)
+        E, se = mean_and_se(np.asarray(df["shift"][499:]))
+        assert abs(E - E0) <= 3 * se, (name, E, se)
+        est[name] = se
+    assert est["st"] > est["dy"]

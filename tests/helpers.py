@@ -97,27 +97,29 @@ def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=Non
     return keys, vals
 
 
-def oracle_solve(m, style, start_key, population, steps, dt, target, seed, zeta=0.08):
+def oracle_solve(m, style, start_key, population, steps, dt, target, seed, zeta=0.08,
+                 initiator=None):
     """The host loop of solve (pmc_simulation.jl:265-310; advance!, fciqmc.jl:126-181) run on
     the oracle's step: one start address with `population` walkers, the initial shift its
-    diagonal element, DoubleLogUpdate (shiftstrategy.jl:174-181) after every step and a
-    ProjectedEnergy onto the start address (poststepstrategy.jl:82-121).  Same step numbers,
+    diagonal element, DoubleLogUpdate (shiftstrategy.jl:174-181) after every step, an optional
+    initiator rule, and a ProjectedEnergy onto the start address (poststepstrategy.jl:82-121)
+    whose frozen H P is the start's diagonal element and offdiagonals.  Same step numbers,
     seed and shift arithmetic as the package's solve, so it is the CPU run of the same
     trajectory.  Returns the report columns shift, vproj and hproj."""
-    basis = O.basis(m)
-    H = O.sparse_matrix(m, basis).tocsc()
-    ia = int(np.searchsorted(basis, np.uint64(start_key)))
-    assert basis[ia] == start_key
-    col = H[:, ia]                      # H P for the projector P = |start>
-    hp_keys, hp_vals = basis[col.indices], col.data
+    hp = {int(start_key): O.diagonal(m, start_key)}
+    for nk, hv in O.offdiagonals(m, start_key):
+        hp[nk] = hp.get(nk, 0.0) + hv
+    hp_keys = np.array(sorted(hp), dtype=np.uint64)
+    hp_vals = np.array([hp[int(k)] for k in hp_keys])
     integer = style.valtype is int
     keys = np.array([start_key], dtype=np.uint64)
     vals = np.array([population], dtype=np.int64 if integer else np.float64)
-    S, pnorm = float(H[ia, ia]), float(abs(population))
+    S, pnorm = float(O.diagonal(m, start_key)), float(abs(population))
     xi = zeta ** 2 / 4
     out = {"shift": [], "vproj": [], "hproj": []}
     for step in range(1, steps + 1):
-        keys, vals, st = O.step(m, oracle_params(style, dt, S, seed, step), keys, vals)
+        keys, vals, st = O.step(m, oracle_params(style, dt, S, seed, step, initiator=initiator),
+                                keys, vals)
         tn = st["norm"]
         if len(keys):
             S -= xi / dt * math.log(tn / target) + zeta / dt * math.log(tn / pnorm)

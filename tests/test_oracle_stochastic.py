@@ -105,3 +105,29 @@ def test_style_comparison_on_the_reference_model():
         assert abs(E - E0) <= 3 * se, (name, E, se)
         est[name] = se
     assert est["st"] > est["dy"]
+
+
+def test_initiator_energies_below_the_plateau():
+    """The reference's initiator test (test/lomc.jl:611-673) through the oracle:
+    HubbardMom1D(BoseFS{10,10} with all bosons in k = 0; u = 4), IsDynamicSemistochastic, one
+    walker to start, DoubleLogUpdate(zeta=0.05, xi=zeta^2/4, target 300), dt = 5e-4, 6 000
+    steps, shift averaged from step 2 000.  Below the plateau the run without a rule (and with
+    NonInitiator) falls below E0; the initiator rules are biased above E0, SimpleInitiator
+    most; Initiator and CoherentInitiator agree within 3 errors."""
+    import rimugpu as R
+    from rimugpu.stats import mean_and_se
+    from helpers import oracle_solve
+    m = O.mom1d(10, 10, 4.0, 1.0)
+    key = O.bose_key([0] * 4 + [10] + [0] * 5)
+    E0 = -9.251592973178997
+    E, S = {}, {}
+    for name, rule in (("no", None), ("i1", R.Initiator(1)), ("i2", R.SimpleInitiator(1)),
+                       ("i3", R.CoherentInitiator(1)), ("ni", R.NonInitiator())):
+        df = oracle_solve(m, R.IsDynamicSemistochastic(), key, 1.0, 6000, 5e-4, 300, 8008,
+                          zeta=0.05, initiator=rule)
+        E[name], S[name] = mean_and_se(np.asarray(df["shift"][1999:]))
+    assert E["no"] < E0 and E["ni"] < E0
+    assert abs(E["no"] - E["ni"]) <= 3 * S["no"]
+    assert E["i1"] > E0 and E["i2"] > E0 and E["i3"] > E0
+    assert E["i2"] > E["i1"]
+    assert abs(E["i1"] - E["i3"]) <= max(3 * S["i1"], 3 * S["i3"])

@@ -131,3 +131,21 @@ def test_initiator_energies_below_the_plateau():
     assert E["i1"] > E0 and E["i2"] > E0 and E["i3"] > E0
     assert E["i2"] > E["i1"]
     assert abs(E["i1"] - E["i3"]) <= max(3 * S["i1"], 3 * S["i3"])
+
+
+def test_initiator_energies_above_the_plateau():
+    """The second half of the reference's initiator test (test/lomc.jl:675-702) through the
+    oracle: HubbardMom1D(BoseFS{10,10}, all bosons in k = 0; u = 1), IsDynamicSemistochastic,
+    target 3 000, dt = 1e-2, 2 500 steps, shift averaged from step 500.  Above the plateau
+    every rule, and none, gives E0 = -16.36048582876015 within 3 errors."""
+    import rimugpu as R
+    from rimugpu.stats import mean_and_se
+    from helpers import oracle_solve
+    m = O.mom1d(10, 10, 1.0, 1.0)
+    key = O.bose_key([0] * 4 + [10] + [0] * 5)
+    E0 = -16.36048582876015
+    for rule in (None, R.Initiator(1), R.SimpleInitiator(1), R.CoherentInitiator(1)):
+        df = oracle_solve(m, R.IsDynamicSemistochastic(), key, 1.0, 2500, 1e-2, 3000, 1337,
+                          zeta=0.05, initiator=rule)
+        E, se = mean_and_se(np.asarray(df["shift"][499:]))
+        assert abs(E - E0) <= 3 * se, (rule, E, se)

@@ -149,3 +149,31 @@ def test_initiator_energies_above_the_plateau():
                           zeta=0.05, initiator=rule)
         E, se = mean_and_se(np.asarray(df["shift"][499:]))
         assert abs(E - E0) <= 3 * se, (rule, E, se)
+
+
+def test_ground_state_energy_estimates_of_the_seven_site_model():
+    """The reference's ground-state estimates (test/mpi_runtests.jl:157-203) through the
+    oracle, E0 = -4.628524493494574 for HubbardReal1D(BoseFS(1,1,1,1,1,1,1); u=6).
+    IsDynamicSemistochastic from 3 walkers with the default target 1 000 and dt = 0.01, 5 000
+    steps: the 3-error interval of the shift (from step 2 000) and of the projected energy
+    contain E0.  Integer walkers under Initiator(1) on the momentum-space form
+    HubbardMom1D(BoseFS(0,0,0,7,0,0,0); u=6), target 100: the shift stays above E0 (the
+    initiator bias).  The reference's other post-step observables are outside this path."""
+    import rimugpu as R
+    from rimugpu.stats import mean_and_se
+    from helpers import oracle_solve
+    E0 = -4.628524493494574
+    m = O.real1d(7, 7, 6.0, 1.0)
+    df = oracle_solve(m, R.IsDynamicSemistochastic(), O.bose_key([1] * 7), 3.0, 5000, 0.01,
+                      1000, 13)
+    Es, se = mean_and_se(np.asarray(df["shift"][1999:]))
+    assert Es - 3 * se < E0 < Es + 3 * se
+    pe, pe_err = R.projected_energy(df, skip=1999)
+    assert pe - 3 * pe_err < E0 < pe + 3 * pe_err
+    mm = O.mom1d(7, 7, 6.0, 1.0)
+    k0 = O.bose_key([0, 0, 0, 7, 0, 0, 0])
+    assert O.ground_energy(mm, start=k0) == pytest.approx(E0, abs=1e-9)
+    df = oracle_solve(mm, R.IsStochasticInteger(), k0, 3, 5000, 0.01, 100, 13,
+                      initiator=R.Initiator(1))
+    Es, _ = mean_and_se(np.asarray(df["shift"][1999:]))
+    assert E0 <= Es

@@ -135,12 +135,14 @@ typedef struct {
   int32_t nb_bits;
 } rimu_step_stats;
 
-/* Library and errors. */
+/* Library and errors (plumbing of the C ABI, no counterpart in the reference, whose errors are
+ * Julia exceptions such as the ArgumentError of pdvec.jl:814-818). */
 int rimu_version(void);
 int rimu_last_error(char *buf, size_t len);
 
 /* Context: one device and one stream; stream NULL means the CUDA default stream.  All work
- * of the context is ordered on that stream. */
+ * of the context is ordered on that stream.  No counterpart in the reference (its vectors live
+ * in host memory). */
 int rimu_ctx_create(int device, void *stream, rimu_ctx **out);
 int rimu_ctx_destroy(rimu_ctx *ctx);
 int rimu_ctx_synchronize(rimu_ctx *ctx);

@@ -73,7 +73,8 @@ def eigsolve(op: BasisOperator, v0=None, howmany=1, which="SR", tol=1e-10, krylo
     torch = _torch()
     if which != "SR":
         raise ValueError("only which=:SR is implemented")
-    dev = torch.device("cuda", _lib.default_context().device)
+    # the Krylov vectors live where the start vector does (the context's device by default)
+    dev = v0.device if v0 is not None else torch.device("cuda", _lib.default_context().device)
     v = v0.clone() if v0 is not None else torch.randn(op.dim, dtype=torch.float64, device=dev,
                                                       generator=torch.Generator(dev).manual_seed(1))
     v /= torch.linalg.norm(v)

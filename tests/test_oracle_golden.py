@@ -231,3 +231,32 @@ def test_oracle_momentum_transfer_excitations():
         key = (O.fermi_key(a) << M) | O.fermi_key(b)
         offs = O.offdiagonals(O.mom1d_2c(1, 1, M, u=u), key)
         assert len(offs) == 3 and all(v == pytest.approx(u / M) for _, v in offs)
+
+
+@pytest.mark.parametrize("n", [6, 8])
+def test_lanczos_host_loop_against_dense_eigenvalues(n):
+    """The host side of the KrylovKit path (eigsolve, ext/KrylovKitExt.jl:36-46) with the
+    oracle's sparse HubbardReal1D(n, n; u=6) as the operator, on the CPU: the lowest eigenvalue
+    agrees with scipy's to 1e-10, and for n = 6 it is the reference's -4.0215
+    (test/KrylovKit.jl:6-15)."""
+    import scipy.sparse.linalg as sla
+    import torch
+    import rimugpu as R
+    m = O.real1d(n, n, 6.0, 1.0)
+    H = O.sparse_matrix(m).tocsr()
+
+    class Op:
+        dim = H.shape[0]
+
+        def __call__(self, v):
+            return torch.as_tensor(H @ v.numpy())
+
+    v0 = torch.as_tensor(np.random.default_rng(2).normal(size=Op.dim))
+    vals, vecs, info = R.eigsolve(Op(), v0=v0, tol=1e-10)
+    assert info["converged"]
+    want = sla.eigsh(H, k=1, which="SA")[0][0]
+    assert vals[0] == pytest.approx(want, abs=1e-10)
+    if n == 6:
+        assert vals[0] == pytest.approx(-4.0215, abs=1e-4)
+    r = H @ vecs[0].numpy() - vals[0] * vecs[0].numpy()
+    assert np.linalg.norm(r) / np.linalg.norm(vecs[0].numpy()) < 1e-8

@@ -6,6 +6,7 @@ to attach error bars to the shift and projected-energy estimators.
 from __future__ import annotations
 
 import math
+import warnings
 from dataclasses import dataclass
 
 import numpy as np
@@ -44,7 +45,9 @@ def blocks_with_m(v, corrected=True):
         m = float(np.mean(v))
         var = float(np.sum((v - m) ** 2) / (n - int(corrected)))
         gamma = autocovariance(v, 1, corrected, m)
-        mj = n * ((n - 1) * var / (n ** 2) + gamma) ** 2 / (var ** 2) if var > 0 else 0.0
+        # Eq. (12) of Jonsson; a series without variance gives 0/0 = NaN as in the reference,
+        # so the M-test fails on it instead of passing
+        mj = n * ((n - 1) * var / (n ** 2) + gamma) ** 2 / (var ** 2) if var > 0 else math.nan
         se = math.sqrt(var / n)
         out["blocks"].append(n)
         out["mean"].append(m)
@@ -72,10 +75,14 @@ def blocking_analysis(v, alpha=0.01, corrected=True, skip=0) -> BlockingResult:
     """blocking_analysis (blocking.jl:134-159)."""
     v = np.asarray(v, dtype=float)[skip:]
     if len(v) < 2:
+        warnings.warn("Attempted blocking on an empty vector." if len(v) == 0 else
+                      f"Attempted blocking on a vector of length {len(v)}.")
         return BlockingResult(float(v[0]) if len(v) else 0.0, math.nan, math.nan, math.nan, -1, len(v))
     nt = blocks_with_m(v, corrected)
     k = mtest(nt["mj"], alpha)
     if k < 0:
+        warnings.warn("Hypothesis testing failed during blocking_analysis. "
+                      "Try using more time steps!")
         return BlockingResult(nt["mean"][0], math.nan, math.nan, math.nan, k, 0)
     return BlockingResult(nt["mean"][0], nt["std_err"][k - 1], nt["std_err_err"][k - 1],
                           nt["p_cov"][k - 1], k, nt["blocks"][k - 1])

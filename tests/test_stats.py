@@ -38,3 +38,37 @@ def test_blocking_fails_on_series_without_information():
             r = blocking_analysis(x)
         assert r.k == -1 and math.isnan(r.err), len(x)
         assert caught, len(x)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_ratio_of_means_against_linear_error_propagation(seed):
+    """The projected-energy estimator on the reference's well-behaved example
+    (test/StatsTools.jl:131-155): 2 000 samples of a bivariate normal with means 2 and 3,
+    standard errors of the means 0.5 and 0.1 and their covariance 0.02.  The ratio lies within
+    2 sigma_f of 2/3 and the error agrees with linear error propagation (x_by_y_linear,
+    ratio_of_means.jl:166-171) to 8/sqrt(n); after correlating the series by smoothing over
+    2^3 and 2^6 points the blocked ratio and error stay within 2 sigma_f."""
+    from rimugpu.stats import ratio_of_means
+    n, ma, mb, sa, sb, rho = 2000, 2.0, 3.0, 0.5, 0.1, 0.02
+    f = ma / mb
+    sf = math.sqrt((sa / mb) ** 2 + (ma * sb / mb ** 2) ** 2 - 2 * rho * ma / mb ** 3)
+    cov = np.array([[sa ** 2, rho], [rho, sb ** 2]]) * n
+    ab = np.random.default_rng(seed).multivariate_normal([ma, mb], cov, size=n)
+    a, b = ab[:, 0], ab[:, 1]
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        r, err = ratio_of_means(a, b)
+        rs, errs = ratio_of_means(smoothen(a, 2 ** 3), smoothen(b, 2 ** 6))
+    assert abs(r - f) <= 2 * sf
+    assert err == pytest.approx(sf, rel=8 / math.sqrt(n))
+    assert abs(rs - f) <= 2 * sf and abs(errs - sf) <= 2 * sf
+
+
+def test_ratio_of_means_without_variance():
+    """Zero-variance examples of test/StatsTools.jl:105-109: value and error are 0 for a zero
+    numerator, and the ratio of two constant series is exact."""
+    from rimugpu.stats import ratio_of_means
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        assert ratio_of_means([0, 0, 0, 0, 0, 0], [1, 1, 1, 1, 1, 2]) == (0.0, 0.0)
+        assert ratio_of_means(np.ones(2000), np.ones(2000)) == (1.0, 0.0)

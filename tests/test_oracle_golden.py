@@ -260,3 +260,22 @@ def test_lanczos_host_loop_against_dense_eigenvalues(n):
         assert vals[0] == pytest.approx(-4.0215, abs=1e-4)
     r = H @ vecs[0].numpy() - vals[0] * vecs[0].numpy()
     assert np.linalg.norm(r) / np.linalg.norm(vecs[0].numpy()) < 1e-8
+
+
+@pytest.mark.parametrize("name,m", [
+    ("real1d", O.real1d(5, 6, u=2.0, t=0.7)),
+    ("realspace-periodic", O.realspace(4, (2, 3), u=1.5, t=0.8)),
+    ("realspace-hardwall", O.realspace(3, (3, 3), u=2.0, periodic=(False, False))),
+    ("realspace-fermion", O.realspace(3, (2, 4), u=0.0, fermion=True)),
+    ("mom1d", O.mom1d(4, 6, u=3.0)),
+    ("mom1d-fermi2c", O.mom1d_2c(2, 2, 5, u=1.5)),
+    ("realspace-2c", O.realspace2(((False, 2), (True, 2)), (2, 2), t=(1.0, 0.5),
+                                  u=((1.0, 2.0), (2.0, 0.0)))),
+])
+def test_oracle_hamiltonians_are_symmetric(name, m):
+    """Every model's matrix over its full sorted basis is real symmetric, the LOStructure
+    IsHermitian the pull-form H*v relies on (HubbardReal1D.jl:44 and its siblings): row i
+    read from the offdiagonals of column i is row i of H."""
+    H = O.sparse_matrix(m).tocsr()
+    assert H.shape[0] > 1
+    assert abs(H - H.T).max() <= 1e-14 * max(abs(H).max(), 1.0)

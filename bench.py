@@ -155,16 +155,19 @@ def _cpu_worker(args):
     return walkers, time.time() - t0, steps
 
 
-def cpu_baseline(keys, vals, shift, seconds, procs):
-    import numpy as np
+def cpu_baseline(keys, vals, shift, seconds, procs, pool=None):
+    """Walker-steps/s of `procs` processes stepping independent copies of the sample for
+    `seconds` each (timed inside the workers), and the oracle steps they made; `pool` is an
+    open spawn pool of `procs` workers to reuse, else one is made for this call."""
     import multiprocessing as mp
-    ctx = mp.get_context("spawn")
     jobs = [(keys, vals, shift, seconds, 1000 + i) for i in range(procs)]
-    if procs == 1:
+    if procs == 1 and pool is None:
         res = [_cpu_worker(jobs[0])]
+    elif pool is not None:
+        res = pool.map(_cpu_worker, jobs)
     else:
-        with ctx.Pool(procs) as pool:
-            res = pool.map(_cpu_worker, jobs)
+        with mp.get_context("spawn").Pool(procs) as own:
+            res = own.map(_cpu_worker, jobs)
     walkers = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
     return walkers / wall, sum(r[2] for r in res)
@@ -516,13 +519,17 @@ def run_reference(args, ws, rank, local):
         pn = tn
     procs = os.cpu_count() or 1
     vals_per_step = []
-    per = max(args.cpu_seconds / max(args.steps, 1), 1.0)
-    for _ in range(args.warmup):          # untimed: same sample, results discarded
-        cpu_baseline(keys, vals, S, per, procs)
-    t_all = time.time()
-    for _ in range(args.steps):
-        thr, _ = cpu_baseline(keys, vals, S, per, procs)
-        vals_per_step.append(thr)
+    # every step samples `per` seconds on all processes of one pool, so that K steps take
+    # about cpu_seconds (at least a quarter second per step)
+    per = max(args.cpu_seconds / max(args.steps, 1), 0.25)
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for _ in range(args.warmup):      # untimed: same sample, results discarded
+            cpu_baseline(keys, vals, S, per, procs, pool)
+        t_all = time.time()
+        for _ in range(args.steps):
+            thr, _ = cpu_baseline(keys, vals, S, per, procs, pool)
+            vals_per_step.append(thr)
     value = float(np.mean(vals_per_step))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
@@ -532,7 +539,7 @@ def run_reference(args, ws, rank, local):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                              "sample": f"{len(keys)} walkers (norm {float(np.abs(vals).sum()):.3g}) grown by "
                                        f"the oracle from the start address; {procs} processes stepping "
-                                       f"independent copies, {per:.1f} s per step sample"},
+                                       f"independent copies, {per:.2f} s per step sample"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "Julia is not installed; this is the C restatement of the reference step (oracle/)"}
     print(json.dumps(line), flush=True)
@@ -541,7 +548,7 @@ def run_reference(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--target", type=float, default=1e8)

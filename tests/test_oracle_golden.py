@@ -279,3 +279,28 @@ def test_oracle_hamiltonians_are_symmetric(name, m):
     H = O.sparse_matrix(m).tocsr()
     assert H.shape[0] > 1
     assert abs(H - H.T).max() <= 1e-14 * max(abs(H).max(), 1.0)
+
+
+@pytest.mark.parametrize("name,m,key", [
+    ("real1d", O.real1d(5, 6, u=2.0, t=0.7), O.bose_key([2, 0, 1, 0, 2, 0])),
+    ("realspace-hardwall", O.realspace(4, (2, 3), u=1.5, periodic=(False, True)),
+     O.bose_key([1, 0, 2, 0, 0, 1])),
+    ("realspace-fermion", O.realspace(3, (2, 4), fermion=True), O.fermi_key([1, 1, 0, 0, 1, 0, 0, 0])),
+    ("mom1d", O.mom1d(4, 6, u=3.0), O.bose_key([0, 1, 2, 0, 1, 0])),
+    ("mom1d-fermi2c", O.mom1d_2c(2, 2, 5, u=1.5),
+     (O.fermi_key([1, 1, 0, 0, 0]) << 5) | O.fermi_key([0, 0, 1, 1, 0])),
+])
+def test_oracle_hamiltonian_action_on_one_address(name, m, key):
+    """The interface test's Hamiltonian action (InterfaceTests.jl:211-226): H applied to
+    2 e_addr by one plain-Hamiltonian step equals 2 (diagonal_element e_addr + the sum of the
+    offdiagonals), entry by entry."""
+    k, v, _ = O.step(m, O.StepParams(O.STYLE_DETERMINISTIC, op=O.OP_HAMILTONIAN), [key],
+                     np.array([2.0]))
+    want = {key: 2 * O.diagonal(m, key)}
+    for nk, hv in O.offdiagonals(m, key):
+        want[nk] = want.get(nk, 0.0) + 2 * hv
+    want = {a: x for a, x in want.items() if x != 0.0}
+    got = dict(zip((int(a) for a in k), v))
+    assert set(got) == set(want)
+    for a, x in want.items():
+        assert got[a] == pytest.approx(x, rel=1e-14, abs=1e-14), a

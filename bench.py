@@ -258,8 +258,8 @@ def run_ours(args, ws, rank, local):
                 "traffic": args.traffic if args.traffic is not None else
                 round(TRAFFIC_PER_ALGORITHMIC_BYTE * k_bytes / steps_t),
                 "traffic_source": "ncu dram bytes per algorithmic byte of k_spawn + k_annihilate "
-                                  "at norm 3e7 (profiles/step_hubbardreal1d_m20_1e8.md), scaled by "
-                                  "this run's records per step" if args.traffic is None else "given",
+                                  "measured at an equilibrated norm of 3e7, scaled by this run's "
+                                  "records per step" if args.traffic is None else "given",
                 "peak_source": peak_kind,
                 "kernel": "k_spawn + k_spawn_heavy + k_annihilate (one step)",
                 "bytes_per_step": k_bytes / steps_t, "ms_per_step": k_ms / steps_t,

@@ -312,19 +312,24 @@ int rimu_hv_basis(rimu_model *m, const double *v, double *w, int64_t dim);
 int rimu_hv_basis_adjoint(rimu_model *m, const double *v, const double *gw, double *gv,
                           double *gu, double *gt, int64_t dim);
 
-/* Allocation-free variant of rimu_hv_basis_adjoint, for callers that cannot allocate device
- * memory: code recorded into a CUDA graph, or programs whose GPU memory belongs to their own
- * allocator or budget.  No counterpart in the reference.  Takes the plain model description
- * instead of a handle (creating a handle allocates) and runs on `stream` (NULL: the default
- * stream); v, gw and gv are device arrays of length dim, gu and gt host outputs.  It calls no
- * cudaMalloc, cudaFree or other allocating routine: its tables and partial sums live in one
- * static device array of about 160 KB that every GPU loading the library keeps until exit.
+/* Allocation-free variant of rimu_hv_basis_adjoint.  No counterpart in the reference.  It is
+ * for callers that cannot let a library allocate device memory: applications whose GPU memory
+ * is owned by their own allocator or budget (a server that reserves the memory at start-up, a
+ * Julia program whose CUDA.jl pool holds it), where cudaMalloc fails or takes memory promised
+ * elsewhere, and loops that cannot afford the device-wide synchronisation that cudaMalloc and
+ * cudaFree may imply.  It takes the plain model description instead of a handle (creating a
+ * handle allocates) and runs on `stream` (NULL: the default stream); v, gw and gv are device
+ * arrays of length dim, gu and gt host outputs.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine: its tables and partial sums live in one static device array of about
+ * 160 KB that every GPU loading the library keeps until the process exits.  It waits for its
+ * stream before returning, to hand gu and gt back on the host.
  * Limits: HubbardReal1D or bosonic one-component HubbardRealSpace without trap, with
- * (N+M)(N+1) <= 4096 and N(N+1)+1 <= 4096; larger models return RIMU_ERR_BADARG.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress) and should
- * therefore come before any stream capture.  All calls share the array and it keeps the last
- * call's contents; calls whose kernels overlap on the GPU race on it, so they must be ordered
- * on one stream (the host-side table staging is not thread safe either). */
+ * N+M-1 <= 63 address bits, (N+M)(N+1) <= 4096 and N(N+1)+1 <= 4096; anything else returns
+ * RIMU_ERR_BADARG.  The first call on a device does the set-up (it looks up the array's device
+ * address with cudaGetSymbolAddress) and should come before any stream capture.  All calls
+ * share the array and it keeps the last call's contents; calls whose kernels overlap on the
+ * GPU race on it, so they must be ordered on one stream (the host-side table staging is not
+ * thread safe either). */
 int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *desc, const double *v, const double *gw,
                                   double *gv, double *gu, double *gt, int64_t dim, void *stream);
 

@@ -399,11 +399,13 @@ int rimu_launch_hv_adjoint(rimu_ctx *ctx, const DevModel &h, const uint64_t *bin
 // Allocation-free adjoint.
 //
 // rimu_hv_basis_adjoint keeps its tables and its per-block partial sums in device memory that
-// the library allocates.  Some callers cannot let a library allocate: code that records work
-// into a CUDA graph, and applications whose device memory is owned by their own allocator or
-// budget (an inference server, a Julia/CUDA.jl program with a memory pool).  This entry point
-// does the same computation with all of its scratch in one file-scope device array of fixed
-// size, so that it calls no allocator at all.
+// the library allocates.  Some callers cannot let a library allocate: applications whose device
+// memory is owned by their own allocator or budget (an inference server that reserves the GPU's
+// memory at start-up, a Julia/CUDA.jl program whose memory pool holds it), where a cudaMalloc
+// either fails or takes memory the owner has promised elsewhere; and loops that cannot afford
+// the device-wide synchronisation cudaMalloc and cudaFree may imply.  This entry point does the
+// same computation with all of its scratch in one file-scope device array of fixed size, so
+// that it calls no allocator at all.
 //
 // The array is global to the library: every GPU that loads the library holds it until the
 // process exits, every call shares it, and it keeps the last call's contents.  Calls whose
@@ -450,8 +452,8 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
     return RIMU_ERR_BADARG;
   }
   const bool realspace = d->kind == RIMU_MODEL_REALSPACE;
-  if (d->n_components == 2 ||
-      !(d->kind == RIMU_MODEL_REAL1D || (realspace && !d->fermion && !d->potential))) {
+  if (d->n_components == 2 || d->fermion ||
+      !(d->kind == RIMU_MODEL_REAL1D || (realspace && !d->potential))) {
     rimu_set_error("rimu_hv_basis_adjoint_noalloc: needs HubbardReal1D or one-component bosonic HubbardRealSpace without trap");
     return RIMU_ERR_BADARG;
   }
@@ -470,6 +472,21 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
   if (ndim < 1 || ndim > 3) {
     rimu_set_error("rimu_hv_basis_adjoint_noalloc: ndim must be 1..3");
     return RIMU_ERR_BADARG;
+  }
+  if (realspace) {
+    // the checks of rimu_model_create: every extent at least 2, product n_modes
+    long long prod = 1;
+    for (int i = 0; i < ndim; ++i) {
+      if (d->dims[i] < 2 || d->dims[i] > M) {
+        rimu_set_error("rimu_hv_basis_adjoint_noalloc: all dimensions must be at least 2");
+        return RIMU_ERR_BADARG;
+      }
+      prod *= d->dims[i];
+    }
+    if (prod != M) {
+      rimu_set_error("rimu_hv_basis_adjoint_noalloc: geometry does not match n_modes");
+      return RIMU_ERR_BADARG;
+    }
   }
   // dimension C(B, N) must fit int64 and match dim
   unsigned __int128 D = 1;
@@ -532,14 +549,6 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
   for (int i = 0; i < 3; ++i) {
     h.dims[i] = realspace ? (i < ndim ? d->dims[i] : 1) : (i == 0 ? M : 1);
     h.periodic[i] = realspace ? (i < ndim ? d->periodic[i] : 1) : 1;
-  }
-  if (realspace) {
-    int prod = 1;
-    for (int i = 0; i < ndim; ++i) prod *= h.dims[i];
-    if (prod != M) {
-      rimu_set_error("rimu_hv_basis_adjoint_noalloc: geometry does not match n_modes");
-      return RIMU_ERR_BADARG;
-    }
   }
   h.hoff = s->hoff;
   h.aoff = s->hoff;

@@ -103,3 +103,31 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_noalloc_adjoint_rejects_bad_descriptors_before_any_cuda_call():
+    """rimu_hv_basis_adjoint_noalloc repeats rimu_model_create's checks on the plain
+    description: every lattice extent at least 2 (an extent of 1 or a negative pair whose
+    product is n_modes would let neighbour sites leave the lattice) and no FermiFS flag on a
+    bosonic model.  All are rejected before the library touches a GPU."""
+    import ctypes as C
+    import numpy as np
+    lib = _lib.load()
+    buf = np.zeros(8)
+    p = C.c_void_p(buf.ctypes.data)
+    gu, gt = C.c_double(), C.c_double()
+
+    def call(desc, dim):
+        return lib.rimu_hv_basis_adjoint_noalloc(C.byref(desc), p, p, p, C.byref(gu),
+                                                 C.byref(gt), dim, None)
+
+    h = rimugpu.HubbardRealSpace(rimugpu.BoseFS([1, 0, 1, 0, 1, 0]), rimugpu.PeriodicBoundaries(2, 3))
+    for dims in ((1, 6), (-2, -3), (6, 1)):
+        d = h._desc()
+        d.dims[0], d.dims[1] = dims
+        assert call(d, 56) == _lib.RIMU_ERR_BADARG, dims
+        assert "at least 2" in _lib.last_error()
+    d = rimugpu.HubbardReal1D(rimugpu.BoseFS([1] * 4), u=1.0)._desc()
+    d.fermion = 1
+    assert call(d, 35) == _lib.RIMU_ERR_BADARG
+    assert "bosonic" in _lib.last_error()

@@ -30,7 +30,7 @@ def build(force: bool = False) -> str:
     """Compile the oracle with gcc (no FMA contraction, so float results are portable)."""
     os.makedirs(BUILD, exist_ok=True)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
+        cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
                "-o", LIB, SRC, "-lm"]
         subprocess.run(cmd, check=True)
     return LIB
@@ -103,6 +103,8 @@ def lib():
         _lib.o_diagonal_w.restype = C.c_double
         _lib.o_step_w.argtypes = [P(_OModel), P(_OParams), u64p, f64p, i64p, C.c_int64,
                                   P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
+        _lib.o_step_mt.argtypes = [P(_OModel), P(_OParams), u64p, f64p, i64p, C.c_int64, C.c_int,
+                                   C.c_int64, P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
     return _lib
 
 
@@ -354,6 +356,44 @@ def step(m: Model, prm: StepParams, keys, vals):
         v = np.ctypeslib.as_array(ov, shape=(on.value,)).copy() if on.value else np.zeros(0)
     for p in (ok, ov, oi):
         lib().o_free(C.cast(p, C.c_void_p))
+    stats = {f: getattr(st, f) for f, _ in _OStats._fields_}
+    return k, v, stats
+
+
+def step_mt(m: Model, prm: StepParams, keys, vals, threads: int = 0, mem_budget: float = 8e9,
+            sort: bool = True):
+    """One projector step on `threads` host threads (0: all), restating the PDVec step
+    (perform_spawns!, collect_local!, move_and_compress!, pdworkingmemory.jl:191-309).  Same
+    results as step(); the output is sorted only when `sort`.  Contributions beyond
+    `mem_budget` bytes are processed in passes.  Addresses of at most 64 bits, no initiator
+    rule."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    n = len(keys)
+    is_int = prm.style == STYLE_INTEGER
+    fv = np.ascontiguousarray(vals if not is_int else np.zeros(n), dtype=np.float64)
+    iv = np.ascontiguousarray(vals if is_int else np.zeros(n), dtype=np.int64)
+    ok, ov, oi = C.POINTER(C.c_uint64)(), C.POINTER(C.c_double)(), C.POINTER(C.c_int64)()
+    on = C.c_int64()
+    st = _OStats()
+    ms, ps = m.struct(), prm.struct()
+    rc = lib().o_step_mt(C.byref(ms), C.byref(ps), _p(keys, C.c_uint64), _p(fv, C.c_double),
+                         _p(iv, C.c_int64), n, int(threads), int(mem_budget), C.byref(ok),
+                         C.byref(ov), C.byref(oi), C.byref(on), C.byref(st))
+    if rc == 2:
+        raise ValueError("step_mt: needs addresses of at most 64 bits and no initiator rule")
+    if rc != 0:
+        raise MemoryError("oracle step failed")
+    nn = on.value
+    k = np.ctypeslib.as_array(ok, shape=(nn,)).copy() if nn else np.zeros(0, np.uint64)
+    if is_int:
+        v = np.ctypeslib.as_array(oi, shape=(nn,)).copy() if nn else np.zeros(0, np.int64)
+    else:
+        v = np.ctypeslib.as_array(ov, shape=(nn,)).copy() if nn else np.zeros(0)
+    for p in (ok, ov, oi):
+        lib().o_free(C.cast(p, C.c_void_p))
+    if sort:
+        order = np.argsort(k, kind="stable")
+        k, v = k[order], v[order]
     stats = {f: getattr(st, f) for f, _ in _OStats._fields_}
     return k, v, stats
 

@@ -672,10 +672,126 @@ static void o_initiator_value(const o_params *p, const double f[3], const int64_
   }
 }
 
+/* Receiver of the contributions of one column: (target address, class, kind 0 = diagonal
+ * term / 1 = spawn, float value, integer value). */
+typedef void (*o_emit_fn)(void *ctx, okey key, int cls, int kind, double v, int64_t iv);
+
+/* The contributions of one source walker (apply_column!, styles.jl:21-25, 101-105, 210-214):
+ * its diagonal step and its spawns, handed to `emit`; the statistics go to *st and the spawn
+ * magnitudes (float walkers) to *spawn_acc in exact fixed point. */
+static void o_apply_column(const o_model *h, const o_params *p, okey key, double sval,
+                           int64_t sival, o_emit_fn emit, void *ctx, o_stats *st,
+                           o_u128 *spawn_acc) {
+  const int is_int = p->style == O_STYLE_INTEGER;
+  double val = is_int ? (double)sival : sval;
+  /* classes of this walker's contributions (_default_to_initiator_value,
+   * initiators.jl:142-157): its diagonal term counts as "initiator" and its spawns as
+   * "safe" when |value| > threshold, else as "safe" and "unsafe" */
+  const int parent_init = fabs(val) > p->init_threshold;
+  const int diag_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
+                                                    : (parent_init ? O_CLS_INITIATOR : O_CLS_SAFE);
+  const int spawn_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
+                                                     : (parent_init ? O_CLS_SAFE : O_CLS_UNSAFE);
+  /* ---- diagonal_step! (spawning.jl:73-77) ---- */
+  double x = o_t_diag(h, p, key) * val;
+  if (is_int) {
+    uint32_t r[4];
+    o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+    int64_t res = o_round_int(x, o_u53(r));
+    int64_t v = sival;
+    if (res != 0) emit(ctx, key, diag_cls, 0, 0.0, res);
+    /* clones_deaths_zombies, spawning.jl:79-93 */
+    int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+    if (res > v) st->clones += res - v;
+    else if (sr != sv) { st->deaths += v < 0 ? -v : v; st->zombies += res < 0 ? -res : res; }
+    else st->deaths += (res - v) < 0 ? v - res : res - v;
+  } else {
+    double res = x;
+    if (p->proj_threshold > 0) {
+      uint32_t r[4];
+      o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
+      res = o_project(x, p->proj_threshold, o_u53(r));
+    }
+    if (res != 0.0) emit(ctx, key, diag_cls, 0, res, 0);
+  }
+  /* ---- spawn! ---- */
+  int noff = o_noff(h, key);
+  int exact = 0;
+  if (p->style == O_STYLE_DETERMINISTIC) {
+    exact = 1;                       /* apply_column! returns (1,), styles.jl:101-105 */
+    st->exact_steps++;
+  } else if (p->style == O_STYLE_DSS) {
+    /* DynamicSemistochastic, spawning.jl:364-378 */
+    double thresh = p->abs_threshold < (double)noff ? p->abs_threshold : (double)noff;
+    double amount = p->boost * fabs(val) * p->rel_threshold;
+    exact = amount >= thresh;
+    if (exact) st->exact_steps++; else st->inexact_steps++;
+  }
+  /* IsStochasticInteger always samples (WithReplacement); a column without offdiagonals
+   * has nothing to sample from. */
+  if (noff == 0) return;
+  if (exact) {
+    /* Exact, spawning.jl:174-182: deposit val * mat_elem for every offdiagonal. */
+    st->spawn_attempts += noff;
+    for (int c = 1; c <= noff; ++c) {
+      okey nk; double hv; long prod;
+      o_offdiag_k(h, key, c, &nk, &hv, &prod);
+      double y = val * o_t_off(p, hv);
+      if (p->proj_threshold > 0 && p->style == O_STYLE_DSS) {
+        uint32_t r[4];
+        o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
+        y = o_project(y, p->proj_threshold, o_u53(r));
+      }
+      if (y != 0.0) { emit(ctx, nk, spawn_cls, 1, y, 0); *spawn_acc += o_fixed(fabs(y)); }
+    }
+    return;
+  }
+  /* WithReplacement, spawning.jl:232-243.  The per-attempt amplitude is
+   * mat_elem * magnitude / prob with magnitude = val / n_att and prob = 1 / n_off; this
+   * restatement evaluates it as mat_elem * ((val * (1/n_att)) * n_off), which is the same
+   * value up to rounding.  For integer walkers with boost 1, val / n_att = sign(val). */
+  int64_t natt = o_floor_i(fabs(val) * p->boost);
+  if (natt < 1) natt = 1;
+  st->spawn_attempts += natt;
+  double c;
+  if (is_int && p->boost == 1.0) c = (val < 0 ? -1.0 : 1.0) * (double)noff;
+  else c = (val * o_recip(natt)) * (double)noff;
+  /* Float walkers without on-the-fly projection need only the offdiagonal index per
+   * attempt: attempt j takes word j % 4 of Philox block j / 4.  Otherwise attempt j uses
+   * its own block: word 0 for the index, words 1-2 for the rounding. */
+  const int grouped = !is_int && p->proj_threshold == 0;
+  for (int64_t j = 0; j < natt; ++j) {
+    uint32_t r[4];
+    uint32_t word;
+    if (grouped) {
+      o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(j >> 2), r);
+      word = r[j & 3];
+    } else {
+      o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
+      word = r[0];
+    }
+    int chosen = (int)(((uint64_t)word * (uint64_t)noff) >> 32) + 1;
+    okey nk; double hv; long prod;
+    o_offdiag_k(h, key, chosen, &nk, &hv, &prod);
+    double y = c * o_t_off(p, hv);
+    if (is_int) {
+      int64_t k = o_round_int(y, o_u53(r));
+      if (k != 0) { emit(ctx, nk, spawn_cls, 1, 0.0, k); st->spawns += (double)(k < 0 ? -k : k); }
+    } else {
+      if (p->proj_threshold > 0) y = o_project(y, p->proj_threshold, o_u53(r));
+      if (y != 0.0) { emit(ctx, nk, spawn_cls, 1, y, 0); *spawn_acc += o_fixed(fabs(y)); }
+    }
+  }
+}
+
+static void o_emit_buf(void *ctx, okey key, int cls, int kind, double v, int64_t iv) {
+  o_push((o_buf *)ctx, key, cls, kind, v, iv);
+}
+
 /* One apply_operator! step (dictvectors.jl:112-140) from `src` into a sorted `dst`.
- * Values are doubles for the float styles and int64 (passed as double-typed storage of
- * the same bits is NOT used: separate arrays) for IsStochasticInteger.
- * Returns 0 on success, nonzero on allocation failure.  *dst arrays are malloc'd. */
+ * Values are doubles for the float styles and int64 (separate arrays) for
+ * IsStochasticInteger.  Returns 0 on success, nonzero on allocation failure.  *dst arrays
+ * are malloc'd. */
 static int o_step_k(const o_model *h, const o_params *p,
                     const okey *skeys, const double *svals, const int64_t *sivals, int64_t n,
                     okey **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
@@ -683,108 +799,9 @@ static int o_step_k(const o_model *h, const o_params *p,
   o_buf b = {0};
   int is_int = p->style == O_STYLE_INTEGER;
   o_u128 spawn_acc = 0;
-  for (int64_t e = 0; e < n; ++e) {
-    okey key = skeys[e];
-    double val = is_int ? (double)sivals[e] : svals[e];
-    /* classes of this walker's contributions (_default_to_initiator_value,
-     * initiators.jl:142-157): its diagonal term counts as "initiator" and its spawns as
-     * "safe" when |value| > threshold, else as "safe" and "unsafe" */
-    const int parent_init = fabs(val) > p->init_threshold;
-    const int diag_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
-                                                      : (parent_init ? O_CLS_INITIATOR : O_CLS_SAFE);
-    const int spawn_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
-                                                       : (parent_init ? O_CLS_SAFE : O_CLS_UNSAFE);
-    /* ---- diagonal_step! (spawning.jl:73-77) ---- */
-    double x = o_t_diag(h, p, key) * val;
-    if (is_int) {
-      uint32_t r[4];
-      o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
-      int64_t res = o_round_int(x, o_u53(r));
-      int64_t v = sivals[e];
-      if (res != 0) o_push(&b, key, diag_cls, 0, 0.0, res);
-      /* clones_deaths_zombies, spawning.jl:79-93 */
-      int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
-      if (res > v) st->clones += res - v;
-      else if (sr != sv) { st->deaths += v < 0 ? -v : v; st->zombies += res < 0 ? -res : res; }
-      else st->deaths += (res - v) < 0 ? v - res : res - v;
-    } else {
-      double res = x;
-      if (p->proj_threshold > 0) {
-        uint32_t r[4];
-        o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
-        res = o_project(x, p->proj_threshold, o_u53(r));
-      }
-      if (res != 0.0) o_push(&b, key, diag_cls, 0, res, 0);
-    }
-    /* ---- spawn! ---- */
-    int noff = o_noff(h, key);
-    int exact = 0;
-    if (p->style == O_STYLE_DETERMINISTIC) {
-      exact = 1;                       /* apply_column! returns (1,), styles.jl:101-105 */
-      st->exact_steps++;
-    } else if (p->style == O_STYLE_DSS) {
-      /* DynamicSemistochastic, spawning.jl:364-378 */
-      double thresh = p->abs_threshold < (double)noff ? p->abs_threshold : (double)noff;
-      double amount = p->boost * fabs(val) * p->rel_threshold;
-      exact = amount >= thresh;
-      if (exact) st->exact_steps++; else st->inexact_steps++;
-    }
-    /* IsStochasticInteger always samples (WithReplacement); a column without offdiagonals
-     * has nothing to sample from. */
-    if (noff == 0) continue;
-    if (exact) {
-      /* Exact, spawning.jl:174-182: deposit val * mat_elem for every offdiagonal. */
-      st->spawn_attempts += noff;
-      for (int c = 1; c <= noff; ++c) {
-        okey nk; double hv; long prod;
-        o_offdiag_k(h, key, c, &nk, &hv, &prod);
-        double y = val * o_t_off(p, hv);
-        if (p->proj_threshold > 0 && p->style == O_STYLE_DSS) {
-          uint32_t r[4];
-          o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(c - 1), r);
-          y = o_project(y, p->proj_threshold, o_u53(r));
-        }
-        if (y != 0.0) { o_push(&b, nk, spawn_cls, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
-      }
-      continue;
-    }
-    /* WithReplacement, spawning.jl:232-243.  The per-attempt amplitude is
-     * mat_elem * magnitude / prob with magnitude = val / n_att and prob = 1 / n_off; this
-     * restatement evaluates it as mat_elem * ((val * (1/n_att)) * n_off), which is the same
-     * value up to rounding.  For integer walkers with boost 1, val / n_att = sign(val). */
-    int64_t natt = o_floor_i(fabs(val) * p->boost);
-    if (natt < 1) natt = 1;
-    st->spawn_attempts += natt;
-    double c;
-    if (is_int && p->boost == 1.0) c = (val < 0 ? -1.0 : 1.0) * (double)noff;
-    else c = (val * o_recip(natt)) * (double)noff;
-    /* Float walkers without on-the-fly projection need only the offdiagonal index per
-     * attempt: attempt j takes word j % 4 of Philox block j / 4.  Otherwise attempt j uses
-     * its own block: word 0 for the index, words 1-2 for the rounding. */
-    const int grouped = !is_int && p->proj_threshold == 0;
-    for (int64_t j = 0; j < natt; ++j) {
-      uint32_t r[4];
-      uint32_t word;
-      if (grouped) {
-        o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)(j >> 2), r);
-        word = r[j & 3];
-      } else {
-        o_draw_k(p->seed, O_PURPOSE_SPAWN, p->replica, p->step, key, (uint32_t)j, r);
-        word = r[0];
-      }
-      int chosen = (int)(((uint64_t)word * (uint64_t)noff) >> 32) + 1;
-      okey nk; double hv; long prod;
-      o_offdiag_k(h, key, chosen, &nk, &hv, &prod);
-      double y = c * o_t_off(p, hv);
-      if (is_int) {
-        int64_t k = o_round_int(y, o_u53(r));
-        if (k != 0) { o_push(&b, nk, spawn_cls, 1, 0.0, k); st->spawns += (double)(k < 0 ? -k : k); }
-      } else {
-        if (p->proj_threshold > 0) y = o_project(y, p->proj_threshold, o_u53(r));
-        if (y != 0.0) { o_push(&b, nk, spawn_cls, 1, y, 0); spawn_acc += o_fixed(fabs(y)); }
-      }
-    }
-  }
+  for (int64_t e = 0; e < n; ++e)
+    o_apply_column(h, p, skeys[e], is_int ? 0.0 : svals[e], is_int ? sivals[e] : 0, o_emit_buf,
+                   &b, st, &spawn_acc);
   if (b.err) { free(b.c); return 1; }
   if (!is_int) st->spawns = o_fixed_to_double(spawn_acc);
   /* ---- annihilation: sum the contributions per address ----
@@ -895,6 +912,300 @@ int o_step_w(const o_model *h, const o_params *p,
 }
 
 /* ------------------------------------------------------------------------------------ */
+/* Threaded step: the PDVec working-memory step (pdworkingmemory.jl:191-309) on all cores  */
+/* ------------------------------------------------------------------------------------ */
+/* The reference's PDVec splits the vector into segments by a hash of the address
+ * (fastrange_hash, pdvec.jl:6-9) and steps it in three parallel phases:
+ *   perform_spawns!    every thread applies the columns of its source segment and deposits
+ *                      each contribution into its own dictionary for the target's segment
+ *                      (pdworkingmemory.jl:191-217);
+ *   collect_local!     per target segment, the threads' dictionaries are summed into one
+ *                      (:228-235);
+ *   move_and_compress! per segment, the sums become the new vector, compressed (:262-273).
+ * This restatement keeps the phases: per-thread buffers of contributions tagged with their
+ * target segment, then one thread per segment sums its contributions in an open-addressing
+ * hash table and compresses.  Sums follow the summation rule of o_step_k (exact fixed point
+ * when every contribution allows it, else the canonical order), so the result equals
+ * o_step_k's for any thread count.  When the contributions of one step would exceed
+ * `mem_budget` bytes, the segments are processed in passes and the columns re-applied in
+ * each pass (their draws are counter-based, so every pass sees the same contributions).
+ * Addresses of at most 64 bits, no initiator rule. */
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { uint64_t key; uint64_t vb; uint32_t row; uint32_t kind; } o_rec;   /* 24 B */
+typedef struct { o_rec *r; int64_t n, cap; int err; } o_rbuf;
+typedef struct { o_rbuf *buf; int pass, rows_per_pass, rows; int is_int; } o_mtctx;
+
+static uint32_t o_row_of(uint64_t key, int rows) {       /* fastrange on a mixed hash */
+  return (uint32_t)(((unsigned __int128)o_mix64(key) * (uint64_t)rows) >> 64);
+}
+static void o_emit_rec(void *vctx, okey key, int cls, int kind, double v, int64_t iv) {
+  (void)cls;
+  o_mtctx *c = (o_mtctx *)vctx;
+  const uint64_t k = o_lo(key);
+  const uint32_t row = o_row_of(k, c->rows);
+  if ((int)(row / (uint32_t)c->rows_per_pass) != c->pass) return;
+  o_rbuf *b = c->buf;
+  if (b->n == b->cap) {
+    int64_t nc = b->cap ? 2 * b->cap : 4096;
+    o_rec *q = realloc(b->r, (size_t)nc * sizeof(o_rec));
+    if (!q) { b->err = 1; return; }
+    b->r = q; b->cap = nc;
+  }
+  uint64_t vb;
+  if (c->is_int) vb = (uint64_t)iv; else memcpy(&vb, &v, 8);
+  b->r[b->n].key = k; b->r[b->n].vb = vb; b->r[b->n].row = row; b->r[b->n].kind = (uint32_t)kind;
+  b->n++;
+}
+
+/* One slot of a segment's table: the address, the head of its contribution list, whether
+ * every contribution so far is exact in fixed point, and their fixed-point (or integer) sum. */
+typedef struct { uint64_t key; int64_t head; int used, exact; __int128 fx; } o_slot;
+typedef struct { uint64_t ob; int kind; } o_ord;
+static int o_cmp_ord(const void *a, const void *b) {
+  const o_ord *x = a, *y = b;
+  if (x->kind != y->kind) return x->kind < y->kind ? -1 : 1;
+  return x->ob < y->ob ? -1 : x->ob > y->ob;
+}
+
+/* collect_local! + move_and_compress! of one segment: `rec` holds its m contributions.
+ * Writes the surviving entries to (ok, ov, oi) and returns their number, or -1 when out of
+ * memory; *len_before and *acc get the compression statistic and the exact norm. */
+static int64_t o_reduce_segment(const o_params *p, const o_rec *rec, int64_t m, uint64_t *ok,
+                                double *ov, int64_t *oi, int64_t *len_before, o_u128 *acc) {
+  const int is_int = p->style == O_STYLE_INTEGER;
+  int64_t T = 16;
+  while (T < 2 * m) T <<= 1;
+  o_slot *tab = calloc((size_t)T, sizeof(o_slot));
+  int64_t *nxt = malloc((size_t)(m ? m : 1) * sizeof(int64_t));
+  if (!tab || !nxt) { free(tab); free(nxt); return -1; }
+  for (int64_t c = 0; c < m; ++c) {
+    int64_t sl = (int64_t)((o_mix64(rec[c].key) * 0x9E3779B97F4A7C15ull) >> 20) & (T - 1);
+    while (tab[sl].used && tab[sl].key != rec[c].key) sl = (sl + 1) & (T - 1);
+    o_slot *s = &tab[sl];
+    if (!s->used) { s->used = 1; s->key = rec[c].key; s->head = -1; s->exact = 1; s->fx = 0; }
+    if (is_int) {
+      s->fx += (int64_t)rec[c].vb;
+    } else if (s->exact) {
+      double v; memcpy(&v, &rec[c].vb, 8);
+      __int128 t;
+      if (o_to_fixed(v, &t)) s->fx += t; else s->exact = 0;
+    }
+    nxt[c] = s->head;
+    s->head = c;
+  }
+  int64_t q = 0, cap_ord = 0;
+  o_ord *ord = NULL;
+  for (int64_t i = 0; i < T; ++i) {
+    const o_slot *s = &tab[i];
+    if (!s->used) continue;
+    double w = 0.0;
+    int64_t wi = 0;
+    if (is_int) {
+      wi = (int64_t)s->fx;
+      if (wi == 0) continue;
+    } else {
+      if (s->exact) {
+        w = o_fixed_signed_to_double(s->fx);
+      } else {
+        /* canonical order: the diagonal term, then the spawns by increasing value */
+        int64_t k = 0;
+        for (int64_t c = s->head; c >= 0; c = nxt[c]) ++k;
+        if (k > cap_ord) {
+          o_ord *no = realloc(ord, (size_t)k * sizeof(o_ord));
+          if (!no) { free(ord); free(tab); free(nxt); return -1; }
+          ord = no; cap_ord = k;
+        }
+        k = 0;
+        for (int64_t c = s->head; c >= 0; c = nxt[c]) {
+          double v; memcpy(&v, &rec[c].vb, 8);
+          ord[k].ob = o_ordered_bits(v); ord[k].kind = (int)rec[c].kind; ++k;
+        }
+        qsort(ord, (size_t)k, sizeof(o_ord), o_cmp_ord);
+        for (int64_t j = 0; j < k; ++j) {
+          const uint64_t o = ord[j].ob;
+          const uint64_t u = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+          double v; memcpy(&v, &u, 8);
+          w = j == 0 ? v : w + v;
+        }
+      }
+      if (w == 0.0) continue;
+    }
+    ++*len_before;
+    if (!is_int && p->compression > 0) {    /* compression.jl:18-42 */
+      const double prob = (p->compression == 1.0) ? fabs(w) : fabs(w) / p->compression;
+      if (prob < 1) {
+        uint32_t r[4];
+        o_draw_k(p->seed, O_PURPOSE_COMPRESS, p->replica, p->step, (okey)s->key, 0, r);
+        w = o_bernoulli(o_u53(r), prob) ? (w < 0 ? -p->compression : p->compression) : 0.0;
+      }
+      if (w == 0.0) continue;
+    }
+    ok[q] = s->key; ov[q] = is_int ? 0.0 : w; oi[q] = is_int ? wi : 0;
+    *acc += o_fixed(fabs(is_int ? (double)wi : w));
+    ++q;
+  }
+  free(ord); free(tab); free(nxt);
+  return q;
+}
+
+/* One step on `nthreads` threads (0: all available); same arguments and results as o_step
+ * except that the output is not sorted.  Returns 0 on success, 1 when out of memory, 2 for
+ * an unsupported model or rule. */
+int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const double *svals,
+              const int64_t *sivals, int64_t n, int nthreads, int64_t mem_budget,
+              uint64_t **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
+  memset(st, 0, sizeof(*st));
+  if (p->init_rule != O_INIT_NONE) return 2;
+  {
+    int B = h->ncomp == 2 ? o_comp_bits(h, 0) + o_comp_bits(h, 1)
+                          : (h->fermion ? h->M : h->N + h->M - 1);
+    if (B > 64) return 2;
+  }
+  int nt = 1;
+#ifdef _OPENMP
+  nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+  (void)nthreads;
+#endif
+  const int is_int = p->style == O_STYLE_INTEGER;
+  /* contributions of the step (an upper bound: the diagonal term and every unit) */
+  int64_t total = 0;
+#pragma omp parallel for num_threads(nt) reduction(+ : total) schedule(static)
+  for (int64_t e = 0; e < n; ++e) {
+    const double val = is_int ? (double)sivals[e] : svals[e];
+    const int noff = o_noff(h, (okey)skeys[e]);
+    int64_t units = noff;
+    if (p->style == O_STYLE_INTEGER || (p->style == O_STYLE_DSS &&
+        !(p->boost * fabs(val) * p->rel_threshold >=
+          (p->abs_threshold < (double)noff ? p->abs_threshold : (double)noff)))) {
+      int64_t natt = o_floor_i(fabs(val) * p->boost);
+      units = noff == 0 ? 0 : (natt < 1 ? 1 : natt);
+    }
+    total += 1 + units;
+  }
+  const int64_t per_rec = 2 * (int64_t)sizeof(o_rec);   /* thread buffers + grouped copy */
+  int passes = 1;
+  if (mem_budget > 0 && total * per_rec > mem_budget)
+    passes = (int)((total * per_rec + mem_budget - 1) / mem_budget);
+  const int rows_per_pass = 8 * nt;
+  const int rows = passes * rows_per_pass;
+  o_rbuf *bufs = calloc((size_t)nt, sizeof(o_rbuf));
+  o_stats *tst = calloc((size_t)nt, sizeof(o_stats));
+  o_u128 *tacc = calloc((size_t)nt, sizeof(o_u128)), *tspawn = calloc((size_t)nt, sizeof(o_u128));
+  int64_t *tlb = calloc((size_t)nt, sizeof(int64_t));
+  /* per-segment outputs, concatenated at the end */
+  uint64_t **sk = calloc((size_t)rows, sizeof(uint64_t *));
+  double **sv = calloc((size_t)rows, sizeof(double *));
+  int64_t **si = calloc((size_t)rows, sizeof(int64_t *));
+  int64_t *sn = calloc((size_t)rows, sizeof(int64_t));
+  int64_t *cnt = calloc((size_t)nt * rows_per_pass + 1, sizeof(int64_t));
+  int err = !bufs || !tst || !tacc || !tspawn || !tlb || !sk || !sv || !si || !sn || !cnt;
+  for (int pass = 0; pass < passes && !err; ++pass) {
+    /* ---- perform_spawns!: each thread into its own buffer ---- */
+#pragma omp parallel num_threads(nt)
+    {
+      int t = 0;
+#ifdef _OPENMP
+      t = omp_get_thread_num();
+#endif
+      o_mtctx ctx = {&bufs[t], pass, rows_per_pass, rows, is_int};
+      bufs[t].n = 0;
+      o_stats junk;
+      o_u128 junk_acc = 0;
+      o_stats *stp = pass == 0 ? &tst[t] : &junk;
+      o_u128 *accp = pass == 0 ? &tspawn[t] : &junk_acc;
+#pragma omp for schedule(dynamic, 1024)
+      for (int64_t e = 0; e < n; ++e)
+        o_apply_column(h, p, (okey)skeys[e], is_int ? 0.0 : svals[e], is_int ? sivals[e] : 0,
+                       o_emit_rec, &ctx, stp, accp);
+    }
+    for (int t = 0; t < nt; ++t) err |= bufs[t].err;
+    if (err) break;
+    /* ---- group by segment: counts per (thread, segment), then a stable scatter ---- */
+    const int R = rows_per_pass;
+    memset(cnt, 0, ((size_t)nt * R + 1) * sizeof(int64_t));
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t)
+      for (int64_t i = 0; i < bufs[t].n; ++i) cnt[(size_t)(bufs[t].r[i].row % R) * nt + t + 1]++;
+    for (size_t i = 1; i <= (size_t)nt * R; ++i) cnt[i] += cnt[i - 1];
+    const int64_t m_all = cnt[(size_t)nt * R];
+    o_rec *grp = malloc((size_t)(m_all ? m_all : 1) * sizeof(o_rec));
+    if (!grp) { err = 1; break; }
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+      int64_t *pos = malloc((size_t)R * sizeof(int64_t));
+      if (!pos) { bufs[t].err = 1; continue; }
+      for (int r = 0; r < R; ++r) pos[r] = cnt[(size_t)r * nt + t];
+      for (int64_t i = 0; i < bufs[t].n; ++i) grp[pos[bufs[t].r[i].row % R]++] = bufs[t].r[i];
+      free(pos);
+    }
+    for (int t = 0; t < nt; ++t) err |= bufs[t].err;
+    /* ---- collect_local! + move_and_compress!, one segment per task ---- */
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+    for (int r = 0; r < R; ++r) {
+      if (err) continue;
+      int t = 0;
+#ifdef _OPENMP
+      t = omp_get_thread_num();
+#endif
+      const int64_t b0 = cnt[(size_t)r * nt], m = cnt[(size_t)(r + 1) * nt] - b0;
+      const int g = pass * R + r;
+      sk[g] = malloc((size_t)(m ? m : 1) * 8);
+      sv[g] = malloc((size_t)(m ? m : 1) * 8);
+      si[g] = malloc((size_t)(m ? m : 1) * 8);
+      if (!sk[g] || !sv[g] || !si[g]) { err = 1; continue; }
+      const int64_t q = o_reduce_segment(p, grp + b0, m, sk[g], sv[g], si[g], &tlb[t], &tacc[t]);
+      if (q < 0) err = 1; else sn[g] = q;
+    }
+    free(grp);
+  }
+  int64_t tot = 0;
+  for (int g = 0; g < rows && !err; ++g) tot += sn[g];
+  uint64_t *ok = NULL; double *ov = NULL; int64_t *oi = NULL;
+  if (!err) {
+    ok = malloc((size_t)(tot ? tot : 1) * 8);
+    ov = malloc((size_t)(tot ? tot : 1) * 8);
+    oi = malloc((size_t)(tot ? tot : 1) * 8);
+    if (!ok || !ov || !oi) err = 1;
+  }
+  if (!err) {
+    int64_t o = 0;
+    for (int g = 0; g < rows; ++g) {
+      memcpy(ok + o, sk[g], (size_t)sn[g] * 8);
+      memcpy(ov + o, sv[g], (size_t)sn[g] * 8);
+      memcpy(oi + o, si[g], (size_t)sn[g] * 8);
+      o += sn[g];
+    }
+    o_u128 acc = 0, sacc = 0;
+    for (int t = 0; t < nt; ++t) {
+      acc += tacc[t]; sacc += tspawn[t];
+      st->len_before += tlb[t];
+      st->exact_steps += tst[t].exact_steps; st->inexact_steps += tst[t].inexact_steps;
+      st->spawn_attempts += tst[t].spawn_attempts; st->spawns += tst[t].spawns;
+      st->clones += tst[t].clones; st->deaths += tst[t].deaths; st->zombies += tst[t].zombies;
+    }
+    if (!is_int) st->spawns = o_fixed_to_double(sacc);
+    st->norm = o_fixed_to_double(acc);
+    st->len = tot;
+    *okeys = ok; *ovals = ov; *oivals = oi; *on = tot;
+  } else {
+    free(ok); free(ov); free(oi);
+  }
+  for (int t = 0; bufs && t < nt; ++t) free(bufs[t].r);
+  for (int g = 0; g < rows; ++g) {
+    if (sk) free(sk[g]);
+    if (sv) free(sv[g]);
+    if (si) free(si[g]);
+  }
+  free(bufs); free(tst); free(tacc); free(tspawn); free(tlb); free(sk); free(sv); free(si);
+  free(sn); free(cnt);
+  return err ? 1 : 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
 /* Matrix-free product on the full sorted basis (abstractdvec.jl:275-284 in pull form).  */
 /* ------------------------------------------------------------------------------------ */
 static int64_t o_bsearch(const uint64_t *keys, int64_t n, uint64_t k) {
@@ -912,6 +1223,8 @@ static int64_t o_bsearch(const uint64_t *keys, int64_t n, uint64_t k) {
  * fused multiply-adds in offdiagonal order. Returns number of missing targets (0). */
 int64_t o_hv_basis(const o_model *h, const uint64_t *keys, int64_t D, const double *v, double *w) {
   int64_t missing = 0;
+  /* rows are independent: the threads change nothing in any row's arithmetic */
+#pragma omp parallel for reduction(+ : missing) schedule(dynamic, 4096)
   for (int64_t i = 0; i < D; ++i) {
     double acc = o_diagonal(h, keys[i]) * v[i];
     int noff = o_num_offdiagonals(h, keys[i]);
@@ -939,7 +1252,12 @@ int64_t o_hv_basis(const o_model *h, const uint64_t *keys, int64_t D, const doub
 int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, const double *v,
                            const double *gw, double *gv, double *gu, double *gt) {
   int64_t missing = 0;
-  double su = 0.0, st = 0.0;
+  /* the rows in parallel (kg_i and gv_i depend on row i alone), then the two sums in row
+   * order on one thread: the same arithmetic as a single sequential pass */
+  double *kgs = malloc((size_t)(D ? D : 1) * sizeof(double));
+  long *bhis = malloc((size_t)(D ? D : 1) * sizeof(long));
+  if (!kgs || !bhis) { free(kgs); free(bhis); return -1; }
+#pragma omp parallel for reduction(+ : missing) schedule(dynamic, 4096)
   for (int64_t i = 0; i < D; ++i) {
     int onr[2 * O_MAXM];
     o_to_onr(h, keys[i], onr);
@@ -956,9 +1274,15 @@ int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, co
       kg = fma(-sqrt((double)prod), gw[j], kg);   /* K_ij = dH_ij/dt = -sqrt(prod) */
     }
     gv[i] = fma(h->t, kg, o_diagonal(h, keys[i]) * gw[i]);
-    su = fma(gw[i], (double)bhi / 2 * v[i], su);
-    st = fma(v[i], kg, st);
+    kgs[i] = kg;
+    bhis[i] = bhi;
   }
+  double su = 0.0, st = 0.0;
+  for (int64_t i = 0; i < D; ++i) {
+    su = fma(gw[i], (double)bhis[i] / 2 * v[i], su);
+    st = fma(v[i], kgs[i], st);
+  }
+  free(kgs); free(bhis);
   *gu = su;
   *gt = st;
   return missing;

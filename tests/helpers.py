@@ -73,19 +73,46 @@ def assert_same_step(gpu, ora, style):
         assert gs[k] == os_[k], (k, gs[k], os_[k])
 
 
-def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=None, seed=0x5EED):
+def oracle_mem_budget():
+    """Bytes the threaded oracle may hold for one step's contributions: a third of the
+    memory available, at most 48 GB."""
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    return min(48e9, int(ln.split()[1]) * 1024 / 3)
+    except OSError:
+        pass
+    return 8e9
+
+
+def popcount64(x):
+    """Number of set bits of each element of a uint64 array."""
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    table = np.array([bin(i).count("1") for i in range(256)], dtype=np.int64)
+    return table[x.view(np.uint8)].reshape(-1, 8).sum(axis=1)
+
+
+def run_trajectory(h, style, start, steps, dt, shift=None, boost=1.0, target=None, seed=0x5EED,
+                   threaded=False, wm=None):
     """`steps` steps from `start` on the GPU and in the oracle, compared after every step;
-    with `target`, DoubleLogUpdate on the (identical) norm."""
+    with `target`, DoubleLogUpdate on the (identical) norm.  `threaded` follows the GPU with
+    the oracle's multi-threaded step (the same results, faster on large lists)."""
     m = oracle_model(h)
     wide = h.address.nbits > 64     # two-chunk addresses travel as Python ints
-    keys = np.array([a.key for a in start], dtype=object if wide else np.uint64)
-    vals = np.array(list(start.values()), dtype=np.int64 if style.valtype is int else np.float64)
-    S = h.diagonal_element(next(iter(start))) if shift is None else shift
+    if isinstance(start, tuple):    # (keys, values) arrays; needs `shift`
+        keys, vals = start
+        S = float(shift)
+    else:
+        keys = np.array([a.key for a in start], dtype=object if wide else np.uint64)
+        vals = np.array(list(start.values()), dtype=np.int64 if style.valtype is int else np.float64)
+        S = h.diagonal_element(next(iter(start))) if shift is None else shift
     pnorm = float(np.abs(vals).sum())
-    wm = R.GPUWorkingMemory(seed)
+    wm = wm or R.GPUWorkingMemory(seed)
+    ostep = (lambda *a: O.step_mt(*a, mem_budget=oracle_mem_budget())) if threaded else O.step
     for step in range(1, steps + 1):
         g = gpu_step(h, style, keys, vals, dt, S, seed, step, boost=boost, wm=wm)
-        o = O.step(m, oracle_params(style, dt, S, seed, step, boost=boost), keys, vals)
+        o = ostep(m, oracle_params(style, dt, S, seed, step, boost=boost), keys, vals)
         assert_same_step(g, o, style)
         keys, vals = o[0], o[1]
         if len(keys) == 0:

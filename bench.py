@@ -133,53 +133,35 @@ def reduce_over_ranks(dist, ms, walker_steps, device):
 
 
 # --------------------------------------------------------------------------------------------
-# CPU baseline: the oracle step (single thread per process) on a bounded sample
+# CPU baseline: the oracle's threaded step (the PDVec step restated in C with OpenMP) on one
+# shared walker list, all host cores
 # --------------------------------------------------------------------------------------------
-def _cpu_worker(args):
-    keys, vals, shift, seconds, seed = args
+def cpu_steps(keys, vals, shift, seconds, min_steps=1, max_steps=10 ** 9, target=None,
+              pnorm=None, step0=1, seed=0x5EED):
+    """Steps the walker list (keys, vals) with the oracle's threaded step (all host threads)
+    until `seconds` have passed (at least `min_steps`, at most `max_steps`), with
+    DoubleLogUpdate towards `target` when given.  Returns (walker-steps/s over the steps,
+    steps, seconds, final keys, vals, shift, norm)."""
     import numpy as np
     import oracle as O
     m = O.real1d(20, 20, 4.0, 1.0)
-    norm0 = float(np.abs(vals).sum())
-    t0 = time.time()
-    steps = 0
-    walkers = 0.0
+    dt = 1e-3
+    S = shift
+    pn = float(np.abs(vals).sum()) if pnorm is None else pnorm
+    walkers, elapsed, steps = 0.0, 0.0, 0
     k, v = keys, vals
-    while time.time() - t0 < seconds:
-        p = O.StepParams(O.STYLE_DSS, dt=1e-3, shift=shift, seed=seed, step=steps + 1, compression=1.0)
-        k2, v2, st = O.step(m, p, k, v)
+    while steps < max_steps and (steps < min_steps or elapsed < seconds):
+        p = O.StepParams(O.STYLE_DSS, dt=dt, shift=S, seed=seed, step=step0 + steps,
+                         compression=1.0)
+        t0 = time.perf_counter()
+        k, v, st = O.step_mt(m, p, k, v, sort=False, bits=True, mem_budget=64e9)
+        elapsed += time.perf_counter() - t0
         walkers += st["norm"]
         steps += 1
-        # keep the sample size bounded: restart from the sample
-        k, v = (k2, v2) if st["norm"] < 2 * norm0 else (keys, vals)
-    return walkers, time.time() - t0, steps
-
-
-def cpu_baseline(keys, vals, shift, seconds, procs, pool=None):
-    """Walker-steps/s of `procs` processes stepping independent copies of the sample for
-    `seconds` each (timed inside the workers), and the oracle steps they made; `pool` is an
-    open spawn pool of `procs` workers to reuse, else one is made for this call."""
-    import multiprocessing as mp
-    jobs = [(keys, vals, shift, seconds, 1000 + i) for i in range(procs)]
-    if procs == 1 and pool is None:
-        res = [_cpu_worker(jobs[0])]
-    elif pool is not None:
-        res = pool.map(_cpu_worker, jobs)
-    else:
-        with mp.get_context("spawn").Pool(procs) as own:
-            res = own.map(_cpu_worker, jobs)
-    walkers = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    return walkers / wall, sum(r[2] for r in res)
-
-
-def sample_state(keys, vals, target_norm, rng):
-    """A bounded random sample of the walker list with about target_norm walkers."""
-    import numpy as np
-    norm = float(np.abs(vals).sum())
-    frac = min(1.0, target_norm / max(norm, 1.0))
-    idx = np.nonzero(rng.random(len(keys)) < frac)[0]
-    return np.ascontiguousarray(keys[idx]), np.ascontiguousarray(vals[idx])
+        if target is not None and st["len"]:
+            S -= 0.08 ** 2 / 4 / dt * math.log(st["norm"] / target) + 0.08 / dt * math.log(st["norm"] / pn)
+            pn = st["norm"]
+    return walkers / max(elapsed, 1e-9), steps, elapsed, k, v, S, pn
 
 
 # --------------------------------------------------------------------------------------------
@@ -333,7 +315,7 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_batch:
         batch_res = bench_batched(R, torch)
 
-    # ---- CPU baseline (oracle port) on a bounded sample ----
+    # ---- CPU baseline: the threaded oracle step on this run's own list ----
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         import numpy as np
@@ -342,13 +324,15 @@ def run_ours(args, ws, rank, local):
         else:
             keys, vals = s.v.download()
             shift_c = s.shift_parameters.shift
-        smp_k, smp_v = sample_state(keys, vals, args.cpu_sample, np.random.default_rng(1))
         import oracle
         oracle.build()
-        thr, nsteps = cpu_baseline(smp_k, smp_v, shift_c, args.cpu_seconds, 1)
-        cpu = {"value": thr, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{len(smp_k)} walkers (norm {float(np.abs(smp_v).sum()):.3g}) sampled from the "
-                         f"steady-state list; {nsteps} oracle steps in {args.cpu_seconds:.0f} s, one thread"}
+        thr, nsteps, secs, *_ = cpu_steps(keys, vals, shift_c, args.cpu_seconds, min_steps=1,
+                                          max_steps=4, step0=10 ** 7)
+        cpu = {"value": thr, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{nsteps} step(s) of the GPU run's own steady-state list ({len(keys)} "
+                         f"entries, norm {float(np.abs(vals).sum()):.3g}) by the oracle's threaded "
+                         f"step (PDVec restated in C/OpenMP, one shared list, "
+                         f"{os.cpu_count()} threads), {secs:.1f} s"}
 
     if rank == 0:
         line = {
@@ -498,50 +482,49 @@ def bench_hv(R, torch, peak):
 # Reference arm: the CPU restatement of the reference step, all host cores
 # --------------------------------------------------------------------------------------------
 def run_reference(args, ws, rank, local):
+    """The reference's CPU step restated: the oracle's threaded step (perform_spawns!,
+    collect_local!, move_and_compress! of the PDVec, pdworkingmemory.jl:191-309, in C with
+    OpenMP) on one shared walker list on every host core.  The population is grown from the
+    unit-filling address by the same step (DoubleLogUpdate towards --ref-target, bounded by
+    --ref-prep-seconds); then W untimed and K timed steps, each one full step of the list."""
     if rank != 0:
         return
     import numpy as np
     import oracle as O
     O.build()
-    # bounded sample: a population grown with the oracle itself from the start address
-    m = O.real1d(20, 20, 4.0, 1.0)
+    target = args.ref_target
     k0 = O.bose_key([1] * 20)
-    keys, vals = np.array([k0], dtype=np.uint64), np.array([10.0])
-    S, pn = 0.0, 10.0
-    target = args.cpu_sample
-    step = 0
-    while float(np.abs(vals).sum()) < 0.9 * target and step < 5000:
-        step += 1
-        keys, vals, st = O.step(m, O.StepParams(O.STYLE_DSS, dt=1e-3, shift=S, seed=0x5EED, step=step,
-                                                  compression=1.0), keys, vals)
-        tn = st["norm"]
-        S -= 0.08 ** 2 / 4 / 1e-3 * math.log(tn / target) + 0.08 / 1e-3 * math.log(tn / pn)
-        pn = tn
-    procs = os.cpu_count() or 1
-    vals_per_step = []
-    # every step samples `per` seconds on all processes of one pool, so that K steps take
-    # about cpu_seconds (at least a quarter second per step)
-    per = max(args.cpu_seconds / max(args.steps, 1), 0.25)
-    import multiprocessing as mp
-    with mp.get_context("spawn").Pool(procs) as pool:
-        for _ in range(args.warmup):      # untimed: same sample, results discarded
-            cpu_baseline(keys, vals, S, per, procs, pool)
-        t_all = time.time()
-        for _ in range(args.steps):
-            thr, _ = cpu_baseline(keys, vals, S, per, procs, pool)
-            vals_per_step.append(thr)
-    value = float(np.mean(vals_per_step))
+    m = O.real1d(20, 20, 4.0, 1.0)
+    keys, vals = np.array([k0], dtype=np.uint64), np.array([target])
+    S = O.diagonal(m, k0)
+    t0 = time.time()
+    _, prep, _, keys, vals, S, pn = cpu_steps(keys, vals, S, args.ref_prep_seconds, min_steps=1,
+                                             max_steps=args.ref_prep_steps, target=target)
+    t_prep = time.time() - t0
+    _, _, _, keys, vals, S, pn = cpu_steps(keys, vals, S, 0.0, min_steps=args.warmup,
+                                           max_steps=args.warmup, target=target, pnorm=pn,
+                                           step0=prep + 1)
+    value, nsteps, secs, keys, vals, S, pn = cpu_steps(
+        keys, vals, S, 0.0, min_steps=args.steps, max_steps=args.steps, target=target, pnorm=pn,
+        step0=prep + args.warmup + 1)
+    threads = os.cpu_count() or 1
+    sample = (f"{nsteps} full steps of one shared list grown by the same step from the "
+              f"unit-filling address for {prep} steps ({t_prep:.0f} s) towards norm {target:.3g}; "
+              f"{len(keys)} entries, norm {pn:.3g} at the end; {threads} threads")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD + " (bounded sample)", "target_walkers": args.target},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                             "sample": f"{len(keys)} walkers (norm {float(np.abs(vals).sum()):.3g}) grown by "
-                                       f"the oracle from the start address; {procs} processes stepping "
-                                       f"independent copies, {per:.2f} s per step sample"},
+            "warmup": args.warmup, "ms_per_step": secs / max(nsteps, 1) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD + f" at target norm {target:.3g}",
+                       "target_walkers": target, "entries": len(keys),
+                       "note": "the GPU arm's list (norm 1e8) would need ~2000 growth steps of "
+                               "~10 s each on these cores; the same routine on that list is "
+                               "the GPU arm's cpu_baseline"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "Julia is not installed; this is the C restatement of the reference step (oracle/)"}
+            "note": "Julia is not installed; this is the C/OpenMP restatement of the reference's "
+                    "PDVec step (oracle/)"}
     print(json.dumps(line), flush=True)
 
 
@@ -555,8 +538,12 @@ def main():
     ap.add_argument("--max-prep", type=int, default=4000)
     ap.add_argument("--equil", type=int, default=2000,
                     help="untimed steps (growth + equilibration) before the warm-up steps")
-    ap.add_argument("--cpu-sample", type=float, default=2e4)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="bound on the CPU baseline's timed steps of the GPU run's list")
+    ap.add_argument("--ref-target", type=float, default=2e6,
+                    help="walker norm of the reference arm's list")
+    ap.add_argument("--ref-prep-seconds", type=float, default=90.0)
+    ap.add_argument("--ref-prep-steps", type=int, default=400)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per step of the roofline kernels, if measured for this run")
     ap.add_argument("--no-e2e", action="store_true")

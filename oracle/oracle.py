@@ -104,7 +104,11 @@ def lib():
         _lib.o_step_w.argtypes = [P(_OModel), P(_OParams), u64p, f64p, i64p, C.c_int64,
                                   P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
         _lib.o_step_mt.argtypes = [P(_OModel), P(_OParams), u64p, f64p, i64p, C.c_int64, C.c_int,
-                                   C.c_int64, P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
+                                   C.c_int64, C.c_int, P(u64p), P(f64p), P(i64p), i64p, P(_OStats)]
+        _lib.o_real1d_bits_offdiag.argtypes = [P(_OModel), C.c_uint64, C.c_int, u64p, f64p]
+        _lib.o_real1d_bits_diagonal.argtypes = [P(_OModel), C.c_uint64]
+        _lib.o_real1d_bits_diagonal.restype = C.c_double
+        _lib.o_to_fixed_agree.argtypes = [C.c_double]
     return _lib
 
 
@@ -361,12 +365,13 @@ def step(m: Model, prm: StepParams, keys, vals):
 
 
 def step_mt(m: Model, prm: StepParams, keys, vals, threads: int = 0, mem_budget: float = 8e9,
-            sort: bool = True):
+            sort: bool = True, bits: bool = False):
     """One projector step on `threads` host threads (0: all), restating the PDVec step
     (perform_spawns!, collect_local!, move_and_compress!, pdworkingmemory.jl:191-309).  Same
     results as step(); the output is sorted only when `sort`.  Contributions beyond
-    `mem_budget` bytes are processed in passes.  Addresses of at most 64 bits, no initiator
-    rule."""
+    `mem_budget` bytes are processed in passes.  With `bits`, HubbardReal1D columns use the
+    reference's bit-level algorithms instead of occupation-number arrays (same results,
+    faster).  Addresses of at most 64 bits, no initiator rule."""
     keys = np.ascontiguousarray(keys, dtype=np.uint64)
     n = len(keys)
     is_int = prm.style == STYLE_INTEGER
@@ -377,7 +382,7 @@ def step_mt(m: Model, prm: StepParams, keys, vals, threads: int = 0, mem_budget:
     st = _OStats()
     ms, ps = m.struct(), prm.struct()
     rc = lib().o_step_mt(C.byref(ms), C.byref(ps), _p(keys, C.c_uint64), _p(fv, C.c_double),
-                         _p(iv, C.c_int64), n, int(threads), int(mem_budget), C.byref(ok),
+                         _p(iv, C.c_int64), n, int(threads), int(mem_budget), int(bits), C.byref(ok),
                          C.byref(ov), C.byref(oi), C.byref(on), C.byref(st))
     if rc == 2:
         raise ValueError("step_mt: needs addresses of at most 64 bits and no initiator rule")
@@ -396,6 +401,21 @@ def step_mt(m: Model, prm: StepParams, keys, vals, threads: int = 0, mem_budget:
         k, v = k[order], v[order]
     stats = {f: getattr(st, f) for f, _ in _OStats._fields_}
     return k, v, stats
+
+
+def real1d_bits_offdiagonals(m: Model, key: int):
+    """Offdiagonals of a HubbardReal1D column by the bit-level path of the threaded step."""
+    s = m.struct()
+    out = []
+    for c in range(1, num_offdiagonals(m, key) + 1):
+        nk, hv = C.c_uint64(), C.c_double()
+        lib().o_real1d_bits_offdiag(C.byref(s), C.c_uint64(key), c, C.byref(nk), C.byref(hv))
+        out.append((int(nk.value), float(hv.value)))
+    return out
+
+
+def real1d_bits_diagonal(m: Model, key: int) -> float:
+    return float(lib().o_real1d_bits_diagonal(C.byref(m.struct()), C.c_uint64(key)))
 
 
 def _step_wide(m: Model, prm: StepParams, keys, vals):

@@ -679,9 +679,114 @@ typedef void (*o_emit_fn)(void *ctx, okey key, int cls, int kind, double v, int6
 /* The contributions of one source walker (apply_column!, styles.jl:21-25, 101-105, 210-214):
  * its diagonal step and its spawns, handed to `emit`; the statistics go to *st and the spawn
  * magnitudes (float walkers) to *spawn_acc in exact fixed point. */
+/* HubbardReal1D on the bit string, for the threaded step's comparator runs: the reference's
+ * own bit-level algorithms on one chunk, hopnextneighbour (bosefs.jl:297-345) walking the
+ * occupied modes with trailing_zeros/trailing_ones (occupied_modes, bitstring.jl:636-656) and
+ * bose_hubbard_interaction (bosefs.jl:415-428).  Same keys and values as the ONR functions
+ * (tests/test_oracle_threaded.py checks every basis state of several sizes). */
+static inline int o_tz(uint64_t x) { return x ? __builtin_ctzll(x) : 64; }
+static inline uint64_t o_shr(uint64_t x, int s) { return s >= 64 ? 0 : x >> s; }
+static long o_bits_interaction(uint64_t chunk) {
+  long acc = 0;
+  while (chunk) {
+    chunk = o_shr(chunk, o_tz(chunk));             /* proceed to the next occupied mode */
+    const int n = o_tz(~chunk);                    /* bosons in it */
+    chunk = o_shr(chunk, n);
+    acc += (long)n * (n - 1);
+  }
+  return acc;
+}
+static int o_bits_noff(uint64_t a) { return 2 * __builtin_popcountll(a & ~(a << 1)); }
+static void o_bits_hop(uint64_t a, int N, int M, int chosen, uint64_t *nk, long *prod) {
+  const int B = N + M - 1;
+  const uint64_t mask = B >= 64 ? ~0ull : ((1ull << B) - 1);
+  const int site = (chosen + 1) >> 1;
+  if (chosen & 1) {                                /* hop to the right */
+    long next = 0, curr = 0;
+    int offset = 0, sc = 0, reached_end = 0, i = 0, mode = 1, bit = 0;
+    uint64_t x = a;
+    while (x) {
+      const int z = o_tz(x);
+      x = o_shr(x, z); mode += z; bit += z;
+      const int num = o_tz(~x);
+      ++i;
+      next = (long)num * (mode == sc + 1);
+      reached_end = i == site + 1;
+      if (reached_end) break;
+      curr = num; offset = bit + num; sc = mode;
+      x = o_shr(x, num); bit += num;
+    }
+    if (sc == M) {
+      *nk = ((a << 1) | 1) & mask;
+      *prod = curr * (o_tz(~a) + 1);
+    } else {
+      next *= reached_end;
+      *nk = a ^ (3ull << (offset - 1));
+      *prod = curr * (next + 1);
+    }
+    return;
+  }
+  if (site == 1 && (a & 1)) {                      /* leftmost site: rotate by one bit */
+    const uint64_t na = (a >> 1) | (1ull << (B - 1));
+    int lead = 0;
+    for (int b = B - 1; b >= 0 && ((na >> b) & 1); --b) ++lead;
+    *nk = na;
+    *prod = (long)o_tz(~a) * lead;
+    return;
+  }
+  long prev = 0, curr = 0;
+  int offset = 0, sp = 0, i = 0, mode = 1, bit = 0;
+  uint64_t x = a;
+  while (x) {
+    const int z = o_tz(x);
+    x = o_shr(x, z); mode += z; bit += z;
+    const int num = o_tz(~x);
+    ++i;
+    prev = curr * (mode == sp + 1);
+    curr = num;
+    offset = bit;
+    if (i == site) break;
+    sp = mode;
+    x = o_shr(x, num); bit += num;
+  }
+  *nk = a ^ (3ull << (offset - 1));
+  *prod = curr * (prev + 1);
+}
+
+/* Exported for the tests: key and value of offdiagonal `chosen` by the bit-level path. */
+void o_real1d_bits_offdiag(const o_model *h, uint64_t key, int chosen, uint64_t *nkey,
+                           double *val) {
+  long prod;
+  o_bits_hop(key, h->N, h->M, chosen, nkey, &prod);
+  *val = -h->t * sqrt((double)prod);
+}
+double o_real1d_bits_diagonal(const o_model *h, uint64_t key) {
+  return h->u * (double)o_bits_interaction(key) / 2;
+}
+
+static int o_use_bits(const o_model *h) {
+  return h->kind == O_REAL1D && h->ncomp != 2 && h->N + h->M - 1 <= 64;
+}
+static int o_noff_f(const o_model *h, okey key, int fast) {
+  return fast ? o_bits_noff(o_lo(key)) : o_noff(h, key);
+}
+static double o_t_diag_f(const o_model *h, const o_params *p, okey key, int fast) {
+  if (!fast) return o_t_diag(h, p, key);
+  const double d = h->u * (double)o_bits_interaction(o_lo(key)) / 2;   /* HubbardReal1D.jl:55-57 */
+  return p->op == O_OP_HAMILTONIAN ? d : 1 - p->dt * (d - p->shift);
+}
+static void o_offdiag_f(const o_model *h, okey key, int chosen, okey *nkey, double *val,
+                        long *prod, int fast) {
+  if (!fast) { o_offdiag_k(h, key, chosen, nkey, val, prod); return; }
+  uint64_t nk;
+  o_bits_hop(o_lo(key), h->N, h->M, chosen, &nk, prod);
+  *nkey = (okey)nk;
+  *val = -h->t * sqrt((double)*prod);                /* HubbardReal1D.jl:59-62 */
+}
+
 static void o_apply_column(const o_model *h, const o_params *p, okey key, double sval,
                            int64_t sival, o_emit_fn emit, void *ctx, o_stats *st,
-                           o_u128 *spawn_acc) {
+                           o_u128 *spawn_acc, int fast) {
   const int is_int = p->style == O_STYLE_INTEGER;
   double val = is_int ? (double)sival : sval;
   /* classes of this walker's contributions (_default_to_initiator_value,
@@ -693,7 +798,7 @@ static void o_apply_column(const o_model *h, const o_params *p, okey key, double
   const int spawn_cls = p->init_rule == O_INIT_NONE ? O_CLS_SAFE
                                                      : (parent_init ? O_CLS_SAFE : O_CLS_UNSAFE);
   /* ---- diagonal_step! (spawning.jl:73-77) ---- */
-  double x = o_t_diag(h, p, key) * val;
+  double x = o_t_diag_f(h, p, key, fast) * val;
   if (is_int) {
     uint32_t r[4];
     o_draw_k(p->seed, O_PURPOSE_DIAG, p->replica, p->step, key, 0, r);
@@ -715,7 +820,7 @@ static void o_apply_column(const o_model *h, const o_params *p, okey key, double
     if (res != 0.0) emit(ctx, key, diag_cls, 0, res, 0);
   }
   /* ---- spawn! ---- */
-  int noff = o_noff(h, key);
+  int noff = o_noff_f(h, key, fast);
   int exact = 0;
   if (p->style == O_STYLE_DETERMINISTIC) {
     exact = 1;                       /* apply_column! returns (1,), styles.jl:101-105 */
@@ -735,7 +840,7 @@ static void o_apply_column(const o_model *h, const o_params *p, okey key, double
     st->spawn_attempts += noff;
     for (int c = 1; c <= noff; ++c) {
       okey nk; double hv; long prod;
-      o_offdiag_k(h, key, c, &nk, &hv, &prod);
+      o_offdiag_f(h, key, c, &nk, &hv, &prod, fast);
       double y = val * o_t_off(p, hv);
       if (p->proj_threshold > 0 && p->style == O_STYLE_DSS) {
         uint32_t r[4];
@@ -772,7 +877,7 @@ static void o_apply_column(const o_model *h, const o_params *p, okey key, double
     }
     int chosen = (int)(((uint64_t)word * (uint64_t)noff) >> 32) + 1;
     okey nk; double hv; long prod;
-    o_offdiag_k(h, key, chosen, &nk, &hv, &prod);
+    o_offdiag_f(h, key, chosen, &nk, &hv, &prod, fast);
     double y = c * o_t_off(p, hv);
     if (is_int) {
       int64_t k = o_round_int(y, o_u53(r));
@@ -801,7 +906,7 @@ static int o_step_k(const o_model *h, const o_params *p,
   o_u128 spawn_acc = 0;
   for (int64_t e = 0; e < n; ++e)
     o_apply_column(h, p, skeys[e], is_int ? 0.0 : svals[e], is_int ? sivals[e] : 0, o_emit_buf,
-                   &b, st, &spawn_acc);
+                   &b, st, &spawn_acc, 0);
   if (b.err) { free(b.c); return 1; }
   if (!is_int) st->spawns = o_fixed_to_double(spawn_acc);
   /* ---- annihilation: sum the contributions per address ----
@@ -929,7 +1034,8 @@ int o_step_w(const o_model *h, const o_params *p,
  * o_step_k's for any thread count.  When the contributions of one step would exceed
  * `mem_budget` bytes, the segments are processed in passes and the columns re-applied in
  * each pass (their draws are counter-based, so every pass sees the same contributions).
- * Addresses of at most 64 bits, no initiator rule. */
+ * Addresses of at most 64 bits, no initiator rule.  With `bits`, HubbardReal1D columns are
+ * applied by the bit-level functions above (same results). */
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -958,6 +1064,35 @@ static void o_emit_rec(void *vctx, okey key, int cls, int kind, double v, int64_
   if (c->is_int) vb = (uint64_t)iv; else memcpy(&vb, &v, 8);
   b->r[b->n].key = k; b->r[b->n].vb = vb; b->r[b->n].row = row; b->r[b->n].kind = (uint32_t)kind;
   b->n++;
+}
+
+/* o_to_fixed on the IEEE bits (the same answers; the threaded step's hot path): x as a signed
+ * multiple of 2^-64 when it is one and |x| < 2^48. */
+static int o_to_fixed_bits(double x, __int128 *out) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  const uint64_t ab = b & 0x7fffffffffffffffull;
+  if (ab == 0) { *out = 0; return 1; }
+  const int e = (int)(ab >> 52);
+  if (e == 0 || e >= 1023 + 48) return 0;          /* subnormal, or |x| >= 2^48 (or inf/nan) */
+  const uint64_t mant = (ab & ((1ull << 52) - 1)) | (1ull << 52);
+  const int sh = e - 1075 + 64;                    /* |x| = mant * 2^(sh - 64) */
+  unsigned __int128 u;
+  if (sh >= 0) {
+    u = (unsigned __int128)mant << sh;
+  } else {
+    if (-sh >= 53 || (mant & ((1ull << -sh) - 1))) return 0;   /* bits below 2^-64 */
+    u = mant >> -sh;
+  }
+  *out = (b >> 63) ? -(__int128)u : (__int128)u;
+  return 1;
+}
+
+/* Exported for the tests: whether the two conversions agree on x (1) or not (0). */
+int o_to_fixed_agree(double x) {
+  __int128 a = 0, b = 0;
+  const int ra = o_to_fixed(x, &a), rb = o_to_fixed_bits(x, &b);
+  return ra == rb && (!ra || a == b);
 }
 
 /* One slot of a segment's table: the address, the head of its contribution list, whether
@@ -991,7 +1126,7 @@ static int64_t o_reduce_segment(const o_params *p, const o_rec *rec, int64_t m, 
     } else if (s->exact) {
       double v; memcpy(&v, &rec[c].vb, 8);
       __int128 t;
-      if (o_to_fixed(v, &t)) s->fx += t; else s->exact = 0;
+      if (o_to_fixed_bits(v, &t)) s->fx += t; else s->exact = 0;
     }
     nxt[c] = s->head;
     s->head = c;
@@ -1055,7 +1190,7 @@ static int64_t o_reduce_segment(const o_params *p, const o_rec *rec, int64_t m, 
  * except that the output is not sorted.  Returns 0 on success, 1 when out of memory, 2 for
  * an unsupported model or rule. */
 int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const double *svals,
-              const int64_t *sivals, int64_t n, int nthreads, int64_t mem_budget,
+              const int64_t *sivals, int64_t n, int nthreads, int64_t mem_budget, int bits,
               uint64_t **okeys, double **ovals, int64_t **oivals, int64_t *on, o_stats *st) {
   memset(st, 0, sizeof(*st));
   if (p->init_rule != O_INIT_NONE) return 2;
@@ -1071,12 +1206,13 @@ int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const 
   (void)nthreads;
 #endif
   const int is_int = p->style == O_STYLE_INTEGER;
+  const int fast = bits && o_use_bits(h);
   /* contributions of the step (an upper bound: the diagonal term and every unit) */
   int64_t total = 0;
 #pragma omp parallel for num_threads(nt) reduction(+ : total) schedule(static)
   for (int64_t e = 0; e < n; ++e) {
     const double val = is_int ? (double)sivals[e] : svals[e];
-    const int noff = o_noff(h, (okey)skeys[e]);
+    const int noff = o_noff_f(h, (okey)skeys[e], fast);
     int64_t units = noff;
     if (p->style == O_STYLE_INTEGER || (p->style == O_STYLE_DSS &&
         !(p->boost * fabs(val) * p->rel_threshold >=
@@ -1090,7 +1226,10 @@ int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const 
   int passes = 1;
   if (mem_budget > 0 && total * per_rec > mem_budget)
     passes = (int)((total * per_rec + mem_budget - 1) / mem_budget);
-  const int rows_per_pass = 8 * nt;
+  /* segments of about 16k contributions, so that each one's table stays in cache */
+  int64_t per_pass = (total + passes - 1) / passes;
+  int rows_per_pass = 8 * nt;
+  if (per_pass / 16384 > rows_per_pass) rows_per_pass = (int)(per_pass / 16384 < 65536 ? per_pass / 16384 : 65536);
   const int rows = passes * rows_per_pass;
   o_rbuf *bufs = calloc((size_t)nt, sizeof(o_rbuf));
   o_stats *tst = calloc((size_t)nt, sizeof(o_stats));
@@ -1120,7 +1259,7 @@ int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const 
 #pragma omp for schedule(dynamic, 1024)
       for (int64_t e = 0; e < n; ++e)
         o_apply_column(h, p, (okey)skeys[e], is_int ? 0.0 : svals[e], is_int ? sivals[e] : 0,
-                       o_emit_rec, &ctx, stp, accp);
+                       o_emit_rec, &ctx, stp, accp, fast);
     }
     for (int t = 0; t < nt; ++t) err |= bufs[t].err;
     if (err) break;

@@ -444,6 +444,7 @@ __global__ void __launch_bounds__(WARPS * 32, 5) k_spawn(StepArgs a, int nb_tota
   __shared__ uint32_t s_excl[WARPS][BATCH];
   __shared__ uint32_t s_meta[WARPS][BATCH];   // noff | exact << 31
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (a.ann_count && blockIdx.x == 0 && threadIdx.x == 0) *a.ann_count = 0;
   const int cb = a.spawn_cb;
   const int nchunks = nb_total / cb;
   const uint32_t step = step_of(a);
@@ -572,7 +573,16 @@ struct PassAcc {
   long long clones, deaths, zombies;
 };
 
-constexpr int MAX_SPLIT = 16;           // at most 2^MAX_SPLIT passes over one bucket
+// A bucket whose contributions overflow the table is processed in passes: pass `sel` at depth
+// `lvl` takes the addresses whose split word agrees with sel in its low lvl bits.  The split
+// word is a bijection of the address word, so any two addresses are separated by depth 64.
+constexpr int MAX_SPLIT = 64;
+__device__ __forceinline__ uint64_t split_word(uint64_t kw) {
+  return mix64(kw ^ 0x5851F42D4C957F2Dull);
+}
+__device__ __forceinline__ uint64_t split_mask(int lvl) {
+  return lvl >= 64 ? ~0ull : (1ull << lvl) - 1ull;
+}
 constexpr uint32_t NIL = 0xffffffffu;   // end of a contribution list
 constexpr int ANN_THREADS = 256;        // threads of one annihilation CTA
 constexpr uint32_t PACK_FAIL = 0x80000000u;   // overflow bit of the packed insertion counter
@@ -632,12 +642,58 @@ __device__ __forceinline__ uint32_t link_next(uint16_t w) {
 __device__ __forceinline__ int link_cls(uint16_t w) { return (w >> 13) & 3; }
 __device__ __forceinline__ bool link_diag(uint16_t w) { return (w >> 15) != 0; }
 
+// Whether contribution a comes before b in the canonical order: the diagonal term first,
+// then by increasing value (order-preserving bits).
+__device__ __forceinline__ bool canon_before(const uint64_t *cval, const uint16_t *clink,
+                                             uint32_t a, uint32_t b) {
+  const bool da = link_diag(clink[a]), db = link_diag(clink[b]);
+  if (da != db) return da;
+  return ordered_bits(bitsd(cval[a])) <= ordered_bits(bitsd(cval[b]));
+}
+__device__ __forceinline__ void link_set_next(uint16_t *clink, uint32_t c, uint32_t nxt) {
+  clink[c] = (uint16_t)((clink[c] & ~LINK_END) | (nxt == NIL ? LINK_END : nxt));
+}
+
+// Sorts the list starting at `head` into canonical order by relinking it in place (bottom-up
+// merge sort of a singly linked list: O(k log k) comparisons, no extra memory) and returns
+// the new head.  Lists hold at most `n` entries; a longer walk means a corrupted list.
+__device__ uint32_t sort_list(uint32_t head, const uint64_t *cval, uint16_t *clink, uint32_t n,
+                              bool *bad) {
+  uint32_t len = 0;
+  for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+    if (c >= n || ++len > n) { *bad = true; return head; }
+  }
+  for (uint32_t width = 1; width < len; width <<= 1) {
+    uint32_t new_head = NIL, tail = NIL, cur = head;
+    while (cur != NIL) {
+      uint32_t a = cur, na = 0;
+      while (cur != NIL && na < width) { cur = link_next(clink[cur]); ++na; }
+      uint32_t b = cur, nb = 0;
+      while (cur != NIL && nb < width) { cur = link_next(clink[cur]); ++nb; }
+      while (na > 0 || nb > 0) {
+        uint32_t take;
+        if (nb == 0 || (na > 0 && canon_before(cval, clink, a, b))) {
+          take = a; a = link_next(clink[a]); --na;
+        } else {
+          take = b; b = link_next(clink[b]); --nb;
+        }
+        if (tail == NIL) new_head = take; else link_set_next(clink, tail, take);
+        tail = take;
+      }
+    }
+    link_set_next(clink, tail, NIL);
+    head = new_head;
+  }
+  return head;
+}
+
 // Canonical-order sum for an address with an inexact contribution: `first` (the diagonal
 // term, when `have`) followed by the spawns of the list starting at `head` (diagonal terms are
-// skipped; with cls >= 0 only that class counts) in increasing order of value.  Lists hold at
-// most `n` entries; a longer walk means a corrupted list and is cut short.
-__device__ double canonical_sum_list(bool have, double first, uint32_t head, const uint64_t *cval,
-                                     const uint16_t *clink, uint32_t n, bool *bad, int cls = -1) {
+// skipped; with cls >= 0 only that class counts) in increasing order of value.  Lists of more
+// than eight such spawns are sorted in place first (`head` is updated).  Lists hold at most
+// `n` entries; a longer walk means a corrupted list and is cut short.
+__device__ double canonical_sum_list(bool have, double first, uint32_t &head, const uint64_t *cval,
+                                     uint16_t *clink, uint32_t n, bool *bad, int cls = -1) {
   double sum = first;
   constexpr int K = 8;
   uint64_t ob[K];
@@ -665,27 +721,16 @@ __device__ double canonical_sum_list(bool have, double first, uint32_t head, con
     }
     return sum;
   }
-  uint64_t last = 0;
-  bool any_last = false;
-  for (uint32_t round = 0; round <= n; ++round) {
-    uint64_t best = ~0ull;
-    uint32_t cnt = 0;
-    steps = 0;
-    for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
-      if (c >= n || ++steps > n) { *bad = true; return sum; }
-      const uint16_t w = clink[c];
-      if (link_diag(w) || (cls >= 0 && link_cls(w) != cls)) continue;
-      const uint64_t o = ordered_bits(bitsd(cval[c]));
-      if (any_last && o <= last) continue;
-      if (o < best) { best = o; cnt = 1; } else if (o == best) ++cnt;
-    }
-    if (cnt == 0) return sum;
-    const double v = from_ordered(best);
-    for (uint32_t i = 0; i < cnt; ++i) { sum = have ? sum + v : v; have = true; }
-    last = best;
-    any_last = true;
+  head = sort_list(head, cval, clink, n, bad);
+  steps = 0;
+  for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+    if (c >= n || ++steps > n) { *bad = true; return sum; }
+    const uint16_t w = clink[c];
+    if (link_diag(w) || (cls >= 0 && link_cls(w) != cls)) continue;
+    const double v = bitsd(cval[c]);
+    sum = have ? sum + v : v;
+    have = true;
   }
-  *bad = true;
   return sum;
 }
 
@@ -716,7 +761,7 @@ __device__ __forceinline__ int64_t initiator_value_i(int rule, double thr, int64
 // summation rule (the diagonal term, when in that class, first in canonical order), then
 // combined.  Also counts the spawn statistics.
 __device__ double initiator_sum_f(const StepArgs &a, uint32_t head, const uint64_t *cval,
-                                  const uint16_t *clink, uint32_t ncon, AnnAcc &acc, bool *bad) {
+                                  uint16_t *clink, uint32_t ncon, AnnAcc &acc, bool *bad) {
   U128 sum[3] = {{0, 0}, {0, 0}, {0, 0}};
   bool exact[3] = {true, true, true};
   int cnt[3] = {0, 0, 0};
@@ -892,7 +937,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
   __shared__ uint32_t s_cnt[2][4];
   __shared__ uint32_t s_out;            // entries written to the target slab of the bucket
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const uint32_t T = a.tsize;
+  const uint32_t T = a.ann_list ? a.tsize_list : a.tsize;
   K *tkey = reinterpret_cast<K *>(smem);
   uint64_t *cval = reinterpret_cast<uint64_t *>(tkey + T);
   uint32_t *thead = reinterpret_cast<uint32_t *>(cval + T);
@@ -914,7 +959,14 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
   AnnAcc acc{};
   int cur_r = -1;
   bool bad = false;
-  for (int gb = blockIdx.x; gb < nb_total; gb += gridDim.x) {
+  // every bucket, or (after k_ann_warp) the buckets it left in the list
+  uint32_t nwork = (uint32_t)nb_total;
+  if (a.ann_list) {
+    const uint32_t n = *a.ann_count;
+    nwork = n < nwork ? n : nwork;
+  }
+  for (uint32_t wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
+    const int gb = a.ann_list ? (int)a.ann_list[wi] : (int)wi;
     const int r = replica_of(a, (uint32_t)gb);
     if (r != cur_r) {
       if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
@@ -932,12 +984,12 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
     int lvl0 = 0;
     if (need > lim) {
       lvl0 = 1;
-      while (lvl0 < MAX_SPLIT && need > ((lim * 3 / 4) << lvl0)) ++lvl0;
+      while (lvl0 < 30 && (uint64_t)need > ((uint64_t)(lim * 3 / 4) << lvl0)) ++lvl0;
     }
     int lvl = lvl0;
-    uint32_t sel = 0;
+    uint64_t sel = 0;
     for (;;) {
-      const uint32_t mask = (1u << lvl) - 1u;
+      const uint64_t mask = split_mask(lvl);
       // s_pack: contribution entries (bits 0-15), occupied slots (bits 16-30), overflow (bit 31)
       uint32_t *const s_pack = &s_cnt[par][0], *const s_nq = &s_cnt[par][1];
       uint32_t *const s_nslow = &s_cnt[par][2];
@@ -965,7 +1017,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             else cls = (rec.key & UNSAFE_BIT) ? CLS_UNSAFE : CLS_SAFE;
             rec.key &= ~UNSAFE_BIT;
           }
-          if (lvl == 0 || ((uint32_t)(mix64(kword(rec.key)) >> 16) & mask) == sel) {
+          if (lvl == 0 || (split_word(kword(rec.key)) & mask) == sel) {
             slot = table_insert(tkey, T, tbits, rec.key, claimed);
             if (slot < 0) {
               lfail = true;
@@ -1124,7 +1176,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
             if (i < nslow && nq + i < T) {
               const int slot = qlist[T - 1 - i];
               key = tkey[slot];
-              const uint32_t head = thead[slot];
+              uint32_t head = thead[slot];
               tkey[slot] = EMPTY; thead[slot] = NIL;
               double fv;
               if (a.init_rule) {
@@ -1198,20 +1250,242 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
       par ^= 1;
       if (fail) {
         if (lvl >= MAX_SPLIT) { bad = true; break; }
-        ++lvl;                       // first half of this pass: hash bit lvl-1 clear
+        ++lvl;                       // first half of this pass: split bit lvl-1 clear
         continue;
       }
       // next pass: depth first over the splits
-      while (lvl > lvl0 && ((sel >> (lvl - 1)) & 1u)) { sel &= ~(1u << (lvl - 1)); --lvl; }
+      while (lvl > lvl0 && ((sel >> (lvl - 1)) & 1ull)) { sel &= ~(1ull << (lvl - 1)); --lvl; }
       if (lvl == lvl0) {
-        if (++sel >= (1u << lvl0)) break;
+        if (++sel >= (1ull << lvl0)) break;
       } else {
-        sel |= 1u << (lvl - 1);
+        sel |= 1ull << (lvl - 1);
       }
     }
     if (tid == 0) {
       const uint32_t out = s_out;
       s_out = 0;                     // next used after the next bucket's first barrier
+      a.cnt_out[gb] = out < a.capv ? out : a.capv;
+      if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
+      if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
+      atomicMax(&a.stats[r].max_v_bucket, out);
+      atomicMax(&a.stats[r].max_spawn_bucket, nsp);
+      a.scount[gb] = 0;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0)
+    atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
+  if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
+}
+
+// ------------------------------------------------------------------------------------------
+// Annihilation, one warp per bucket
+// ------------------------------------------------------------------------------------------
+// The common case.  A bucket of at most AW_CAP contributions is annihilated by one warp in a
+// table of its own in shared memory, so no warp ever waits for another (k_annihilate's CTA
+// barriers were its main stall).  Same arithmetic as k_annihilate: the summation rule,
+// compression, statistics and ProjectedEnergy terms, for one-word addresses without an
+// initiator rule.  A bucket with more contributions is appended to ann_list and left to
+// k_annihilate, launched after this kernel.
+constexpr int AW_WARPS = 4;              // warps per CTA
+constexpr int AW_CAP = 512;              // contributions per bucket, and table slots per warp
+constexpr int AW_TBITS = 9;
+// per warp: keys [AW_CAP] u64, contribution values [AW_CAP] u64, list heads [AW_CAP] u32,
+// contribution links [AW_CAP] u16 (the k_annihilate link word), occupied-slot list [AW_CAP]
+// u16: 24 bytes per slot, 12 KB per warp, 48 KB per CTA; four CTAs (16 warps) per SM
+constexpr size_t AW_WARP_SMEM = (size_t)AW_CAP * (8 + 8 + 4 + 2 + 2);
+
+template <int KIND, int STYLE>
+__global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int nb_total) {
+  using K = uint64_t;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned char *base = smem + (size_t)w * AW_WARP_SMEM;
+  uint64_t *tkey = reinterpret_cast<uint64_t *>(base);
+  uint64_t *cval = tkey + AW_CAP;
+  uint32_t *thead = reinterpret_cast<uint32_t *>(cval + AW_CAP);
+  uint16_t *clink = reinterpret_cast<uint16_t *>(thead + AW_CAP);
+  uint16_t *slist = clink + AW_CAP;
+  for (int i = lane; i < AW_CAP; i += 32) { tkey[i] = EMPTY_KEY; thead[i] = NIL; }
+  __syncwarp();
+  const uint32_t lt = lanemask_lt();
+  const uint32_t step = step_of(a);
+  AnnAcc acc{};
+  int cur_r = -1;
+  bool bad = false;
+  for (int gb = blockIdx.x * AW_WARPS + w; gb < nb_total; gb += gridDim.x * AW_WARPS) {
+    const int r = replica_of(a, (uint32_t)gb);
+    if (r != cur_r) {
+      if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
+      cur_r = r;
+    }
+    const uint32_t rep = a.replica_base + (uint32_t)r;
+    const uint32_t nsp = a.scount[gb];
+    const uint32_t ns = nsp < a.caps ? nsp : a.caps;
+    const uint32_t nv0 = a.cnt_in[gb];
+    const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
+    const uint32_t need = nv + ns;
+    if (need > (uint32_t)AW_CAP) {              // for k_annihilate
+      if (lane == 0) {
+        const uint32_t idx = atomicAdd(a.ann_count, 1u);
+        if (idx < (uint32_t)nb_total) a.ann_list[idx] = (uint32_t)gb;
+      }
+      continue;
+    }
+    const Rec *sp = static_cast<const Rec *>(a.spawn) + (size_t)gb * a.caps;
+    const Rec *vbase = static_cast<const Rec *>(a.v_in) + (size_t)gb * a.capv_in;
+    Rec *vout = static_cast<Rec *>(a.v_out) + (size_t)gb * a.capv;
+    // ---- every contribution onto the list of its address ----
+    uint32_t ncon = 0, nsl = 0;
+    Rec nxt{};
+    if ((uint32_t)lane < need) nxt = (uint32_t)lane < nv ? vbase[lane] : sp[lane - nv];
+    for (uint32_t f0 = 0; f0 < need; f0 += 32) {
+      const uint32_t f = f0 + lane;
+      Rec rec = nxt;
+      if (f + 32 < need) nxt = f + 32 < nv ? vbase[f + 32] : sp[f + 32 - nv];
+      const bool src = f < nv;
+      bool add = f < need;
+      uint64_t vbits = rec.val;
+      if (add && src) {                         // diagonal step of a source walker
+        if (STYLE == STYLE_INTEGER) {
+          const int64_t v = (int64_t)rec.val;
+          const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
+          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
+          const int64_t res = round_stochastic(x, u53_of(rr));
+          // clones_deaths_zombies (spawning.jl:79-93)
+          const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
+          if (res > v) acc.clones += res - v;
+          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
+          else acc.deaths += (res - v) < 0 ? v - res : res - v;
+          vbits = (uint64_t)res;
+          add = res != 0;
+        } else {
+          const double y = diag_float<KIND>(a, r, rep, step, rec);
+          vbits = dbits(y);
+          add = !is_zero_d(y);
+        }
+      }
+      int slot = -1;
+      bool claimed = false;
+      if (add) {
+        uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - AW_TBITS));
+        for (int p = 0; p < AW_CAP; ++p) {
+          const uint64_t k = *(volatile uint64_t *)&tkey[sl];
+          if (k == rec.key) { slot = (int)sl; break; }
+          if (k == EMPTY_KEY) {
+            const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
+                                                     (unsigned long long)EMPTY_KEY,
+                                                     (unsigned long long)rec.key);
+            if (old == EMPTY_KEY) { slot = (int)sl; claimed = true; break; }
+            if (old == rec.key) { slot = (int)sl; break; }
+          }
+          sl = (sl + 1) & (AW_CAP - 1);
+        }
+        if (slot < 0) { bad = true; add = false; }   // cannot happen: slots >= contributions
+      }
+      const uint32_t madd = __ballot_sync(0xffffffffu, add);
+      const uint32_t mcl = __ballot_sync(0xffffffffu, claimed);
+      if (add) {
+        const uint32_t c = ncon + (uint32_t)__popc(madd & lt);
+        cval[c] = vbits;
+        const uint32_t old = atomicExch(&thead[slot], c);
+        clink[c] = (uint16_t)((old == NIL ? LINK_END : old) | (src ? 0x8000u : 0u));
+      }
+      if (claimed) slist[nsl + (uint32_t)__popc(mcl & lt)] = (uint16_t)slot;
+      ncon += (uint32_t)__popc(madd);
+      nsl += (uint32_t)__popc(mcl);
+    }
+    __syncwarp();
+    // ---- finalize: sum, compression, statistics, output ----
+    uint32_t out = 0;
+    for (uint32_t i0 = 0; i0 < nsl; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      bool keep = false;
+      uint64_t key = 0, vb = 0;
+      if (i < nsl) {
+        const int slot = slist[i];
+        key = tkey[slot];
+        uint32_t head = thead[slot];
+        tkey[slot] = EMPTY_KEY;
+        thead[slot] = NIL;
+        if (STYLE == STYLE_INTEGER) {
+          int64_t iv = 0;
+          uint32_t steps = 0;
+          for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+            if (c >= ncon || ++steps > ncon) { bad = true; break; }
+            const int64_t k = (int64_t)cval[c];
+            iv += k;
+            if (!link_diag(clink[c])) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
+          }
+          if (iv != 0) {
+            acc.len_before++;
+            keep = true;
+            vb = (uint64_t)iv;
+            const uint64_t mag = (uint64_t)(iv < 0 ? -iv : iv);
+            account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, mag}, acc);
+          }
+        } else {
+          double fv;
+          const uint16_t w0 = clink[head];
+          const uint32_t c1 = link_next(w0);
+          const uint16_t w1 = c1 == NIL ? (uint16_t)LINK_END : clink[c1];
+          if (c1 == NIL || link_next(w1) == NIL) {
+            // one or two contributions: a single IEEE addition is correctly rounded, so it
+            // equals both the exact fixed-point sum and the canonical-order sum
+            const double y0 = bitsd(cval[head]);
+            if (!link_diag(w0)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
+            fv = y0;
+            if (c1 != NIL) {
+              const double y1 = bitsd(cval[c1]);
+              if (!link_diag(w1)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
+              fv = __dadd_rn(y0, y1);
+            }
+          } else {
+            U128 sum{0, 0};
+            bool exact = true, have_d = false;
+            double first = 0.0;
+            uint32_t steps = 0;
+            for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+              if (c >= ncon || ++steps > ncon) { bad = true; break; }
+              const uint64_t v = cval[c];
+              U128 m;
+              const bool ex = fixed_magnitude(bitsd(v), m);
+              if (link_diag(clink[c])) {
+                have_d = true;
+                first = bitsd(v);
+              } else {
+                acc.records++;
+                acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
+              }
+              exact = exact && ex;
+              sum = add128(sum, (v >> 63) ? neg128(m) : m);
+            }
+            fv = exact ? signed_fixed_to_double(sum)
+                       : canonical_sum_list(have_d && !is_zero_d(first), first, head, cval, clink,
+                                            ncon, &bad);
+          }
+          if (!is_zero_d(fv)) {
+            acc.len_before++;
+            bool small = false;
+            if (a.comp_mode == 1) small = abs_lt_one(fv);
+            else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
+            if (small) {
+              keep = compress_draw<STYLE>(a, r, step, key, fv);
+              if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
+            } else {
+              keep = true;
+              account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+            }
+          }
+          vb = dbits(fv);
+        }
+      }
+      const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+      const uint32_t pos = out + (uint32_t)__popc(mk & lt);
+      if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+      out += (uint32_t)__popc(mk);
+    }
+    __syncwarp();
+    if (lane == 0) {
       a.cnt_out[gb] = out < a.capv ? out : a.capv;
       if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
       if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
@@ -1351,14 +1625,28 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
   if (ev) cudaEventRecord(ev[1], st);
   k_spawn_heavy<KIND, STYLE, K><<<ctx->num_sms * 4, 256, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  const size_t smem = ann_smem<K>(a.tsize);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_annihilate<KIND, STYLE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
+    if constexpr (KT<K>::BITS == 64)
+      cudaFuncSetAttribute(k_ann_warp<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(AW_WARPS * AW_WARP_SMEM));
     attr_set = true;
   }
-  k_annihilate<KIND, STYLE, K><<<grid, ANN_THREADS, smem, st>>>(a, nb_total);
+  if constexpr (KT<K>::BITS == 64) {
+    if (a.ann_list) {
+      const int want_w = (nb_total + AW_WARPS - 1) / AW_WARPS;
+      const int cap_w = ctx->num_sms * 4;
+      k_ann_warp<KIND, STYLE><<<want_w < cap_w ? want_w : cap_w, AW_WARPS * 32,
+                                AW_WARPS * AW_WARP_SMEM, st>>>(a, nb_total);
+      // the buckets the warps left: as many CTAs as can be resident
+      k_annihilate<KIND, STYLE, K><<<cap_a, ANN_THREADS, ann_smem<K>(a.tsize_list), st>>>(a, nb_total);
+      if (ev) cudaEventRecord(ev[3], st);
+      return rimu_cuda_check(cudaGetLastError(), "step kernels");
+    }
+  }
+  k_annihilate<KIND, STYLE, K><<<grid, ANN_THREADS, ann_smem<K>(a.tsize), st>>>(a, nb_total);
   if (ev) cudaEventRecord(ev[3], st);
   return rimu_cuda_check(cudaGetLastError(), "step kernels");
 }

@@ -96,6 +96,13 @@ struct StepArgs {
   const double *proj_h;
   double *proj_out_v;         // [nrep * nproj]
   double *proj_out_h;
+  // Annihilation kernels: when `ann_list` is set, buckets run first one warp each
+  // (k_ann_warp); a bucket with more contributions than a warp's table holds is appended to
+  // ann_list (count in *ann_count, reset by k_spawn) and annihilated by a CTA with a table of
+  // tsize_list slots afterwards.  Null: every bucket by a CTA with tsize slots.
+  uint32_t *ann_list;         // [number of buckets]
+  uint32_t *ann_count;
+  uint32_t tsize_list;
 };
 
 }  // namespace rimu

@@ -310,6 +310,12 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_hv:
         hv_res = bench_hv(R, torch, peak)
 
+    # ---- the small and the momentum-space configurations ----
+    c1_res = c3_res = None
+    if rank == 0 and not args.no_configs:
+        c1_res = bench_c1(R, torch)
+        c3_res = bench_c3(R, torch)
+
     # ---- batched replicas (64 runs in one launch per kernel) ----
     batch_res = None
     if rank == 0 and not args.no_batch:
@@ -354,6 +360,8 @@ def run_ours(args, ws, rank, local):
             "clocks": clocks.summary(),
             "hv": hv_res,
             "batched": batch_res,
+            "c1": c1_res,
+            "c3": c3_res,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -435,6 +443,89 @@ def bench_batched(R, torch, prep_steps=1200, batched_steps=256, seq_steps=32):
                    "update on the device; sequential: rimu_apply_operator per replica and step "
                    "with the host DoubleLogUpdate; both from the same equilibrated states; equal "
                    "step counts give equal blocking error bars (the steps are the same process)"}
+
+
+def bench_c1(R, torch):
+    """The small plain configuration.  (a) The reference's published example
+    (scripts/BHM-example.jl: HubbardReal1D(near_uniform(BoseFS{6,6}); u=6, t=1),
+    IsDynamicSemistochastic, 1 000 target walkers, dt=1e-3, 3 000 steps, ProjectedEnergy onto
+    the start vector), whose main computation the reference reports at 2.69 s on one process
+    (docs/src/index.md:100-103): wall time of `solve` here, host loop included.  (b) The same
+    Hamiltonian with IsStochasticInteger walkers for 20 000 steps: walker-steps/s through
+    `solve`, and the shift and projected energy with blocking errors against E0 = -4.0215."""
+    import numpy as np
+    addr = R.near_uniform(R.BoseFS, 6, 6)
+    H = R.HubbardReal1D(addr, u=6.0, t=1.0)
+    out = {"workload": "HubbardReal1D M=N=6 u=6 t=1"}
+    style = R.IsDynamicSemistochastic()
+    start = {addr: 10.0}
+    p = R.ProjectorMonteCarloProblem(H, start_at=start, style=style, last_step=3000,
+                                     time_step=1e-3, target_walkers=1000, random_seed=0x5EED,
+                                     post_step_strategy=R.ProjectedEnergy(H, start))
+    R.solve(p)                                  # warm-up (first-use allocations)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    sim = R.solve(p)
+    torch.cuda.synchronize()
+    out["bhm_example_seconds"] = time.time() - t0
+    out["bhm_example_reference_seconds"] = 2.69
+    df = sim.report.data
+    out["bhm_example_steps"] = len(df["shift"])
+    out["bhm_example_shift"] = list(R.mean_and_se(np.asarray(df["shift"]), skip=1000))
+    style = R.IsStochasticInteger()
+    start = {addr: 10}
+    p = R.ProjectorMonteCarloProblem(H, start_at=start, style=style, last_step=20000,
+                                     time_step=1e-3, target_walkers=1000, random_seed=0x5EED + 1,
+                                     post_step_strategy=R.ProjectedEnergy(H, start))
+    torch.cuda.synchronize()
+    t0 = time.time()
+    sim = R.solve(p)
+    torch.cuda.synchronize()
+    wall = time.time() - t0
+    df = sim.report.data
+    norms = np.asarray(df["norm"], dtype=float)
+    out["c1_steps"] = len(norms)
+    out["c1_seconds"] = wall
+    out["c1_walker_steps_per_s"] = float(norms.sum()) / wall
+    out["c1_ms_per_step"] = wall / len(norms) * 1e3
+    out["c1_shift"] = list(R.mean_and_se(np.asarray(df["shift"]), skip=5000))
+    pe = R.projected_energy(df, skip=5000)
+    out["c1_projected_energy"] = [float(pe.mean), float(pe.err)] if hasattr(pe, "mean") else list(pe)
+    out["c1_exact_energy"] = -4.0215
+    return out
+
+
+def bench_c3(R, torch, prep_steps=300, steps=50):
+    """The momentum-space configuration: HubbardMom1D(BoseFS(20, k=0 => 10); u=6, t=1),
+    IsStochasticInteger, target 1e7, dt=5e-4.  The run starts from 1e7 walkers on the k=0
+    address and is stepped `prep_steps` times; then `steps` steps are timed (device time of
+    the whole loop, host shift update and statistics read-back included)."""
+    import numpy as np
+    addr = R.BoseFS(20, {10: 10})
+    H = R.HubbardMom1D(addr, u=6.0, t=1.0)
+    p = R.ProjectorMonteCarloProblem(H, start_at={addr: 10 ** 7}, style=R.IsStochasticInteger(),
+                                     time_step=5e-4, target_walkers=1e7, last_step=10 ** 9,
+                                     random_seed=0x5EED, max_length=10 ** 8)
+    sim = R.init(p)
+    s = sim.states[0]
+    for _ in range(prep_steps):
+        sim.step_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    norms = []
+    e0.record()
+    for _ in range(steps):
+        sim.step_()
+        norms.append(s.wm.last_stats["norm"])
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"workload": "HubbardMom1D M=20 N=10 (all in k=0) u=6 t=1, IsStochasticInteger, "
+                        "target 1e7, dt=5e-4",
+            "prep_steps": prep_steps, "steps": steps, "ms_per_step": ms / steps,
+            "walker_steps_per_s": float(np.sum(norms)) / (ms / 1e3),
+            "walkers_per_step": float(np.mean(norms)),
+            "entries": int(s.wm.last_stats["len"])}
 
 
 def bench_hv(R, torch, peak):
@@ -550,6 +641,8 @@ def main():
     ap.add_argument("--no-hv", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the small (C1) and momentum-space (C3) configuration lines")
     ap.add_argument("--shape", default=None,
                     help="launch shape KEYS_PER_BUCKET,TABLE_SLOTS of the step kernels (0 slots = automatic)")
     args = ap.parse_args()

@@ -217,10 +217,13 @@ int rimu_wm_timing(rimu_wm *wm, double *out7);
 /* Launch shape of the step kernels (no counterpart in the reference, whose walker list is a
  * hash dictionary per thread, pdvec.jl:1-120).  keys_per_bucket: the bucket count is chosen
  * so that the expected number of contributions (source walkers plus spawns) per bucket lies
- * between keys_per_bucket / 2 and keys_per_bucket; 16..4096, default 1024.  table_slots:
- * slots of the shared-memory table of one annihilation CTA, a power of two in 512..4096, or
- * 0 to size it from the expected bucket load; buckets that do not fit are processed in
- * several passes.  Results do not depend on either value. */
+ * between keys_per_bucket / 2 and keys_per_bucket; 16..4096; by default 384 for addresses of
+ * up to 64 bits without an initiator rule, else 1024.  Such buckets of at most 512
+ * contributions are annihilated by one warp each, larger ones (and all buckets of other
+ * steps) by one CTA each.  table_slots: slots of the shared-memory table of one annihilation
+ * CTA, a power of two in 512..4096, or 0 to size it from the expected bucket load and the
+ * model's largest column; buckets that do not fit are processed in several passes.  Results
+ * do not depend on either value. */
 int rimu_wm_set_launch_shape(rimu_wm *wm, int keys_per_bucket, int table_slots);
 
 /* One projector step target = T(source), with stats: apply_operator!(wm, target, source,
@@ -252,8 +255,10 @@ typedef struct {
   double zeta, xi;               /* DoubleLogUpdate damping (reference defaults 0.08, zeta^2/4) */
   int segment_steps;             /* steps per segment (rounded up to even; 0: 64) */
   int use_graph;                 /* replay each full segment as one captured CUDA graph */
-  int autotune;                  /* time the launch shapes 2048/1024/512 on the first steps
-                                    with at least 2^20 entries and keep the fastest */
+  int autotune;                  /* time the bucket sizes 2048/1024/384/256 (the first two
+                                    annihilated one CTA per bucket, the others one warp per
+                                    bucket) on the first steps with at least 2^20 entries
+                                    and keep the fastest */
 } rimu_batch_params;
 
 /* Per replica and step: the step statistics of rimu_step_stats and the shift after the update

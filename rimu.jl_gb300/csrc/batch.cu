@@ -104,6 +104,7 @@ struct rimu_batch {
   // working memory
   Rec *spawn = nullptr;
   uint32_t *scount = nullptr;
+  uint32_t *ann_list = nullptr, *ann_count = nullptr;   // buckets left to the CTA annihilation
   uint32_t caps = 0, sp_nb = 0;
   HeavyChunk *heavy = nullptr;
   uint32_t heavy_cap = 0;
@@ -119,7 +120,7 @@ struct rimu_batch {
   uint64_t *proj_keys = nullptr;
   double *proj_v = nullptr, *proj_h = nullptr, *proj_out_v = nullptr, *proj_out_h = nullptr;
   // launch shape and the captured segment
-  int kpb = 1024, tslots = 0;
+  int kpb = 384, tslots = 0;
   bool tuned = false;
   uint32_t T = 512;
   int spawn_cb = 1;
@@ -253,8 +254,11 @@ static int plan(rimu_batch *b, const rimu_batch_params *p, int ksteps, int min_c
   if (b->sp_nb != nb_total || b->caps != caps) {
     dfree(ctx, b->spawn);
     dfree(ctx, b->scount);
-    if ((rc = dalloc(ctx, &b->spawn, (size_t)nb_total * caps)) || (rc = dalloc(ctx, &b->scount, nb_total)))
+    dfree(ctx, b->ann_list);
+    if ((rc = dalloc(ctx, &b->spawn, (size_t)nb_total * caps)) || (rc = dalloc(ctx, &b->scount, nb_total)) ||
+        (rc = dalloc(ctx, &b->ann_list, nb_total)))
       return rc;
+    if (!b->ann_count && (rc = dalloc(ctx, &b->ann_count, 1))) return rc;
     RIMU_CUDA(cudaMemsetAsync(b->scount, 0, (size_t)nb_total * sizeof(uint32_t), ctx->stream));
     b->sp_nb = nb_total;
     b->caps = caps;
@@ -378,6 +382,15 @@ static int enqueue_step(rimu_batch *b, const rimu_batch_params *p, int j) {
   a.capv = b->capv;
   a.caps = b->caps;
   a.tsize = b->T;
+  // buckets of up to 512 contributions one warp each, the others one CTA each with room for
+  // the largest number of contributions one address can receive
+  a.ann_list = b->ann_list;
+  a.ann_count = b->ann_count;
+  {
+    uint32_t TL = std::max<uint32_t>(b->T, 2048);
+    if ((uint32_t)m0->max_offdiag + 1 > TL - 256) TL = 4096;
+    a.tsize_list = b->tslots ? (uint32_t)b->tslots : TL;
+  }
   a.kw = 1;
   a.spawn_cb = b->spawn_cb;
   a.v_in = b->recs[src];
@@ -526,6 +539,7 @@ extern "C" int rimu_batch_destroy(rimu_batch *b) {
   dfree(c, b->d_pnorm); dfree(c, b->d_target); dfree(c, b->s_shift); dfree(c, b->s_pnorm);
   dfree(c, b->d_step); dfree(c, b->s_step); dfree(c, b->dtab); dfree(c, b->spawn);
   dfree(c, b->scount); dfree(c, b->heavy); dfree(c, b->heavy_count); dfree(c, b->stats);
+  dfree(c, b->ann_list); dfree(c, b->ann_count);
   dfree(c, b->rec); dfree(c, b->proj_keys); dfree(c, b->proj_v); dfree(c, b->proj_h);
   dfree(c, b->proj_out_v); dfree(c, b->proj_out_h);
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -659,7 +673,8 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
   // them, so that the growth within one segment stays within the planned room
   int seg = b->steps_done == 0 ? std::min(p.segment_steps, 8) : p.segment_steps;
   std::vector<double> trial_cost;
-  const int shapes[3] = {2048, 1024, 512};
+  // bucket sizes: up to 512 contributions go to one warp each, larger buckets to one CTA each
+  const int shapes[4] = {2048, 1024, 384, 256};
   int trial = -1;
   while (pos < nsteps) {
     int64_t tot_len = 0;
@@ -752,7 +767,7 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
     if (trial < 0) seg = std::min(p.segment_steps, seg * 2);
     if (trial >= 0) {
       trial_cost.push_back(ms / std::max(contributions, 1.0));
-      if (++trial == 3) {
+      if (++trial == 4) {
         const int best = (int)(std::min_element(trial_cost.begin(), trial_cost.end()) - trial_cost.begin());
         b->kpb = shapes[best];
         b->tuned = true;

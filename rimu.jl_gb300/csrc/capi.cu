@@ -662,6 +662,7 @@ extern "C" int rimu_wm_destroy(rimu_wm *w) {
   dfree(ctx, w->stats); dfree(ctx, w->dtab); dfree(ctx, w->d_shift);
   dfree(ctx, w->proj_keys); dfree(ctx, w->proj_v); dfree(ctx, w->proj_h);
   dfree(ctx, w->proj_out_v); dfree(ctx, w->proj_out_h);
+  dfree(ctx, w->ann_list); dfree(ctx, w->ann_count);
   cudaStreamSynchronize(ctx->stream);
   for (int i = 0; i < 4; ++i) if (w->ev[i]) cudaEventDestroy(w->ev[i]);
   if (w->h_stats) cudaFreeHost(w->h_stats);
@@ -687,6 +688,7 @@ extern "C" int rimu_wm_set_launch_shape(rimu_wm *w, int keys_per_bucket, int tab
     return bad("rimu_wm_set_launch_shape: table_slots must be 0 or a power of two in 512..4096");
   w->keys_per_bucket = keys_per_bucket;
   w->table_slots = table_slots;
+  w->shape_set = true;
   return RIMU_OK;
 }
 
@@ -728,7 +730,10 @@ static int wm_ensure(rimu_wm *w, int nb_total, uint32_t caps, uint32_t heavy_cap
   if (w->nb_total != nb_total || w->caps != caps || w->kw != kw) {
     dfree(ctx, w->spawn);
     dfree(ctx, w->scount);
-    if ((rc = dalloc(ctx, &w->spawn, (size_t)nb_total * caps * kw)) || (rc = dalloc(ctx, &w->scount, nb_total))) return rc;
+    dfree(ctx, w->ann_list);
+    if ((rc = dalloc(ctx, &w->spawn, (size_t)nb_total * caps * kw)) || (rc = dalloc(ctx, &w->scount, nb_total)) ||
+        (rc = dalloc(ctx, &w->ann_list, nb_total)))
+      return rc;
     w->kw = kw;
     RIMU_CUDA(cudaMemsetAsync(w->scount, 0, (size_t)nb_total * sizeof(uint32_t), ctx->stream));
     w->nb_total = nb_total;
@@ -740,6 +745,7 @@ static int wm_ensure(rimu_wm *w, int nb_total, uint32_t caps, uint32_t heavy_cap
     w->heavy_cap = heavy_cap;
   }
   if (!w->heavy_count && (rc = dalloc(ctx, &w->heavy_count, 1))) return rc;
+  if (!w->ann_count && (rc = dalloc(ctx, &w->ann_count, 1))) return rc;
   if (!w->stats) {
     if ((rc = dalloc(ctx, &w->stats, 1))) return rc;
     RIMU_CUDA(cudaMallocHost((void **)&w->h_stats, sizeof(DevStats)));
@@ -799,7 +805,16 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   // about one spawn per attempt, and max(floor(|v| boost), 1) attempts per walker; an
   // underestimate only costs a re-run of this first step with larger slabs
   else S_est = std::max<int64_t>((int64_t)(norm * p->boost), L) + 256;
-  const double kKeys = (double)w->keys_per_bucket;
+  // Buckets of one-word addresses without an initiator rule are annihilated one warp each
+  // (up to 512 contributions), about 200-400 of them per bucket by default; the others one
+  // CTA each, about 512-1024 per bucket.
+  const bool warp_ann = m->dm.nbits <= 64 && p->initiator == RIMU_INIT_NONE;
+  double kKeys = (double)(w->shape_set ? w->keys_per_bucket : (warp_ann ? 384 : 1024));
+  // An exact (deterministic) step gives each address all the contributions of its column's
+  // length at once: buckets of about eight such lumps keep the fullest bucket, which sets the
+  // slab capacity of all of them, within a small factor of the mean.
+  if (!w->shape_set && p->style == RIMU_STYLE_DETERMINISTIC)
+    kKeys = std::max(kKeys, 8.0 * (double)(m->max_offdiag + 1));
   int need_bits = ceil_log2((uint64_t)((double)(L + S_est) / kKeys) + 1);
   // A source with more than twice the buckets the step needs (a list uploaded or grown for a
   // larger load) is re-bucketed once to need_bits; otherwise buckets only grow.
@@ -866,6 +881,15 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     uint32_t T = 512;
     while ((double)T < 1.25 * mu_k + 256.0 && T < 4096) T <<= 1;
     a.tsize = w->table_slots ? (uint32_t)w->table_slots : T;
+    if (warp_ann) {
+      // the buckets the warps leave hold more than 512 contributions, and one address can
+      // receive max_offdiag + 1 of them: the table leaves room for that plus one round
+      uint32_t TL = std::max<uint32_t>(T, 2048);
+      if ((uint32_t)m->max_offdiag + 1 > TL - 256) TL = 4096;
+      a.ann_list = w->ann_list;
+      a.ann_count = w->ann_count;
+      a.tsize_list = w->table_slots ? (uint32_t)w->table_slots : TL;
+    }
     // spawn chunks of about 256 source walkers per warp
     const double mu_v = (double)L / (double)nb;
     int cb = 1;

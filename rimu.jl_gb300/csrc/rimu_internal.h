@@ -157,6 +157,9 @@ struct rimu_wm {
   int kw = 1;                           // address words of the spawn slabs
   int keys_per_bucket = 1024;           // expected contributions per bucket (launch shape)
   int table_slots = 0;                  // annihilation table slots per CTA (0: automatic)
+  bool shape_set = false;               // launch shape chosen by the caller
+  uint32_t *ann_list = nullptr;         // [nb_total] buckets left to the CTA annihilation
+  uint32_t *ann_count = nullptr;
   // projector
   int nproj = 0;
   uint64_t *proj_keys = nullptr;

@@ -51,8 +51,8 @@ def test_reference_arm_under_two_ranks_prints_one_line():
     port = free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl",
-           "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--cpu-sample", "300",
-           "--cpu-seconds", "0.5"]
+           "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-target", "300",
+           "--ref-prep-seconds", "0.5", "--ref-prep-steps", "20"]
     out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]

@@ -495,21 +495,27 @@ def bench_c1(R, torch):
     return out
 
 
-def bench_c3(R, torch, prep_steps=300, steps=50):
+def bench_c3(R, torch, steps=50, max_prep=20000):
     """The momentum-space configuration: HubbardMom1D(BoseFS(20, k=0 => 10); u=6, t=1),
-    IsStochasticInteger, target 1e7, dt=5e-4.  The run starts from 1e7 walkers on the k=0
-    address and is stepped `prep_steps` times; then `steps` steps are timed (device time of
-    the whole loop, host shift update and statistics read-back included)."""
+    IsStochasticInteger, target 1e7, dt=5e-4.  The run grows from 100 walkers on the k=0
+    address until its norm reaches 0.9 of the target and 500 more steps have passed; then
+    `steps` steps are timed (device time of the whole loop, host shift update and statistics
+    read-back included)."""
     import numpy as np
     addr = R.BoseFS(20, {10: 10})
     H = R.HubbardMom1D(addr, u=6.0, t=1.0)
-    p = R.ProjectorMonteCarloProblem(H, start_at={addr: 10 ** 7}, style=R.IsStochasticInteger(),
+    p = R.ProjectorMonteCarloProblem(H, start_at={addr: 100}, style=R.IsStochasticInteger(),
                                      time_step=5e-4, target_walkers=1e7, last_step=10 ** 9,
                                      random_seed=0x5EED, max_length=10 ** 8)
     sim = R.init(p)
     s = sim.states[0]
-    for _ in range(prep_steps):
+    prep, reached = 0, None
+    while prep < max_prep and (reached is None or prep < reached + 500):
         sim.step_()
+        prep += 1
+        if reached is None and s.wm.last_stats["norm"] >= 0.9e7:
+            reached = prep
+    prep_steps = prep
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     norms = []

@@ -120,7 +120,7 @@ struct rimu_batch {
   uint64_t *proj_keys = nullptr;
   double *proj_v = nullptr, *proj_h = nullptr, *proj_out_v = nullptr, *proj_out_h = nullptr;
   // launch shape and the captured segment
-  int kpb = 384, tslots = 0;
+  int kpb = AW_DEFAULT_KPB, tslots = 0;
   bool tuned = false;
   uint32_t T = 512;
   int spawn_cb = 1;
@@ -674,7 +674,7 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
   int seg = b->steps_done == 0 ? std::min(p.segment_steps, 8) : p.segment_steps;
   std::vector<double> trial_cost;
   // bucket sizes: up to 512 contributions go to one warp each, larger buckets to one CTA each
-  const int shapes[4] = {2048, 1024, 384, 256};
+  const int shapes[4] = {2048, 1024, AW_DEFAULT_KPB, AW_CAP / 2};
   int trial = -1;
   while (pos < nsteps) {
     int64_t tot_len = 0;

@@ -806,10 +806,10 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
   // underestimate only costs a re-run of this first step with larger slabs
   else S_est = std::max<int64_t>((int64_t)(norm * p->boost), L) + 256;
   // Buckets of one-word addresses without an initiator rule are annihilated one warp each
-  // (up to 512 contributions), about 200-400 of them per bucket by default; the others one
-  // CTA each, about 512-1024 per bucket.
+  // (up to AW_CAP contributions; by default 7/16 to 7/8 of that per bucket, the few fuller
+  // buckets left to the CTA kernel); the others one CTA each, 512-1024 per bucket.
   const bool warp_ann = m->dm.nbits <= 64 && p->initiator == RIMU_INIT_NONE;
-  double kKeys = (double)(w->shape_set ? w->keys_per_bucket : (warp_ann ? 384 : 1024));
+  double kKeys = (double)(w->shape_set ? w->keys_per_bucket : (warp_ann ? AW_DEFAULT_KPB : 1024));
   // An exact (deterministic) step gives each address all the contributions of its column's
   // length at once: buckets of about eight such lumps keep the fullest bucket, which sets the
   // slab capacity of all of them, within a small factor of the mean.

@@ -25,6 +25,11 @@
 
 namespace rimu {
 
+// x / y out of line.  A division inlined next to a common path that does not need it (the
+// compression threshold one, a tabulated reciprocal) was evaluated speculatively, and on
+// GB300 its reciprocal iterations occupied the scarce FP64 pipe for every address.
+__device__ __noinline__ double ratio_to_threshold(double x, double y) { return x / y; }
+
 
 // ------------------------------------------------------------------------------------------
 // Model dispatch
@@ -348,7 +353,7 @@ __device__ __forceinline__ double dint_of(const DevModel &h, int n) {
 // 1/n from the host table (the division only beyond it)
 __device__ __forceinline__ double recip_of(const DevModel &h, uint64_t n) {
   if (n < (uint64_t)h.recip_len) return h.recip[n];
-  return 1.0 / (double)n;
+  return ratio_to_threshold(1.0, (double)n);
 }
 
 // Work of one column: units (offdiagonals if exact, attempts otherwise) and the spawn
@@ -878,12 +883,18 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *count, bool flag) {
   return base + __popc(m & lanemask_lt());
 }
 
+__device__ __forceinline__ bool below_threshold(const StepArgs &a, double fv) {
+  if (a.comp_mode == 1) return abs_lt_one(fv);
+  if (a.comp_mode == 2) return ratio_to_threshold(abs_d(fv), a.compression) < 1;
+  return false;
+}
+
 // Compression draw (compression.jl:28-42) for an address whose |value| is below the
 // threshold: kept at +-threshold with probability |value| / threshold.
 template <int STYLE, class K>
 __device__ __forceinline__ bool compress_draw(const StepArgs &a, int r, uint32_t step, K key,
                                               double &fv) {
-  const double prob = a.comp_mode == 1 ? abs_d(fv) : abs_d(fv) / a.compression;
+  const double prob = a.comp_mode == 1 ? abs_d(fv) : ratio_to_threshold(abs_d(fv), a.compression);
   const U4 rr = draw(a.seed, PURPOSE_COMPRESS, a.replica_base + (uint32_t)r, step, kword(key), 0);
   if (!bernoulli53(u53_of(rr), prob)) return false;
   fv = signed_like(a.compression, fv);
@@ -1135,9 +1146,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
                 vb = dbits(fv);
                 if (!is_zero_d(fv)) {
                   acc.len_before++;
-                  bool small = false;
-                  if (a.comp_mode == 1) small = abs_lt_one(fv);
-                  else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
+                  const bool small = below_threshold(a, fv);
                   if (small) {
                     queue = true;
                   } else {
@@ -1210,9 +1219,7 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
               }
               if (!is_zero_d(fv)) {
                 acc.len_before++;
-                bool small = false;
-                if (a.comp_mode == 1) small = abs_lt_one(fv);
-                else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
+                const bool small = below_threshold(a, fv);
                 if (small) {
                   keep = compress_draw<STYLE>(a, r, step, key, fv);
                   if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
@@ -1280,32 +1287,110 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
 // ------------------------------------------------------------------------------------------
 // Annihilation, one warp per bucket
 // ------------------------------------------------------------------------------------------
-// The common case.  A bucket of at most AW_CAP contributions is annihilated by one warp in a
-// table of its own in shared memory, so no warp ever waits for another (k_annihilate's CTA
-// barriers were its main stall).  Same arithmetic as k_annihilate: the summation rule,
-// compression, statistics and ProjectedEnergy terms, for one-word addresses without an
-// initiator rule.  A bucket with more contributions is appended to ann_list and left to
-// k_annihilate, launched after this kernel.
+// The common case.  One warp annihilates one bucket in a table of its own in shared memory,
+// so no warp ever waits for another (k_annihilate's CTA barriers were its main stall).  Only
+// the spawns go into the table: each address's spawns on a list.  The source walkers, whose
+// addresses are distinct, then stream past it: each takes its diagonal step, looks its
+// address up (a read, no atomics), adds the spawns found there and is written out, and the
+// addresses that only spawns reached are finished last.  Same arithmetic as k_annihilate (the
+// summation rule, compression, statistics, ProjectedEnergy terms), for one-word addresses
+// without an initiator rule.  A bucket with more than AW_SCAP spawns is appended to ann_list
+// and left to k_annihilate, launched after this kernel.
 constexpr int AW_WARPS = 4;              // warps per CTA
-constexpr int AW_CAP = 512;              // contributions per bucket, and table slots per warp
-constexpr int AW_TBITS = 9;
-// per warp: keys [AW_CAP] u64, contribution values [AW_CAP] u64, list heads [AW_CAP] u32,
-// contribution links [AW_CAP] u16 (the k_annihilate link word), occupied-slot list [AW_CAP]
-// u16: 24 bytes per slot, 12 KB per warp, 48 KB per CTA; four CTAs (16 warps) per SM
-constexpr size_t AW_WARP_SMEM = (size_t)AW_CAP * (8 + 8 + 4 + 2 + 2);
+constexpr int AW_SLOTS = AW_CAP;         // table slots per warp
+constexpr int AW_SCAP = AW_CAP * 3 / 4;  // spawns per bucket
+constexpr int AW_TBITS = AW_CAP == 256 ? 8 : AW_CAP == 512 ? 9 : 10;   // log2 of the table slots
+static_assert((1 << AW_TBITS) == AW_SLOTS, "AW_CAP must be 256, 512 or 1024");
+constexpr uint32_t AW_DONE = 0x80000000u;   // list head flag: a source walker took the slot
+// per warp: keys [AW_SLOTS] u64, list heads [AW_SLOTS] u32, spawn values [AW_SCAP] u64, spawn
+// links [AW_SCAP] u16 (the k_annihilate link word), occupied-slot list [AW_SCAP] u16
+constexpr size_t AW_WARP_SMEM = (size_t)AW_SLOTS * (8 + 4) + (size_t)AW_SCAP * (8 + 2 + 2);
+// resident CTAs per SM that the shared memory allows (at most 8)
+constexpr int AW_MINB = (int)((220 * 1024) / (AW_WARPS * AW_WARP_SMEM)) > 8 ? 8
+                        : (int)((220 * 1024) / (AW_WARPS * AW_WARP_SMEM));
+
+__device__ __forceinline__ double warp_sum_long(uint32_t head, bool have_d, double dv,
+                                                const uint64_t *cval, uint16_t *clink, uint32_t n,
+                                                AnnAcc &acc, bool *bad);
+
+// Sum of the spawns on the list at `head` (n entries at most) and of the diagonal term dv
+// (when have_d) by the summation rule; counts the spawn statistics.
+template <int STYLE>
+__device__ __forceinline__ double warp_sum_float(uint32_t head, bool have_d, double dv,
+                                                 const uint64_t *cval, uint16_t *clink,
+                                                 uint32_t n, AnnAcc &acc, bool *bad) {
+  const uint16_t w0 = clink[head];
+  const uint32_t c1 = link_next(w0);
+  const double y0 = bitsd(cval[head]);
+  acc.records++;
+  acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0)));
+  if (c1 == NIL && !have_d) return y0;
+  if (c1 == NIL) return __dadd_rn(dv, y0);     // two terms: one correctly rounded addition
+  const uint16_t w1 = clink[c1];
+  if (!have_d && link_next(w1) == NIL) {
+    const double y1 = bitsd(cval[c1]);
+    acc.records++;
+    acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1)));
+    return __dadd_rn(y0, y1);
+  }
+  return warp_sum_long(head, have_d, dv, cval, clink, n, acc, bad);
+}
+
+// Three or more terms: exact in fixed point when every term allows it, else canonical order.
+__device__ __forceinline__ double warp_sum_long(uint32_t head, bool have_d, double dv,
+                                                const uint64_t *cval, uint16_t *clink, uint32_t n,
+                                                AnnAcc &acc, bool *bad) {
+  U128 sum{0, 0}, m;
+  bool exact = true;
+  if (have_d) {
+    exact = fixed_magnitude(dv, m);
+    sum = is_neg_d(dv) ? neg128(m) : m;
+  }
+  uint32_t steps = 0;
+  for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+    if (c >= n || ++steps > n) { *bad = true; break; }
+    const uint64_t v = cval[c];
+    const bool ex = fixed_magnitude(bitsd(v), m);
+    if (c != head) {
+      acc.records++;
+      acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
+    }
+    exact = exact && ex;
+    sum = add128(sum, (v >> 63) ? neg128(m) : m);
+  }
+  if (exact) return signed_fixed_to_double(sum);
+  uint32_t h = head;
+  return canonical_sum_list(have_d, dv, h, cval, clink, n, bad);
+}
+
+// Compression (compression.jl:18-42), statistics and ProjectedEnergy terms of one summed
+// address; whether it is kept (fv then holds its value).
+template <int STYLE>
+__device__ __forceinline__ bool warp_settle_float(const StepArgs &a, int r, uint32_t step,
+                                                  uint64_t key, double &fv, AnnAcc &acc) {
+  if (is_zero_d(fv)) return false;
+  acc.len_before++;
+  if (below_threshold(a, fv)) {
+    if (!compress_draw<STYLE>(a, r, step, key, fv)) return false;
+    acc.ncomp++;
+    account_entry<STYLE>(a, r, key, fv, acc);
+    return true;
+  }
+  account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+  return true;
+}
 
 template <int KIND, int STYLE>
-__global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int nb_total) {
-  using K = uint64_t;
+__global__ void __launch_bounds__(AW_WARPS * 32, AW_MINB) k_ann_warp(StepArgs a, int nb_total) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned char *base = smem + (size_t)w * AW_WARP_SMEM;
   uint64_t *tkey = reinterpret_cast<uint64_t *>(base);
-  uint64_t *cval = tkey + AW_CAP;
-  uint32_t *thead = reinterpret_cast<uint32_t *>(cval + AW_CAP);
-  uint16_t *clink = reinterpret_cast<uint16_t *>(thead + AW_CAP);
-  uint16_t *slist = clink + AW_CAP;
-  for (int i = lane; i < AW_CAP; i += 32) { tkey[i] = EMPTY_KEY; thead[i] = NIL; }
+  uint64_t *cval = tkey + AW_SLOTS;
+  uint32_t *thead = reinterpret_cast<uint32_t *>(cval + AW_SCAP);
+  uint16_t *clink = reinterpret_cast<uint16_t *>(thead + AW_SLOTS);
+  uint16_t *slist = clink + AW_SCAP;
+  for (int i = lane; i < AW_SLOTS; i += 32) { tkey[i] = EMPTY_KEY; thead[i] = NIL; }
   __syncwarp();
   const uint32_t lt = lanemask_lt();
   const uint32_t step = step_of(a);
@@ -1323,8 +1408,7 @@ __global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int n
     const uint32_t ns = nsp < a.caps ? nsp : a.caps;
     const uint32_t nv0 = a.cnt_in[gb];
     const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
-    const uint32_t need = nv + ns;
-    if (need > (uint32_t)AW_CAP) {              // for k_annihilate
+    if (ns > (uint32_t)AW_SCAP) {               // for k_annihilate
       if (lane == 0) {
         const uint32_t idx = atomicAdd(a.ann_count, 1u);
         if (idx < (uint32_t)nb_total) a.ann_list[idx] = (uint32_t)gb;
@@ -1334,41 +1418,23 @@ __global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int n
     const Rec *sp = static_cast<const Rec *>(a.spawn) + (size_t)gb * a.caps;
     const Rec *vbase = static_cast<const Rec *>(a.v_in) + (size_t)gb * a.capv_in;
     Rec *vout = static_cast<Rec *>(a.v_out) + (size_t)gb * a.capv;
-    // ---- every contribution onto the list of its address ----
-    uint32_t ncon = 0, nsl = 0;
-    Rec nxt{};
-    if ((uint32_t)lane < need) nxt = (uint32_t)lane < nv ? vbase[lane] : sp[lane - nv];
-    for (uint32_t f0 = 0; f0 < need; f0 += 32) {
+    // the first source records are loaded while the spawns go into the table, and each round
+    // of spawns while the previous one is inserted
+    Rec nxt{}, snxt{};
+    if ((uint32_t)lane < nv) nxt = vbase[lane];
+    if ((uint32_t)lane < ns) snxt = sp[lane];
+    // ---- the spawns, each onto the list of its address ----
+    uint32_t nsl = 0;
+    for (uint32_t f0 = 0; f0 < ns; f0 += 32) {
       const uint32_t f = f0 + lane;
-      Rec rec = nxt;
-      if (f + 32 < need) nxt = f + 32 < nv ? vbase[f + 32] : sp[f + 32 - nv];
-      const bool src = f < nv;
-      bool add = f < need;
-      uint64_t vbits = rec.val;
-      if (add && src) {                         // diagonal step of a source walker
-        if (STYLE == STYLE_INTEGER) {
-          const int64_t v = (int64_t)rec.val;
-          const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
-          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
-          const int64_t res = round_stochastic(x, u53_of(rr));
-          // clones_deaths_zombies (spawning.jl:79-93)
-          const int sr = (res > 0) - (res < 0), sv = (v > 0) - (v < 0);
-          if (res > v) acc.clones += res - v;
-          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += res < 0 ? -res : res; }
-          else acc.deaths += (res - v) < 0 ? v - res : res - v;
-          vbits = (uint64_t)res;
-          add = res != 0;
-        } else {
-          const double y = diag_float<KIND>(a, r, rep, step, rec);
-          vbits = dbits(y);
-          add = !is_zero_d(y);
-        }
-      }
+      const bool add = f < ns;
+      const Rec rec = snxt;
+      if (f + 32 < ns) snxt = sp[f + 32];
       int slot = -1;
       bool claimed = false;
       if (add) {
         uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - AW_TBITS));
-        for (int p = 0; p < AW_CAP; ++p) {
+        for (int p = 0; p < AW_SLOTS; ++p) {
           const uint64_t k = *(volatile uint64_t *)&tkey[sl];
           if (k == rec.key) { slot = (int)sl; break; }
           if (k == EMPTY_KEY) {
@@ -1378,25 +1444,81 @@ __global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int n
             if (old == EMPTY_KEY) { slot = (int)sl; claimed = true; break; }
             if (old == rec.key) { slot = (int)sl; break; }
           }
-          sl = (sl + 1) & (AW_CAP - 1);
+          sl = (sl + 1) & (AW_SLOTS - 1);
         }
-        if (slot < 0) { bad = true; add = false; }   // cannot happen: slots >= contributions
+        if (slot < 0) bad = true;                // cannot happen: slots > spawns
+        else {
+          cval[f] = rec.val;
+          const uint32_t old = atomicExch(&thead[slot], f);
+          clink[f] = (uint16_t)(old == NIL ? LINK_END : old);
+        }
       }
-      const uint32_t madd = __ballot_sync(0xffffffffu, add);
       const uint32_t mcl = __ballot_sync(0xffffffffu, claimed);
-      if (add) {
-        const uint32_t c = ncon + (uint32_t)__popc(madd & lt);
-        cval[c] = vbits;
-        const uint32_t old = atomicExch(&thead[slot], c);
-        clink[c] = (uint16_t)((old == NIL ? LINK_END : old) | (src ? 0x8000u : 0u));
-      }
       if (claimed) slist[nsl + (uint32_t)__popc(mcl & lt)] = (uint16_t)slot;
-      ncon += (uint32_t)__popc(madd);
       nsl += (uint32_t)__popc(mcl);
     }
     __syncwarp();
-    // ---- finalize: sum, compression, statistics, output ----
+    // ---- the source walkers: diagonal step, lookup, sum, settle, output ----
     uint32_t out = 0;
+    for (uint32_t f0 = 0; f0 < nv; f0 += 32) {
+      const uint32_t f = f0 + lane;
+      const Rec rec = nxt;
+      if (f + 32 < nv) nxt = vbase[f + 32];
+      bool keep = false;
+      uint64_t vb = 0;
+      if (f < nv) {
+        int slot = -1;
+        uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - AW_TBITS));
+        if (ns) {
+          for (int p = 0; p < AW_SLOTS; ++p) {
+            const uint64_t k = tkey[sl];
+            if (k == rec.key) { slot = (int)sl; break; }
+            if (k == EMPTY_KEY) break;
+            sl = (sl + 1) & (AW_SLOTS - 1);
+          }
+        }
+        uint32_t head = NIL;
+        if (slot >= 0) { head = thead[slot]; thead[slot] = head | AW_DONE; }
+        if (STYLE == STYLE_INTEGER) {
+          const int64_t v = (int64_t)rec.val;
+          const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
+          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
+          int64_t iv = round_stochastic(x, u53_of(rr));
+          // clones_deaths_zombies (spawning.jl:79-93)
+          const int sr = (iv > 0) - (iv < 0), sv = (v > 0) - (v < 0);
+          if (iv > v) acc.clones += iv - v;
+          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += iv < 0 ? -iv : iv; }
+          else acc.deaths += (iv - v) < 0 ? v - iv : iv - v;
+          uint32_t steps = 0;
+          for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
+            if (c >= ns || ++steps > ns) { bad = true; break; }
+            const int64_t k = (int64_t)cval[c];
+            iv += k;
+            acc.records++;
+            acc.spawns_i += k < 0 ? -k : k;
+          }
+          if (iv != 0) {
+            acc.len_before++;
+            keep = true;
+            vb = (uint64_t)iv;
+            account_kept<STYLE>(a, r, rec.key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
+          }
+        } else {
+          const double dv = diag_float<KIND>(a, r, rep, step, rec);
+          double fv = head == NIL ? dv
+                                  : warp_sum_float<STYLE>(head, !is_zero_d(dv), dv, cval, clink,
+                                                          ns, acc, &bad);
+          keep = warp_settle_float<STYLE>(a, r, step, rec.key, fv, acc);
+          vb = dbits(fv);
+        }
+      }
+      const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+      const uint32_t pos = out + (uint32_t)__popc(mk & lt);
+      if (keep && pos < a.capv) vout[pos] = Rec{rec.key, vb};
+      out += (uint32_t)__popc(mk);
+    }
+    __syncwarp();
+    // ---- the addresses only spawns reached ----
     for (uint32_t i0 = 0; i0 < nsl; i0 += 32) {
       const uint32_t i = i0 + lane;
       bool keep = false;
@@ -1404,79 +1526,31 @@ __global__ void __launch_bounds__(AW_WARPS * 32, 4) k_ann_warp(StepArgs a, int n
       if (i < nsl) {
         const int slot = slist[i];
         key = tkey[slot];
-        uint32_t head = thead[slot];
+        const uint32_t head = thead[slot];
         tkey[slot] = EMPTY_KEY;
         thead[slot] = NIL;
-        if (STYLE == STYLE_INTEGER) {
-          int64_t iv = 0;
-          uint32_t steps = 0;
-          for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
-            if (c >= ncon || ++steps > ncon) { bad = true; break; }
-            const int64_t k = (int64_t)cval[c];
-            iv += k;
-            if (!link_diag(clink[c])) { acc.records++; acc.spawns_i += k < 0 ? -k : k; }
-          }
-          if (iv != 0) {
-            acc.len_before++;
-            keep = true;
-            vb = (uint64_t)iv;
-            const uint64_t mag = (uint64_t)(iv < 0 ? -iv : iv);
-            account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, mag}, acc);
-          }
-        } else {
-          double fv;
-          const uint16_t w0 = clink[head];
-          const uint32_t c1 = link_next(w0);
-          const uint16_t w1 = c1 == NIL ? (uint16_t)LINK_END : clink[c1];
-          if (c1 == NIL || link_next(w1) == NIL) {
-            // one or two contributions: a single IEEE addition is correctly rounded, so it
-            // equals both the exact fixed-point sum and the canonical-order sum
-            const double y0 = bitsd(cval[head]);
-            if (!link_diag(w0)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0))); }
-            fv = y0;
-            if (c1 != NIL) {
-              const double y1 = bitsd(cval[c1]);
-              if (!link_diag(w1)) { acc.records++; acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1))); }
-              fv = __dadd_rn(y0, y1);
-            }
-          } else {
-            U128 sum{0, 0};
-            bool exact = true, have_d = false;
-            double first = 0.0;
+        if (!(head & AW_DONE)) {
+          if (STYLE == STYLE_INTEGER) {
+            int64_t iv = 0;
             uint32_t steps = 0;
             for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
-              if (c >= ncon || ++steps > ncon) { bad = true; break; }
-              const uint64_t v = cval[c];
-              U128 m;
-              const bool ex = fixed_magnitude(bitsd(v), m);
-              if (link_diag(clink[c])) {
-                have_d = true;
-                first = bitsd(v);
-              } else {
-                acc.records++;
-                acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(bitsd(v))));
-              }
-              exact = exact && ex;
-              sum = add128(sum, (v >> 63) ? neg128(m) : m);
+              if (c >= ns || ++steps > ns) { bad = true; break; }
+              const int64_t k = (int64_t)cval[c];
+              iv += k;
+              acc.records++;
+              acc.spawns_i += k < 0 ? -k : k;
             }
-            fv = exact ? signed_fixed_to_double(sum)
-                       : canonical_sum_list(have_d && !is_zero_d(first), first, head, cval, clink,
-                                            ncon, &bad);
-          }
-          if (!is_zero_d(fv)) {
-            acc.len_before++;
-            bool small = false;
-            if (a.comp_mode == 1) small = abs_lt_one(fv);
-            else if (a.comp_mode == 2) small = abs_d(fv) / a.compression < 1;
-            if (small) {
-              keep = compress_draw<STYLE>(a, r, step, key, fv);
-              if (keep) { acc.ncomp++; account_entry<STYLE>(a, r, key, fv, acc); }
-            } else {
+            if (iv != 0) {
+              acc.len_before++;
               keep = true;
-              account_kept<STYLE>(a, r, key, fv, fixed_of(abs_d(fv)), acc);
+              vb = (uint64_t)iv;
+              account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
             }
+          } else {
+            double fv = warp_sum_float<STYLE>(head, false, 0.0, cval, clink, ns, acc, &bad);
+            keep = warp_settle_float<STYLE>(a, r, step, key, fv, acc);
+            vb = dbits(fv);
           }
-          vb = dbits(fv);
         }
       }
       const uint32_t mk = __ballot_sync(0xffffffffu, keep);
@@ -1637,7 +1711,7 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
   if constexpr (KT<K>::BITS == 64) {
     if (a.ann_list) {
       const int want_w = (nb_total + AW_WARPS - 1) / AW_WARPS;
-      const int cap_w = ctx->num_sms * 4;
+      const int cap_w = ctx->num_sms * AW_MINB;
       k_ann_warp<KIND, STYLE><<<want_w < cap_w ? want_w : cap_w, AW_WARPS * 32,
                                 AW_WARPS * AW_WARP_SMEM, st>>>(a, nb_total);
       // the buckets the warps left: as many CTAs as can be resident

@@ -180,14 +180,10 @@ RIMU_HD U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-#ifdef __CUDA_ARCH__
-    uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-    uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-#else
-    uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
-    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-#endif
+    // one 32 x 32 -> 64-bit product gives both halves (a single wide multiply on the GPU)
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
     U4 n;
     n.x = hi1 ^ c.y ^ k0; n.y = lo1; n.z = hi0 ^ c.w ^ k1; n.w = lo0;
     c = n;
@@ -315,7 +311,22 @@ RIMU_HD uint64_t ordered_bits(double v) {
 
 // Unsigned 128-bit fixed point with 2^-64 resolution: |x| -> floor(|x| * 2^64).
 struct U128 { uint64_t lo, hi; };
+RIMU_HD U128 fixed_of_general(double ax);
+// |x| in [2^-12, 2^52), the range of nearly every walker value, takes the short path: the
+// 53-bit significand shifted left by sh = e - 1011 in [0, 64); other values the general one.
 RIMU_HD U128 fixed_of(double ax) {
+  const uint64_t b = dbits(ax) & 0x7fffffffffffffffull;
+  const int sh = (int)(b >> 52) - 1011;
+  if ((unsigned)sh < 64u) {
+    const uint64_t mant = (b & lowmask(52)) | (1ull << 52);
+    U128 r;
+    r.lo = mant << sh;
+    r.hi = sh ? mant >> (64 - sh) : 0;
+    return r;
+  }
+  return fixed_of_general(ax);
+}
+RIMU_HD U128 fixed_of_general(double ax) {
   uint64_t b = dbits(ax) & 0x7fffffffffffffffull;
   int e = (int)(b >> 52);
   U128 r{0, 0};

@@ -51,6 +51,14 @@ enum Flags : unsigned int {
 };
 
 // Parameters of one launch of the step kernels.
+// Warp-per-bucket annihilation: contributions (and table slots) one warp takes, and the
+// default expected contributions per bucket of the steps that use it.
+#ifndef RIMU_AW_CAP
+#define RIMU_AW_CAP 512
+#endif
+constexpr int AW_CAP = RIMU_AW_CAP;
+constexpr int AW_DEFAULT_KPB = AW_CAP * 7 / 8;
+
 struct StepArgs {
   DevModel h;
   int style, op;

@@ -534,6 +534,88 @@ def bench_c3(R, torch, steps=50, max_prep=20000):
             "entries": int(s.wm.last_stats["len"])}
 
 
+def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), krylovdim=24):
+    """The batched configuration at its full length, both ways.  64 x HubbardRealSpace 4x4
+    periodic, N=16, u_i = 1 + 15 i/63, targets log-uniform in [1e4, 1e6],
+    IsDynamicSemistochastic, dt=1e-3, 5 000 steps from 10 walkers on the unit filling, with a
+    ProjectedEnergy onto it: once stepped together (solve_batched) and once one problem after
+    another with the plain step (solve).  Per replica the shift and projected energy with
+    blocking errors (after `skip` steps); walker-steps/s of both; the error-bar ratio; and
+    Lanczos ground energies (tol 1e-10) of some u_i on the full basis (D = 300 540 195)."""
+    import numpy as np
+    nrep = 64
+    geo = R.PeriodicBoundaries(4, 4)
+    addr = R.BoseFS([1] * 16)
+    us = [1.0 + 15.0 * i / 63 for i in range(nrep)]
+    hs = [R.HubbardRealSpace(addr, geo, u=[[u]], t=[1.0]) for u in us]
+    targets = list(10.0 ** np.random.default_rng(2024).uniform(4.0, 6.0, nrep))
+    style = R.IsDynamicSemistochastic()
+
+    def problem(i, seed):
+        return R.ProjectorMonteCarloProblem(
+            hs[i], style=style, time_step=1e-3, last_step=steps, target_walkers=targets[i],
+            start_at={addr: 10.0}, random_seed=seed, max_length=int(4 * targets[i] + 1000),
+            post_step_strategy=R.ProjectedEnergy(hs[i], {addr: 1.0}))
+
+    R.solve_batched([problem(i, 1) for i in range(nrep)][:2], segment_steps=64)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.time()
+    sims_b = R.solve_batched([problem(i, 0x5EED) for i in range(nrep)], segment_steps=64)
+    torch.cuda.synchronize()
+    wall_b = time.time() - t0
+    sims_s, wall_s = [], 0.0
+    for i in range(nrep):
+        p = problem(i, 0x5EED + 1 + i)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        sims_s.append(R.solve(p))
+        torch.cuda.synchronize()
+        wall_s += time.time() - t0
+
+    def estimates(sim):
+        df = sim.df
+        r = R.shift_estimator(df, skip=skip)
+        pe, pe_err = R.projected_energy(df, skip=skip)
+        return {"shift": [float(r.mean), float(r.err)], "projected": [float(pe), float(pe_err)],
+                "walker_steps": float(np.sum(np.asarray(df["norm"], dtype=float)))}
+    eb = [estimates(x) for x in sims_b]
+    es = [estimates(x) for x in sims_s]
+    wb = sum(e["walker_steps"] for e in eb) / wall_b
+    ws = sum(e["walker_steps"] for e in es) / wall_s
+    ratio_err = [eb[i]["shift"][1] / es[i]["shift"][1] for i in range(nrep)]
+    lanczos = {}
+    for i in lanczos_i:
+        op = R.BasisOperator(hs[i])
+        E, _, info = R.eigsolve(op, tol=1e-10, krylovdim=krylovdim)
+        lanczos[i] = {"u": us[i], "E0": E[0], "converged": info["converged"],
+                      "numops": info["numops"], "batched_shift": eb[i]["shift"],
+                      "batched_projected": eb[i]["projected"],
+                      "sequential_shift": es[i]["shift"],
+                      "sequential_projected": es[i]["projected"]}
+        del op
+        torch.cuda.empty_cache()
+    # 2-sigma agreement of each replica's batched and sequential estimates
+    def within(a, b):
+        return abs(a[0] - b[0]) <= 2 * (a[1] ** 2 + b[1] ** 2) ** 0.5
+    agree_shift = sum(within(eb[i]["shift"], es[i]["shift"]) for i in range(nrep))
+    agree_pe = sum(within(eb[i]["projected"], es[i]["projected"]) for i in range(nrep))
+    med = float(np.median(ratio_err))
+    return {"workload": "64 x HubbardRealSpace 4x4 periodic N=16, u_i = 1+15i/63, targets "
+                        "log-uniform [1e4, 1e6], IsDynamicSemistochastic, dt=1e-3, 5000 steps",
+            "steps": steps, "skip": skip,
+            "batched_seconds": wall_b, "sequential_seconds": wall_s,
+            "batched_walker_steps_per_s": wb, "sequential_walker_steps_per_s": ws,
+            "batched_over_sequential": wb / ws,
+            "shift_error_ratio_median": med,
+            "shift_error_ratio_range": [float(np.min(ratio_err)), float(np.max(ratio_err))],
+            "batched_over_sequential_at_equal_error": wb / ws / med ** 2,
+            "replicas_shift_within_2sigma": agree_shift,
+            "replicas_projected_within_2sigma": agree_pe,
+            "lanczos": lanczos,
+            "per_replica": [{"u": us[i], "target": targets[i], "batched": eb[i],
+                             "sequential": es[i]} for i in range(nrep)]}
+
+
 def bench_hv(R, torch, peak):
     """H*v nonzeros/s on HubbardReal1D M=N=14 (D = 20 058 300), forward and adjoint."""
     h = R.HubbardReal1D(R.BoseFS([1] * 14), u=4.0, t=1.0)
@@ -647,6 +729,9 @@ def main():
     ap.add_argument("--no-hv", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--c5-full", action="store_true",
+                    help="only the batched configuration at full length, batched and one by one "
+                         "(about ten minutes), as its own JSON line")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the small (C1) and momentum-space (C3) configuration lines")
     ap.add_argument("--shape", default=None,
@@ -655,6 +740,14 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_setup()
+    if args.c5_full:
+        import torch
+        sys.path.insert(0, os.path.join(ROOT, "rimu.jl_gb300"))
+        from rimugpu import _build
+        _build.build()
+        import rimugpu as R
+        print(json.dumps(bench_c5_full(R, torch)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank, local)
     else:

@@ -78,20 +78,24 @@ def eigsolve(op: BasisOperator, v0=None, howmany=1, which="SR", tol=1e-10, krylo
     v = v0.clone() if v0 is not None else torch.randn(op.dim, dtype=torch.float64, device=dev,
                                                       generator=torch.Generator(dev).manual_seed(1))
     v /= torch.linalg.norm(v)
-    theta_prev = None
     converged = False
     it = 0
+    # the Krylov basis in one preallocated block (rows are vectors), filled in place: memory
+    # is krylovdim + 1 vectors, which matters for bases of 10^8 and more
+    Vm = torch.empty((krylovdim + 1, op.dim), dtype=torch.float64, device=dev)
     for restart in range(maxiter):
-        V = [v]
+        Vm[0] = v
         alphas, betas = [], []
-        w = op(v)
+        w = op(Vm[0])
+        n = 1
         for j in range(krylovdim):
-            a = torch.dot(V[j], w)
+            a = torch.dot(Vm[j], w)
             alphas.append(a.item())
-            w = w - a * V[j] - (betas[-1] * V[j - 1] if j > 0 else 0.0)
-            # full reorthogonalisation
-            Vm = torch.stack(V)
-            w = w - Vm.T @ (Vm @ w)
+            w -= a * Vm[j]
+            if j > 0:
+                w -= betas[-1] * Vm[j - 1]
+            # full reorthogonalisation against the basis so far
+            w -= Vm[:j + 1].T @ (Vm[:j + 1] @ w)
             b = torch.linalg.norm(w).item()
             it += 1
             T = np.diag(alphas) + np.diag(betas, 1) + np.diag(betas, -1)
@@ -100,17 +104,16 @@ def eigsolve(op: BasisOperator, v0=None, howmany=1, which="SR", tol=1e-10, krylo
             if resid < tol or b < 1e-300 or j == krylovdim - 1:
                 break
             betas.append(b)
-            V.append(w / b)
-            w = op(V[-1])
-        Vm = torch.stack(V)
+            torch.div(w, b, out=Vm[j + 1])
+            n = j + 2
+            w = op(Vm[j + 1])
         coef = torch.as_tensor(evecs[:, :howmany], dtype=torch.float64, device=dev)
-        vecs = (Vm.T @ coef).T
+        vecs = (Vm[:n].T @ coef).T
         theta = evals[:howmany]
         if resid < tol:
             converged = True
             break
         v = vecs[0] / torch.linalg.norm(vecs[0])
-        theta_prev = theta
     info = {"converged": converged, "numops": it, "residual": float(resid)}
     return list(map(float, theta)), [vecs[i] for i in range(howmany)], info
 

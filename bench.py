@@ -308,7 +308,7 @@ def run_ours(args, ws, rank, local):
     # ---- matrix-free H*v on the full basis (M = N = 14, D = 20 058 300) ----
     hv_res = None
     if rank == 0 and not args.no_hv:
-        hv_res = bench_hv(R, torch, peak)
+        hv_res = bench_hv(R, torch, peak, with_cpu=not args.no_cpu)
 
     # ---- the small and the momentum-space configurations ----
     c1_res = c3_res = None
@@ -534,7 +534,8 @@ def bench_c3(R, torch, steps=50, max_prep=20000):
             "entries": int(s.wm.last_stats["len"])}
 
 
-def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), krylovdim=24):
+def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), krylovdim=24,
+                  seed=0x5EED):
     """The batched configuration at its full length, both ways.  64 x HubbardRealSpace 4x4
     periodic, N=16, u_i = 1 + 15 i/63, targets log-uniform in [1e4, 1e6],
     IsDynamicSemistochastic, dt=1e-3, 5 000 steps from 10 walkers on the unit filling, with a
@@ -560,12 +561,12 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
     R.solve_batched([problem(i, 1) for i in range(nrep)][:2], segment_steps=64)  # warm-up
     torch.cuda.synchronize()
     t0 = time.time()
-    sims_b = R.solve_batched([problem(i, 0x5EED) for i in range(nrep)], segment_steps=64)
+    sims_b = R.solve_batched([problem(i, seed) for i in range(nrep)], segment_steps=64)
     torch.cuda.synchronize()
     wall_b = time.time() - t0
     sims_s, wall_s = [], 0.0
     for i in range(nrep):
-        p = problem(i, 0x5EED + 1 + i)
+        p = problem(i, seed + 1 + i)
         torch.cuda.synchronize()
         t0 = time.time()
         sims_s.append(R.solve(p))
@@ -576,7 +577,8 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
         df = sim.df
         r = R.shift_estimator(df, skip=skip)
         pe, pe_err = R.projected_energy(df, skip=skip)
-        return {"shift": [float(r.mean), float(r.err)], "projected": [float(pe), float(pe_err)],
+        proj = None if math.isnan(pe) else [float(pe), float(pe_err)]
+        return {"shift": [float(r.mean), float(r.err)], "projected": proj,
                 "walker_steps": float(np.sum(np.asarray(df["norm"], dtype=float)))}
     eb = [estimates(x) for x in sims_b]
     es = [estimates(x) for x in sims_s]
@@ -587,7 +589,10 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
     for i in lanczos_i:
         op = R.BasisOperator(hs[i])
         E, _, info = R.eigsolve(op, tol=1e-10, krylovdim=krylovdim)
+        zb = (eb[i]["shift"][0] - E[0]) / eb[i]["shift"][1]
+        zs = (es[i]["shift"][0] - E[0]) / es[i]["shift"][1]
         lanczos[i] = {"u": us[i], "E0": E[0], "converged": info["converged"],
+                      "batched_shift_z": zb, "sequential_shift_z": zs,
                       "numops": info["numops"], "batched_shift": eb[i]["shift"],
                       "batched_projected": eb[i]["projected"],
                       "sequential_shift": es[i]["shift"],
@@ -596,9 +601,10 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
         torch.cuda.empty_cache()
     # 2-sigma agreement of each replica's batched and sequential estimates
     def within(a, b):
-        return abs(a[0] - b[0]) <= 2 * (a[1] ** 2 + b[1] ** 2) ** 0.5
+        return a is not None and b is not None and abs(a[0] - b[0]) <= 2 * (a[1] ** 2 + b[1] ** 2) ** 0.5
     agree_shift = sum(within(eb[i]["shift"], es[i]["shift"]) for i in range(nrep))
     agree_pe = sum(within(eb[i]["projected"], es[i]["projected"]) for i in range(nrep))
+    n_pe = sum(eb[i]["projected"] is not None and es[i]["projected"] is not None for i in range(nrep))
     med = float(np.median(ratio_err))
     return {"workload": "64 x HubbardRealSpace 4x4 periodic N=16, u_i = 1+15i/63, targets "
                         "log-uniform [1e4, 1e6], IsDynamicSemistochastic, dt=1e-3, 5000 steps",
@@ -611,12 +617,13 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
             "batched_over_sequential_at_equal_error": wb / ws / med ** 2,
             "replicas_shift_within_2sigma": agree_shift,
             "replicas_projected_within_2sigma": agree_pe,
+            "replicas_with_projected_energy": n_pe,
             "lanczos": lanczos,
             "per_replica": [{"u": us[i], "target": targets[i], "batched": eb[i],
                              "sequential": es[i]} for i in range(nrep)]}
 
 
-def bench_hv(R, torch, peak):
+def bench_hv(R, torch, peak, with_cpu=True):
     """H*v nonzeros/s on HubbardReal1D M=N=14 (D = 20 058 300), forward and adjoint."""
     h = R.HubbardReal1D(R.BoseFS([1] * 14), u=4.0, t=1.0)
     op = R.BasisOperator(h)
@@ -650,11 +657,26 @@ def bench_hv(R, torch, peak):
     torch.cuda.synchronize()
     adj_ms = (time.time() - t0) / 3 * 1e3
     bytes_fwd = 8 * D * 2 + 8 * nnz_off
+    # the oracle's H*v on the same basis and vector, all host threads (rows in parallel)
+    cpu = None
+    if with_cpu:
+        import numpy as np
+        import oracle as O
+        O.build()
+        m = O.real1d(14, 14, 4.0, 1.0)
+        keys = O.basis(m)
+        x = v.cpu().numpy()
+        t0 = time.perf_counter()
+        O.hv_basis(m, keys, x)
+        secs = time.perf_counter() - t0
+        cpu = {"value": nnz / secs, "unit": "nnz/s", "seconds": secs, "cores": os.cpu_count(),
+               "kind": "port", "sample": "one full-basis product by the oracle (rows in parallel; "
+                                         "addresses looked up by binary search in the sorted basis)"}
     return {"workload": "HubbardReal1D M=N=14 full basis, D=20058300", "value": nnz / (ms / 1e3),
             "unit": "nnz/s", "ms": ms, "nnz": nnz,
             "achieved_gbs": bytes_fwd / (ms / 1e3) / 1e9, "frac_hbm": bytes_fwd / (ms / 1e3) / 1e9 / peak,
             "fp64_fma_per_s": nnz / (ms / 1e3),
-            "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / ms}
+            "adjoint_ms": adj_ms, "adjoint_over_forward": adj_ms / ms, "cpu_baseline": cpu}
 
 
 # --------------------------------------------------------------------------------------------

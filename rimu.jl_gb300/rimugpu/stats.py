@@ -104,6 +104,8 @@ def ratio_of_means(num, denom, skip=0):
     num = np.asarray(num, float)[skip:]
     den = np.asarray(denom, float)[skip:]
     rn, rd = blocking_analysis(num), blocking_analysis(den)
+    if rd.mean == 0:             # the projector never saw a walker: no estimate
+        return math.nan, math.nan
     r = rn.mean / rd.mean
     k = max(rn.k, rd.k, 1)
     b = 2 ** (k - 1)

@@ -1458,37 +1458,63 @@ __global__ void __launch_bounds__(AW_WARPS * 32, AW_MINB) k_ann_warp(StepArgs a,
       nsl += (uint32_t)__popc(mcl);
     }
     __syncwarp();
-    // ---- the source walkers: diagonal step, lookup, sum, settle, output ----
+    // ---- the source walkers (diagonal step, lookup, the spawns found there), then the
+    // addresses only spawns reached: one loop over both, so the summing and settling code
+    // appears once in the kernel.  The slots start on a fresh round, after every source has
+    // marked the slot it took.
     uint32_t out = 0;
-    for (uint32_t f0 = 0; f0 < nv; f0 += 32) {
+    const uint32_t nvr = (nv + 31u) & ~31u;
+    for (uint32_t f0 = 0; f0 < nvr + nsl; f0 += 32) {
       const uint32_t f = f0 + lane;
-      const Rec rec = nxt;
-      if (f + 32 < nv) nxt = vbase[f + 32];
-      bool keep = false;
-      uint64_t vb = 0;
-      if (f < nv) {
+      const bool is_src = f0 < nvr;
+      Rec rec{};
+      if (is_src) {
+        rec = nxt;
+        if (f + 32 < nv) nxt = vbase[f + 32];
+      }
+      bool keep = false, item = false, have_d = false;
+      uint64_t key = 0, vb = 0;
+      uint32_t head = NIL;
+      double dv = 0.0;
+      int64_t iv = 0;
+      if (is_src && f < nv) {
+        item = true;
+        key = rec.key;
         int slot = -1;
-        uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - AW_TBITS));
         if (ns) {
+          uint32_t sl = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - AW_TBITS));
           for (int p = 0; p < AW_SLOTS; ++p) {
             const uint64_t k = tkey[sl];
-            if (k == rec.key) { slot = (int)sl; break; }
+            if (k == key) { slot = (int)sl; break; }
             if (k == EMPTY_KEY) break;
             sl = (sl + 1) & (AW_SLOTS - 1);
           }
         }
-        uint32_t head = NIL;
         if (slot >= 0) { head = thead[slot]; thead[slot] = head | AW_DONE; }
         if (STYLE == STYLE_INTEGER) {
           const int64_t v = (int64_t)rec.val;
-          const double x = op_diagonal<KIND>(a, r, rec.key) * i2d_exact(v);
-          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, rec.key, 0);
-          int64_t iv = round_stochastic(x, u53_of(rr));
+          const double x = op_diagonal<KIND>(a, r, key) * i2d_exact(v);
+          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, key, 0);
+          iv = round_stochastic(x, u53_of(rr));
           // clones_deaths_zombies (spawning.jl:79-93)
           const int sr = (iv > 0) - (iv < 0), sv = (v > 0) - (v < 0);
           if (iv > v) acc.clones += iv - v;
           else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += iv < 0 ? -iv : iv; }
           else acc.deaths += (iv - v) < 0 ? v - iv : iv - v;
+        } else {
+          dv = diag_float<KIND>(a, r, rep, step, rec);
+          have_d = !is_zero_d(dv);
+        }
+      } else if (!is_src && f - nvr < nsl) {
+        const int slot = slist[f - nvr];
+        key = tkey[slot];
+        head = thead[slot];
+        tkey[slot] = EMPTY_KEY;
+        thead[slot] = NIL;
+        item = !(head & AW_DONE);
+      }
+      if (item) {
+        if (STYLE == STYLE_INTEGER) {
           uint32_t steps = 0;
           for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
             if (c >= ns || ++steps > ns) { bad = true; break; }
@@ -1501,56 +1527,13 @@ __global__ void __launch_bounds__(AW_WARPS * 32, AW_MINB) k_ann_warp(StepArgs a,
             acc.len_before++;
             keep = true;
             vb = (uint64_t)iv;
-            account_kept<STYLE>(a, r, rec.key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
+            account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
           }
         } else {
-          const double dv = diag_float<KIND>(a, r, rep, step, rec);
           double fv = head == NIL ? dv
-                                  : warp_sum_float<STYLE>(head, !is_zero_d(dv), dv, cval, clink,
-                                                          ns, acc, &bad);
-          keep = warp_settle_float<STYLE>(a, r, step, rec.key, fv, acc);
+                                  : warp_sum_float<STYLE>(head, have_d, dv, cval, clink, ns, acc, &bad);
+          keep = warp_settle_float<STYLE>(a, r, step, key, fv, acc);
           vb = dbits(fv);
-        }
-      }
-      const uint32_t mk = __ballot_sync(0xffffffffu, keep);
-      const uint32_t pos = out + (uint32_t)__popc(mk & lt);
-      if (keep && pos < a.capv) vout[pos] = Rec{rec.key, vb};
-      out += (uint32_t)__popc(mk);
-    }
-    __syncwarp();
-    // ---- the addresses only spawns reached ----
-    for (uint32_t i0 = 0; i0 < nsl; i0 += 32) {
-      const uint32_t i = i0 + lane;
-      bool keep = false;
-      uint64_t key = 0, vb = 0;
-      if (i < nsl) {
-        const int slot = slist[i];
-        key = tkey[slot];
-        const uint32_t head = thead[slot];
-        tkey[slot] = EMPTY_KEY;
-        thead[slot] = NIL;
-        if (!(head & AW_DONE)) {
-          if (STYLE == STYLE_INTEGER) {
-            int64_t iv = 0;
-            uint32_t steps = 0;
-            for (uint32_t c = head; c != NIL; c = link_next(clink[c])) {
-              if (c >= ns || ++steps > ns) { bad = true; break; }
-              const int64_t k = (int64_t)cval[c];
-              iv += k;
-              acc.records++;
-              acc.spawns_i += k < 0 ? -k : k;
-            }
-            if (iv != 0) {
-              acc.len_before++;
-              keep = true;
-              vb = (uint64_t)iv;
-              account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
-            }
-          } else {
-            double fv = warp_sum_float<STYLE>(head, false, 0.0, cval, clink, ns, acc, &bad);
-            keep = warp_settle_float<STYLE>(a, r, step, key, fv, acc);
-            vb = dbits(fv);
-          }
         }
       }
       const uint32_t mk = __ballot_sync(0xffffffffu, keep);

@@ -36,9 +36,9 @@ WORKLOAD = "HubbardReal1D M=N=20 u=4 t=1, IsDynamicSemistochastic(threshold=1), 
 
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one k_spawn plus one
-# k_annihilate launch per algorithmic byte (16-byte records read and written), measured at an
-# equilibrated norm of 3e7: (409.8 + 421.6 + 838.1 + 355.5) MB / (830 + 1211) MB.
-TRAFFIC_PER_ALGORITHMIC_BYTE = (409.8 + 421.6 + 838.1 + 355.5) / (830.0 + 1211.0)
+# k_ann_warp launch per algorithmic byte (16-byte records read and written), measured at an
+# equilibrated norm of 3e7: (568.6 + 571.6 + 864.2 + 358.4) MB / (830 + 1211) MB.
+TRAFFIC_PER_ALGORITHMIC_BYTE = (568.6 + 571.6 + 864.2 + 358.4) / (830.0 + 1211.0)
 
 
 def peaks():
@@ -239,11 +239,11 @@ def run_ours(args, ws, rank, local):
                 "frac": round(achieved / peak, 4),
                 "traffic": args.traffic if args.traffic is not None else
                 round(TRAFFIC_PER_ALGORITHMIC_BYTE * k_bytes / steps_t),
-                "traffic_source": "ncu dram bytes per algorithmic byte of k_spawn + k_annihilate "
+                "traffic_source": "ncu dram bytes per algorithmic byte of k_spawn + k_ann_warp "
                                   "measured at an equilibrated norm of 3e7, scaled by this run's "
                                   "records per step" if args.traffic is None else "given",
                 "peak_source": peak_kind,
-                "kernel": "k_spawn + k_spawn_heavy + k_annihilate (one step)",
+                "kernel": "k_spawn + k_spawn_heavy + k_ann_warp + k_annihilate (one step)",
                 "bytes_per_step": k_bytes / steps_t, "ms_per_step": k_ms / steps_t,
                 "spawn": {"ms": tim["spawn_ms"] / steps_t,
                           "gbs": tim["spawn_bytes"] / (tim["spawn_ms"] / 1e3) / 1e9 if tim["spawn_ms"] else 0},
@@ -352,7 +352,8 @@ def run_ours(args, ws, rank, local):
                        "equilibration": f"{prep} untimed steps from the unit-filling start address",
                        "l2": "inputs larger than L2 (walker list > 1 GB), no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "launch_shape": args.shape or "default (1024 contributions per bucket, automatic table)"},
+                       "launch_shape": args.shape or "default (at most 448 contributions per bucket on "
+                                       "average, one warp per bucket)"},
             "gpu_launches": 4 * args.steps,
             "roofline": roofline,
             "e2e": e2e,

@@ -57,3 +57,33 @@ def test_files_that_are_not_state_files_are_rejected(tmp_path):
             w.write_table(t)
         with pytest.raises(ValueError):
             rimuio.load_pairs(f)
+
+
+def test_save_and_load_a_product_vector(tmp_path):
+    """The reference's "save DVec" case (test/RimuIO.jl:110-115): H * v for
+    HubbardReal1D(BoseFS(1,1,1)) and v = {BoseFS(1,1,1) => 1.0, BoseFS(2,1,0) => pi}, saved and
+    loaded back equal, key for key and bit for bit.  The product is the oracle's exact step with
+    the plain Hamiltonian (IsDeterministic, no transition factor)."""
+    import math
+    import oracle as O
+    m = O.real1d(3, 3, 1.0, 1.0)
+    keys = np.array(sorted([R.BoseFS(1, 1, 1).key, R.BoseFS(2, 1, 0).key]), dtype=np.uint64)
+    vals = np.array([1.0 if k == R.BoseFS(1, 1, 1).key else math.pi for k in keys])
+    hk, hv, _ = O.step(m, O.StepParams(O.STYLE_DETERMINISTIC, op=O.OP_HAMILTONIAN), keys, vals)
+    assert len(hk) > 2
+    f = tmp_path / "dvec.arrow"
+    rimuio.save_pairs(f, hk, hv, R.BoseFS(1, 1, 1))
+    k, v, p, _ = rimuio.load_pairs(f)
+    o = np.argsort(k)
+    assert np.array_equal(k[o], hk) and np.array_equal(np.asarray(v)[o].view(np.uint64), hv.view(np.uint64))
+    assert isinstance(p, R.BoseFS) and (p.N, p.M) == (3, 3)
+
+
+@pytest.mark.parametrize("dtype", [np.int64, np.float64])
+def test_empty_vectors_of_both_value_types(tmp_path, dtype):
+    """The reference's "save empty vector" case (test/RimuIO.jl:136-145) for integer and float
+    values."""
+    f = tmp_path / "empty.arrow"
+    rimuio.save_pairs(f, np.zeros(0, dtype=np.uint64), np.zeros(0, dtype=dtype), R.BoseFS([1, 1, 1, 1]))
+    k, v, _, meta = rimuio.load_pairs(f)
+    assert len(k) == 0 and len(v) == 0 and meta["RIMU_PACKAGE_VERSION"] == "0.14.0"

@@ -58,9 +58,10 @@ typedef struct rimu_wm rimu_wm;
 
 /* Hamiltonian description.  Addresses are bit strings (BoseFS: n_particles + n_modes - 1
  * bits; FermiFS: n_modes bits) with the layout of src/BitStringAddresses/bitstring.jl:464-472
- * (bosons) and 713-723 (fermions).  Up to 64 bits an address is one uint64_t.  HubbardReal1D
- * and one-component HubbardRealSpace also take addresses of 65-128 bits (the reference's
- * two-chunk BitString, bitstring.jl:6-18): wherever such an address crosses this interface it
+ * (bosons) and 713-723 (fermions).  Up to 64 bits an address is one uint64_t.  HubbardReal1D,
+ * one-component HubbardRealSpace and HubbardMom1D (BoseFS, at most 64 modes) also take
+ * addresses of 65-128 bits (the reference's two-chunk BitString, bitstring.jl:6-18): wherever
+ * such an address crosses this interface it
  * is a pair of uint64_t, (lo, hi), bit k of the address being bit k of lo for k < 64 and bit
  * k - 64 of hi otherwise; key arrays then hold 2 words per address.  Walker lists for them
  * are created with rimu_vec_create_kw(..., key_words = 2, ...).
@@ -111,7 +112,8 @@ typedef struct {
 } rimu_step_params;
 
 /* Initiator rules (initiators.jl:132-234): NonInitiator, Initiator, SimpleInitiator,
- * CoherentInitiator.  With a rule, addresses must fit in 63 bits. */
+ * CoherentInitiator.  With a rule, addresses must fit in 63 bits, or in 127 bits of two words
+ * (a spawn's class travels in the top bit of its address's top word). */
 enum { RIMU_INIT_NONE = 0, RIMU_INIT_INITIATOR = 1, RIMU_INIT_SIMPLE = 2, RIMU_INIT_COHERENT = 3 };
 
 /* Step statistics (step_stats, styles.jl:14-19,94-96,203-208; compression.jl:16) plus the
@@ -170,8 +172,8 @@ int rimu_model_offdiagonals(rimu_model *m, uint64_t key, uint64_t *keys, double 
 int rimu_vec_create(rimu_ctx *ctx, int val_kind, int64_t capacity_hint, rimu_vec **out);
 /* A walker list with key_words = 1 (addresses of at most 64 bits) or 2 (65-128 bits; its key
  * arrays in upload, download and lookup hold (lo, hi) pairs).  Two-word lists step with
- * rimu_apply_operator (without initiator rules or projectors); dot products, conversions and
- * batched runs take one-word lists. */
+ * rimu_apply_operator (without projectors), and take dot products and conversions with lists
+ * of the same width; batched runs take one-word lists. */
 int rimu_vec_create_kw(rimu_ctx *ctx, int val_kind, int key_words, int64_t capacity_hint,
                        rimu_vec **out);
 int rimu_vec_key_words(const rimu_vec *v, int *key_words);

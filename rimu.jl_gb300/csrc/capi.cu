@@ -186,9 +186,10 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     nbits = cbits[0] + cbits[1];
   }
   if (nbits > 128) return bad("rimu_model_create: address does not fit 128 bits");
-  if ((nbits > 64 || d->n_modes > 64) && (two || d->kind == RIMU_MODEL_MOM1D))
-    return bad("rimu_model_create: addresses wider than 64 bits need HubbardReal1D or "
-               "one-component HubbardRealSpace");
+  if ((nbits > 64 || d->n_modes > 64) && two)
+    return bad("rimu_model_create: two-component addresses must fit 64 bits");
+  if (d->n_modes > 64 && d->kind == RIMU_MODEL_MOM1D)
+    return bad("rimu_model_create: HubbardMom1D takes at most 64 modes");
   if (d->fermion && d->kind != RIMU_MODEL_REALSPACE)
     return bad("rimu_model_create: FermiFS is supported with HubbardRealSpace only");
   if (d->fermion && d->n_particles > d->n_modes) return bad("rimu_model_create: too many fermions");
@@ -349,6 +350,11 @@ extern "C" int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t 
 
 static int host_num_offdiagonals(const rimu_model *m, uint64_t key, uint64_t key_hi = 0) {
   const DevModel &h = m->dm;
+  if (h.nbits > 64 && h.kind == MODEL_MOM1D) {
+    MomMap mm;
+    mom_map(k128(key, key_hi), mm);
+    return num_offdiagonals_mom(h, mm);
+  }
   if (h.nbits > 64) return num_offdiagonals_real(h, k128(key, key_hi));
   if (h.kind == MODEL_MOM1D && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
   if (h.kind == MODEL_MOM1D) {
@@ -778,15 +784,16 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     return bad("rimu_apply_operator: thresholding not supported for integer walkers");
   if (p->initiator < RIMU_INIT_NONE || p->initiator > RIMU_INIT_COHERENT)
     return bad("rimu_apply_operator: unknown initiator rule");
-  if (p->initiator != RIMU_INIT_NONE && m->dm.nbits > 63)
-    return bad("rimu_apply_operator: initiator rules need addresses of at most 63 bits");
+  if (p->initiator != RIMU_INIT_NONE && (m->dm.nbits == 64 || m->dm.nbits > 127))
+    return bad("rimu_apply_operator: initiator rules need addresses of at most 63 bits or of "
+               "65-127 bits (a flag bit above the address)");
   if (!(p->boost > 0)) return bad("rimu_apply_operator: boost must be positive");
   {
     const int need_kw = m->dm.nbits > 64 ? 2 : 1;
     if (source->kw != need_kw)
       return bad("rimu_apply_operator: the vector's address width does not match the model's");
-    if (need_kw == 2 && (p->initiator != RIMU_INIT_NONE || w->nproj != 0))
-      return bad("rimu_apply_operator: initiator rules and projectors need addresses of at most 64 bits");
+    if (need_kw == 2 && w->nproj != 0)
+      return bad("rimu_apply_operator: projectors need addresses of at most 64 bits");
     if (target->kw != need_kw) {
       target->kw = need_kw;
       target->nb_bits = -1;                   // forces a new allocation below

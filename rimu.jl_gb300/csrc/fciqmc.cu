@@ -37,8 +37,8 @@ __device__ __noinline__ double ratio_to_threshold(double x, double y) { return x
 template <int KIND, class K>
 __device__ __forceinline__ int column_noff(const DevModel &h, K key) {
   if constexpr (KIND == MODEL_MOM1D) {
-    // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144)
-    if (h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
+    // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144); one-word keys only
+    if (KT<K>::BITS == 64 && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
     MomMap m;
     mom_map(key, m);
     return num_offdiagonals_mom(h, m);
@@ -53,7 +53,9 @@ __device__ __forceinline__ OffdiagT<K> column_offdiag(const DevModel &h, K key, 
   } else if constexpr (KIND == MODEL_REALSPACE) {
     return realspace_offdiag(h, key, chosen);
   } else {
-    if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
+    if constexpr (KT<K>::BITS == 64) {
+      if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
+    }
     MomMap m;
     mom_map(key, m);
     return mom1d_offdiag(h, key, m, chosen);
@@ -111,7 +113,28 @@ template <int KIND, class K>
 __device__ double model_diagonal(const DevModel &h, K key) {
   if constexpr (KT<K>::BITS == 64) return model_diagonal64<KIND>(h, key);
   else if constexpr (KIND == MODEL_REAL1D) return h.u * (double)bose_interaction(key) / 2;
-  else {
+  else if constexpr (KIND == MODEL_MOM1D) {
+    // dot(h.kes, map) + u/(2M) * momentum_transfer_diagonal(map) (HubbardMom1D.jl:174-177),
+    // the same arithmetic as on one-word addresses
+    K x = key;
+    int mode = 1, s = 0;
+    int occ[MAX_MODES];
+    double kin = 0.0;
+    while (!kzero(x)) {
+      int z = kctz(x);
+      x = kshr(x, z); mode += z;
+      int n = kctz(~x);
+      kin += h.kes[mode - 1] * (double)n;
+      occ[s++] = n;
+      x = kshr(x, n);
+    }
+    long long onp = 0;
+    for (int i = 0; i < s; ++i) {
+      onp += (long long)occ[i] * (occ[i] - 1);
+      for (int j = 0; j < i; ++j) onp += 4LL * occ[i] * occ[j];
+    }
+    return kin + h.u / (2 * h.M) * (double)onp;
+  } else {
     // HubbardRealSpace one component (HubbardRealSpace.jl:284-293)
     double in = 0.0;
     if (!h.fermion && h.u != 0.0) in = h.u * (double)bose_interaction(key) / 2;
@@ -258,9 +281,16 @@ __device__ __forceinline__ uint32_t step_of(const StepArgs &a) {
   return a.step_dev ? a.step + *a.step_dev : a.step;
 }
 
-// A spawn of a non-initiator parent carries bit 63 of its address (initiator rules only;
-// addresses then fit in 63 bits); the bucket is that of the address itself.
+// A spawn of a non-initiator parent carries bit 63 of its address's top word (initiator rules
+// only; addresses then fit in 63 bits, or in 127 bits of two words); the bucket is that of the
+// address itself.
 constexpr uint64_t UNSAFE_BIT = 1ull << 63;
+__device__ __forceinline__ uint64_t with_flag(uint64_t k, uint64_t flag) { return k | flag; }
+__device__ __forceinline__ Key128 with_flag(Key128 k, uint64_t flag) { k.hi |= flag; return k; }
+__device__ __forceinline__ bool has_flag(uint64_t k) { return (k & UNSAFE_BIT) != 0; }
+__device__ __forceinline__ bool has_flag(Key128 k) { return (k.hi & UNSAFE_BIT) != 0; }
+__device__ __forceinline__ uint64_t without_flag(uint64_t k) { return k & ~UNSAFE_BIT; }
+__device__ __forceinline__ Key128 without_flag(Key128 k) { k.hi &= ~UNSAFE_BIT; return k; }
 
 template <class K>
 __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout lay, K nk,
@@ -269,8 +299,7 @@ __device__ __forceinline__ void emit_spawn(const StepArgs &a, int r, RepLayout l
   const uint32_t pos = atomicAdd(&a.scount[b], 1u);
   if (pos < a.caps) {
     RecT<K> *sp = static_cast<RecT<K> *>(a.spawn);
-    if constexpr (KT<K>::BITS == 64) sp[(size_t)b * a.caps + pos] = RecT<K>{nk | flag, vb};
-    else sp[(size_t)b * a.caps + pos] = RecT<K>{nk, vb};   // no initiator rules: flag is 0
+    sp[(size_t)b * a.caps + pos] = RecT<K>{with_flag(nk, flag), vb};
   } else {
     atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
   }
@@ -1021,12 +1050,13 @@ __global__ void __launch_bounds__(ANN_THREADS, 4) k_annihilate(StepArgs a, int n
         if (f < need) {
           src = f < nv;
           RecT<K> rec = src ? vbase[f] : sp[f - nv];
-          if constexpr (KT<K>::BITS == 64) if (a.init_rule) {
+          if (a.init_rule) {
             // classes of the initiator rules (initiators.jl:142-157): a spawn carries its
-            // parent's class in bit 63; a diagonal term is "initiator" for an initiator
+            // parent's class in bit 63 of the top word; a diagonal term is "initiator" for an
+            // initiator
             if (src) cls = parent_unsafe<STYLE>(a, rec.val) ? CLS_SAFE : CLS_INITIATOR;
-            else cls = (rec.key & UNSAFE_BIT) ? CLS_UNSAFE : CLS_SAFE;
-            rec.key &= ~UNSAFE_BIT;
+            else cls = has_flag(rec.key) ? CLS_UNSAFE : CLS_SAFE;
+            rec.key = without_flag(rec.key);
           }
           if (lvl == 0 || (split_word(kword(rec.key)) & mask) == sel) {
             slot = table_insert(tkey, T, tbits, rec.key, claimed);
@@ -1722,11 +1752,11 @@ static int launch_step_k(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
 using namespace rimu;
 
 int rimu_launch_step(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
-  if (a.kw == 2) {   // two-word addresses: HubbardReal1D and one-component HubbardRealSpace
+  if (a.kw == 2) {   // two-word addresses: one-component models
     switch (a.h.kind) {
       case MODEL_REAL1D: return launch_step_k<MODEL_REAL1D, Key128>(ctx, a, nb_total, ev);
       case MODEL_REALSPACE: return launch_step_k<MODEL_REALSPACE, Key128>(ctx, a, nb_total, ev);
-      default: rimu_set_error("two-word addresses: model not supported"); return RIMU_ERR_BADARG;
+      default: return launch_step_k<MODEL_MOM1D, Key128>(ctx, a, nb_total, ev);
     }
   }
   switch (a.h.kind) {
@@ -1821,7 +1851,8 @@ int rimu_launch_diagonal(rimu_ctx *ctx, const DevModel &h, const uint64_t *keys,
   if (h.nbits > 64) {
     const Key128 *k2 = reinterpret_cast<const Key128 *>(keys);
     if (h.kind == MODEL_REAL1D) k_diagonal<MODEL_REAL1D><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
-    else k_diagonal<MODEL_REALSPACE><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
+    else if (h.kind == MODEL_REALSPACE) k_diagonal<MODEL_REALSPACE><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
+    else k_diagonal<MODEL_MOM1D><<<g, 256, 0, ctx->stream>>>(h, k2, n, out);
     return rimu_cuda_check(cudaGetLastError(), "k_diagonal");
   }
   switch (h.kind) {
@@ -1842,7 +1873,8 @@ int rimu_launch_offdiagonals(rimu_ctx *ctx, const DevModel &h, uint64_t key_lo, 
     const Key128 key = k128(key_lo, key_hi);
     Key128 *k2 = reinterpret_cast<Key128 *>(keys);
     if (h.kind == MODEL_REAL1D) k_offdiagonals<MODEL_REAL1D><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
-    else k_offdiagonals<MODEL_REALSPACE><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
+    else if (h.kind == MODEL_REALSPACE) k_offdiagonals<MODEL_REALSPACE><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
+    else k_offdiagonals<MODEL_MOM1D><<<g, 128, 0, ctx->stream>>>(h, key, noff, k2, vals);
     return rimu_cuda_check(cudaGetLastError(), "k_offdiagonals");
   }
   const uint64_t key = key_lo;

@@ -727,24 +727,27 @@ RIMU_HD Offdiag mom2c_offdiag(const DevModel &h, uint64_t key, int chosen) {
 
 // HubbardMom1D occupied mode map in registers (OccupiedModeMap, fockaddress.jl:258-281).
 struct MomMap { int s, d; uint8_t mode[MAX_MODES]; uint8_t occ[MAX_MODES]; };
-RIMU_HD void mom_map(uint64_t key, MomMap &m) {
-  uint64_t x = key;
+template <class K>
+RIMU_HD void mom_map(K key, MomMap &m) {
+  K x = key;
   int mode = 1;
   m.s = 0; m.d = 0;
-  while (x) {
-    int z = ctz64(x);
-    x = shr64(x, z); mode += z;
-    int n = ctz64(~x);
+  while (!kzero(x)) {
+    int z = kctz(x);
+    x = kshr(x, z); mode += z;
+    int n = kctz(~x);
     m.mode[m.s] = (uint8_t)mode; m.occ[m.s] = (uint8_t)n; m.s++; m.d += n > 1;
-    x = shr64(x, n);
+    x = kshr(x, n);
   }
 }
 RIMU_HD int num_offdiagonals_mom(const DevModel &h, const MomMap &m) {
   return m.s * (m.s - 1) * (h.M - 2) + m.d * (h.M - 1);
 }
 
-// momentum_transfer_excitation with fold=true (excitations.jl:26-80).
-RIMU_HD Offdiag mom1d_offdiag(const DevModel &h, uint64_t key, const MomMap &m, int chosen) {
+// momentum_transfer_excitation with fold=true (excitations.jl:26-80), on one- or two-word
+// addresses.
+template <class K>
+RIMU_HD OffdiagT<K> mom1d_offdiag(const DevModel &h, K key, const MomMap &m, int chosen) {
   int M = h.M, s = m.s;
   int dbl = chosen - s * (s - 1) * (M - 2);
   int p_idx, q_idx, mom;
@@ -783,11 +786,11 @@ RIMU_HD Offdiag mom1d_offdiag(const DevModel &h, uint64_t key, const MomMap &m, 
   v *= c_d2 + 1;
   int c_d1 = o_d1 - (dst1 == src2) - (dst1 == src1) + (dst1 == dst2);
   v *= c_d1 + 1;
-  Offdiag r{key, 0, 1};
+  OffdiagT<K> r{key, 0, 1};
   if (v == 0) return r;
   // apply the moves on the bit string: destroy at src offsets, create at dst offsets,
   // one particle at a time with fresh offsets each time
-  uint64_t k1 = key;
+  K k1 = key;
   {
     ModeIdx a = bose_find_mode(k1, src2), b = bose_find_mode(k1, dst2);
     k1 = bose_move(k1, a.offset, b.offset);

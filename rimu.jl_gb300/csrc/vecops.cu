@@ -18,51 +18,62 @@ using namespace rimu;
 namespace {
 
 constexpr int DOT_THREADS = 256;
-constexpr uint32_t DOT_SLOTS = 2048;     // table slots (32 KB of keys and values)
-constexpr uint32_t DOT_CHUNK = DOT_SLOTS / 2;
+
+// Table of the coarse bucket: 2048 slots for one-word addresses (32 KB of keys and values),
+// 1024 for two-word ones (24 KB), half of them filled per chunk.
+template <class K> struct DotSlots { static constexpr uint32_t n = KT<K>::BITS == 64 ? 2048 : 1024; };
 
 __device__ __forceinline__ double value_of(uint64_t bits, int kind) {
   return kind == RIMU_VAL_I64 ? (double)(int64_t)bits : bitsd(bits);
 }
 
+__device__ __forceinline__ bool claim(uint64_t *slot, uint64_t key) {
+  return atomicCAS((unsigned long long *)slot, (unsigned long long)EMPTY_KEY,
+                   (unsigned long long)key) == EMPTY_KEY;
+}
+__device__ __forceinline__ bool claim(Key128 *slot, Key128 key) {
+  return atomicCAS(slot, KT<Key128>::empty(), key) == KT<Key128>::empty();
+}
+
+template <class K>
 __global__ void __launch_bounds__(DOT_THREADS) k_vec_dot(
-    const Rec *ra, const uint32_t *ca, int bits_a, uint32_t capv_a, int kind_a,
-    const Rec *rb, const uint32_t *cb, int bits_b, uint32_t capv_b, int kind_b,
+    const RecT<K> *ra, const uint32_t *ca, int bits_a, uint32_t capv_a, int kind_a,
+    const RecT<K> *rb, const uint32_t *cb, int bits_b, uint32_t capv_b, int kind_b,
     double *partials) {
-  __shared__ uint64_t tkey[DOT_SLOTS];
-  __shared__ double tval[DOT_SLOTS];
+  constexpr uint32_t SLOTS = DotSlots<K>::n, CHUNK = SLOTS / 2;
+  constexpr int TBITS = SLOTS == 2048 ? 11 : 10;
+  __shared__ K tkey[SLOTS];
+  __shared__ double tval[SLOTS];
   __shared__ double red[DOT_THREADS];
   const int tid = threadIdx.x;
   const int nba = 1 << bits_a, sub = 1 << (bits_b - bits_a);
+  const K EMPTY = KT<K>::empty();
   double acc = 0.0;
   for (int i = blockIdx.x; i < nba; i += gridDim.x) {
     const uint32_t na = ca[i] < capv_a ? ca[i] : capv_a;
-    for (uint32_t c0 = 0; c0 < na; c0 += DOT_CHUNK) {
-      const uint32_t c1 = c0 + DOT_CHUNK < na ? c0 + DOT_CHUNK : na;
-      for (uint32_t s = tid; s < DOT_SLOTS; s += DOT_THREADS) tkey[s] = EMPTY_KEY;
+    for (uint32_t c0 = 0; c0 < na; c0 += CHUNK) {
+      const uint32_t c1 = c0 + CHUNK < na ? c0 + CHUNK : na;
+      for (uint32_t s = tid; s < SLOTS; s += DOT_THREADS) tkey[s] = EMPTY;
       __syncthreads();
       for (uint32_t e = c0 + tid; e < c1; e += DOT_THREADS) {
-        const Rec rec = ra[(size_t)i * capv_a + e];
-        uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - 11));
-        for (uint32_t p = 0; p < DOT_SLOTS; ++p) {     // addresses of a list are distinct
-          const unsigned long long old = atomicCAS((unsigned long long *)&tkey[sl],
-                                                   (unsigned long long)EMPTY_KEY,
-                                                   (unsigned long long)rec.key);
-          if (old == EMPTY_KEY) { tval[sl] = value_of(rec.val, kind_a); break; }
-          sl = (sl + 1) & (DOT_SLOTS - 1);
+        const RecT<K> rec = ra[(size_t)i * capv_a + e];
+        uint32_t sl = (uint32_t)((kword(rec.key) * 0x9E3779B97F4A7C15ull) >> (64 - TBITS));
+        for (uint32_t p = 0; p < SLOTS; ++p) {     // addresses of a list are distinct
+          if (claim(&tkey[sl], rec.key)) { tval[sl] = value_of(rec.val, kind_a); break; }
+          sl = (sl + 1) & (SLOTS - 1);
         }
       }
       __syncthreads();
       for (int j = i * sub; j < (i + 1) * sub; ++j) {
         const uint32_t nb = cb[j] < capv_b ? cb[j] : capv_b;
         for (uint32_t e = tid; e < nb; e += DOT_THREADS) {
-          const Rec rec = rb[(size_t)j * capv_b + e];
-          uint32_t sl = (uint32_t)((rec.key * 0x9E3779B97F4A7C15ull) >> (64 - 11));
-          for (uint32_t p = 0; p < DOT_SLOTS; ++p) {
-            const uint64_t k = tkey[sl];
+          const RecT<K> rec = rb[(size_t)j * capv_b + e];
+          uint32_t sl = (uint32_t)((kword(rec.key) * 0x9E3779B97F4A7C15ull) >> (64 - TBITS));
+          for (uint32_t p = 0; p < SLOTS; ++p) {
+            const K k = tkey[sl];
             if (k == rec.key) { acc += tval[sl] * value_of(rec.val, kind_b); break; }
-            if (k == EMPTY_KEY) break;
-            sl = (sl + 1) & (DOT_SLOTS - 1);
+            if (k == EMPTY) break;
+            sl = (sl + 1) & (SLOTS - 1);
           }
         }
       }
@@ -86,11 +97,12 @@ __global__ void k_sum_partials(const double *partials, int n, double *out) {
   }
 }
 
-__global__ void k_convert_i64_f64(const Rec *src, Rec *dst, size_t n) {
+template <class K>
+__global__ void k_convert_i64_f64(const RecT<K> *src, RecT<K> *dst, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const Rec r = src[i];
-    dst[i] = Rec{r.key, dbits((double)(int64_t)r.val)};
+    const RecT<K> r = src[i];
+    dst[i] = RecT<K>{r.key, dbits((double)(int64_t)r.val)};
   }
 }
 
@@ -104,7 +116,7 @@ int fail_arg(const std::string &msg) {
 extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
   if (!a || !b || !out) return fail_arg("rimu_vec_dot: NULL argument");
   if (a->ctx != b->ctx) return fail_arg("rimu_vec_dot: vectors of different contexts");
-  if (a->kw != 1 || b->kw != 1) return fail_arg("rimu_vec_dot: addresses of at most 64 bits only");
+  if (a->kw != b->kw) return fail_arg("rimu_vec_dot: vectors of different address widths");
   if (a->nb_bits > b->nb_bits) std::swap(a, b);
   rimu_ctx *ctx = a->ctx;
   const int nba = 1 << a->nb_bits;
@@ -112,9 +124,14 @@ extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
   double *partials = nullptr, *res = nullptr;
   int rc;
   if ((rc = dalloc(ctx, &partials, grid)) || (rc = dalloc(ctx, &res, 1))) return rc;
-  k_vec_dot<<<grid, DOT_THREADS, 0, ctx->stream>>>(a->recs, a->count, a->nb_bits, a->capv,
-                                                   a->val_kind, b->recs, b->count, b->nb_bits,
-                                                   b->capv, b->val_kind, partials);
+  if (a->kw == 2)
+    k_vec_dot<Key128><<<grid, DOT_THREADS, 0, ctx->stream>>>(
+        reinterpret_cast<const Rec2 *>(a->recs), a->count, a->nb_bits, a->capv, a->val_kind,
+        reinterpret_cast<const Rec2 *>(b->recs), b->count, b->nb_bits, b->capv, b->val_kind, partials);
+  else
+    k_vec_dot<uint64_t><<<grid, DOT_THREADS, 0, ctx->stream>>>(
+        a->recs, a->count, a->nb_bits, a->capv, a->val_kind,
+        b->recs, b->count, b->nb_bits, b->capv, b->val_kind, partials);
   k_sum_partials<<<1, 32, 0, ctx->stream>>>(partials, grid, res);
   rc = rimu_cuda_check(cudaGetLastError(), "k_vec_dot");
   if (!rc) rc = d2h(ctx, out, res, 1);
@@ -127,7 +144,6 @@ extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
 extern "C" int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind) {
   if (!dst || !src) return fail_arg("rimu_vec_convert: NULL argument");
   if (dst == src) return fail_arg("rimu_vec_convert: dst and src must differ");
-  if (src->kw != 1) return fail_arg("rimu_vec_convert: addresses of at most 64 bits only");
   if (val_kind != RIMU_VAL_F64 && val_kind != RIMU_VAL_I64) return fail_arg("rimu_vec_convert: bad val_kind");
   if (src->val_kind != val_kind && val_kind != RIMU_VAL_F64)
     return fail_arg("rimu_vec_convert: only Int64 to Float64 converts");
@@ -136,7 +152,12 @@ extern "C" int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind
   if (src->val_kind == val_kind) return RIMU_OK;
   rimu_ctx *ctx = dst->ctx;
   const size_t n = ((size_t)1 << dst->nb_bits) * dst->capv;
-  k_convert_i64_f64<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(dst->recs, dst->recs, n);
+  if (dst->kw == 2)
+    k_convert_i64_f64<Key128><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
+        reinterpret_cast<Rec2 *>(dst->recs), reinterpret_cast<Rec2 *>(dst->recs), n);
+  else
+    k_convert_i64_f64<uint64_t><<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(
+        dst->recs, dst->recs, n);
   dst->val_kind = RIMU_VAL_F64;
   return rimu_cuda_check(cudaGetLastError(), "k_convert_i64_f64");
 }

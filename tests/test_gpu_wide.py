@@ -1,8 +1,10 @@
 """Addresses of 65-128 bits (the reference's two-chunk BitString, bitstring.jl:6-18) on the
 GPU against the oracle, bit for bit: HubbardReal1D with BoseFS{50,50} (99 bits) and
 BoseFS{40,30} (69 bits), HubbardRealSpace with bosons on an 8x8 lattice (103 bits) and with
-fermions on a 10x10 lattice (100 bits); matrix elements and step trajectories of the three
-styles, whose random numbers are keyed on lo ^ mix64(hi) of the address."""
+fermions on a 10x10 lattice (100 bits), HubbardMom1D with 20 bosons in 50 momentum modes
+(69 bits); matrix elements and step trajectories of the three styles, whose random numbers are
+keyed on lo ^ mix64(hi) of the address; initiator rules (the flag in bit 63 of the top word)
+and dot products of two-word lists."""
 import numpy as np
 import pytest
 
@@ -25,6 +27,7 @@ def _models():
         "realspace-bose-103": R.HubbardRealSpace(R.BoseFS(b8), geometry=R.PeriodicBoundaries(8, 8),
                                                  u=[[3.0]], v=[1.5, 0.5]),
         "realspace-fermi-100": R.HubbardRealSpace(R.FermiFS(f10), geometry=R.HardwallBoundaries(10, 10)),
+        "mom1d-69": R.HubbardMom1D(R.BoseFS(50, {25: 20}), u=2.0),
     }
 
 
@@ -65,6 +68,9 @@ CASES = [
     ("det-real1d-69", "real1d-69", R.IsDeterministic, 1.0, 5, 0.02),
     ("dss-realspace-bose-103", "realspace-bose-103", R.IsDynamicSemistochastic, 300.0, 20, 0.005),
     ("int-realspace-fermi-100", "realspace-fermi-100", R.IsStochasticInteger, 300, 20, 0.01),
+    ("det-mom1d-69", "mom1d-69", R.IsDeterministic, 1.0, 3, 0.01),
+    ("int-mom1d-69", "mom1d-69", R.IsStochasticInteger, 300, 15, 0.005),
+    ("dss-mom1d-69", "mom1d-69", R.IsDynamicSemistochastic, 300.0, 15, 0.005),
 ]
 
 
@@ -94,15 +100,51 @@ def test_wide_vectors_store_and_step_many_buckets():
     assert_same_step(g, o, R.IsDynamicSemistochastic())
 
 
-def test_wide_addresses_reject_what_they_cannot_do():
+@pytest.mark.parametrize("rule", [R.Initiator(2.0), R.SimpleInitiator(2.0), R.CoherentInitiator(2.0)],
+                         ids=["initiator", "simple", "coherent"])
+def test_wide_initiator_rules_match_oracle(rule):
+    """Initiator rules on 99-bit addresses: the class of a spawn travels in bit 63 of the
+    address's top word.  Ten DSS steps from 40 walkers, bit for bit against the oracle."""
     h = _models()["real1d-99"]
-    v = R.GPUDVec({h.address: 1.0}, style=R.IsDeterministic())
-    with pytest.raises(R.RimuError):
-        v.dot(v)
-    with pytest.raises(R.RimuError):     # initiator rules use bit 63 of the address
-        R.apply_operator(R.GPUWorkingMemory(1),
-                         R.GPUDVec(style=R.IsDynamicSemistochastic(), address_type=h.address,
-                                   initiator=R.Initiator(1.0)),
-                         R.GPUDVec({h.address: 5.0}, style=R.IsDynamicSemistochastic(),
-                                   initiator=R.Initiator(1.0)),
+    m = oracle_model(h)
+    style = R.IsDynamicSemistochastic()
+    keys = np.array([h.address.key], dtype=object)
+    vals = np.array([40.0])
+    S = h.diagonal_element(h.address)
+    wm = R.GPUWorkingMemory(SEED)
+    for step in range(1, 11):
+        g = gpu_step(h, style, keys, vals, 0.01, S, SEED, step, wm=wm, initiator=rule)
+        o = O.step(m, oracle_params(style, 0.01, S, SEED, step, initiator=rule), keys, vals)
+        assert_same_step(g, o, style)
+        keys, vals = o[0], o[1]
+    assert len(keys) > 20
+
+
+def test_wide_dot_products():
+    """<v|w> of two-word lists with different bucket counts and value types, against the
+    products summed on the host."""
+    h = _models()["real1d-99"]
+    m = oracle_model(h)
+    keys = _neighbourhood(m, h.address.key, depth=3, cap=3000)
+    rng = np.random.default_rng(8)
+    va = rng.normal(size=len(keys))
+    ia = rng.choice(len(keys), len(keys) // 2, replace=False)
+    vb = rng.integers(-5, 6, len(ia))
+    a = R.GPUDVec(style=R.IsDeterministic(), address_type=h.address)
+    a.upload(np.array(keys, dtype=object), va)
+    b = R.GPUDVec(style=R.IsStochasticInteger(), address_type=h.address, capacity=64)
+    b.upload(np.array([keys[i] for i in ia], dtype=object), vb)
+    want = float(np.sum(va[ia] * vb))
+    assert a.dot(b) == pytest.approx(want, rel=1e-12, abs=1e-12)
+    assert b.dot(a) == pytest.approx(want, rel=1e-12, abs=1e-12)
+    assert a.dot(a) == pytest.approx(float(np.sum(va * va)), rel=1e-12)
+
+
+def test_wide_addresses_reject_projectors():
+    h = _models()["real1d-99"]
+    wm = R.GPUWorkingMemory(1)
+    wm.set_projector(np.array([1, 2], dtype=np.uint64), np.ones(2), np.ones(2))
+    with pytest.raises(R.RimuError):     # projector keys are one-word addresses
+        R.apply_operator(wm, R.GPUDVec(style=R.IsDynamicSemistochastic(), address_type=h.address),
+                         R.GPUDVec({h.address: 5.0}, style=R.IsDynamicSemistochastic()),
                          R.FirstOrderTransitionOperator(h, 0.0, 0.01))

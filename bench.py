@@ -673,7 +673,14 @@ def bench_hv(R, torch, peak, with_cpu=True):
         cpu = {"value": nnz / secs, "unit": "nnz/s", "seconds": secs, "cores": os.cpu_count(),
                "kind": "port", "sample": "one full-basis product by the oracle (rows in parallel; "
                                          "addresses looked up by binary search in the sorted basis)"}
+    # FP64 floor: one FP64 operation per nonzero (the diagonal term a multiply, each hop a
+    # fused multiply-add) at GB300's 2 FP64 lanes per cycle per SM and the maximum SM clock
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    fp64_per_s = 2 * props.multi_processor_count * 2.07e9
+    floor_ms = nnz / fp64_per_s * 1e3
     return {"workload": "HubbardReal1D M=N=14 full basis, D=20058300", "value": nnz / (ms / 1e3),
+            "fp64_floor_ms": floor_ms, "frac_fp64": floor_ms / ms,
+            "adjoint_fp64_floor_ms": 2 * floor_ms - D / fp64_per_s * 1e3,
             "unit": "nnz/s", "ms": ms, "nnz": nnz,
             "achieved_gbs": bytes_fwd / (ms / 1e3) / 1e9, "frac_hbm": bytes_fwd / (ms / 1e3) / 1e9 / peak,
             "fp64_fma_per_s": nnz / (ms / 1e3),

@@ -578,7 +578,7 @@ def bench_c5_full(R, torch, steps=5000, skip=2000, lanczos_i=(0, 21, 42, 63), kr
         df = sim.df
         r = R.shift_estimator(df, skip=skip)
         pe, pe_err = R.projected_energy(df, skip=skip)
-        proj = None if math.isnan(pe) else [float(pe), float(pe_err)]
+        proj = [float(pe), float(pe_err)] if math.isfinite(pe) else None
         return {"shift": [float(r.mean), float(r.err)], "projected": proj,
                 "walker_steps": float(np.sum(np.asarray(df["norm"], dtype=float)))}
     eb = [estimates(x) for x in sims_b]

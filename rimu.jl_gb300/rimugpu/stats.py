@@ -98,30 +98,107 @@ def shift_estimator(df, shift="shift", skip=0):
     return blocking_analysis(np.asarray(df[shift]), skip=skip)
 
 
-def ratio_of_means(num, denom, skip=0):
-    """Ratio of means with a first-order (delta method) error from blocked series;
-    a simplified ratio_of_means (ratio_of_means.jl:126)."""
+def x_by_y_linear(mu_x, mu_y, sigma_x, sigma_y, rho):
+    """Ratio mu_x / mu_y of two correlated normal variables and its standard deviation by linear
+    error propagation (x_by_y_linear, ratio_of_means.jl:166-171); rho is the covariance of x
+    and y.  A variance that rounding makes slightly negative gives 0."""
+    mu_x, mu_y = np.float64(mu_x), np.float64(mu_y)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        f = mu_x / mu_y
+        var = (sigma_x / mu_y) ** 2 + (mu_x * sigma_y / mu_y ** 2) ** 2 - 2 * rho * mu_x / mu_y ** 3
+    return float(f), float(np.sqrt(var)) if not var < 0 else 0.0
+
+
+@dataclass
+class RatioBlockingResult:
+    """Result of ratio_of_means (RatioBlockingResult, ratio_of_means.jl:3-31): Monte Carlo
+    samples of the ratio (`ratio`), the ratio of the means `f`, its linear-propagation error
+    `sigma_f`, the denominator's coefficient of variation `delta_y` (the normal approximation
+    holds for |delta_y| < 0.1), the blocking level k (k - 1 blocking steps), the number of
+    blocks, and whether both blocking analyses succeeded.  Unpacks as (f, sigma_f)."""
+    ratio: np.ndarray
+    f: float
+    sigma_f: float
+    delta_y: float
+    k: int
+    blocks: int
+    success: bool
+
+    def __iter__(self):
+        yield self.f
+        yield self.sigma_f
+
+    def pmedian(self) -> float:
+        return float(np.median(self.ratio))
+
+    def pquantile(self, q):
+        return np.quantile(self.ratio, q)
+
+    def val_and_errs(self, n=1):
+        """Median and the distances to the quantiles that bound the central erf(n/sqrt 2)
+        probability (val_and_errs, convenience.jl:99-107)."""
+        p = math.erf(n / math.sqrt(2))
+        q1, q2, q3 = self.pquantile([(1 - p) / 2, 0.5, 1 - (1 - p) / 2])
+        return float(q2), float(q2 - q1), float(q3 - q2)
+
+
+def ratio_estimators(x, y, k=None, corrected=True, mc_samples=2000, rng=None):
+    """ratio_estimators (ratio_of_means.jl:196-230): after k - 1 blocking steps of both series,
+    the means, the variances and the covariance of the means, Monte Carlo samples of the ratio
+    of a bivariate normal with those moments (a variable without variance stays at its mean),
+    the linear estimate and delta_y.  Returns (samples, f, sigma_f, delta_y, n)."""
+    x = np.asarray(x, float)
+    y = np.asarray(y, float)
+    for _ in range((k or 1) - 1):
+        x, y = blocker(x), blocker(y)
+    n = len(x)
+    mu_x, mu_y = float(np.mean(x)), float(np.mean(y))
+    dd = int(corrected)
+    var_x = float(np.sum((x - mu_x) ** 2) / (n - dd)) / n
+    var_y = float(np.sum((y - mu_y) ** 2) / (n - dd)) / n
+    rho = float(np.sum((x - mu_x) * (y - mu_y)) / (n - dd)) / n
+    f, sigma_f = x_by_y_linear(mu_x, mu_y, math.sqrt(var_x), math.sqrt(var_y), rho)
+    rng = np.random.default_rng(rng)
+    z = rng.standard_normal((2, int(mc_samples)))
+    eps = math.sqrt(np.finfo(float).eps)
+    if abs(var_x) < eps or abs(var_y) < eps:     # singular: independent (or constant) draws
+        px = mu_x + math.sqrt(var_x) * z[0]
+        py = mu_y + math.sqrt(var_y) * z[1]
+    else:
+        c = np.linalg.cholesky(np.array([[var_x, rho], [rho, var_y]]))
+        px = mu_x + c[0, 0] * z[0]
+        py = mu_y + c[1, 0] * z[0] + c[1, 1] * z[1]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        samples = px / py
+        delta_y = math.sqrt(var_y) / mu_y if mu_y != 0 else math.inf
+    return samples, f, sigma_f, delta_y, n
+
+
+def ratio_of_means(num, denom, alpha=0.01, corrected=True, mc_samples=2000, skip=0, warn=True,
+                   rng=None) -> RatioBlockingResult:
+    """ratio_of_means (ratio_of_means.jl:126-157): both series are blocked to the larger of
+    the levels their M-tests pick, the error of the ratio is propagated linearly and by Monte
+    Carlo sampling, and `f` is the ratio of the unblocked means.  A zero denominator mean gives
+    a NaN or infinite ratio, as the floating-point division does."""
     num = np.asarray(num, float)[skip:]
     den = np.asarray(denom, float)[skip:]
-    rn, rd = blocking_analysis(num), blocking_analysis(den)
-    if rd.mean == 0:             # the projector never saw a walker: no estimate
-        return math.nan, math.nan
-    r = rn.mean / rd.mean
-    k = max(rn.k, rd.k, 1)
-    b = 2 ** (k - 1)
-    nb = len(num) // b
-    if nb >= 2:
-        bn = num[: nb * b].reshape(nb, b).mean(1)
-        bd = den[: nb * b].reshape(nb, b).mean(1)
-        cov = np.cov(bn, bd)
-        var = (cov[0, 0] / rd.mean ** 2 - 2 * r * cov[0, 1] / rd.mean ** 2
-               + r ** 2 * cov[1, 1] / rd.mean ** 2) / nb
-        err = math.sqrt(max(var, 0.0))
-    else:
-        err = math.nan
-    return r, err
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        bn = blocking_analysis(num, alpha=alpha, corrected=corrected)
+        bd = blocking_analysis(den, alpha=alpha, corrected=corrected)
+    success = bn.k >= 0 and bd.k >= 0
+    if warn and not success:
+        warnings.warn(f"Blocking failed in `ratio_of_means`: k = {(bn.k, bd.k)}")
+    k = max(bn.k, bd.k)
+    samples, _, sigma_f, delta_y, n = ratio_estimators(num, den, k if k > 1 else None, corrected,
+                                                      mc_samples, rng)
+    if warn and abs(delta_y) >= 0.1:
+        warnings.warn("Large coefficient of variation in `ratio_of_means`: |delta_y| >= 0.1")
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = float(np.float64(bn.mean) / np.float64(bd.mean))
+    return RatioBlockingResult(samples, f, sigma_f, delta_y, k, n, success)
 
 
-def projected_energy(df, hproj="hproj", vproj="vproj", skip=0):
+def projected_energy(df, hproj="hproj", vproj="vproj", skip=0, **kw):
     """projected_energy (reweighting.jl:721-726): ratio of means of hproj and vproj."""
-    return ratio_of_means(df[hproj], df[vproj], skip)
+    return ratio_of_means(df[hproj], df[vproj], skip=skip, **kw)

@@ -192,6 +192,7 @@ def run_ours(args, ws, rank, local):
     if args.shape:
         kpb, slots = (int(x) for x in args.shape.split(","))
         s.wm.set_launch_shape(kpb, slots)
+    s.wm.set_annihilation(args.annihilation)
     t_prep = time.time()
     prep = 0
     # growth to the target norm, then equilibration: the list keeps spreading over the
@@ -243,7 +244,8 @@ def run_ours(args, ws, rank, local):
                                   "measured at an equilibrated norm of 3e7, scaled by this run's "
                                   "records per step" if args.traffic is None else "given",
                 "peak_source": peak_kind,
-                "kernel": "k_spawn + k_spawn_heavy + k_ann_warp + k_annihilate (one step)",
+                "kernel": "k_spawn + k_spawn_heavy + %s + k_annihilate (one step)"
+                          % ("k_ann_sort" if args.annihilation == "sort" else "k_ann_warp"),
                 "bytes_per_step": k_bytes / steps_t, "ms_per_step": k_ms / steps_t,
                 "spawn": {"ms": tim["spawn_ms"] / steps_t,
                           "gbs": tim["spawn_bytes"] / (tim["spawn_ms"] / 1e3) / 1e9 if tim["spawn_ms"] else 0},
@@ -353,7 +355,8 @@ def run_ours(args, ws, rank, local):
                        "l2": "inputs larger than L2 (walker list > 1 GB), no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "launch_shape": args.shape or "default (at most 448 contributions per bucket on "
-                                       "average, one warp per bucket)"},
+                                       "average, one warp per bucket)",
+                       "annihilation": args.annihilation},
             "gpu_launches": 4 * args.steps,
             "roofline": roofline,
             "e2e": e2e,
@@ -767,6 +770,9 @@ def main():
                     help="skip the small (C1) and momentum-space (C3) configuration lines")
     ap.add_argument("--shape", default=None,
                     help="launch shape KEYS_PER_BUCKET,TABLE_SLOTS of the step kernels (0 slots = automatic)")
+    ap.add_argument("--annihilation", default="hash", choices=["hash", "sort"],
+                    help="how the one-warp buckets group their spawns: shared-memory hash table "
+                         "(default) or bitonic sort")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -228,6 +228,14 @@ int rimu_wm_timing(rimu_wm *wm, double *out7);
  * do not depend on either value. */
 int rimu_wm_set_launch_shape(rimu_wm *wm, int keys_per_bucket, int table_slots);
 
+/* How the buckets that one warp annihilates group their spawns by address: RIMU_ANN_HASH (the
+ * default) inserts them into a shared-memory hash table with a list per address; RIMU_ANN_SORT
+ * sorts them by (address, value) with a bitonic network and takes the runs of equal addresses.
+ * Both give the same results bit for bit (no counterpart in the reference, whose annihilation
+ * is a dictionary insertion, dictvectors.jl:49-51); the choice only changes the speed. */
+enum { RIMU_ANN_HASH = 0, RIMU_ANN_SORT = 1 };
+int rimu_wm_set_annihilation(rimu_wm *wm, int mode);
+
 /* One projector step target = T(source), with stats: apply_operator!(wm, target, source,
  * op, boost) of src/Interfaces/dictvectors.jl:112-140 and pdworkingmemory.jl:297-309,
  * including the compression of compression.jl:28-42.  source is not modified. */
@@ -257,10 +265,10 @@ typedef struct {
   double zeta, xi;               /* DoubleLogUpdate damping (reference defaults 0.08, zeta^2/4) */
   int segment_steps;             /* steps per segment (rounded up to even; 0: 64) */
   int use_graph;                 /* replay each full segment as one captured CUDA graph */
-  int autotune;                  /* time the bucket sizes 2048/1024/384/256 (the first two
-                                    annihilated one CTA per bucket, the others one warp per
-                                    bucket) on the first steps with at least 2^20 entries
-                                    and keep the fastest */
+  int autotune;                  /* time five launch shapes on the first steps with at least
+                                    2^20 entries and keep the fastest: 2048 and 1024
+                                    contributions per bucket (one CTA per bucket), 448 and 256
+                                    (one warp per bucket, hashed), and 448 sorted */
 } rimu_batch_params;
 
 /* Per replica and step: the step statistics of rimu_step_stats and the shift after the update
@@ -285,7 +293,7 @@ typedef struct {
 int rimu_batch_create(rimu_ctx *ctx, int nrep, int val_kind, rimu_batch **out);
 int rimu_batch_destroy(rimu_batch *b);
 /* Model, start vector (host pairs), initial shift and target walker number of one replica;
- * only before the first run. */
+ * only before the first run.  Batched runs take addresses of at most 64 bits. */
 int rimu_batch_set_replica(rimu_batch *b, int replica, rimu_model *m, const uint64_t *keys,
                            const void *vals, int64_t n, double shift, double target_walkers);
 /* ProjectedEnergy projector of one replica (as rimu_wm_set_projector). */
@@ -293,6 +301,9 @@ int rimu_batch_set_projector(rimu_batch *b, int replica, const uint64_t *keys,
                              const double *pvals, const double *hpvals, int n);
 /* Launch shape (as rimu_wm_set_launch_shape); setting it turns the autotuner off. */
 int rimu_batch_set_launch_shape(rimu_batch *b, int keys_per_bucket, int table_slots);
+/* Annihilation of the warp-sized buckets (as rimu_wm_set_annihilation); setting it turns the
+ * autotuner off. */
+int rimu_batch_set_annihilation(rimu_batch *b, int mode);
 /* nsteps steps with step numbers first_step+1 ... ; out receives nsteps * nrep records,
  * step-major. */
 int rimu_batch_run(rimu_batch *b, const rimu_batch_params *p, uint64_t first_step, int nsteps,
@@ -303,6 +314,8 @@ int rimu_batch_download(rimu_batch *b, int replica, uint64_t *keys, void *vals, 
 /* out8: keys per bucket in use, annihilation table slots, buckets, graph segments, eager
  * segments, re-run segments, milliseconds in the segments (CUDA events), steps run. */
 int rimu_batch_info(rimu_batch *b, double *out8);
+/* The annihilation mode in use (RIMU_ANN_*: the one set, or the autotuner's choice). */
+int rimu_batch_annihilation(rimu_batch *b, int *mode);
 
 /* Full sorted basis (build_basis, ExactDiagonalization/basis_fock.jl:33-36): all BoseFS
  * (FermiFS) addresses in increasing bit-string order. */

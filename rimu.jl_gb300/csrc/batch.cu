@@ -121,6 +121,7 @@ struct rimu_batch {
   double *proj_v = nullptr, *proj_h = nullptr, *proj_out_v = nullptr, *proj_out_h = nullptr;
   // launch shape and the captured segment
   int kpb = AW_DEFAULT_KPB, tslots = 0;
+  int ann_mode = RIMU_ANN_HASH;
   bool tuned = false;
   uint32_t T = 512;
   int spawn_cb = 1;
@@ -391,6 +392,7 @@ static int enqueue_step(rimu_batch *b, const rimu_batch_params *p, int j) {
     if ((uint32_t)m0->max_offdiag + 1 > TL - 256) TL = 4096;
     a.tsize_list = b->tslots ? (uint32_t)b->tslots : TL;
   }
+  a.ann_sort = b->ann_mode == RIMU_ANN_SORT;
   a.kw = 1;
   a.spawn_cb = b->spawn_cb;
   a.v_in = b->recs[src];
@@ -627,6 +629,15 @@ extern "C" int rimu_batch_set_launch_shape(rimu_batch *b, int keys_per_bucket, i
   return RIMU_OK;
 }
 
+extern "C" int rimu_batch_set_annihilation(rimu_batch *b, int mode) {
+  if (!b) return fail_arg("rimu_batch_set_annihilation: NULL batch");
+  if (mode != RIMU_ANN_HASH && mode != RIMU_ANN_SORT)
+    return fail_arg("rimu_batch_set_annihilation: mode must be RIMU_ANN_HASH or RIMU_ANN_SORT");
+  b->ann_mode = mode;
+  b->tuned = true;
+  return RIMU_OK;
+}
+
 extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint64_t first_step,
                               int nsteps, rimu_batch_stats *out) {
   if (!b || !pin) return fail_arg("rimu_batch_run: NULL argument");
@@ -673,14 +684,18 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
   // them, so that the growth within one segment stays within the planned room
   int seg = b->steps_done == 0 ? std::min(p.segment_steps, 8) : p.segment_steps;
   std::vector<double> trial_cost;
-  // bucket sizes: up to 512 contributions go to one warp each, larger buckets to one CTA each
-  const int shapes[4] = {2048, 1024, AW_DEFAULT_KPB, AW_CAP / 2};
+  // bucket sizes: up to 512 contributions go to one warp each, larger buckets to one CTA
+  // each; the warps hash the spawns, or sort them (the last shape)
+  constexpr int kShapes = 5;
+  const int shapes[kShapes] = {2048, 1024, AW_DEFAULT_KPB, AW_CAP / 2, AW_DEFAULT_KPB};
+  const int modes[kShapes] = {RIMU_ANN_HASH, RIMU_ANN_HASH, RIMU_ANN_HASH, RIMU_ANN_HASH,
+                              RIMU_ANN_SORT};
   int trial = -1;
   while (pos < nsteps) {
     int64_t tot_len = 0;
     for (int r = 0; r < b->nrep; ++r) tot_len += b->len[r];
     if (p.autotune && !b->tuned && tot_len >= (1 << 20) && trial < 0) trial = 0;
-    if (trial >= 0) b->kpb = shapes[trial];
+    if (trial >= 0) { b->kpb = shapes[trial]; b->ann_mode = modes[trial]; }
     if ((rc = plan(b, &p, seg, min_caps, min_capv, heavy_min))) return rc;
     int k = std::min(seg, nsteps - pos);
     if (trial >= 0) k = std::min(k, 4);
@@ -767,9 +782,10 @@ extern "C" int rimu_batch_run(rimu_batch *b, const rimu_batch_params *pin, uint6
     if (trial < 0) seg = std::min(p.segment_steps, seg * 2);
     if (trial >= 0) {
       trial_cost.push_back(ms / std::max(contributions, 1.0));
-      if (++trial == 4) {
+      if (++trial == kShapes) {
         const int best = (int)(std::min_element(trial_cost.begin(), trial_cost.end()) - trial_cost.begin());
         b->kpb = shapes[best];
+        b->ann_mode = modes[best];
         b->tuned = true;
         trial = -1;
       }
@@ -815,6 +831,12 @@ extern "C" int rimu_batch_download(rimu_batch *b, int replica, uint64_t *keys, v
   dfree(ctx, dv);
   if (rc) return rc;
   return rimu_cuda_check(cudaStreamSynchronize(ctx->stream), "rimu_batch_download");
+}
+
+extern "C" int rimu_batch_annihilation(rimu_batch *b, int *mode) {
+  if (!b || !mode) return fail_arg("rimu_batch_annihilation: NULL argument");
+  *mode = b->ann_mode;
+  return RIMU_OK;
 }
 
 extern "C" int rimu_batch_info(rimu_batch *b, double *out8) {

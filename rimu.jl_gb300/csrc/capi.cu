@@ -685,6 +685,14 @@ extern "C" int rimu_wm_set_timing(rimu_wm *w, int enable) {
   return RIMU_OK;
 }
 
+extern "C" int rimu_wm_set_annihilation(rimu_wm *w, int mode) {
+  if (!w) return bad("rimu_wm_set_annihilation: NULL working memory");
+  if (mode != RIMU_ANN_HASH && mode != RIMU_ANN_SORT)
+    return bad("rimu_wm_set_annihilation: mode must be RIMU_ANN_HASH or RIMU_ANN_SORT");
+  w->ann_mode = mode;
+  return RIMU_OK;
+}
+
 extern "C" int rimu_wm_set_launch_shape(rimu_wm *w, int keys_per_bucket, int table_slots) {
   if (!w) return bad("rimu_wm_set_launch_shape: NULL working memory");
   if (keys_per_bucket < 16 || keys_per_bucket > 4096)
@@ -896,6 +904,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
       a.ann_list = w->ann_list;
       a.ann_count = w->ann_count;
       a.tsize_list = w->table_slots ? (uint32_t)w->table_slots : TL;
+      a.ann_sort = w->ann_mode == RIMU_ANN_SORT;
     }
     // spawn chunks of about 256 source walkers per warp
     const double mu_v = (double)L / (double)nb;

@@ -1570,6 +1570,7 @@ __global__ void __launch_bounds__(AW_WARPS * 32, AW_MINB) k_ann_warp(StepArgs a,
       const uint32_t pos = out + (uint32_t)__popc(mk & lt);
       if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
       out += (uint32_t)__popc(mk);
+      if (f0 + 32 == nvr) __syncwarp();          // the sources' marks, before the slot rounds
     }
     __syncwarp();
     if (lane == 0) {
@@ -1583,6 +1584,232 @@ __global__ void __launch_bounds__(AW_WARPS * 32, AW_MINB) k_ann_warp(StepArgs a,
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0)
     atomicOr(&a.stats[cur_r < 0 ? 0 : cur_r].flags, (unsigned)FLAG_TABLE);
+  if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
+}
+
+// ------------------------------------------------------------------------------------------
+// Sorting instead of hashing: the work of k_ann_warp with the bucket's spawns ordered in
+// shared memory by a bitonic network on (address, value) -- for float walkers the value's
+// order-preserving bits, so that each address's spawns stand in the canonical summation order
+// and no list is ever sorted.  The runs of equal addresses take the place of the table's
+// lists: a source walker finds its run by binary search and marks it taken, and the runs no
+// source took are finished in the second part of the same loop.  Same buckets, same results
+// bit for bit; which of the two is faster is measured (rimu_wm_set_annihilation and the
+// batched autotuner choose).
+constexpr int AS_P = 512;                       // sort width: a power of two >= AW_SCAP
+static_assert(AS_P >= AW_SCAP && (AS_P & (AS_P - 1)) == 0, "sort width");
+// per warp: records [AS_P] 16 B (address, value bits), run heads [AW_SCAP] u16, taken flags
+// [AS_P] u8
+constexpr size_t AS_WARP_SMEM = (size_t)AS_P * 16 + (size_t)AW_SCAP * 2 + (size_t)AS_P;
+constexpr int AS_MINB = (int)((220 * 1024) / (AW_WARPS * AS_WARP_SMEM)) > 8 ? 8
+                        : (int)((220 * 1024) / (AW_WARPS * AS_WARP_SMEM));
+
+// Sorts s[0, p) ascending by (x, y) (by x alone when !BY_VALUE), p a power of two >= 2: one
+// warp, p / 64 compare-exchanges per lane and stage.
+template <bool BY_VALUE>
+__device__ __forceinline__ void warp_bitonic(ulonglong2 *s, uint32_t p, int lane) {
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = (uint32_t)lane; i < p / 2; i += 32) {
+        const uint32_t lo = ((i & ~(j - 1)) << 1) | (i & (j - 1));
+        const uint32_t hi = lo + j;
+        const ulonglong2 x = s[lo], y = s[hi];
+        const bool gt = x.x > y.x || (BY_VALUE && x.x == y.x && x.y > y.y);
+        if (gt == ((lo & k) == 0)) { s[lo] = y; s[hi] = x; }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Sum of the run of spawns at s[seg..] (address key, canonical order, order-preserving value
+// bits) and of the diagonal term dv (when have_d) by the summation rule; counts the spawn
+// statistics.  Three or more terms: exact in fixed point when every term allows it, else in
+// the run's order after the diagonal term.
+__device__ double run_sum_long(uint32_t seg, uint32_t ns, uint64_t key, bool have_d, double dv,
+                               const ulonglong2 *s, AnnAcc &acc) {
+  U128 sum{0, 0}, m;
+  bool exact = true;
+  if (have_d) {
+    exact = fixed_magnitude(dv, m);
+    sum = is_neg_d(dv) ? neg128(m) : m;
+  }
+  uint32_t c = seg;
+  for (; c < ns && s[c].x == key; ++c) {
+    const double v = from_ordered(s[c].y);
+    const bool ex = fixed_magnitude(v, m);
+    if (c != seg) {
+      acc.records++;
+      acc.spawn_fx = add128(acc.spawn_fx, ex ? m : fixed_of(abs_d(v)));
+    }
+    exact = exact && ex;
+    sum = add128(sum, is_neg_d(v) ? neg128(m) : m);
+  }
+  if (exact) return signed_fixed_to_double(sum);
+  double t = have_d ? dv : from_ordered(s[seg].y);
+  for (uint32_t d = have_d ? seg : seg + 1; d < c; ++d) t = t + from_ordered(s[d].y);
+  return t;
+}
+__device__ __forceinline__ double run_sum_float(uint32_t seg, uint32_t ns, uint64_t key,
+                                                bool have_d, double dv, const ulonglong2 *s,
+                                                AnnAcc &acc) {
+  const double y0 = from_ordered(s[seg].y);
+  acc.records++;
+  acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y0)));
+  const bool one = seg + 1 >= ns || s[seg + 1].x != key;
+  if (one) return have_d ? __dadd_rn(dv, y0) : y0;
+  if (!have_d && (seg + 2 >= ns || s[seg + 2].x != key)) {
+    const double y1 = from_ordered(s[seg + 1].y);
+    acc.records++;
+    acc.spawn_fx = add128(acc.spawn_fx, fixed_of(abs_d(y1)));
+    return __dadd_rn(y0, y1);
+  }
+  return run_sum_long(seg, ns, key, have_d, dv, s, acc);
+}
+
+template <int KIND, int STYLE>
+__global__ void __launch_bounds__(AW_WARPS * 32, AS_MINB) k_ann_sort(StepArgs a, int nb_total) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned char *base = smem + (size_t)w * AS_WARP_SMEM;
+  ulonglong2 *srec = reinterpret_cast<ulonglong2 *>(base);
+  uint16_t *hlist = reinterpret_cast<uint16_t *>(srec + AS_P);
+  uint8_t *taken = reinterpret_cast<uint8_t *>(hlist + AW_SCAP);
+  const uint32_t lt = lanemask_lt();
+  const uint32_t step = step_of(a);
+  AnnAcc acc{};
+  int cur_r = -1;
+  for (int gb = blockIdx.x * AW_WARPS + w; gb < nb_total; gb += gridDim.x * AW_WARPS) {
+    const int r = replica_of(a, (uint32_t)gb);
+    if (r != cur_r) {
+      if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
+      cur_r = r;
+    }
+    const uint32_t rep = a.replica_base + (uint32_t)r;
+    const uint32_t nsp = a.scount[gb];
+    const uint32_t ns = nsp < a.caps ? nsp : a.caps;
+    const uint32_t nv0 = a.cnt_in[gb];
+    const uint32_t nv = nv0 < a.capv_in ? nv0 : a.capv_in;
+    if (ns > (uint32_t)AW_SCAP) {               // for k_annihilate
+      if (lane == 0) {
+        const uint32_t idx = atomicAdd(a.ann_count, 1u);
+        if (idx < (uint32_t)nb_total) a.ann_list[idx] = (uint32_t)gb;
+      }
+      continue;
+    }
+    const Rec *sp = static_cast<const Rec *>(a.spawn) + (size_t)gb * a.caps;
+    const Rec *vbase = static_cast<const Rec *>(a.v_in) + (size_t)gb * a.capv_in;
+    Rec *vout = static_cast<Rec *>(a.v_out) + (size_t)gb * a.capv;
+    Rec nxt{};
+    if ((uint32_t)lane < nv) nxt = vbase[lane];
+    // ---- the spawns, padded to a power of two with keys that sort last, then sorted ----
+    uint32_t p = 2;
+    while (p < ns) p <<= 1;
+    for (uint32_t f = (uint32_t)lane; f < p; f += 32) {
+      ulonglong2 e{EMPTY_KEY, ~0ull};
+      if (f < ns) {
+        const Rec rec = sp[f];
+        e.x = rec.key;
+        e.y = STYLE == STYLE_INTEGER ? rec.val : ordered_bits(bitsd(rec.val));
+      }
+      srec[f] = e;
+      taken[f] = 0;
+    }
+    __syncwarp();
+    if (ns > 1) warp_bitonic<STYLE != STYLE_INTEGER>(srec, p, lane);
+    // ---- run heads ----
+    uint32_t nsl = 0;
+    for (uint32_t f0 = 0; f0 < ns; f0 += 32) {
+      const uint32_t f = f0 + (uint32_t)lane;
+      const bool h = f < ns && (f == 0 || srec[f].x != srec[f - 1].x);
+      const uint32_t m = __ballot_sync(0xffffffffu, h);
+      if (h) hlist[nsl + (uint32_t)__popc(m & lt)] = (uint16_t)f;
+      nsl += (uint32_t)__popc(m);
+    }
+    __syncwarp();
+    // ---- the source walkers, then the runs no source took (as in k_ann_warp) ----
+    uint32_t out = 0;
+    const uint32_t nvr = (nv + 31u) & ~31u;
+    for (uint32_t f0 = 0; f0 < nvr + nsl; f0 += 32) {
+      const uint32_t f = f0 + (uint32_t)lane;
+      const bool is_src = f0 < nvr;
+      Rec rec{};
+      if (is_src) {
+        rec = nxt;
+        if (f + 32 < nv) nxt = vbase[f + 32];
+      }
+      bool keep = false, item = false, have_d = false;
+      uint64_t key = 0, vb = 0;
+      uint32_t seg = NIL;
+      double dv = 0.0;
+      int64_t iv = 0;
+      if (is_src && f < nv) {
+        item = true;
+        key = rec.key;
+        if (ns) {
+          uint32_t lo = 0, n = ns;               // lower bound of key among the spawns
+          while (n > 0) {
+            const uint32_t h = n >> 1;
+            if (srec[lo + h].x < key) { lo += h + 1; n -= h + 1; }
+            else n = h;
+          }
+          if (lo < ns && srec[lo].x == key) { seg = lo; taken[lo] = 1; }
+        }
+        if (STYLE == STYLE_INTEGER) {
+          const int64_t v = (int64_t)rec.val;
+          const double x = op_diagonal<KIND>(a, r, key) * i2d_exact(v);
+          const U4 rr = draw(a.seed, PURPOSE_DIAG, rep, step, key, 0);
+          iv = round_stochastic(x, u53_of(rr));
+          // clones_deaths_zombies (spawning.jl:79-93)
+          const int sr = (iv > 0) - (iv < 0), sv = (v > 0) - (v < 0);
+          if (iv > v) acc.clones += iv - v;
+          else if (sr != sv) { acc.deaths += v < 0 ? -v : v; acc.zombies += iv < 0 ? -iv : iv; }
+          else acc.deaths += (iv - v) < 0 ? v - iv : iv - v;
+        } else {
+          dv = diag_float<KIND>(a, r, rep, step, rec);
+          have_d = !is_zero_d(dv);
+        }
+      } else if (!is_src && f - nvr < nsl) {
+        seg = hlist[f - nvr];
+        key = srec[seg].x;
+        item = !taken[seg];
+      }
+      if (item) {
+        if (STYLE == STYLE_INTEGER) {
+          for (uint32_t c = seg; c < ns && srec[c].x == key; ++c) {
+            const int64_t k = (int64_t)srec[c].y;
+            iv += k;
+            acc.records++;
+            acc.spawns_i += k < 0 ? -k : k;
+          }
+          if (iv != 0) {
+            acc.len_before++;
+            keep = true;
+            vb = (uint64_t)iv;
+            account_kept<STYLE>(a, r, key, i2d_exact(iv), U128{0, (uint64_t)(iv < 0 ? -iv : iv)}, acc);
+          }
+        } else {
+          double fv = seg == NIL ? dv : run_sum_float(seg, ns, key, have_d, dv, srec, acc);
+          keep = warp_settle_float<STYLE>(a, r, step, key, fv, acc);
+          vb = dbits(fv);
+        }
+      }
+      const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+      const uint32_t pos = out + (uint32_t)__popc(mk & lt);
+      if (keep && pos < a.capv) vout[pos] = Rec{key, vb};
+      out += (uint32_t)__popc(mk);
+      if (f0 + 32 == nvr) __syncwarp();          // the sources' marks, before the run rounds
+    }
+    __syncwarp();
+    if (lane == 0) {
+      a.cnt_out[gb] = out < a.capv ? out : a.capv;
+      if (out > a.capv) atomicOr(&a.stats[r].flags, (unsigned)FLAG_V_OVERFLOW);
+      if (nsp > a.caps) atomicOr(&a.stats[r].flags, (unsigned)FLAG_SPAWN_OVERFLOW);
+      atomicMax(&a.stats[r].max_v_bucket, out);
+      atomicMax(&a.stats[r].max_spawn_bucket, nsp);
+      a.scount[gb] = 0;
+    }
+  }
   if (cur_r >= 0) flush_ann_acc(a, cur_r, acc);
 }
 
@@ -1700,8 +1927,15 @@ __global__ void k_offdiagonals(DevModel h, K key, int noff, K *keys, double *val
 // Launchers
 // ------------------------------------------------------------------------------------------
 template <int KIND, int STYLE, class K>
-static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEvent_t *ev) {
+static int launch_step_t(rimu_ctx *ctx, const StepArgs &a_in, int nb_total, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
+  // the warp kernels take one-word addresses only: other steps annihilate every bucket in
+  // the CTA kernel with a table of tsize slots (the size its shared memory is launched with)
+  StepArgs a = a_in;
+  if constexpr (KT<K>::BITS != 64) {
+    a.ann_list = nullptr;
+    a.ann_count = nullptr;
+  }
   const int cap = ctx->num_sms * 64;
   const int want_s = (nb_total / a.spawn_cb + WARPS - 1) / WARPS;
   const int grid_s = want_s < cap ? want_s : cap;
@@ -1716,17 +1950,26 @@ static int launch_step_t(rimu_ctx *ctx, const StepArgs &a, int nb_total, cudaEve
   if (!attr_set) {
     cudaFuncSetAttribute(k_annihilate<KIND, STYLE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          200 * 1024);
-    if constexpr (KT<K>::BITS == 64)
+    if constexpr (KT<K>::BITS == 64) {
       cudaFuncSetAttribute(k_ann_warp<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(AW_WARPS * AW_WARP_SMEM));
+      cudaFuncSetAttribute(k_ann_sort<KIND, STYLE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(AW_WARPS * AS_WARP_SMEM));
+    }
     attr_set = true;
   }
   if constexpr (KT<K>::BITS == 64) {
     if (a.ann_list) {
       const int want_w = (nb_total + AW_WARPS - 1) / AW_WARPS;
-      const int cap_w = ctx->num_sms * AW_MINB;
-      k_ann_warp<KIND, STYLE><<<want_w < cap_w ? want_w : cap_w, AW_WARPS * 32,
-                                AW_WARPS * AW_WARP_SMEM, st>>>(a, nb_total);
+      if (a.ann_sort) {
+        const int cap_w = ctx->num_sms * AS_MINB;
+        k_ann_sort<KIND, STYLE><<<want_w < cap_w ? want_w : cap_w, AW_WARPS * 32,
+                                  AW_WARPS * AS_WARP_SMEM, st>>>(a, nb_total);
+      } else {
+        const int cap_w = ctx->num_sms * AW_MINB;
+        k_ann_warp<KIND, STYLE><<<want_w < cap_w ? want_w : cap_w, AW_WARPS * 32,
+                                  AW_WARPS * AW_WARP_SMEM, st>>>(a, nb_total);
+      }
       // the buckets the warps left: as many CTAs as can be resident
       k_annihilate<KIND, STYLE, K><<<cap_a, ANN_THREADS, ann_smem<K>(a.tsize_list), st>>>(a, nb_total);
       if (ev) cudaEventRecord(ev[3], st);

@@ -111,6 +111,8 @@ struct StepArgs {
   uint32_t *ann_list;         // [number of buckets]
   uint32_t *ann_count;
   uint32_t tsize_list;
+  int ann_sort;               // with ann_list: the warps sort the spawns (k_ann_sort) instead
+                              // of hashing them (k_ann_warp)
 };
 
 }  // namespace rimu
@@ -166,6 +168,7 @@ struct rimu_wm {
   int keys_per_bucket = 1024;           // expected contributions per bucket (launch shape)
   int table_slots = 0;                  // annihilation table slots per CTA (0: automatic)
   bool shape_set = false;               // launch shape chosen by the caller
+  int ann_mode = 0;                     // RIMU_ANN_HASH or RIMU_ANN_SORT
   uint32_t *ann_list = nullptr;         // [nb_total] buckets left to the CTA annihilation
   uint32_t *ann_count = nullptr;
   // projector

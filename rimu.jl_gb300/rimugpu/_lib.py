@@ -16,6 +16,7 @@ VAL_F64, VAL_I64 = 0, 1
 MODEL_REAL1D, MODEL_REALSPACE, MODEL_MOM1D = 1, 2, 3
 STYLE_INTEGER, STYLE_DETERMINISTIC, STYLE_DSS = 0, 1, 2
 OP_TRANSITION, OP_HAMILTONIAN = 0, 1
+ANN_HASH, ANN_SORT = 0, 1
 
 # Names of the C entry points declared in include/rimu_gpu.h.
 EXPORTS = [
@@ -26,12 +27,13 @@ EXPORTS = [
     "rimu_vec_destroy", "rimu_vec_upload", "rimu_vec_download", "rimu_vec_length",
     "rimu_vec_walkernumber_and_length", "rimu_vec_lookup", "rimu_vec_copy", "rimu_vec_empty",
     "rimu_wm_create", "rimu_wm_destroy", "rimu_wm_set_projector", "rimu_wm_set_timing",
-    "rimu_wm_set_launch_shape",
+    "rimu_wm_set_launch_shape", "rimu_wm_set_annihilation",
     "rimu_wm_timing", "rimu_apply_operator",
     "rimu_basis_dimension", "rimu_basis_keys", "rimu_hv_basis", "rimu_hv_basis_adjoint",
     "rimu_hv_basis_adjoint_noalloc",
     "rimu_batch_create", "rimu_batch_destroy", "rimu_batch_set_replica", "rimu_batch_set_projector",
     "rimu_batch_set_launch_shape", "rimu_batch_run", "rimu_batch_download", "rimu_batch_info",
+    "rimu_batch_set_annihilation", "rimu_batch_annihilation",
     "rimu_vec_dot", "rimu_vec_convert",
 ]
 
@@ -135,6 +137,7 @@ def load(build_if_missing: bool = True):
         "rimu_wm_set_projector": ([vp, u64p, f64p, f64p, C.c_int], C.c_int),
         "rimu_wm_set_timing": ([vp, C.c_int], C.c_int),
         "rimu_wm_set_launch_shape": ([vp, C.c_int, C.c_int], C.c_int),
+        "rimu_wm_set_annihilation": ([vp, C.c_int], C.c_int),
         "rimu_wm_timing": ([vp, f64p], C.c_int),
         "rimu_apply_operator": ([vp, vp, vp, vp, P(StepParams), P(StepStats)], C.c_int),
         "rimu_basis_dimension": ([vp, i64p], C.c_int),
@@ -149,6 +152,8 @@ def load(build_if_missing: bool = True):
                                    C.c_int),
         "rimu_batch_set_projector": ([vp, C.c_int, u64p, f64p, f64p, C.c_int], C.c_int),
         "rimu_batch_set_launch_shape": ([vp, C.c_int, C.c_int], C.c_int),
+        "rimu_batch_set_annihilation": ([vp, C.c_int], C.c_int),
+        "rimu_batch_annihilation": ([vp, C.POINTER(C.c_int)], C.c_int),
         "rimu_batch_run": ([vp, P(BatchParams), C.c_uint64, C.c_int, vp], C.c_int),
         "rimu_batch_download": ([vp, C.c_int, u64p, vp, C.c_int64, i64p], C.c_int),
         "rimu_batch_info": ([vp, f64p], C.c_int),

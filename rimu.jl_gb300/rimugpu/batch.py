@@ -31,8 +31,10 @@ class BatchedReplicas:
     def __init__(self, hamiltonians, style, time_step, targets, starts=None, shifts=None,
                  seed=0, projectors=None, zeta=0.08, xi=None, shift_update=True,
                  segment_steps=64, use_graph=True, autotune=True, launch_shape=None,
-                 population=10):
+                 population=10, annihilation=None):
         self.hamiltonians = list(hamiltonians)
+        if any(H.address.nbits > 64 for H in self.hamiltonians):
+            raise ValueError("batched runs take addresses of at most 64 bits")
         self.nrep = len(self.hamiltonians)
         self.style = style
         self.time_step = float(time_step)
@@ -75,6 +77,9 @@ class BatchedReplicas:
                     ph.ctypes.data_as(C.POINTER(C.c_double)), len(pk)))
         if launch_shape is not None:
             _lib.check(lib.rimu_batch_set_launch_shape(h, int(launch_shape[0]), int(launch_shape[1])))
+        if annihilation is not None:
+            m = {"hash": _lib.ANN_HASH, "sort": _lib.ANN_SORT}[annihilation]
+            _lib.check(lib.rimu_batch_set_annihilation(h, m))
 
     def _params(self):
         p = _lib.BatchParams()
@@ -130,9 +135,12 @@ class BatchedReplicas:
     def info(self) -> dict:
         out = np.zeros(8)
         _lib.check(_lib.load().rimu_batch_info(self.handle, out.ctypes.data_as(C.POINTER(C.c_double))))
+        mode = C.c_int()
+        _lib.check(_lib.load().rimu_batch_annihilation(self.handle, C.byref(mode)))
         return dict(keys_per_bucket=int(out[0]), table_slots=int(out[1]), buckets=int(out[2]),
                     graph_segments=int(out[3]), eager_segments=int(out[4]), retries=int(out[5]),
-                    kernel_ms=float(out[6]), steps=int(out[7]))
+                    kernel_ms=float(out[6]), steps=int(out[7]),
+                    annihilation="sort" if mode.value == _lib.ANN_SORT else "hash")
 
     def __del__(self):
         try:
@@ -160,7 +168,8 @@ class BatchedResult:
         return self._batch.sorted_arrays(self._r)
 
 
-def solve_batched(problems, segment_steps=64, use_graph=True, autotune=True, launch_shape=None):
+def solve_batched(problems, segment_steps=64, use_graph=True, autotune=True, launch_shape=None,
+                  annihilation=None):
     """solve(problem) for each problem of the list, all stepped together (one replica each).
     The problems must share the style, time step, step range and shift strategy
     (DoubleLogUpdate or DontUpdate), and their Hamiltonians the lattice (u may differ)."""
@@ -198,7 +207,7 @@ def solve_batched(problems, segment_steps=64, use_graph=True, autotune=True, lau
                         starts=starts, shifts=shifts, seed=p0.random_seed, projectors=projs,
                         zeta=zeta, xi=xi, shift_update=isinstance(strat, DoubleLogUpdate),
                         segment_steps=segment_steps, use_graph=use_graph, autotune=autotune,
-                        launch_shape=launch_shape)
+                        launch_shape=launch_shape, annihilation=annihilation)
     b.step = p0.starting_step
     nsteps = p0.last_step - p0.starting_step
     res = b.run(nsteps)

@@ -235,6 +235,13 @@ class GPUWorkingMemory:
         _lib.check(_lib.load().rimu_wm_set_launch_shape(self.handle, int(keys_per_bucket),
                                                         int(table_slots)))
 
+    def set_annihilation(self, mode: str = "hash"):
+        """How one warp groups the spawns of its bucket by address: "hash" (a shared-memory
+        table, the default) or "sort" (a bitonic sort by address and value).  The results are
+        the same bit for bit."""
+        m = {"hash": _lib.ANN_HASH, "sort": _lib.ANN_SORT}[mode]
+        _lib.check(_lib.load().rimu_wm_set_annihilation(self.handle, m))
+
     def timing(self) -> dict:
         """Per-kernel milliseconds and algorithmic bytes accumulated since set_timing."""
         out = np.zeros(7)

@@ -4,7 +4,8 @@
   large plain FCIQMC configuration): a 250-step trajectory from the unit-filling address at
   target 1e5, and one step of a 1e6-walker list grown on the GPU, under three launch shapes
   (the default; 16 contributions per bucket, i.e. 2^16 buckets as at the 1e8 benchmark;
-  a 512-slot table, i.e. buckets annihilated in several passes).
+  a 512-slot table, i.e. buckets annihilated in several passes) and with the warps' spawns
+  sorted instead of hashed.
 * HubbardReal1D M=N=14 on the full basis (D = 20 058 300, the matrix-free H*v
   configuration): forward and adjoint over every row, and the Hellmann-Feynman gradients
   for u in {1, 2, 4, 8} against central finite differences and the interaction expectation.
@@ -72,13 +73,15 @@ def test_c2_trajectory_250_steps_bit_exact():
     assert len(keys) > 80000
 
 
-@pytest.mark.parametrize("kpb,slots", [(1024, 0), (16, 0), (4096, 512)],
-                         ids=["default", "2^16-buckets", "multipass"])
-def test_c2_step_of_a_1e6_walker_list(kpb, slots):
+@pytest.mark.parametrize("kpb,slots,mode", [(1024, 0, "hash"), (16, 0, "hash"), (4096, 512, "hash"),
+                                            (448, 0, "sort"), (16, 0, "sort")],
+                         ids=["default", "2^16-buckets", "multipass", "sorted", "sorted-2^16-buckets"])
+def test_c2_step_of_a_1e6_walker_list(kpb, slots, mode):
     keys, vals, shift = C2_LIST()
     m = oracle_model(C2_H)
     wm = R.GPUWorkingMemory(SEED)
     wm.set_launch_shape(kpb, slots)
+    wm.set_annihilation(mode)
     g = gpu_step(C2_H, C2_STYLE, keys, vals, 1e-3, shift, SEED, 7001, wm=wm)
     o = O.step_mt(m, oracle_params(C2_STYLE, 1e-3, shift, SEED, 7001), keys, vals,
                   mem_budget=oracle_mem_budget())

@@ -148,3 +148,25 @@ def test_wide_addresses_reject_projectors():
         R.apply_operator(wm, R.GPUDVec(style=R.IsDynamicSemistochastic(), address_type=h.address),
                          R.GPUDVec({h.address: 5.0}, style=R.IsDynamicSemistochastic()),
                          R.FirstOrderTransitionOperator(h, 0.0, 0.01))
+
+
+def test_wide_addresses_are_rejected_by_batches():
+    """Batched runs take one-word addresses only: a two-word model is refused by the Python
+    class and by rimu_batch_set_replica, before anything runs."""
+    import ctypes as C
+    import rimugpu._lib as L
+    h = _models()["real1d-69"]
+    with pytest.raises(ValueError):
+        R.BatchedReplicas([h], R.IsDynamicSemistochastic(), 0.01, targets=1e3,
+                          starts=[{h.address: 10.0}])
+    lib = L.load()
+    b = C.c_void_p()
+    L.check(lib.rimu_batch_create(L.default_context().handle, 1, L.VAL_F64, C.byref(b)))
+    try:
+        k = np.array([h.address.key & ((1 << 64) - 1), h.address.key >> 64], dtype=np.uint64)
+        v = np.array([10.0])
+        rc = lib.rimu_batch_set_replica(b, 0, h.handle, k.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                        v.ctypes.data_as(C.c_void_p), 1, 0.0, 1e3)
+        assert rc == L.RIMU_ERR_BADARG
+    finally:
+        lib.rimu_batch_destroy(b)

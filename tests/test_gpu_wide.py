@@ -170,3 +170,26 @@ def test_wide_addresses_are_rejected_by_batches():
         assert rc == L.RIMU_ERR_BADARG
     finally:
         lib.rimu_batch_destroy(b)
+
+
+@pytest.mark.parametrize("name,style", [("real1d-99", R.IsDynamicSemistochastic()),
+                                        ("realspace-bose-103", R.IsStochasticInteger())])
+def test_wide_step_with_many_buckets_per_cta(name, style):
+    """A two-word list of ~2e4 addresses at 16 contributions per bucket: a few thousand
+    buckets, more than the annihilation CTAs resident on the GPU, so each CTA annihilates
+    several buckets in turn (most of them empty for the integer case)."""
+    h = _models()[name]
+    m = oracle_model(h)
+    keys = _neighbourhood(m, h.address.key, depth=3, cap=20000)
+    rng = np.random.default_rng(41)
+    if style.valtype is int:
+        vals = rng.integers(1, 6, len(keys)) * rng.choice([-1, 1], len(keys))
+    else:
+        vals = rng.normal(size=len(keys)) * 3
+    wm = R.GPUWorkingMemory(SEED)
+    wm.set_launch_shape(16, 0)
+    ka = np.array(keys, dtype=object)
+    g = gpu_step(h, style, ka, vals, 0.005, -1.0, SEED, 6, wm=wm)
+    o = O.step(m, oracle_params(style, 0.005, -1.0, SEED, 6), keys, vals)
+    assert_same_step(g, o, style)
+    assert g[2]["nb_bits"] >= 11

@@ -66,13 +66,15 @@ typedef struct rimu_wm rimu_wm;
  * k - 64 of hi otherwise; key arrays then hold 2 words per address.  Walker lists for them
  * are created with rimu_vec_create_kw(..., key_words = 2, ...).
  *
- * Two-component addresses (CompositeFS of two components, multicomponent.jl:10-30, and its
- * alias FermiFS2C, :87-103): n_components = 2, each component a BoseFS or FermiFS with the
- * same n_modes, both in one 64-bit key: component 1 in the high bits, component 2 in the low
- * comp_bits(2) bits, so that unsigned key order is the reference's order of the component
- * tuple (multicomponent.jl:79).  The two widths must add up to at most 64 bits.  Supported
- * for HubbardRealSpace (CompositeFS of BoseFS/FermiFS components, HubbardRealSpace.jl:18-61,
- * 100-107, 344-391) and HubbardMom1D (FermiFS2C, HubbardMom1D.jl:141-205). */
+ * Multi-component addresses (CompositeFS, multicomponent.jl:10-30, and its alias FermiFS2C,
+ * :87-103): n_components = C in 2..RIMU_MAX_COMPONENTS, each component a BoseFS or FermiFS
+ * with the same n_modes, all in one 64-bit key: component C in the low comp_bits(C) bits,
+ * component C-1 above it, ..., component 1 in the highest bits, so that unsigned key order is
+ * the reference's order of the component tuple (multicomponent.jl:79).  The widths must add
+ * up to at most 64 bits.  Supported for HubbardRealSpace (CompositeFS of BoseFS/FermiFS
+ * components, HubbardRealSpace.jl:18-61, 100-107, 344-391) and, with C = 2, HubbardMom1D
+ * (FermiFS2C, HubbardMom1D.jl:141-205). */
+#define RIMU_MAX_COMPONENTS 4
 typedef struct {
   int kind;                 /* RIMU_MODEL_* */
   int fermion;              /* 1: FermiFS addresses (RIMU_MODEL_REALSPACE only) */
@@ -83,14 +85,17 @@ typedef struct {
   int ndim;                 /* HubbardRealSpace CubicGrid dimensions (1..3) */
   int dims[3];
   int periodic[3];          /* 1: PeriodicBoundaries, 0: HardwallBoundaries per dimension */
-  const double *potential;  /* HubbardRealSpace trap energy per site (n_modes; with two
-                               components 2 * n_modes, component 1 first) or NULL */
+  const double *potential;  /* HubbardRealSpace trap energy per site (n_modes; with C
+                               components C * n_modes, component 1's sites first: the
+                               reference's h.potential matrix in column order) or NULL */
   const double *dispersion; /* HubbardMom1D kinetic energies h.kes (n_modes), required */
-  int n_components;         /* 0 or 1: one component; 2: two components */
-  int comp_fermion[2];      /* per component: 1 FermiFS, 0 BoseFS */
-  int comp_particles[2];    /* particles per component */
-  double comp_t[2];         /* HubbardRealSpace hopping t[c] */
-  double comp_u[3];         /* HubbardRealSpace interaction u[1,1], u[1,2] = u[2,1], u[2,2] */
+  int n_components;         /* 0 or 1: one component; C >= 2: C components */
+  int comp_fermion[RIMU_MAX_COMPONENTS];    /* per component: 1 FermiFS, 0 BoseFS */
+  int comp_particles[RIMU_MAX_COMPONENTS];  /* particles per component */
+  double comp_t[RIMU_MAX_COMPONENTS];       /* HubbardRealSpace hopping t[c] */
+  /* HubbardRealSpace interaction matrix u (symmetric C x C), its upper triangle row by row:
+   * u[1,1], u[1,2], ..., u[1,C], u[2,2], ..., u[C,C] (for C = 2: u[1,1], u[1,2], u[2,2]) */
+  double comp_u[RIMU_MAX_COMPONENTS * (RIMU_MAX_COMPONENTS + 1) / 2];
 } rimu_model_desc;
 
 /* Parameters of one projector step (apply_operator!, src/Interfaces/dictvectors.jl:112). */

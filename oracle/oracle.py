@@ -36,13 +36,16 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+MAXC = 4   # O_MAXC: components of a CompositeFS
+
+
 class _OModel(C.Structure):
     _fields_ = [("kind", C.c_int), ("fermion", C.c_int), ("N", C.c_int), ("M", C.c_int),
                 ("u", C.c_double), ("t", C.c_double), ("ndim", C.c_int),
                 ("dims", C.c_int * 3), ("periodic", C.c_int * 3),
                 ("pot", C.POINTER(C.c_double)), ("kes", C.POINTER(C.c_double)),
-                ("ncomp", C.c_int), ("cferm", C.c_int * 2), ("cN", C.c_int * 2),
-                ("ct", C.c_double * 2), ("cu", C.c_double * 3)]
+                ("ncomp", C.c_int), ("cferm", C.c_int * MAXC), ("cN", C.c_int * MAXC),
+                ("ct", C.c_double * MAXC), ("cu", C.c_double * (MAXC * (MAXC + 1) // 2))]
 
 
 class _OParams(C.Structure):
@@ -131,8 +134,8 @@ class Model:
     periodic: tuple = ()
     pot: np.ndarray | None = None
     kes: np.ndarray | None = None
-    # two components (CompositeFS / FermiFS2C): per-component fermion flags, particle numbers,
-    # HubbardRealSpace hoppings and the interactions (u11, u12, u22)
+    # C >= 2 components (CompositeFS / FermiFS2C): per-component fermion flags, particle
+    # numbers, HubbardRealSpace hoppings and the interactions (upper triangle of u, row by row)
     comps: tuple = ()
     ct: tuple = (1.0, 1.0)
     cu: tuple = (0.0, 0.0, 0.0)
@@ -156,12 +159,13 @@ class Model:
             arr = np.ascontiguousarray(self.kes, dtype=np.float64)
             self._keep.append(arr)
             m.kes = _p(arr, C.c_double)
-        m.ncomp = 2 if self.comps else 1
+        m.ncomp = len(self.comps) if self.comps else 1
         for c, (ferm, n) in enumerate(self.comps):
             m.cferm[c], m.cN[c] = int(ferm), int(n)
-        m.ct[0], m.ct[1] = (float(x) for x in self.ct)
-        for i in range(3):
-            m.cu[i] = float(self.cu[i])
+        for c, x in enumerate(self.ct):
+            m.ct[c] = float(x)
+        for i, x in enumerate(self.cu):
+            m.cu[i] = float(x)
         return m
 
     def comp_bits(self, c: int) -> int:
@@ -171,7 +175,7 @@ class Model:
     @property
     def nbits(self) -> int:
         if self.comps:
-            return self.comp_bits(0) + self.comp_bits(1)
+            return sum(self.comp_bits(c) for c in range(len(self.comps)))
         return self.M if self.fermion else self.N + self.M - 1
 
 
@@ -198,17 +202,25 @@ def mom1d(N, M, u=1.0, t=1.0):
     return Model(MOM1D, N, M, u, t, kes=mom1d_kes(M, t))
 
 
-def realspace2(comps, dims, t=(1.0, 1.0), u=((1.0, 1.0), (1.0, 1.0)), periodic=None, pot=None):
-    """HubbardRealSpace with a two-component CompositeFS: `comps` = ((fermion, N), (fermion,
-    N)) for components 1 and 2; `u` the symmetric 2x2 interaction matrix; `pot` (2, M) or None."""
+def realspace_multi(comps, dims, t=None, u=None, periodic=None, pot=None):
+    """HubbardRealSpace with a CompositeFS of C = len(comps) components (2..4): `comps` =
+    ((fermion, N), ...) in component order; `t` the C hoppings (default ones); `u` the
+    symmetric C x C interaction matrix (default ones); `pot` (C, M) or None."""
+    Cn = len(comps)
     M = int(np.prod(dims))
     periodic = periodic if periodic is not None else tuple(True for _ in dims)
-    u = np.asarray(u, dtype=float)
+    u = np.ones((Cn, Cn)) if u is None else np.asarray(u, dtype=float).reshape(Cn, Cn)
+    t = tuple(1.0 for _ in range(Cn)) if t is None else tuple(float(x) for x in t)
     p = None if pot is None else np.ascontiguousarray(np.ravel(np.asarray(pot, dtype=float)))
     N = sum(n for _, n in comps)
     return Model(REALSPACE, N, M, 0.0, 0.0, False, tuple(dims), tuple(periodic), p,
-                 comps=tuple((bool(f), int(n)) for f, n in comps), ct=tuple(t),
-                 cu=(u[0, 0], u[0, 1], u[1, 1]))
+                 comps=tuple((bool(f), int(n)) for f, n in comps), ct=t,
+                 cu=tuple(u[i, j] for i in range(Cn) for j in range(i, Cn)))
+
+
+def realspace2(comps, dims, t=(1.0, 1.0), u=((1.0, 1.0), (1.0, 1.0)), periodic=None, pot=None):
+    """HubbardRealSpace with a two-component CompositeFS (realspace_multi with C = 2)."""
+    return realspace_multi(comps, dims, t=t, u=u, periodic=periodic, pot=pot)
 
 
 def mom1d_2c(N1, N2, M, u=1.0, t=1.0):
@@ -462,9 +474,11 @@ def basis(m: Model) -> np.ndarray:
     """All addresses with the model's particle numbers, in increasing order (build_basis,
     basis_fock.jl:12-36); for two components the product of the component bases."""
     if m.comps:
-        b0 = _fixed_weight(m.comp_bits(0), m.comps[0][1])
-        b1 = _fixed_weight(m.comp_bits(1), m.comps[1][1])
-        return ((b0[:, None] << np.uint64(m.comp_bits(1))) | b1[None, :]).ravel()
+        out = _fixed_weight(m.comp_bits(0), m.comps[0][1])
+        for c in range(1, len(m.comps)):
+            bc = _fixed_weight(m.comp_bits(c), m.comps[c][1])
+            out = ((out[:, None] << np.uint64(m.comp_bits(c))) | bc[None, :]).ravel()
+        return out
     return _fixed_weight(m.nbits, m.N)
 
 

@@ -47,6 +47,7 @@
 #include <math.h>
 
 #define O_MAXM 128
+#define O_MAXC 4      /* components of a CompositeFS */
 
 /* Addresses are handled as 128-bit integers: a single 64-bit chunk has hi = 0, a two-chunk
  * address (65-128 bits, bitstring.jl:6-18) keeps the same bit positions across both words.
@@ -161,33 +162,45 @@ typedef struct {
   const double *pot; /* HubbardRealSpace trap energy per site (two components: 2M, component
                         1 first), or NULL */
   const double *kes; /* HubbardMom1D dispersion per mode */
-  /* Two components: the key holds component 1 in its high bits and component 2 in the low
-   * cbits[1] bits; the ONR of such an address is component 1's M modes then component 2's. */
-  int ncomp;         /* 1 or 2 */
-  int cferm[2];      /* FermiFS (1) or BoseFS (0) per component */
-  int cN[2];         /* particles per component */
-  double ct[2];      /* HubbardRealSpace t per component */
-  double cu[3];      /* HubbardRealSpace u[1,1], u[1,2], u[2,2] */
+  /* C = ncomp >= 2 components: the key holds the last component in its low bits, the one
+   * before it above them, and so on (component 1 highest); the ONR of such an address is
+   * component 1's M modes, then component 2's, and so on. */
+  int ncomp;             /* 1 .. O_MAXC */
+  int cferm[O_MAXC];     /* FermiFS (1) or BoseFS (0) per component */
+  int cN[O_MAXC];        /* particles per component */
+  double ct[O_MAXC];     /* HubbardRealSpace t per component */
+  double cu[O_MAXC * (O_MAXC + 1) / 2];   /* HubbardRealSpace u, upper triangle row by row */
 } o_model;
 
 static int o_comp_bits(const o_model *h, int c) {
   return h->cferm[c] ? h->M : h->cN[c] + h->M - 1;
 }
+/* u[i, j] (0-based, i <= j) in the upper triangle of the C x C matrix, row by row */
+static double o_cu(const o_model *h, int i, int j) {
+  return h->cu[i * h->ncomp - i * (i - 1) / 2 + (j - i)];
+}
 static void o_to_onr(const o_model *h, okey key, int *onr) {
-  if (h->ncomp == 2) {
-    int b1 = o_comp_bits(h, 1);
-    okey k0 = key >> b1, k1 = key & ((OKEY_ONE << b1) - 1);
-    if (h->cferm[0]) o_fermi_to_onr_k(k0, h->M, onr); else o_bose_to_onr_k(k0, h->M, onr);
-    if (h->cferm[1]) o_fermi_to_onr_k(k1, h->M, onr + h->M); else o_bose_to_onr_k(k1, h->M, onr + h->M);
+  if (h->ncomp >= 2) {
+    for (int c = h->ncomp - 1; c >= 0; --c) {
+      int b = o_comp_bits(h, c);
+      okey kc = key & ((OKEY_ONE << b) - 1);
+      key >>= b;
+      if (h->cferm[c]) o_fermi_to_onr_k(kc, h->M, onr + c * h->M);
+      else o_bose_to_onr_k(kc, h->M, onr + c * h->M);
+    }
     return;
   }
   if (h->fermion) o_fermi_to_onr_k(key, h->M, onr); else o_bose_to_onr_k(key, h->M, onr);
 }
 static okey o_from_onr(const o_model *h, const int *onr) {
-  if (h->ncomp == 2) {
-    okey k0 = h->cferm[0] ? o_fermi_from_onr_k(onr, h->M) : o_bose_from_onr_k(onr, h->M);
-    okey k1 = h->cferm[1] ? o_fermi_from_onr_k(onr + h->M, h->M) : o_bose_from_onr_k(onr + h->M, h->M);
-    return (k0 << o_comp_bits(h, 1)) | k1;
+  if (h->ncomp >= 2) {
+    okey key = 0;
+    for (int c = 0; c < h->ncomp; ++c) {
+      const int *oc = onr + c * h->M;
+      okey kc = h->cferm[c] ? o_fermi_from_onr_k(oc, h->M) : o_bose_from_onr_k(oc, h->M);
+      key = (key << o_comp_bits(h, c)) | kc;
+    }
+    return key;
   }
   return h->fermion ? o_fermi_from_onr_k(onr, h->M) : o_bose_from_onr_k(onr, h->M);
 }
@@ -221,12 +234,14 @@ static int o_neighbor_site(const o_model *h, int mode, int chosen) {
 }
 
 static int o_noff(const o_model *h, okey key) {
-  int onr[2 * O_MAXM];
+  int onr[O_MAXC * O_MAXM];
   o_to_onr(h, key, onr);
-  if (h->ncomp == 2) {
+  if (h->ncomp >= 2) {
     if (h->kind == O_MOM1D) return h->cN[0] * h->cN[1] * (h->M - 1);   /* HubbardMom1D.jl:141-144 */
     /* each component's hops (HubbardRealSpace.jl:316-321, 366-371) */
-    return (o_num_occupied(onr, h->M) + o_num_occupied(onr + h->M, h->M)) * 2 * h->ndim;
+    int s = 0;
+    for (int c = 0; c < h->ncomp; ++c) s += o_num_occupied(onr + c * h->M, h->M);
+    return s * 2 * h->ndim;
   }
   int s = o_num_occupied(onr, h->M);
   if (h->kind == O_REAL1D) return 2 * s;                        /* HubbardReal1D.jl:51-53 */
@@ -276,21 +291,26 @@ static double o_realspace_hop(const o_model *h, int *onr, int fermion, double t,
 
 static void o_offdiag_k(const o_model *h, okey key, int chosen, okey *nkey, double *val,
                         long *prod) {
-  int onr[2 * O_MAXM];
+  int onr[O_MAXC * O_MAXM];
   *prod = 0;
   o_to_onr(h, key, onr);
   int M = h->M;
-  if (h->ncomp == 2 && h->kind == O_REALSPACE) {
-    /* component 1's hops, then component 2's (HubbardRealSpace.jl:344-391) */
-    int n0 = o_num_occupied(onr, M) * 2 * h->ndim;
-    int c = chosen <= n0 ? 0 : 1;
-    double v = o_realspace_hop(h, onr + c * M, h->cferm[c], h->ct[c], c ? chosen - n0 : chosen, prod);
+  if (h->ncomp >= 2 && h->kind == O_REALSPACE) {
+    /* component 1's hops, then component 2's, and so on (HubbardRealSpace.jl:344-391) */
+    int c = 0;
+    for (;;) {
+      int nc = o_num_occupied(onr + c * M, M) * 2 * h->ndim;
+      if (chosen <= nc || c + 1 == h->ncomp) break;
+      chosen -= nc;
+      ++c;
+    }
+    double v = o_realspace_hop(h, onr + c * M, h->cferm[c], h->ct[c], chosen, prod);
     if (*prod == 0) { *nkey = key; *val = 0.0; return; }
     *nkey = o_from_onr(h, onr);
     *val = v;
     return;
   }
-  if (h->ncomp == 2) {
+  if (h->ncomp >= 2) {
     /* FermiFS2C: momentum_transfer_excitation of two components, fold=true
      * (excitations.jl:82-119); element u/M * (val_a * val_b) (HubbardMom1D.jl:196-205) */
     int *oa = onr, *ob = onr + M;
@@ -424,7 +444,7 @@ double o_diagonal(const o_model *h, uint64_t key) { return o_diag_k(h, key); }
 double o_diagonal_w(const o_model *h, uint64_t lo, uint64_t hi) { return o_diag_k(h, o_key_of(lo, hi)); }
 
 static double o_diag_k(const o_model *h, okey key) {
-  int onr[2 * O_MAXM];
+  int onr[O_MAXC * O_MAXM];
   o_to_onr(h, key, onr);
   int M = h->M;
   if (h->ncomp == 2 && h->kind == O_MOM1D) {
@@ -435,27 +455,52 @@ static double o_diag_k(const o_model *h, okey key) {
     for (int i = 0; i < M; ++i) if (onr[M + i]) { kb += h->kes[i] * 1; ++nb; }
     return ka + kb + h->u / (2 * M) * (double)(2 * na * nb);
   }
-  if (h->ncomp == 2) {
-    /* _interactions of two components: (self_1 + (u12 * dot + 0)) + ((self_2 + 0) + 0.0),
-     * local_interaction of a FermiFS being 0 (HubbardRealSpace.jl:18-61); then the trap,
-     * (0.0 + pot_1) + pot_2 (:100-107); diagonal = int + pot (:284-287). */
+  if (h->ncomp >= 2) {
+    /* local_interaction(CompositeFS, u) = _interactions(components, u) (HubbardRealSpace.jl:
+     * 18-61), evaluated as the reference's recursion does:
+     *   _interactions((a, as...)) = self + row + _interactions(as),  _interactions(()) = 0.0,
+     *   row = _interaction_col(a, as) = li(a, b1) + (li(a, b2) + (... + 0)),
+     * where self = u[s,s] * bose_hubbard_interaction / 2 for a BoseFS and the integer 0 for a
+     * FermiFS, li(a, b) = u[s,j] * dot(occupations), and the closing 0 of _interaction_col is
+     * an integer: integer 0 + double x is 0.0 + x.  Here the integer zeros are the flags
+     * *_int.  Then the trap, pe = 0.0 + pot_1 + pot_2 + ... (:100-107); diagonal = int + pot
+     * (:284-287).  The interaction term is 0.0 when u is all zero (h.u === nothing). */
+    const int C = h->ncomp;
+    int any_u = 0;
+    for (int i = 0; i < C * (C + 1) / 2; ++i) any_u |= h->cu[i] != 0.0;
     double in = 0.0;
-    if (h->cu[0] != 0.0 || h->cu[1] != 0.0 || h->cu[2] != 0.0) {
-      double self[2];
-      for (int c = 0; c < 2; ++c) {
-        long bhi = 0;
-        for (int i = 0; i < M; ++i) bhi += (long)onr[c * M + i] * (onr[c * M + i] - 1);
-        self[c] = h->cferm[c] ? 0.0 : h->cu[c == 0 ? 0 : 2] * (double)bhi / 2;
+    if (any_u) {
+      double rest = 0.0;
+      for (int s2 = C - 1; s2 >= 0; --s2) {
+        const int *os = onr + s2 * M;
+        double row = 0.0;
+        int row_int = 1;
+        for (int j = C - 1; j > s2; --j) {
+          long dot = 0;
+          for (int i = 0; i < M; ++i) dot += (long)os[i] * onr[j * M + i];
+          double li = o_cu(h, s2, j) * (double)dot;
+          row = row_int ? li + 0.0 : li + row;
+          row_int = 0;
+        }
+        double first;
+        int first_int;
+        if (h->cferm[s2]) {
+          first = row_int ? 0.0 : 0.0 + row;
+          first_int = row_int;
+        } else {
+          long bhi = 0;
+          for (int i = 0; i < M; ++i) bhi += (long)os[i] * (os[i] - 1);
+          double self = o_cu(h, s2, s2) * (double)bhi / 2;
+          first = row_int ? self + 0.0 : self + row;
+          first_int = 0;
+        }
+        rest = first_int ? 0.0 + rest : first + rest;
       }
-      long dot = 0;
-      for (int i = 0; i < M; ++i) dot += (long)onr[i] * onr[M + i];
-      double row = h->cu[1] * (double)dot + 0.0;
-      in = (self[0] + row) + (self[1] + 0.0);
+      in = rest;
     }
     double pe = 0.0;
     if (h->pot) {
-      pe += o_potential(onr, M, h->pot);
-      pe += o_potential(onr + M, M, h->pot + M);
+      for (int c = 0; c < C; ++c) pe += o_potential(onr + c * M, M, h->pot + c * M);
     }
     return in + pe;
   }
@@ -765,7 +810,7 @@ double o_real1d_bits_diagonal(const o_model *h, uint64_t key) {
 }
 
 static int o_use_bits(const o_model *h) {
-  return h->kind == O_REAL1D && h->ncomp != 2 && h->N + h->M - 1 <= 64;
+  return h->kind == O_REAL1D && h->ncomp < 2 && h->N + h->M - 1 <= 64;
 }
 static int o_noff_f(const o_model *h, okey key, int fast) {
   return fast ? o_bits_noff(o_lo(key)) : o_noff(h, key);
@@ -1195,8 +1240,11 @@ int o_step_mt(const o_model *h, const o_params *p, const uint64_t *skeys, const 
   memset(st, 0, sizeof(*st));
   if (p->init_rule != O_INIT_NONE) return 2;
   {
-    int B = h->ncomp == 2 ? o_comp_bits(h, 0) + o_comp_bits(h, 1)
-                          : (h->fermion ? h->M : h->N + h->M - 1);
+    int B = h->fermion ? h->M : h->N + h->M - 1;
+    if (h->ncomp >= 2) {
+      B = 0;
+      for (int c = 0; c < h->ncomp; ++c) B += o_comp_bits(h, c);
+    }
     if (B > 64) return 2;
   }
   int nt = 1;
@@ -1398,7 +1446,7 @@ int64_t o_hv_basis_adjoint(const o_model *h, const uint64_t *keys, int64_t D, co
   if (!kgs || !bhis) { free(kgs); free(bhis); return -1; }
 #pragma omp parallel for reduction(+ : missing) schedule(dynamic, 4096)
   for (int64_t i = 0; i < D; ++i) {
-    int onr[2 * O_MAXM];
+    int onr[O_MAXC * O_MAXM];
     o_to_onr(h, keys[i], onr);
     long bhi = 0;
     for (int k = 0; k < h->M; ++k) bhi += (long)onr[k] * (onr[k] - 1);

@@ -110,16 +110,16 @@ int rimu_ctx_synchronize(rimu_ctx *ctx) {
 // ---------------------------------------------------------------------------------------------
 // Helpers
 // ---------------------------------------------------------------------------------------------
-static bool two_components(const rimu_model_desc &d) { return d.n_components == 2; }
+static bool two_components(const rimu_model_desc &d) { return d.n_components >= 2; }
 
 // Largest occupation product under the square root of an offdiagonal element (one table
-// block; with two HubbardRealSpace components, of either component).
+// block; with several HubbardRealSpace components, of any component).
 static int model_max_prod(const rimu_model_desc &d) {
   int N = d.n_particles;
   if (d.kind == RIMU_MODEL_MOM1D) return two_components(d) ? 4 : (N + 1) * (N + 1) * (N + 1) * (N + 1);
   if (two_components(d)) {
     int p = 1;
-    for (int c = 0; c < 2; ++c)
+    for (int c = 0; c < d.n_components; ++c)
       if (!d.comp_fermion[c]) p = std::max(p, d.comp_particles[c] * (d.comp_particles[c] + 1));
     return p;
   }
@@ -165,29 +165,33 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
   if (d->kind < 1 || d->kind > 3) return bad("rimu_model_create: unknown model kind");
   if (d->n_particles < 0 || d->n_modes < 1 || d->n_modes > 128)
     return bad("rimu_model_create: need 1 <= n_modes <= 128");
-  if (d->n_components < 0 || d->n_components > 2)
-    return bad("rimu_model_create: n_components must be 0, 1 or 2");
+  if (d->n_components < 0 || d->n_components > RIMU_MAX_COMPONENTS)
+    return bad("rimu_model_create: n_components must be 0 .. RIMU_MAX_COMPONENTS");
   const bool two = two_components(*d);
+  const int C = two ? d->n_components : 1;
   int nbits = d->fermion ? d->n_modes : d->n_particles + d->n_modes - 1;
-  int cbits[2] = {0, 0};
+  int cbits[RIMU_MAX_COMPONENTS] = {0, 0, 0, 0};
   if (two) {
     if (d->kind == RIMU_MODEL_REAL1D)
       return bad("rimu_model_create: HubbardReal1D takes a single-component BoseFS");
-    if (d->kind == RIMU_MODEL_MOM1D && !(d->comp_fermion[0] && d->comp_fermion[1]))
+    if (d->kind == RIMU_MODEL_MOM1D && !(C == 2 && d->comp_fermion[0] && d->comp_fermion[1]))
       return bad("rimu_model_create: HubbardMom1D takes two components only as FermiFS2C");
-    for (int c = 0; c < 2; ++c) {
+    int nsum = 0;
+    nbits = 0;
+    for (int c = 0; c < C; ++c) {
       if (d->comp_particles[c] < 0) return bad("rimu_model_create: negative particle number");
       if (d->comp_fermion[c] && d->comp_particles[c] > d->n_modes)
         return bad("rimu_model_create: too many fermions in a component");
       cbits[c] = d->comp_fermion[c] ? d->n_modes : d->comp_particles[c] + d->n_modes - 1;
+      nsum += d->comp_particles[c];
+      nbits += cbits[c];
     }
-    if (d->comp_particles[0] + d->comp_particles[1] != d->n_particles)
+    if (nsum != d->n_particles)
       return bad("rimu_model_create: n_particles must be the sum over the components");
-    nbits = cbits[0] + cbits[1];
   }
   if (nbits > 128) return bad("rimu_model_create: address does not fit 128 bits");
   if ((nbits > 64 || d->n_modes > 64) && two)
-    return bad("rimu_model_create: two-component addresses must fit 64 bits");
+    return bad("rimu_model_create: multi-component addresses must fit 64 bits");
   if (d->n_modes > 64 && d->kind == RIMU_MODEL_MOM1D)
     return bad("rimu_model_create: HubbardMom1D takes at most 64 modes");
   if (d->fermion && d->kind != RIMU_MODEL_REALSPACE)
@@ -215,15 +219,25 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
   DevModel &h = m->dm;
   h.kind = d->kind; h.fermion = two ? 0 : d->fermion; h.N = d->n_particles; h.M = d->n_modes;
   h.nbits = nbits; h.u = d->u; h.t = d->t;
-  h.ncomp = two ? 2 : 1;
-  for (int c = 0; c < 2; ++c) {
-    h.cferm[c] = two ? (d->comp_fermion[c] != 0) : 0;
-    h.cN[c] = two ? d->comp_particles[c] : 0;
-    h.cbits[c] = cbits[c];
-    h.ct[c] = two ? d->comp_t[c] : d->t;
+  h.ncomp = C;
+  {
+    int off = 0;                          // the last component in the lowest bits
+    for (int c = RIMU_MAX_COMPONENTS - 1; c >= 0; --c) {
+      const bool in = two && c < C;
+      h.cferm[c] = in ? (d->comp_fermion[c] != 0) : 0;
+      h.cN[c] = in ? d->comp_particles[c] : 0;
+      h.cbits[c] = in ? cbits[c] : 0;
+      h.coff[c] = in ? off : 0;
+      if (in) off += cbits[c];
+      h.ct[c] = in ? d->comp_t[c] : d->t;
+    }
   }
-  for (int i = 0; i < 3; ++i) h.cu[i] = two ? d->comp_u[i] : 0.0;
-  h.u_nonzero = two && (d->comp_u[0] != 0.0 || d->comp_u[1] != 0.0 || d->comp_u[2] != 0.0);
+  h.u_nonzero = 0;
+  for (int i = 0; i < RIMU_MAX_COMPONENTS * (RIMU_MAX_COMPONENTS + 1) / 2; ++i) {
+    const bool in = two && i < C * (C + 1) / 2;
+    h.cu[i] = in ? d->comp_u[i] : 0.0;
+    if (in && d->comp_u[i] != 0.0) h.u_nonzero = 1;
+  }
   h.ndim = ndim;
   for (int i = 0; i < 3; ++i) {
     h.dims[i] = d->kind == RIMU_MODEL_REALSPACE ? (i < ndim ? d->dims[i] : 1) : (i == 0 ? d->n_modes : 1);
@@ -236,7 +250,7 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     h.kes = m->d_kes;
   }
   if (d->kind == RIMU_MODEL_REALSPACE && d->potential) {
-    const int np = two ? 2 * M : M;    // with two components: component 1's sites first
+    const int np = C * M;              // with several components: component 1's sites first
     if ((rc = dalloc(ctx, &m->d_pot, np)) || (rc = h2d(ctx, m->d_pot, d->potential, np))) goto fail;
     h.pot = m->d_pot;
   }
@@ -252,12 +266,12 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
     h.dint = m->d_recip + nr;
     h.recip_len = nr;
     // Hamiltonian offdiagonal magnitudes by occupation product, one block per component
-    // with its own t for two HubbardRealSpace components
+    // with its own t for several HubbardRealSpace components
     const int pmax = model_max_prod(*d);
-    const int blocks = (two && d->kind == RIMU_MODEL_REALSPACE) ? 2 : 1;
+    const int blocks = (two && d->kind == RIMU_MODEL_REALSPACE) ? C : 1;
     const int len = blocks * (pmax + 1);
     m->aoff_len = len;
-    h.cstride = blocks == 2 ? pmax + 1 : 0;
+    h.cstride = blocks > 1 ? pmax + 1 : 0;
     std::vector<double> hoff(len);
     for (int c = 0; c < blocks; ++c)
       for (int p = 0; p <= pmax; ++p) hoff[c * (pmax + 1) + p] = hoff_value(*d, c, p);
@@ -278,7 +292,9 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
       int s = std::min(N, M);
       m->max_offdiag = s * (s - 1) * (M - 2) + s * (M - 1);
     } else if (two) {
-      m->max_offdiag = (std::min(d->comp_particles[0], M) + std::min(d->comp_particles[1], M)) * 2 * ndim;
+      int s = 0;
+      for (int c = 0; c < C; ++c) s += std::min(d->comp_particles[c], M);
+      m->max_offdiag = s * 2 * ndim;
     } else {
       int s = std::min(N, M);
       m->max_offdiag = s * 2 * ndim;
@@ -996,7 +1012,7 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
 static int basis_dim(const rimu_model *m, int64_t *dim) {
   bool ovf = false;
   int B = m->dm.nbits, w = m->dm.N;
-  if (m->dm.ncomp == 2) { g_err = "basis: two-component addresses are not supported"; return RIMU_ERR_BADARG; }
+  if (m->dm.ncomp >= 2) { g_err = "basis: multi-component addresses are not supported"; return RIMU_ERR_BADARG; }
   if (B > 63) { g_err = "basis: address wider than 63 bits"; return RIMU_ERR_BADARG; }
   *dim = binomial_u(B, w, &ovf);
   if (ovf) { g_err = "basis: dimension does not fit int64"; return RIMU_ERR_BADARG; }

@@ -153,22 +153,46 @@ __device__ double model_diagonal64(const DevModel &h, uint64_t key) {
     const long long nab = 2LL * popc64(ka) * popc64(kb);
     return fermi_kinetic(ka, h.kes) + fermi_kinetic(kb, h.kes) + h.u / (2 * h.M) * (double)nab;
   }
-  if (KIND == MODEL_REALSPACE && h.ncomp == 2) {
-    // local_interaction of the two components with the u matrix, then the trap
-    // (HubbardRealSpace.jl:18-61, 100-107, 284-287).  _interactions evaluates
-    // (self_1 + (u12 * dot + 0)) + ((self_2 + 0) + 0.0); the "+ 0.0" terms keep its signed zeros.
-    const uint64_t k0 = component_of(h, key, 0), k1 = component_of(h, key, 1);
+  if (KIND == MODEL_REALSPACE && h.ncomp >= 2) {
+    // local_interaction of the components with the u matrix, then the trap
+    // (HubbardRealSpace.jl:18-61, 100-107, 284-287), in the reference's order of operations:
+    // _interactions((a_s, ...)) = (self_s + row_s) + _interactions((a_{s+1}, ...)), ending in
+    // 0.0; row_s = li(a_s, a_{s+1}) + (li(a_s, a_{s+2}) + (... + 0)), ending in the integer 0;
+    // the self-interaction of a FermiFS is the integer 0.  Adding an integer 0 to a double is
+    // "+ 0.0" (it turns -0.0 into +0.0); integer + integer stays the integer 0.
+    const int C = h.ncomp;
     double in = 0.0;
     if (h.u_nonzero) {
-      const double s0 = h.cferm[0] ? 0.0 : h.cu[0] * (double)bose_interaction(k0) / 2;
-      const double row = h.cu[1] * (double)component_overlap(h, k0, k1) + 0.0;
-      const double s1 = (h.cferm[1] ? 0.0 : h.cu[2] * (double)bose_interaction(k1) / 2) + 0.0;
-      in = (s0 + row) + s1;
+      double rest = 0.0;                         // _interactions of the empty tuple: 0.0
+      for (int s = C - 1; s >= 0; --s) {
+        const uint64_t ks = component_of(h, key, s);
+        double row = 0.0;
+        bool row_int = true;                     // the integer 0 closing _interaction_col
+        for (int j = C - 1; j > s; --j) {
+          const double li = h.cu[cu_index(C, s, j)] *
+                            (double)component_overlap(h, ks, h.cferm[s], component_of(h, key, j),
+                                                      h.cferm[j]);
+          row = row_int ? li + 0.0 : li + row;
+          row_int = false;
+        }
+        double first;
+        bool first_int;
+        if (h.cferm[s]) {                        // self + row with self the integer 0
+          first = row_int ? 0.0 : row + 0.0;
+          first_int = row_int;
+        } else {
+          const double self = h.cu[cu_index(C, s, s)] * (double)bose_interaction(ks) / 2;
+          first = row_int ? self + 0.0 : self + row;
+          first_int = false;
+        }
+        rest = first_int ? rest + 0.0 : first + rest;
+      }
+      in = rest;
     }
     double pe = 0.0;
     if (h.pot) {
-      pe += component_potential(k0, h.cferm[0], h.pot);
-      pe += component_potential(k1, h.cferm[1], h.pot + h.M);
+      for (int c = 0; c < C; ++c)
+        pe += component_potential(component_of(h, key, c), h.cferm[c], h.pot + c * h.M);
     }
     return in + pe;
   }

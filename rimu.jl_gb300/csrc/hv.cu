@@ -452,7 +452,7 @@ extern "C" int rimu_hv_basis_adjoint_noalloc(const rimu_model_desc *d, const dou
     return RIMU_ERR_BADARG;
   }
   const bool realspace = d->kind == RIMU_MODEL_REALSPACE;
-  if (d->n_components == 2 || d->fermion ||
+  if (d->n_components >= 2 || d->fermion ||
       !(d->kind == RIMU_MODEL_REAL1D || (realspace && !d->potential))) {
     rimu_set_error("rimu_hv_basis_adjoint_noalloc: needs HubbardReal1D or one-component bosonic HubbardRealSpace without trap");
     return RIMU_ERR_BADARG;

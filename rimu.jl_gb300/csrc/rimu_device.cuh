@@ -32,6 +32,8 @@ constexpr uint64_t EMPTY_KEY = ~0ull;   // never a valid address: would need 64 
 // ------------------------------------------------------------------------------------------
 // Device model description (immutable during a step).
 // ------------------------------------------------------------------------------------------
+constexpr int MAXC = 4;   // components of a multi-component address
+
 struct DevModel {
   int kind, fermion, N, M, nbits;
   int ndim, dims[3], periodic[3];
@@ -44,16 +46,17 @@ struct DevModel {
   const double *recip;   // recip[n] = 1.0 / n for n < recip_len
   int recip_len;
   const double *dint;    // dint[n] = (double)n for n < recip_len
-  // Two-component addresses (CompositeFS, FermiFS2C): component 1 in the high bits
-  // [cbits[1], cbits[1] + cbits[0]) of the key, component 2 in the low cbits[1] bits.
-  int ncomp;             // 1 or 2
-  int cferm[2];          // per component: FermiFS (1) or BoseFS (0)
-  int cN[2];             // particles per component
-  int cbits[2];          // bits per component
-  double ct[2];          // HubbardRealSpace hopping t[c]
-  double cu[3];          // HubbardRealSpace u[1,1], u[1,2], u[2,2]
+  // Multi-component addresses (CompositeFS, FermiFS2C): component c in the bits
+  // [coff[c], coff[c] + cbits[c]) of the key, the last component in the lowest bits.
+  int ncomp;             // 1 .. MAXC
+  int cferm[MAXC];       // per component: FermiFS (1) or BoseFS (0)
+  int cN[MAXC];          // particles per component
+  int cbits[MAXC];       // bits per component
+  int coff[MAXC];        // lowest key bit of each component
+  double ct[MAXC];       // HubbardRealSpace hopping t[c]
+  double cu[MAXC * (MAXC + 1) / 2];   // HubbardRealSpace u, upper triangle row by row
   int u_nonzero;         // HubbardRealSpace: some interaction is nonzero
-  int cstride;           // offdiagonal-table offset of component 2 (HubbardRealSpace)
+  int cstride;           // offdiagonal-table block size per component (HubbardRealSpace)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -465,10 +468,13 @@ using Offdiag = OffdiagT<uint64_t>;
 template <class K>
 RIMU_HD int num_offdiagonals_real(const DevModel &h, K key) {
   if constexpr (KT<K>::BITS == 64) {
-    if (h.ncomp == 2) {   // component 1 in the high bits, component 2 in the low cbits[1]
-      const uint64_t k0 = shr64(key, h.cbits[1]), k1 = key & lowmask(h.cbits[1]);
-      return ((h.cferm[0] ? popc64(k0) : bose_num_occupied(k0)) +
-              (h.cferm[1] ? popc64(k1) : bose_num_occupied(k1))) * 2 * h.ndim;
+    if (h.ncomp >= 2) {   // every component's hops
+      int s = 0;
+      for (int c = 0; c < h.ncomp; ++c) {
+        const uint64_t kc = shr64(key, h.coff[c]) & lowmask(h.cbits[c]);
+        s += h.cferm[c] ? popc64(kc) : bose_num_occupied(kc);
+      }
+      return s * 2 * h.ndim;
     }
   }
   int s = h.fermion ? kpopc(key) : bose_num_occupied(key);
@@ -641,12 +647,14 @@ RIMU_HD OffdiagT<K> realspace_hop(const DevModel &h, K key, int chosen, bool fer
 
 // ---- two-component addresses -------------------------------------------------------------
 RIMU_HD uint64_t component_of(const DevModel &h, uint64_t key, int c) {
-  return c == 0 ? shr64(key, h.cbits[1]) : (key & lowmask(h.cbits[1]));
+  return shr64(key, h.coff[c]) & lowmask(h.cbits[c]);
 }
 RIMU_HD uint64_t with_component(const DevModel &h, uint64_t key, int c, uint64_t ck) {
-  const uint64_t lo = lowmask(h.cbits[1]);
-  return c == 0 ? ((key & lo) | shl64(ck, h.cbits[1])) : ((key & ~lo) | ck);
+  const uint64_t m = shl64(lowmask(h.cbits[c]), h.coff[c]);
+  return (key & ~m) | shl64(ck, h.coff[c]);
 }
+// Position of u[i, j] (i <= j, 0-based) in the upper triangle of a C x C matrix, row by row.
+RIMU_HD int cu_index(int C, int i, int j) { return i * C - i * (i - 1) / 2 + (j - i); }
 RIMU_HD int component_occupied(uint64_t ck, int fermion) {
   return fermion ? popc64(ck) : bose_num_occupied(ck);
 }
@@ -669,28 +677,33 @@ RIMU_HD void component_occupations(uint64_t ck, int fermion, int M, uint8_t *occ
 }
 // sum_i n_{a,i} n_{b,i} (dot of occupied modes, fockaddress.jl:692-717; two FermiFS chunks:
 // the popcount of their intersection, bitstring.jl:833-838)
-RIMU_HD int component_overlap(const DevModel &h, uint64_t a, uint64_t b) {
-  if (h.cferm[0] && h.cferm[1]) return popc64(a & b);
+RIMU_HD int component_overlap(const DevModel &h, uint64_t a, int fa, uint64_t b, int fb) {
+  if (fa && fb) return popc64(a & b);
   uint8_t oa[MAX_MODES], ob[MAX_MODES];
-  component_occupations(a, h.cferm[0], h.M, oa);
-  component_occupations(b, h.cferm[1], h.M, ob);
+  component_occupations(a, fa, h.M, oa);
+  component_occupations(b, fb, h.M, ob);
   int acc = 0;
   for (int i = 0; i < h.M; ++i) acc += (int)oa[i] * (int)ob[i];
   return acc;
 }
 
 // HubbardRealSpace offdiagonal: one component, or component 1's hops followed by component
-// 2's (HubbardRealSpaceOffdiagonals, HubbardRealSpace.jl:344-391), each with its own t
-// (table block c).
+// 2's, and so on (HubbardRealSpaceOffdiagonals, HubbardRealSpace.jl:344-391), each with its
+// own t (table block c).
 template <class K>
 RIMU_HD OffdiagT<K> realspace_offdiag(const DevModel &h, K key, int chosen) {
   if constexpr (KT<K>::BITS == 64) {
-    if (h.ncomp == 2) {
-      const uint64_t k0 = component_of(h, key, 0);
-      const int n0 = component_occupied(k0, h.cferm[0]) * 2 * h.ndim;
-      const int c = chosen <= n0 ? 0 : 1;
-      Offdiag r = realspace_hop(h, c ? component_of(h, key, 1) : k0, c ? chosen - n0 : chosen,
-                                h.cferm[c] != 0);
+    if (h.ncomp >= 2) {
+      int c = 0;
+      uint64_t kc = component_of(h, key, 0);
+      for (;;) {
+        const int nc = component_occupied(kc, h.cferm[c]) * 2 * h.ndim;
+        if (chosen <= nc || c + 1 == h.ncomp) break;
+        chosen -= nc;
+        ++c;
+        kc = component_of(h, key, c);
+      }
+      Offdiag r = realspace_hop(h, kc, chosen, h.cferm[c] != 0);
       if (r.prod == 0) { r.key = key; return r; }
       r.key = with_component(h, key, c, r.key);
       r.prod += c * h.cstride;
@@ -719,7 +732,7 @@ RIMU_HD Offdiag mom2c_offdiag(const DevModel &h, uint64_t key, int chosen) {
   uint64_t na, nbk;
   int ga, gb;
   if (!fermi_move(ka, sa, dst_a, na, ga) || !fermi_move(kb, sb, dst_b, nbk, gb)) return r;
-  r.key = shl64(na, h.cbits[1]) | nbk;
+  r.key = shl64(na, h.coff[0]) | nbk;
   r.prod = 4;
   r.sign = ga * gb;
   return r;

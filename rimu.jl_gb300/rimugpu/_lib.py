@@ -17,6 +17,7 @@ MODEL_REAL1D, MODEL_REALSPACE, MODEL_MOM1D = 1, 2, 3
 STYLE_INTEGER, STYLE_DETERMINISTIC, STYLE_DSS = 0, 1, 2
 OP_TRANSITION, OP_HAMILTONIAN = 0, 1
 ANN_HASH, ANN_SORT = 0, 1
+MAX_COMPONENTS = 4          # RIMU_MAX_COMPONENTS
 
 # Names of the C entry points declared in include/rimu_gpu.h.
 EXPORTS = [
@@ -49,9 +50,10 @@ class ModelDesc(C.Structure):
                 ("n_modes", C.c_int), ("u", C.c_double), ("t", C.c_double), ("ndim", C.c_int),
                 ("dims", C.c_int * 3), ("periodic", C.c_int * 3),
                 ("potential", C.POINTER(C.c_double)), ("dispersion", C.POINTER(C.c_double)),
-                ("n_components", C.c_int), ("comp_fermion", C.c_int * 2),
-                ("comp_particles", C.c_int * 2), ("comp_t", C.c_double * 2),
-                ("comp_u", C.c_double * 3)]
+                ("n_components", C.c_int), ("comp_fermion", C.c_int * MAX_COMPONENTS),
+                ("comp_particles", C.c_int * MAX_COMPONENTS),
+                ("comp_t", C.c_double * MAX_COMPONENTS),
+                ("comp_u", C.c_double * (MAX_COMPONENTS * (MAX_COMPONENTS + 1) // 2))]
 
 
 class StepParams(C.Structure):

@@ -167,36 +167,43 @@ def near_uniform(kind, N: int, M: int):
 
 @total_ordering
 class CompositeFS:
-    """CompositeFS(a, b) of two single-component addresses with the same number of modes
-    (multicomponent.jl:10-30).  One 64-bit key: component 1 in the high bits, component 2 in
-    the low ``b.nbits`` bits."""
+    """CompositeFS(a, b, ...) of two to four single-component addresses with the same number
+    of modes (multicomponent.jl:10-30).  One 64-bit key: the last component in the low bits,
+    the one before it above them, and so on, so that key order is the order of the component
+    tuple."""
 
     __slots__ = ("components", "N", "M", "key")
     fermion = False
 
     def __init__(self, *components):
-        if len(components) != 2:
-            raise ValueError("CompositeFS with two components is supported")
-        a, b = components
+        if not 2 <= len(components) <= 4:
+            raise ValueError("CompositeFS with two to four components is supported")
         if not all(isinstance(c, (BoseFS, FermiFS)) for c in components):
             raise TypeError("CompositeFS components must be BoseFS or FermiFS")
-        if a.M != b.M:
+        if any(c.M != components[0].M for c in components):
             raise ValueError("all addresses must have the same number of modes")
-        if a.nbits + b.nbits > 64:
+        if sum(c.nbits for c in components) > 64:
             raise ValueError("CompositeFS wider than 64 bits is not supported")
-        self.components = (a, b)
-        self.N, self.M = a.N + b.N, a.M
-        self.key = (a.key << b.nbits) | b.key
+        self.components = tuple(components)
+        self.N, self.M = sum(c.N for c in components), components[0].M
+        key = 0
+        for c in components:
+            key = (key << c.nbits) | c.key
+        self.key = key
 
     @property
     def nbits(self) -> int:
-        return self.components[0].nbits + self.components[1].nbits
+        return sum(c.nbits for c in self.components)
 
     def with_key(self, key: int) -> "CompositeFS":
-        a, b = self.components
         key = int(key)
+        parts = []
+        rest = key
+        for comp in reversed(self.components):
+            parts.append(comp.with_key(rest & ((1 << comp.nbits) - 1)))
+            rest >>= comp.nbits
         c = CompositeFS.__new__(CompositeFS)
-        c.components = (a.with_key(key >> b.nbits), b.with_key(key & ((1 << b.nbits) - 1)))
+        c.components = tuple(reversed(parts))
         c.N, c.M, c.key = self.N, self.M, key
         return c
 
@@ -208,6 +215,7 @@ class CompositeFS:
 
     def __eq__(self, o):
         return (isinstance(o, CompositeFS) and self.key == o.key and
+                len(self.components) == len(o.components) and
                 all(type(x) is type(y) and x.N == y.N and x.M == y.M
                     for x, y in zip(self.components, o.components)))
 
@@ -219,7 +227,7 @@ class CompositeFS:
                     (self.key,))
 
     def __repr__(self):
-        return f"CompositeFS({self.components[0]!r}, {self.components[1]!r})"
+        return "CompositeFS(" + ", ".join(repr(c) for c in self.components) + ")"
 
 
 def FermiFS2C(*args):
@@ -244,5 +252,5 @@ def FermiFS2C(*args):
 
 
 def is_fermi2c(address) -> bool:
-    return (isinstance(address, CompositeFS) and
+    return (isinstance(address, CompositeFS) and len(address.components) == 2 and
             all(isinstance(c, FermiFS) for c in address.components))

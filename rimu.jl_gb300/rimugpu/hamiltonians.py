@@ -1,7 +1,7 @@
 """Hamiltonians: the AbstractHamiltonian interface on device-side model handles.
 
 HubbardReal1D (src/Hamiltonians/HubbardReal1D.jl), HubbardRealSpace with one component or a
-two-component CompositeFS (HubbardRealSpace.jl, geometry.jl) and HubbardMom1D with BoseFS or
+multi-component CompositeFS (HubbardRealSpace.jl, geometry.jl) and HubbardMom1D with BoseFS or
 FermiFS2C (HubbardMom1D.jl).  Matrix
 elements are evaluated by librimu_gpu; this module only holds parameters and converts.
 """
@@ -206,9 +206,9 @@ def _trap_potential(dims, vrow):
 
 class HubbardRealSpace(AbstractHamiltonian):
     """HubbardRealSpace(address; geometry, t, u, v) (HubbardRealSpace.jl:182-231) with a
-    BoseFS/FermiFS address or a CompositeFS of two components.  One component: `t` and `u`
-    scalars or 1-element sequences.  Two components: `t` of length 2, `u` a symmetric 2x2
-    matrix (defaults all ones), `v` a 2 x D matrix of trap strengths."""
+    BoseFS/FermiFS address or a CompositeFS of C = 2..4 components.  One component: `t` and `u`
+    scalars or 1-element sequences.  C components: `t` of length C, `u` a symmetric C x C
+    matrix (defaults all ones), `v` a C x D matrix of trap strengths."""
     kind = _lib.MODEL_REALSPACE
 
     def __init__(self, address, geometry: CubicGrid | None = None, t=None, u=None, v=None):
@@ -219,7 +219,7 @@ class HubbardRealSpace(AbstractHamiltonian):
         if len(self.geometry) != address.M:
             raise ValueError("`geometry` does not have the correct number of sites")
         D = len(self.geometry.dims)
-        self.ncomp = 2 if isinstance(address, CompositeFS) else 1
+        self.ncomp = len(address.components) if isinstance(address, CompositeFS) else 1
         C_ = self.ncomp
         tv = np.ravel(np.asarray(1.0 if t is None else t, dtype=float))
         um = np.asarray(1.0 if u is None else u, dtype=float)
@@ -229,23 +229,23 @@ class HubbardRealSpace(AbstractHamiltonian):
             self.v = None if v is None or not np.any(v) else np.ravel(np.asarray(v, dtype=float))
             self.potential = None if self.v is None else _trap_potential(self.geometry.dims, self.v)
             return
-        if t is not None and tv.size != 2:
-            raise ValueError("`t` must be a vector of length 2")
-        self.t = tuple(float(x) for x in (tv if tv.size == 2 else np.ones(2)))
-        if u is not None and um.size != 4:
-            raise ValueError("`u` must be a 2 × 2 matrix")
-        um = um.reshape(2, 2) if um.size == 4 else np.ones((2, 2))
-        if um[0, 1] != um[1, 0]:
+        if t is not None and tv.size != C_:
+            raise ValueError(f"`t` must be a vector of length {C_}")
+        self.t = tuple(float(x) for x in (tv if tv.size == C_ else np.ones(C_)))
+        if u is not None and um.size != C_ * C_:
+            raise ValueError(f"`u` must be a {C_} × {C_} matrix")
+        um = um.reshape(C_, C_) if um.size == C_ * C_ else np.ones((C_, C_))
+        if not np.array_equal(um, um.T):
             raise ValueError("`u` must be symmetric")
         self.u = um
         vm = None if v is None else np.asarray(v, dtype=float)
-        if vm is not None and vm.size != 2 * D:
-            raise ValueError(f"`v` must be a 2 × {D} matrix")
-        self.v = None if vm is None or not np.any(vm) else vm.reshape(2, D)
+        if vm is not None and vm.size != C_ * D:
+            raise ValueError(f"`v` must be a {C_} × {D} matrix")
+        self.v = None if vm is None or not np.any(vm) else vm.reshape(C_, D)
         self.potential = None
         if self.v is not None:
             self.potential = np.concatenate([_trap_potential(self.geometry.dims, self.v[c])
-                                             for c in range(2)])
+                                             for c in range(C_)])
 
     def _desc(self):
         d = _lib.ModelDesc()
@@ -260,13 +260,16 @@ class HubbardRealSpace(AbstractHamiltonian):
             d.u, d.t = self.u, self.t
         else:
             d.fermion = 0
-            d.n_components = 2
+            d.n_components = self.ncomp
             d.u, d.t = float(self.u[0, 0]), self.t[0]
             for c, comp in enumerate(self.address.components):
                 d.comp_fermion[c] = 1 if isinstance(comp, FermiFS) else 0
                 d.comp_particles[c] = comp.N
                 d.comp_t[c] = self.t[c]
-            d.comp_u[0], d.comp_u[1], d.comp_u[2] = self.u[0, 0], self.u[0, 1], self.u[1, 1]
+            # the upper triangle of u, row by row
+            upper = [self.u[i, j] for i in range(self.ncomp) for j in range(i, self.ncomp)]
+            for i, x in enumerate(upper):
+                d.comp_u[i] = float(x)
         if self.potential is not None:
             arr = np.ascontiguousarray(self.potential)
             self._keep.append(arr)

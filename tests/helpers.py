@@ -22,8 +22,8 @@ def oracle_model(h):
     g = h.geometry
     if isinstance(h.address, R.CompositeFS):
         comps = tuple((isinstance(c, R.FermiFS), c.N) for c in h.address.components)
-        pot = None if h.potential is None else np.asarray(h.potential).reshape(2, h.M)
-        return O.realspace2(comps, g.dims, t=h.t, u=h.u, periodic=g.fold, pot=pot)
+        pot = None if h.potential is None else np.asarray(h.potential).reshape(len(comps), h.M)
+        return O.realspace_multi(comps, g.dims, t=h.t, u=h.u, periodic=g.fold, pot=pot)
     return O.realspace(h.N, g.dims, u=h.u, t=h.t, periodic=g.fold,
                        fermion=isinstance(h.address, R.FermiFS), pot=h.potential)
 

@@ -1,6 +1,7 @@
-"""Two-component addresses on the GPU against the oracle, bit for bit: matrix elements of
-HubbardRealSpace with a CompositeFS (bosons and fermions, hard-wall and periodic, trap) and of
-HubbardMom1D with FermiFS2C over whole bases, and step trajectories of the three styles."""
+"""Multi-component addresses on the GPU against the oracle, bit for bit: matrix elements of
+HubbardRealSpace with a CompositeFS of two, three and four components (bosons and fermions,
+hard-wall and periodic, trap, interactions of both signs) and of HubbardMom1D with FermiFS2C
+over whole bases, and step trajectories of the three styles."""
 import numpy as np
 import pytest
 
@@ -23,6 +24,23 @@ MODELS = {
     "realspace-fermi-fermi-2d": lambda: R.HubbardRealSpace(
         R.CompositeFS(R.FermiFS((1, 1, 0, 0, 0, 0, 0, 0, 0)), R.FermiFS((0, 0, 0, 1, 1, 0, 0, 0, 0))),
         geometry=R.PeriodicBoundaries(3, 3), t=[1.0, 2.0], u=[[0.0, 4.0], [4.0, 0.0]]),
+    # three and four components (one 64-bit key, the last component lowest)
+    "realspace-3c-trap": lambda: R.HubbardRealSpace(
+        R.CompositeFS(R.BoseFS((1, 0, 1, 0, 0, 0)), R.FermiFS((0, 1, 0, 1, 0, 0)),
+                      R.BoseFS((0, 0, 0, 0, 2, 0))),
+        geometry=R.CubicGrid((2, 3), (False, True)), t=[1.0, 0.5, 2.0],
+        u=[[1.5, 2.0, 0.5], [2.0, 0.0, -1.0], [0.5, -1.0, 3.0]],
+        v=[[0.5, 0.25], [1.0, 2.0], [0.0, 0.5]]),
+    "realspace-4c": lambda: R.HubbardRealSpace(
+        R.CompositeFS(R.BoseFS((2, 0, 0)), R.FermiFS((1, 0, 1)), R.BoseFS((0, 2, 0)),
+                      R.BoseFS((1, 0, 0))),
+        t=[1.0, 2.0, 0.5, 1.0],
+        u=[[1.0, 2.0, 0.0, -1.0], [2.0, 0.0, 1.5, 0.5], [0.0, 1.5, 2.0, 1.0], [-1.0, 0.5, 1.0, 0.25]]),
+    "realspace-3f-2d": lambda: R.HubbardRealSpace(
+        R.CompositeFS(R.FermiFS((1, 1, 0, 0, 0, 0, 0, 0, 0)), R.FermiFS((0, 0, 0, 1, 1, 0, 0, 0, 0)),
+                      R.FermiFS((0, 0, 0, 0, 0, 0, 0, 0, 1))),
+        geometry=R.PeriodicBoundaries(3, 3), t=[1.0, 2.0, 1.5],
+        u=[[0.0, 4.0, 1.0], [4.0, 0.0, -2.0], [1.0, -2.0, 0.0]]),
     "mom1d-fermi2c": lambda: R.HubbardMom1D(R.FermiFS2C((0, 1, 1, 1, 0, 0), (0, 0, 1, 1, 0, 0)), u=3.0),
     "mom1d-fermi2c-odd": lambda: R.HubbardMom1D(R.FermiFS2C((0, 0, 1, 1, 0, 0, 0), (0, 1, 1, 1, 0, 0, 0)),
                                                 u=-2.0, t=0.5),
@@ -54,6 +72,9 @@ CASES = [
     ("int-mom2c", "mom1d-fermi2c", R.IsStochasticInteger, 300, 25, 0.01),
     ("dss-mom2c", "mom1d-fermi2c-odd", R.IsDynamicSemistochastic, 300.0, 30, 0.01),
     ("det-mom2c", "mom1d-fermi2c", R.IsDeterministic, 1.0, 6, 0.02),
+    ("int-realspace3", "realspace-3c-trap", R.IsStochasticInteger, 300, 25, 0.01),
+    ("dss-realspace4", "realspace-4c", R.IsDynamicSemistochastic, 400.0, 30, 0.01),
+    ("det-realspace3f", "realspace-3f-2d", R.IsDeterministic, 1.0, 6, 0.02),
 ]
 
 

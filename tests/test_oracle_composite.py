@@ -104,3 +104,71 @@ def test_fermi2c_constructors_agree():
     f3 = R.FermiFS2C(3, [(1, 1), (2, -1), (3, -1)])
     assert f1 == f2 == f3
     assert R.FermiFS2C(3, {1: 1}).N == 1 and R.FermiFS2C(3, {1: -1}).N == 1
+
+
+# ---- three and four components --------------------------------------------------------------
+def test_three_noninteracting_fermion_components_add_up():
+    """test/Hamiltonians.jl:365-377 with a third component: FermiFS((1,1,1,0,0,0)) with t = 3.5
+    alone has E0 = -14 (:366-369), so the three components without interaction have
+    -3 + -6 + -14."""
+    m = O.realspace_multi(((True, 4), (True, 2), (True, 3)), (6,), t=(1.0, 2.0, 3.5),
+                          u=np.zeros((3, 3)))
+    assert len(O.basis(m)) == 15 * 15 * 20
+    assert O.ground_energy(m) == pytest.approx(-3 - 6 - 14, rel=1e-10)
+
+
+def test_four_component_offdiagonals_reach_the_whole_basis():
+    """test/ExactDiagonalization.jl:152-163: for HubbardRealSpace(CompositeFS(BoseFS(2,0,0),
+    FermiFS(1,0,1), BoseFS(0,2,0), BoseFS(1,0,0))) the basis built by following the
+    Hamiltonian's offdiagonals equals the address type's basis (product of the component
+    bases, in key order)."""
+    addr = R.CompositeFS(R.BoseFS((2, 0, 0)), R.FermiFS((1, 0, 1)), R.BoseFS((0, 2, 0)),
+                         R.BoseFS((1, 0, 0)))
+    m = O.realspace_multi(((False, 2), (True, 2), (False, 2), (False, 1)), (3,))
+    assert m.nbits == addr.nbits == 14
+    keys = O.basis(m)
+    assert len(keys) == 6 * 3 * 6 * 3 and addr.key in set(int(k) for k in keys)
+    assert np.array_equal(O.connected_basis(m, addr.key), keys)
+
+
+@pytest.mark.parametrize("perm", [(1, 2, 0), (2, 0, 1), (0, 2, 1)])
+def test_component_order_does_not_change_the_energy(perm):
+    """The pattern of test/Hamiltonians.jl:326-362 for three components (bosons and a
+    fermion, hopping and interactions all different): listing the components in another order,
+    with t and the rows and columns of u permuted alike, gives the same ground-state energy."""
+    comps = ((False, 2), (True, 1), (False, 1))
+    t = np.array([1.0, 4.0, 2.0])
+    u = np.array([[2.0, 3.0, 1.0], [3.0, 0.0, 0.5], [1.0, 0.5, 4.0]])
+    e0 = O.ground_energy(O.realspace_multi(comps, (5,), t=t, u=u))
+    p = list(perm)
+    e1 = O.ground_energy(O.realspace_multi(tuple(comps[i] for i in p), (5,), t=t[p],
+                                           u=u[np.ix_(p, p)]))
+    assert e1 == pytest.approx(e0, rel=1e-10)
+
+
+def test_multi_component_diagonal_follows_the_reference_recursion():
+    """The diagonal element of a CompositeFS is local_interaction's recursion over the
+    components plus the trap (HubbardRealSpace.jl:18-61, 100-107, 284-287): for integer
+    occupations every term is exact, so the value equals the closed form
+    sum_s u[s,s]/2 sum_i n_si(n_si - 1) (bosons) + sum_{s<j} u[s,j] sum_i n_si n_ji + trap."""
+    comps = ((False, 3), (True, 2), (False, 2), (True, 1))
+    u = np.array([[1.5, 2.0, 0.5, -1.0], [2.0, 0.0, 1.0, 0.25], [0.5, 1.0, 3.0, 2.0],
+                  [-1.0, 0.25, 2.0, 0.0]])
+    x = np.arange(4) - 2
+    pot = np.array([[0.5 * xx * xx for xx in x], [0.0] * 4, [0.25 * xx * xx for xx in x],
+                    [1.0 * xx * xx for xx in x]])
+    m = O.realspace_multi(comps, (4,), t=(1.0, 0.5, 2.0, 1.0), u=u, pot=pot)
+    rng = np.random.default_rng(5)
+    keys = O.basis(m)
+    for k in rng.choice(keys, 60, replace=False):
+        addr = R.CompositeFS(R.BoseFS((3, 0, 0, 0)), R.FermiFS((1, 1, 0, 0)),
+                             R.BoseFS((2, 0, 0, 0)), R.FermiFS((1, 0, 0, 0))).with_key(int(k))
+        occ = [np.array(c.onr()) for c in addr.components]
+        want = 0.0
+        for s in range(4):
+            if not comps[s][0]:
+                want += u[s, s] * np.sum(occ[s] * (occ[s] - 1)) / 2
+            for j in range(s + 1, 4):
+                want += u[s, j] * np.sum(occ[s] * occ[j])
+            want += np.sum(occ[s] * pot[s])
+        assert O.diagonal(m, int(k)) == pytest.approx(want, abs=1e-12)

@@ -68,10 +68,11 @@ typedef struct rimu_wm rimu_wm;
  *
  * Multi-component addresses (CompositeFS, multicomponent.jl:10-30, and its alias FermiFS2C,
  * :87-103): n_components = C in 2..RIMU_MAX_COMPONENTS, each component a BoseFS or FermiFS
- * with the same n_modes, all in one 64-bit key: component C in the low comp_bits(C) bits,
- * component C-1 above it, ..., component 1 in the highest bits, so that unsigned key order is
- * the reference's order of the component tuple (multicomponent.jl:79).  The widths must add
- * up to at most 64 bits.  Supported for HubbardRealSpace (CompositeFS of BoseFS/FermiFS
+ * with the same n_modes (at most 64), all in one key: component C in the low comp_bits(C)
+ * bits, component C-1 above it, ..., component 1 in the highest bits, so that unsigned key
+ * order is the reference's order of the component tuple (multicomponent.jl:79).  Each
+ * component takes at most 64 bits; up to 64 bits in all the key is one word, up to 128 a
+ * (lo, hi) pair as above.  Supported for HubbardRealSpace (CompositeFS of BoseFS/FermiFS
  * components, HubbardRealSpace.jl:18-61, 100-107, 344-391) and, with C = 2, HubbardMom1D
  * (FermiFS2C, HubbardMom1D.jl:141-205). */
 #define RIMU_MAX_COMPONENTS 4

@@ -190,8 +190,12 @@ extern "C" int rimu_model_create(rimu_ctx *ctx, const rimu_model_desc *d, rimu_m
       return bad("rimu_model_create: n_particles must be the sum over the components");
   }
   if (nbits > 128) return bad("rimu_model_create: address does not fit 128 bits");
-  if ((nbits > 64 || d->n_modes > 64) && two)
-    return bad("rimu_model_create: multi-component addresses must fit 64 bits");
+  if (two) {
+    // a multi-component address takes one or two words, each component at most one word
+    if (d->n_modes > 64) return bad("rimu_model_create: multi-component addresses take at most 64 modes");
+    for (int c = 0; c < C; ++c)
+      if (cbits[c] > 64) return bad("rimu_model_create: a component of more than 64 bits");
+  }
   if (d->n_modes > 64 && d->kind == RIMU_MODEL_MOM1D)
     return bad("rimu_model_create: HubbardMom1D takes at most 64 modes");
   if (d->fermion && d->kind != RIMU_MODEL_REALSPACE)
@@ -366,6 +370,7 @@ extern "C" int rimu_model_diagonal(rimu_model *m, const uint64_t *keys, int64_t 
 
 static int host_num_offdiagonals(const rimu_model *m, uint64_t key, uint64_t key_hi = 0) {
   const DevModel &h = m->dm;
+  if (h.kind == MODEL_MOM1D && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
   if (h.nbits > 64 && h.kind == MODEL_MOM1D) {
     MomMap mm;
     mom_map(k128(key, key_hi), mm);

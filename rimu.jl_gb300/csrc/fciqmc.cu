@@ -37,11 +37,13 @@ __device__ __noinline__ double ratio_to_threshold(double x, double y) { return x
 template <int KIND, class K>
 __device__ __forceinline__ int column_noff(const DevModel &h, K key) {
   if constexpr (KIND == MODEL_MOM1D) {
-    // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144); one-word keys only
-    if (KT<K>::BITS == 64 && h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
+    // FermiFS2C: N1 * N2 * (M - 1) (HubbardMom1D.jl:141-144)
+    if (h.ncomp == 2) return h.cN[0] * h.cN[1] * (h.M - 1);
     MomMap m;
     mom_map(key, m);
     return num_offdiagonals_mom(h, m);
+  } else if constexpr (KIND == MODEL_REAL1D) {
+    return 2 * bose_num_occupied(key);       // HubbardReal1D.jl:51-53 (one BoseFS)
   }
   return num_offdiagonals_real(h, key);
 }
@@ -53,9 +55,7 @@ __device__ __forceinline__ OffdiagT<K> column_offdiag(const DevModel &h, K key, 
   } else if constexpr (KIND == MODEL_REALSPACE) {
     return realspace_offdiag(h, key, chosen);
   } else {
-    if constexpr (KT<K>::BITS == 64) {
-      if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
-    }
+    if (h.ncomp == 2) return mom2c_offdiag(h, key, chosen);
     MomMap m;
     mom_map(key, m);
     return mom1d_offdiag(h, key, m, chosen);
@@ -105,14 +105,72 @@ __device__ __forceinline__ double fermi_kinetic(uint64_t ck, const double *kes) 
   return kin;
 }
 
-// Hamiltonian diagonal computed per address (HubbardRealSpace with trap, HubbardMom1D).
+// FermiFS2C diagonal (one- or two-word address).
+template <class K>
+__device__ double mom2c_diagonal(const DevModel &h, K key) {
+  // FermiFS2C: dot(kes, map_a) + dot(kes, map_b) + u/(2M) * 2 n_a n_b
+  // (HubbardMom1D.jl:168-171, 182-187; excitations.jl:172-180)
+  const uint64_t ka = component_of(h, key, 0), kb = component_of(h, key, 1);
+  const long long nab = 2LL * popc64(ka) * popc64(kb);
+  return fermi_kinetic(ka, h.kes) + fermi_kinetic(kb, h.kes) + h.u / (2 * h.M) * (double)nab;
+}
+
+// Multi-component HubbardRealSpace diagonal (one- or two-word address).
+template <class K>
+__device__ double composite_diagonal(const DevModel &h, K key) {
+  // local_interaction of the components with the u matrix, then the trap
+  // (HubbardRealSpace.jl:18-61, 100-107, 284-287), in the reference's order of operations:
+  // _interactions((a_s, ...)) = (self_s + row_s) + _interactions((a_{s+1}, ...)), ending in
+  // 0.0; row_s = li(a_s, a_{s+1}) + (li(a_s, a_{s+2}) + (... + 0)), ending in the integer 0;
+  // the self-interaction of a FermiFS is the integer 0.  Adding an integer 0 to a double is
+  // "+ 0.0" (it turns -0.0 into +0.0); integer + integer stays the integer 0.
+  const int C = h.ncomp;
+  double in = 0.0;
+  if (h.u_nonzero) {
+    double rest = 0.0;                         // _interactions of the empty tuple: 0.0
+    for (int s = C - 1; s >= 0; --s) {
+      const uint64_t ks = component_of(h, key, s);
+      double row = 0.0;
+      bool row_int = true;                     // the integer 0 closing _interaction_col
+      for (int j = C - 1; j > s; --j) {
+        const double li = h.cu[cu_index(C, s, j)] *
+                          (double)component_overlap(h, ks, h.cferm[s], component_of(h, key, j),
+                                                    h.cferm[j]);
+        row = row_int ? li + 0.0 : li + row;
+        row_int = false;
+      }
+      double first;
+      bool first_int;
+      if (h.cferm[s]) {                        // self + row with self the integer 0
+        first = row_int ? 0.0 : row + 0.0;
+        first_int = row_int;
+      } else {
+        const double self = h.cu[cu_index(C, s, s)] * (double)bose_interaction(ks) / 2;
+        first = row_int ? self + 0.0 : self + row;
+        first_int = false;
+      }
+      rest = first_int ? rest + 0.0 : first + rest;
+    }
+    in = rest;
+  }
+  double pe = 0.0;
+  if (h.pot) {
+    for (int c = 0; c < C; ++c)
+      pe += component_potential(component_of(h, key, c), h.cferm[c], h.pot + c * h.M);
+  }
+  return in + pe;
+}
+
 template <int KIND>
 __device__ double model_diagonal64(const DevModel &h, uint64_t key);
 
+// Hamiltonian diagonal computed per address (HubbardRealSpace with trap, HubbardMom1D).
 template <int KIND, class K>
 __device__ double model_diagonal(const DevModel &h, K key) {
   if constexpr (KT<K>::BITS == 64) return model_diagonal64<KIND>(h, key);
   else if constexpr (KIND == MODEL_REAL1D) return h.u * (double)bose_interaction(key) / 2;
+  else if (KIND == MODEL_MOM1D && h.ncomp == 2) return mom2c_diagonal(h, key);
+  else if (KIND == MODEL_REALSPACE && h.ncomp >= 2) return composite_diagonal(h, key);
   else if constexpr (KIND == MODEL_MOM1D) {
     // dot(h.kes, map) + u/(2M) * momentum_transfer_diagonal(map) (HubbardMom1D.jl:174-177),
     // the same arithmetic as on one-word addresses
@@ -146,56 +204,8 @@ __device__ double model_diagonal(const DevModel &h, K key) {
 // The same for 64-bit addresses, with the momentum-space and two-component models.
 template <int KIND>
 __device__ double model_diagonal64(const DevModel &h, uint64_t key) {
-  if (KIND == MODEL_MOM1D && h.ncomp == 2) {
-    // FermiFS2C: dot(kes, map_a) + dot(kes, map_b) + u/(2M) * 2 n_a n_b
-    // (HubbardMom1D.jl:168-171, 182-187; excitations.jl:172-180)
-    const uint64_t ka = component_of(h, key, 0), kb = component_of(h, key, 1);
-    const long long nab = 2LL * popc64(ka) * popc64(kb);
-    return fermi_kinetic(ka, h.kes) + fermi_kinetic(kb, h.kes) + h.u / (2 * h.M) * (double)nab;
-  }
-  if (KIND == MODEL_REALSPACE && h.ncomp >= 2) {
-    // local_interaction of the components with the u matrix, then the trap
-    // (HubbardRealSpace.jl:18-61, 100-107, 284-287), in the reference's order of operations:
-    // _interactions((a_s, ...)) = (self_s + row_s) + _interactions((a_{s+1}, ...)), ending in
-    // 0.0; row_s = li(a_s, a_{s+1}) + (li(a_s, a_{s+2}) + (... + 0)), ending in the integer 0;
-    // the self-interaction of a FermiFS is the integer 0.  Adding an integer 0 to a double is
-    // "+ 0.0" (it turns -0.0 into +0.0); integer + integer stays the integer 0.
-    const int C = h.ncomp;
-    double in = 0.0;
-    if (h.u_nonzero) {
-      double rest = 0.0;                         // _interactions of the empty tuple: 0.0
-      for (int s = C - 1; s >= 0; --s) {
-        const uint64_t ks = component_of(h, key, s);
-        double row = 0.0;
-        bool row_int = true;                     // the integer 0 closing _interaction_col
-        for (int j = C - 1; j > s; --j) {
-          const double li = h.cu[cu_index(C, s, j)] *
-                            (double)component_overlap(h, ks, h.cferm[s], component_of(h, key, j),
-                                                      h.cferm[j]);
-          row = row_int ? li + 0.0 : li + row;
-          row_int = false;
-        }
-        double first;
-        bool first_int;
-        if (h.cferm[s]) {                        // self + row with self the integer 0
-          first = row_int ? 0.0 : row + 0.0;
-          first_int = row_int;
-        } else {
-          const double self = h.cu[cu_index(C, s, s)] * (double)bose_interaction(ks) / 2;
-          first = row_int ? self + 0.0 : self + row;
-          first_int = false;
-        }
-        rest = first_int ? rest + 0.0 : first + rest;
-      }
-      in = rest;
-    }
-    double pe = 0.0;
-    if (h.pot) {
-      for (int c = 0; c < C; ++c)
-        pe += component_potential(component_of(h, key, c), h.cferm[c], h.pot + c * h.M);
-    }
-    return in + pe;
-  }
+  if (KIND == MODEL_MOM1D && h.ncomp == 2) return mom2c_diagonal(h, key);
+  if (KIND == MODEL_REALSPACE && h.ncomp >= 2) return composite_diagonal(h, key);
   if (KIND == MODEL_MOM1D) {
     // dot(h.kes, map) + u/(2M) * momentum_transfer_diagonal(map)  (HubbardMom1D.jl:174-177)
     uint64_t x = key;

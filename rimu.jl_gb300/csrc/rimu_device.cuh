@@ -476,6 +476,15 @@ RIMU_HD int num_offdiagonals_real(const DevModel &h, K key) {
       }
       return s * 2 * h.ndim;
     }
+  } else {
+    if (h.ncomp >= 2) {   // the same on a two-word address (each component one word)
+      int s = 0;
+      for (int c = 0; c < h.ncomp; ++c) {
+        const uint64_t kc = kshr(key, h.coff[c]).lo & lowmask(h.cbits[c]);
+        s += h.cferm[c] ? popc64(kc) : bose_num_occupied(kc);
+      }
+      return s * 2 * h.ndim;
+    }
   }
   int s = h.fermion ? kpopc(key) : bose_num_occupied(key);
   return h.kind == MODEL_REAL1D ? 2 * s : s * 2 * h.ndim;
@@ -646,12 +655,20 @@ RIMU_HD OffdiagT<K> realspace_hop(const DevModel &h, K key, int chosen, bool fer
 }
 
 // ---- two-component addresses -------------------------------------------------------------
+// A component has at most 64 bits; a multi-component address has one or two words.
 RIMU_HD uint64_t component_of(const DevModel &h, uint64_t key, int c) {
   return shr64(key, h.coff[c]) & lowmask(h.cbits[c]);
 }
 RIMU_HD uint64_t with_component(const DevModel &h, uint64_t key, int c, uint64_t ck) {
   const uint64_t m = shl64(lowmask(h.cbits[c]), h.coff[c]);
   return (key & ~m) | shl64(ck, h.coff[c]);
+}
+RIMU_HD uint64_t component_of(const DevModel &h, Key128 key, int c) {
+  return kshr(key, h.coff[c]).lo & lowmask(h.cbits[c]);
+}
+RIMU_HD Key128 with_component(const DevModel &h, Key128 key, int c, uint64_t ck) {
+  const Key128 m = kshl(k128(lowmask(h.cbits[c]), 0), h.coff[c]);
+  return (key & ~m) | kshl(k128(ck, 0), h.coff[c]);
 }
 // Position of u[i, j] (i <= j, 0-based) in the upper triangle of a C x C matrix, row by row.
 RIMU_HD int cu_index(int C, int i, int j) { return i * C - i * (i - 1) / 2 + (j - i); }
@@ -692,23 +709,22 @@ RIMU_HD int component_overlap(const DevModel &h, uint64_t a, int fa, uint64_t b,
 // own t (table block c).
 template <class K>
 RIMU_HD OffdiagT<K> realspace_offdiag(const DevModel &h, K key, int chosen) {
-  if constexpr (KT<K>::BITS == 64) {
-    if (h.ncomp >= 2) {
-      int c = 0;
-      uint64_t kc = component_of(h, key, 0);
-      for (;;) {
-        const int nc = component_occupied(kc, h.cferm[c]) * 2 * h.ndim;
-        if (chosen <= nc || c + 1 == h.ncomp) break;
-        chosen -= nc;
-        ++c;
-        kc = component_of(h, key, c);
-      }
-      Offdiag r = realspace_hop(h, kc, chosen, h.cferm[c] != 0);
-      if (r.prod == 0) { r.key = key; return r; }
-      r.key = with_component(h, key, c, r.key);
-      r.prod += c * h.cstride;
-      return r;
+  if (h.ncomp >= 2) {
+    int c = 0;
+    uint64_t kc = component_of(h, key, 0);
+    for (;;) {
+      const int nc = component_occupied(kc, h.cferm[c]) * 2 * h.ndim;
+      if (chosen <= nc || c + 1 == h.ncomp) break;
+      chosen -= nc;
+      ++c;
+      kc = component_of(h, key, c);
     }
+    const Offdiag r = realspace_hop(h, kc, chosen, h.cferm[c] != 0);
+    OffdiagT<K> out{key, r.prod, r.sign};
+    if (r.prod == 0) return out;
+    out.key = with_component(h, key, c, r.key);
+    out.prod += c * h.cstride;
+    return out;
   }
   return realspace_hop(h, key, chosen, h.fermion != 0);
 }
@@ -716,14 +732,15 @@ RIMU_HD OffdiagT<K> realspace_offdiag(const DevModel &h, K key, int chosen) {
 // HubbardMom1D with FermiFS2C: momentum_transfer_excitation of two components with fold=true
 // (excitations.jl:82-119) and element u/M * (sign_a * sign_b) (HubbardMom1D.jl:196-205).  The
 // magnitude u/M = u/(2M) * sqrt(4) is entry 4 of the u/(2M) sqrt(p) table (exact: scaling by 2).
-RIMU_HD Offdiag mom2c_offdiag(const DevModel &h, uint64_t key, int chosen) {
+template <class K>
+RIMU_HD OffdiagT<K> mom2c_offdiag(const DevModel &h, K key, int chosen) {
   const int M = h.M, nb = h.cN[1];
   const uint64_t ka = component_of(h, key, 0), kb = component_of(h, key, 1);
   const int per_a = (M - 1) * nb;
   const int src_a = (chosen - 1) / per_a + 1, rem = (chosen - 1) % per_a + 1;
   int dst_a = (rem - 1) / nb + 1;
   const int src_b = (rem - 1) % nb + 1;
-  Offdiag r{key, 0, 1};
+  OffdiagT<K> r{key, 0, 1};
   if (src_a > popc64(ka) || src_b > popc64(kb)) return r;
   const int sa = select_bit(ka, src_a - 1) + 1, sb = select_bit(kb, src_b - 1) + 1;
   if (dst_a >= sa) dst_a += 1;               // skip the source mode
@@ -732,7 +749,7 @@ RIMU_HD Offdiag mom2c_offdiag(const DevModel &h, uint64_t key, int chosen) {
   uint64_t na, nbk;
   int ga, gb;
   if (!fermi_move(ka, sa, dst_a, na, ga) || !fermi_move(kb, sb, dst_b, nbk, gb)) return r;
-  r.key = shl64(na, h.coff[0]) | nbk;
+  r.key = with_component(h, with_component(h, key, 0, na), 1, nbk);
   r.prod = 4;
   r.sign = ga * gb;
   return r;

@@ -168,9 +168,9 @@ def near_uniform(kind, N: int, M: int):
 @total_ordering
 class CompositeFS:
     """CompositeFS(a, b, ...) of two to four single-component addresses with the same number
-    of modes (multicomponent.jl:10-30).  One 64-bit key: the last component in the low bits,
-    the one before it above them, and so on, so that key order is the order of the component
-    tuple."""
+    of modes (multicomponent.jl:10-30).  One key of up to 128 bits (each component at most 64):
+    the last component in the low bits, the one before it above them, and so on, so that key
+    order is the order of the component tuple."""
 
     __slots__ = ("components", "N", "M", "key")
     fermion = False
@@ -182,8 +182,9 @@ class CompositeFS:
             raise TypeError("CompositeFS components must be BoseFS or FermiFS")
         if any(c.M != components[0].M for c in components):
             raise ValueError("all addresses must have the same number of modes")
-        if sum(c.nbits for c in components) > 64:
-            raise ValueError("CompositeFS wider than 64 bits is not supported")
+        if sum(c.nbits for c in components) > 128 or any(c.nbits > 64 for c in components):
+            raise ValueError("CompositeFS wider than 128 bits, or with a component wider than "
+                             "64 bits, is not supported")
         self.components = tuple(components)
         self.N, self.M = sum(c.N for c in components), components[0].M
         key = 0

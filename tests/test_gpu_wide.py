@@ -193,3 +193,70 @@ def test_wide_step_with_many_buckets_per_cta(name, style):
     o = O.step(m, oracle_params(style, 0.005, -1.0, SEED, 6), keys, vals)
     assert_same_step(g, o, style)
     assert g[2]["nb_bits"] >= 11
+
+
+# ---- multi-component addresses of 65-128 bits (each component at most one word) -------------
+def _wide_composites():
+    f36a = [0] * 36
+    f36b = [0] * 36
+    for i in (0, 7, 14):
+        f36a[i] = 1
+    for i in (3, 10, 21):
+        f36b[i] = 1
+    b30 = [0] * 30
+    b30[4] = 2
+    f30 = [0] * 30
+    for i in (1, 2, 17):
+        f30[i] = 1
+    c30 = [0] * 30
+    c30[25] = 1
+    ma = [0] * 40
+    mb = [0] * 40
+    for i in (18, 19, 20):
+        ma[i] = 1
+    for i in (19, 20, 21):
+        mb[i] = 1
+    return {
+        "realspace-2f-6x6": R.HubbardRealSpace(R.CompositeFS(R.FermiFS(f36a), R.FermiFS(f36b)),
+                                               geometry=R.PeriodicBoundaries(6, 6), t=[1.0, 1.5],
+                                               u=[[0.0, 4.0], [4.0, 0.0]]),
+        "realspace-3c-5x6-trap": R.HubbardRealSpace(
+            R.CompositeFS(R.BoseFS(b30), R.FermiFS(f30), R.BoseFS(c30)),
+            geometry=R.HardwallBoundaries(5, 6), t=[1.0, 0.5, 2.0],
+            u=[[2.0, 1.0, -0.5], [1.0, 0.0, 3.0], [-0.5, 3.0, 1.0]],
+            v=[[0.5, 0.25], [0.0, 1.0], [1.0, 0.0]]),
+        "mom1d-fermi2c-40": R.HubbardMom1D(R.FermiFS2C(ma, mb), u=3.0, t=0.5),
+    }
+
+
+@pytest.mark.parametrize("name", list(_wide_composites()))
+def test_wide_composite_matrix_elements_match_oracle(name):
+    h = _wide_composites()[name]
+    m = oracle_model(h)
+    assert h.address.nbits > 64 and m.nbits == h.address.nbits
+    keys = _neighbourhood(m, h.address.key, depth=2, cap=400)
+    got = h.diagonal_elements(keys)
+    want = np.array([O.diagonal(m, k) for k in keys])
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    for k in keys[:: max(1, len(keys) // 60)]:
+        gk, gv = h.offdiagonal_keys(k)
+        ref = O.offdiagonals(m, k)
+        assert [int(x) for x in gk] == [r[0] for r in ref]
+        assert np.array_equal(np.asarray(gv).view(np.uint64),
+                              np.array([r[1] for r in ref]).view(np.uint64))
+
+
+WIDE_COMPOSITE_CASES = [
+    ("dss-realspace-2f-6x6", "realspace-2f-6x6", R.IsDynamicSemistochastic, 300.0, 20, 0.005),
+    ("int-realspace-3c-5x6", "realspace-3c-5x6-trap", R.IsStochasticInteger, 300, 20, 0.005),
+    ("det-mom1d-fermi2c-40", "mom1d-fermi2c-40", R.IsDeterministic, 1.0, 3, 0.01),
+    ("dss-mom1d-fermi2c-40", "mom1d-fermi2c-40", R.IsDynamicSemistochastic, 300.0, 12, 0.005),
+]
+
+
+@pytest.mark.parametrize("case,model,style,pop,steps,dt", WIDE_COMPOSITE_CASES,
+                         ids=[c[0] for c in WIDE_COMPOSITE_CASES])
+def test_wide_composite_trajectory_matches_oracle(case, model, style, pop, steps, dt):
+    h = _wide_composites()[model]
+    target = None if style is R.IsDeterministic else pop
+    run_trajectory(h, style(), {h.address: pop}, steps, dt, target=target)

@@ -172,3 +172,19 @@ def test_multi_component_diagonal_follows_the_reference_recursion():
                 want += u[s, j] * np.sum(occ[s] * occ[j])
             want += np.sum(occ[s] * pot[s])
         assert O.diagonal(m, int(k)) == pytest.approx(want, abs=1e-12)
+
+
+def test_composite_key_layout_up_to_128_bits():
+    """The host CompositeFS: each component above the bits of the ones after it, keys of up to
+    128 bits (each component at most 64), with_key inverting the packing; wider layouts are
+    refused."""
+    a, b, c = R.BoseFS([0, 0, 0, 0, 2] + [0] * 25), R.FermiFS([1, 1] + [0] * 28), R.BoseFS([1] + [0] * 29)
+    comp = R.CompositeFS(a, b, c)
+    assert comp.nbits == 31 + 30 + 30 == 91
+    assert comp.key == (a.key << 60) | (b.key << 30) | c.key
+    back = comp.with_key(comp.key)
+    assert back == comp and [x.key for x in back.components] == [a.key, b.key, c.key]
+    with pytest.raises(ValueError):
+        R.CompositeFS(R.BoseFS([1] * 40), R.BoseFS([1] * 40))          # a 79-bit component
+    with pytest.raises(ValueError):
+        R.CompositeFS(R.FermiFS([1] + [0] * 63), R.FermiFS([1] + [0] * 63), R.FermiFS([1] + [0] * 63))

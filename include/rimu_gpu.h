@@ -212,6 +212,11 @@ int rimu_wm_destroy(rimu_wm *wm);
  * n = 0 removes the projector. */
 int rimu_wm_set_projector(rimu_wm *wm, const uint64_t *keys, const double *pvals,
                           const double *hpvals, int n);
+/* The same for models with addresses of 65-128 bits: keys2 holds n (lo, hi) pairs, sorted by
+ * (hi, lo) and distinct.  A working memory steps two-word vectors only with such a projector
+ * (or none), one-word vectors only with the plain form. */
+int rimu_wm_set_projector_w(rimu_wm *wm, const uint64_t *keys2, const double *pvals,
+                            const double *hpvals, int n);
 
 /* Per-kernel timing of the steps run with this working memory (CUDA events on the context
  * stream; the reference times steps with its Timer post-step strategy and communicator

@@ -734,28 +734,44 @@ extern "C" int rimu_wm_timing(rimu_wm *w, double *out7) {
   return RIMU_OK;
 }
 
-extern "C" int rimu_wm_set_projector(rimu_wm *w, const uint64_t *keys, const double *pvals,
-                                     const double *hpvals, int n) {
+// Projector of kw-word addresses (keys: n addresses, kw words each, (lo, hi) for kw = 2).
+static int wm_set_projector(rimu_wm *w, const uint64_t *keys, const double *pvals,
+                            const double *hpvals, int n, int kw) {
   if (!w || n < 0 || (n > 0 && (!keys || !pvals || !hpvals))) return bad("rimu_wm_set_projector: bad argument");
   rimu_ctx *ctx = w->ctx;
-  for (int i = 1; i < n; ++i)
-    if (keys[i] <= keys[i - 1]) return bad("rimu_wm_set_projector: keys must be sorted and distinct");
+  for (int i = 1; i < n; ++i) {
+    const bool up = kw == 1 ? keys[i] > keys[i - 1]
+                            : (keys[2 * i + 1] > keys[2 * i - 1] ||
+                               (keys[2 * i + 1] == keys[2 * i - 1] && keys[2 * i] > keys[2 * i - 2]));
+    if (!up) return bad("rimu_wm_set_projector: keys must be sorted and distinct");
+  }
+  w->proj_kw = kw;
   dfree(ctx, w->proj_keys); dfree(ctx, w->proj_v); dfree(ctx, w->proj_h);
   dfree(ctx, w->proj_out_v); dfree(ctx, w->proj_out_h);
   if (w->h_proj_out) { cudaStreamSynchronize(ctx->stream); cudaFreeHost(w->h_proj_out); w->h_proj_out = nullptr; }
   w->nproj = n;
   if (n == 0) return RIMU_OK;
   int rc;
-  if ((rc = dalloc(ctx, &w->proj_keys, n)) || (rc = dalloc(ctx, &w->proj_v, n)) ||
+  if ((rc = dalloc(ctx, &w->proj_keys, (size_t)n * kw)) || (rc = dalloc(ctx, &w->proj_v, n)) ||
       (rc = dalloc(ctx, &w->proj_h, n)) || (rc = dalloc(ctx, &w->proj_out_v, n)) ||
       (rc = dalloc(ctx, &w->proj_out_h, n)))
     return rc;
-  if ((rc = h2d(ctx, w->proj_keys, keys, n)) || (rc = h2d(ctx, w->proj_v, pvals, n)) ||
+  if ((rc = h2d(ctx, w->proj_keys, keys, (size_t)n * kw)) || (rc = h2d(ctx, w->proj_v, pvals, n)) ||
       (rc = h2d(ctx, w->proj_h, hpvals, n)))
     return rc;
   RIMU_CUDA(cudaMallocHost((void **)&w->h_proj_out, 2 * n * sizeof(double)));
   RIMU_CUDA(cudaStreamSynchronize(ctx->stream));
   return RIMU_OK;
+}
+
+extern "C" int rimu_wm_set_projector(rimu_wm *w, const uint64_t *keys, const double *pvals,
+                                     const double *hpvals, int n) {
+  return wm_set_projector(w, keys, pvals, hpvals, n, 1);
+}
+
+extern "C" int rimu_wm_set_projector_w(rimu_wm *w, const uint64_t *keys2, const double *pvals,
+                                       const double *hpvals, int n) {
+  return wm_set_projector(w, keys2, pvals, hpvals, n, 2);
 }
 
 static int wm_ensure(rimu_wm *w, int nb_total, uint32_t caps, uint32_t heavy_cap, int ndiag,
@@ -821,8 +837,8 @@ extern "C" int rimu_apply_operator(rimu_model *m, rimu_wm *w, rimu_vec *target, 
     const int need_kw = m->dm.nbits > 64 ? 2 : 1;
     if (source->kw != need_kw)
       return bad("rimu_apply_operator: the vector's address width does not match the model's");
-    if (need_kw == 2 && w->nproj != 0)
-      return bad("rimu_apply_operator: projectors need addresses of at most 64 bits");
+    if (w->nproj != 0 && w->proj_kw != need_kw)
+      return bad("rimu_apply_operator: the projector's address width does not match the model's");
     if (target->kw != need_kw) {
       target->kw = need_kw;
       target->nb_bits = -1;                   // forces a new allocation below

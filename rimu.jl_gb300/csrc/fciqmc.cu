@@ -970,20 +970,20 @@ template <int STYLE, class K>
 __device__ __forceinline__ void account_entry(const StepArgs &a, int r, K key, double dv,
                                               AnnAcc &acc) {
   acc.len++;
-  if constexpr (KT<K>::BITS == 64) {   // projectors hold 64-bit addresses
-    if (a.nproj == 0) return;
-    const uint64_t *pk = a.proj_keys + (size_t)r * a.nproj;
-    int lo = 0, hi = a.nproj - 1;
-    while (lo <= hi) {
-      const int mid = (lo + hi) >> 1;
-      if (pk[mid] == key) {
-        const size_t o = (size_t)r * a.nproj + mid;
-        a.proj_out_v[o] = a.proj_v[o] * dv;
-        a.proj_out_h[o] = a.proj_h[o] * dv;
-        break;
-      }
-      if (pk[mid] < key) lo = mid + 1; else hi = mid - 1;
+  if (a.nproj == 0) return;
+  // the projector's addresses, sorted, in the words of K (Key128: (lo, hi) pairs)
+  const K *pk = reinterpret_cast<const K *>(a.proj_keys) + (size_t)r * a.nproj;
+  int lo = 0, hi = a.nproj - 1;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const K pm = pk[mid];
+    if (pm == key) {
+      const size_t o = (size_t)r * a.nproj + mid;
+      a.proj_out_v[o] = a.proj_v[o] * dv;
+      a.proj_out_h[o] = a.proj_h[o] * dv;
+      break;
     }
+    if (pm < key) lo = mid + 1; else hi = mid - 1;
   }
 }
 template <int STYLE, class K>

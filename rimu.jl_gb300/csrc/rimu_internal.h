@@ -169,6 +169,7 @@ struct rimu_wm {
   int table_slots = 0;                  // annihilation table slots per CTA (0: automatic)
   bool shape_set = false;               // launch shape chosen by the caller
   int ann_mode = 0;                     // RIMU_ANN_HASH or RIMU_ANN_SORT
+  int proj_kw = 1;                      // projector address words: 1, or 2 ((lo, hi) pairs)
   uint32_t *ann_list = nullptr;         // [nb_total] buckets left to the CTA annihilation
   uint32_t *ann_count = nullptr;
   // projector

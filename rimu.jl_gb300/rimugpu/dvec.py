@@ -215,16 +215,21 @@ class GPUWorkingMemory:
         self.replica = 0
         self.projector_keys = None
 
-    def set_projector(self, keys, pvals, hpvals):
-        keys = np.ascontiguousarray(keys, dtype=np.uint64)
-        o = np.argsort(keys)
-        keys, pvals, hpvals = keys[o], np.asarray(pvals, float)[o], np.asarray(hpvals, float)[o]
-        pv = np.ascontiguousarray(pvals)
-        hv = np.ascontiguousarray(hpvals)
-        _lib.check(_lib.load().rimu_wm_set_projector(
-            self.handle, _u64p(keys), pv.ctypes.data_as(C.POINTER(C.c_double)),
-            hv.ctypes.data_as(C.POINTER(C.c_double)), len(keys)))
-        self.projector_keys = keys if len(keys) else None
+    def set_projector(self, keys, pvals, hpvals, key_words=None):
+        """ProjectedEnergy projector: addresses with P and H'P values.  key_words 2 for a
+        model of 65-128-bit addresses (keys as Python ints); by default 2 when a key needs it."""
+        ik = [int(k) for k in keys]
+        kw = key_words or (2 if any(k >> 64 for k in ik) else 1)
+        o = sorted(range(len(ik)), key=lambda i: ik[i])
+        ik = [ik[i] for i in o]
+        pv = np.ascontiguousarray(np.asarray(pvals, float)[o] if len(o) else np.zeros(0))
+        hv = np.ascontiguousarray(np.asarray(hpvals, float)[o] if len(o) else np.zeros(0))
+        words = pack_keys(np.array(ik, dtype=object if kw == 2 else np.uint64), kw)
+        fn = _lib.load().rimu_wm_set_projector_w if kw == 2 else _lib.load().rimu_wm_set_projector
+        _lib.check(fn(self.handle, _u64p(words), pv.ctypes.data_as(C.POINTER(C.c_double)),
+                      hv.ctypes.data_as(C.POINTER(C.c_double)), len(ik)))
+        self.projector_keys = (np.array(ik, dtype=object if kw == 2 else np.uint64)
+                               if len(ik) else None)
 
     def set_timing(self, enable=True):
         _lib.check(_lib.load().rimu_wm_set_timing(self.handle, int(enable)))

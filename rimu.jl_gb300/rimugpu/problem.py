@@ -106,7 +106,9 @@ class ProjectedEnergy:
                     hp[int(k)] = hp.get(int(k), 0.0) + h * p
         keys = sorted(set(hp) | {a.key for a in self.projector})
         pv = {a.key: v for a, v in self.projector.items()}
-        self.keys = np.array(keys, dtype=np.uint64)
+        # addresses of 65-128 bits stay Python ints
+        self.key_words = 2 if hamiltonian.address.nbits > 64 else 1
+        self.keys = np.array(keys, dtype=object if self.key_words == 2 else np.uint64)
         self.pvals = np.array([pv.get(k, 0.0) for k in keys])
         self.hpvals = np.array([hp.get(k, 0.0) for k in keys])
 
@@ -253,7 +255,7 @@ class PMCSimulation:
             wm = GPUWorkingMemory(problem.random_seed)
             wm.replica = r
             if pe:
-                wm.set_projector(pe[0].keys, pe[0].pvals, pe[0].hpvals)
+                wm.set_projector(pe[0].keys, pe[0].pvals, pe[0].hpvals, key_words=pe[0].key_words)
             if problem.shift is None:
                 shift = self._initial_shift(H, v)
             else:

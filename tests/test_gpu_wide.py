@@ -140,14 +140,62 @@ def test_wide_dot_products():
     assert a.dot(a) == pytest.approx(float(np.sum(va * va)), rel=1e-12)
 
 
-def test_wide_addresses_reject_projectors():
+def test_wide_addresses_reject_one_word_projectors():
     h = _models()["real1d-99"]
     wm = R.GPUWorkingMemory(1)
-    wm.set_projector(np.array([1, 2], dtype=np.uint64), np.ones(2), np.ones(2))
-    with pytest.raises(R.RimuError):     # projector keys are one-word addresses
+    wm.set_projector(np.array([1, 2], dtype=np.uint64), np.ones(2), np.ones(2), key_words=1)
+    with pytest.raises(R.RimuError):     # a one-word projector with a two-word model
         R.apply_operator(wm, R.GPUDVec(style=R.IsDynamicSemistochastic(), address_type=h.address),
                          R.GPUDVec({h.address: 5.0}, style=R.IsDynamicSemistochastic()),
                          R.FirstOrderTransitionOperator(h, 0.0, 0.01))
+
+
+@pytest.mark.parametrize("name", ["real1d-99", "realspace-bose-103"])
+def test_wide_projector_terms(name):
+    """ProjectedEnergy with two-word addresses (rimu_wm_set_projector_w): after every step
+    vproj = sum_i P_i v'(k_i) and hproj = sum_i (H'P)_i v'(k_i), summed in projector-key order
+    exactly as the library does, from the downloaded vector; the vector itself matches the
+    oracle step."""
+    h = _models()[name]
+    m = oracle_model(h)
+    pe = R.ProjectedEnergy(h, {h.address: 1.0})
+    assert pe.key_words == 2 and len(pe.keys) > 5
+    style = R.IsDynamicSemistochastic()
+    keys = np.array([h.address.key], dtype=object)
+    vals = np.array([400.0])
+    S = h.diagonal_element(h.address)
+    wm = R.GPUWorkingMemory(SEED)
+    wm.set_projector(pe.keys, pe.pvals, pe.hpvals, key_words=2)
+    P = dict(zip((int(k) for k in pe.keys), pe.pvals))
+    HP = dict(zip((int(k) for k in pe.keys), pe.hpvals))
+    order = sorted(P)
+    seen = 0
+    for step in range(1, 9):
+        g = gpu_step(h, style, keys, vals, 0.005, S, SEED, step, wm=wm)
+        o = O.step(m, oracle_params(style, 0.005, S, SEED, step), keys, vals)
+        assert_same_step(g, o, style)
+        v = dict(zip((int(k) for k in g[0]), g[1]))
+        vp = hp = 0.0
+        for k in order:
+            x = v.get(k, 0.0)
+            vp += P[k] * x
+            hp += HP[k] * x
+        assert g[2]["vproj"] == vp and g[2]["hproj"] == hp
+        seen += hp != 0.0
+        keys, vals = o[0], o[1]
+    assert seen > 0
+
+
+def test_wide_projected_energy_through_solve():
+    """solve() with a ProjectedEnergy on a two-word model reports finite vproj and hproj."""
+    h = _models()["real1d-69"]
+    p = R.ProjectorMonteCarloProblem(h, style=R.IsDynamicSemistochastic(), time_step=0.005,
+                                     target_walkers=300, last_step=60, random_seed=7,
+                                     post_step_strategy=R.ProjectedEnergy(h, {h.address: 1.0}))
+    sim = R.solve(p)
+    df = sim.df
+    assert np.all(np.isfinite(df["vproj"])) and np.any(np.asarray(df["vproj"]) != 0)
+    assert np.all(np.isfinite(df["hproj"]))
 
 
 def test_wide_addresses_are_rejected_by_batches():

@@ -202,6 +202,17 @@ int rimu_vec_dot(rimu_vec *v, rimu_vec *w, double *out);
 /* dst = src with values converted to val_kind (Int64 to Float64, exact below 2^53, or a plain
  * copy): the promotion of an integer vector before dot(w, H, v) with a Float64 operator. */
 int rimu_vec_convert(rimu_vec *dst, const rimu_vec *src, int val_kind);
+/* scale!(v, alpha) (VectorInterface, abstractdvec.jl:131-140): every value times alpha; alpha
+ * = 0 empties v, alpha = 1 leaves it; values that become exact zeros are removed.  An Int64
+ * list takes integer alpha only (its products wrap as Int64 arithmetic does). */
+int rimu_vec_scale(rimu_vec *v, double alpha);
+/* add!(w, v, alpha, beta) = axpby!(alpha, v, beta, w) (abstractdvec.jl:180-208): w becomes
+ * beta*w + alpha*v address by address, computed as (beta*w_k) + (alpha*v_k) with one IEEE
+ * rounding per operation, exact zeros removed; beta = 0 empties w first.  v may be w itself
+ * (then w is scaled first, as the reference does) and may use another bucket count; an
+ * Int64 v is added to a Float64 w as Float64 values; an Int64 w takes an Int64 v and integer
+ * factors only. */
+int rimu_vec_add(rimu_vec *w, const rimu_vec *v, double alpha, double beta);
 
 /* Working memory: stands behind working_memory(v) (Interfaces/dictvectors.jl:87,
  * pdworkingmemory.jl:295). */

@@ -672,6 +672,139 @@ static int vec_regrid(rimu_vec *v, int nb_bits, uint32_t capv) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// scale! and add! (VectorInterface on AbstractDVec, src/DictVectors/abstractdvec.jl:121-188)
+// ---------------------------------------------------------------------------------------------
+// An integer list takes only integer factors (Julia would throw InexactError storing a
+// non-integer product into an Int64 list).
+static bool int_factor(double x, long long *out) {
+  if (!(std::fabs(x) <= 9007199254740992.0) || std::trunc(x) != x) return false;
+  *out = (long long)x;
+  return true;
+}
+
+extern "C" int rimu_vec_scale(rimu_vec *v, double alpha) {
+  if (!v) return bad("rimu_vec_scale: NULL vector");
+  long long ia = 0;
+  if (v->val_kind == RIMU_VAL_I64 && !int_factor(alpha, &ia))
+    return bad("rimu_vec_scale: an Int64 list takes integer factors only");
+  if (alpha == 0.0) return rimu_vec_empty(v);     // scale!(v, 0) = zerovector!(v)
+  if (alpha == 1.0) return RIMU_OK;               // scale!(v, one) leaves v as it is
+  rimu_ctx *ctx = v->ctx;
+  unsigned long long *removed = nullptr, h = 0;
+  int rc;
+  if ((rc = dalloc(ctx, &removed, 1))) return rc;
+  RIMU_CUDA(cudaMemsetAsync(removed, 0, sizeof(unsigned long long), ctx->stream));
+  rc = rimu_launch_vec_scale(ctx, v->recs, v->count, 1 << v->nb_bits, v->capv, v->val_kind, v->kw,
+                             alpha, ia, removed);
+  if (!rc) rc = d2h(ctx, &h, removed, 1);
+  if (!rc) rc = rimu_cuda_check(cudaStreamSynchronize(ctx->stream), "rimu_vec_scale");
+  dfree(ctx, removed);
+  if (rc) return rc;
+  return rimu_vec_walkernumber_and_length(v, nullptr, nullptr);
+}
+
+// w = beta*w + alpha*v for lists with the same bucket count, into new buckets of w;
+// kCrowded when a bucket of v does not fit the kernel's shared memory.
+constexpr int kCrowded = -1;
+static int vec_axpby_same_layout(rimu_vec *w, const rimu_vec *v, double alpha, double beta,
+                                 long long ia, long long ib, bool w_empty) {
+  rimu_ctx *ctx = w->ctx;
+  const int nb = 1 << w->nb_bits;
+  const int64_t lw = w_empty ? 0 : w->len;
+  uint32_t capo = std::max<uint32_t>(capv_for(lw + v->len, w->nb_bits), 64);
+  int rc;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    Rec *ro = nullptr;
+    uint32_t *co = nullptr;
+    unsigned int *flag = nullptr;
+    unsigned long long *total = nullptr;
+    if ((rc = dalloc(ctx, &ro, (size_t)nb * capo * w->kw)) || (rc = dalloc(ctx, &co, nb)) ||
+        (rc = dalloc(ctx, &flag, 1)) || (rc = dalloc(ctx, &total, 1)))
+      return rc;
+    RIMU_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
+    RIMU_CUDA(cudaMemsetAsync(total, 0, sizeof(unsigned long long), ctx->stream));
+    unsigned int hflag = 0;
+    unsigned long long htot = 0;
+    rc = rimu_launch_vec_axpby(ctx, w->recs, w->count, w->capv, v->recs, v->count, v->capv, ro, co,
+                               capo, nb, w->val_kind, w->kw, alpha, beta, ia, ib, w_empty ? 1 : 0,
+                               flag, total);
+    if (!rc) rc = d2h(ctx, &hflag, flag, 1);
+    if (!rc) rc = d2h(ctx, &htot, total, 1);
+    if (!rc) rc = rimu_cuda_check(cudaStreamSynchronize(ctx->stream), "rimu_vec_add");
+    dfree(ctx, flag);
+    dfree(ctx, total);
+    if (rc || hflag) {
+      dfree(ctx, ro);
+      dfree(ctx, co);
+      if (rc) return rc;
+      if (hflag & 1u) return kCrowded;               // the caller splits the buckets further
+      capo *= 2;
+      continue;
+    }
+    dfree(ctx, w->recs);
+    dfree(ctx, w->count);
+    w->recs = ro;
+    w->count = co;
+    w->capv = capo;
+    w->len = (int64_t)htot;
+    return RIMU_OK;
+  }
+  g_err = "rimu_vec_add: capacity overflow";
+  return RIMU_ERR_OVERFLOW;
+}
+
+extern "C" int rimu_vec_add(rimu_vec *w, const rimu_vec *v, double alpha, double beta) {
+  if (!w || !v) return bad("rimu_vec_add: NULL vector");
+  if (w->ctx != v->ctx) return bad("rimu_vec_add: vectors of different contexts");
+  if (w->kw != v->kw) return bad("rimu_vec_add: vectors of different address widths");
+  if (w->val_kind == RIMU_VAL_I64 && v->val_kind != RIMU_VAL_I64)
+    return bad("rimu_vec_add: an Int64 list cannot take Float64 values");
+  long long ia = 0, ib = 0;
+  if (w->val_kind == RIMU_VAL_I64 && (!int_factor(alpha, &ia) || !int_factor(beta, &ib)))
+    return bad("rimu_vec_add: an Int64 list takes integer factors only");
+  int rc;
+  if (w == v) {
+    // add!(w, w, alpha, beta): w is scaled first and the scaled w is what gets added
+    if ((rc = rimu_vec_scale(w, beta))) return rc;
+    rimu_vec tmp;
+    tmp.ctx = w->ctx;
+    rc = rimu_vec_copy(&tmp, w);
+    if (!rc) rc = rimu_vec_add(w, &tmp, alpha, 1.0);
+    vec_free(&tmp);
+    return rc;
+  }
+  // v as a list of w's value type with at least w's bucket count, and both bucket counts at
+  // least the one that puts about 128 entries of the two lists into a bucket
+  rimu_vec tv;
+  tv.ctx = v->ctx;
+  const rimu_vec *src = v;
+  if (v->val_kind != w->val_kind) {                 // Int64 values into a Float64 list
+    if ((rc = rimu_vec_convert(&tv, v, w->val_kind))) { vec_free(&tv); return rc; }
+    src = &tv;
+  }
+  const bool w_empty = beta == 0.0;                 // scale!(w, 0) empties w
+  int nbits = std::max(std::max(w->nb_bits, src->nb_bits),
+                       ceil_log2((uint64_t)((w_empty ? 0 : w->len) + src->len) / 128 + 1));
+  for (int attempt = 0; attempt < 6; ++attempt, ++nbits) {
+    if (nbits > 26) { rc = RIMU_ERR_OVERFLOW; g_err = "rimu_vec_add: too many buckets"; break; }
+    if (src->nb_bits != nbits) {
+      if (src != &tv) {
+        if ((rc = rimu_vec_copy(&tv, src))) break;
+        src = &tv;
+      }
+      if ((rc = vec_regrid(&tv, nbits, capv_for(tv.len, nbits)))) break;
+    }
+    if (w->nb_bits != nbits && (rc = vec_regrid(w, nbits, capv_for(w->len, nbits)))) break;
+    rc = vec_axpby_same_layout(w, src, alpha, beta, ia, ib, w_empty);
+    if (rc != kCrowded) break;                      // a crowded bucket: split further
+  }
+  if (rc == kCrowded) { rc = RIMU_ERR_OVERFLOW; g_err = "rimu_vec_add: buckets too crowded"; }
+  vec_free(&tv);
+  if (rc) return rc;
+  return rimu_vec_walkernumber_and_length(w, nullptr, nullptr);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Working memory
 // ---------------------------------------------------------------------------------------------
 extern "C" int rimu_wm_create(rimu_ctx *ctx, rimu_wm **out) {

@@ -239,6 +239,15 @@ int rimu_launch_rebucket(rimu_ctx *ctx, const void *old_recs, const uint32_t *ol
 int rimu_launch_compact(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
                         uint32_t capv, const uint64_t *offsets, uint64_t *keys, uint64_t *vals,
                         int kw);
+// scale!/add! of walker lists (kw address words, kind RIMU_VAL_*)
+int rimu_launch_vec_scale(rimu_ctx *ctx, void *recs, uint32_t *count, int nb, uint32_t capv,
+                          int kind, int kw, double alpha, long long ialpha,
+                          unsigned long long *removed);
+int rimu_launch_vec_axpby(rimu_ctx *ctx, const void *rw, const uint32_t *cw, uint32_t capw,
+                          const void *rv, const uint32_t *cv, uint32_t capv, void *ro, uint32_t *co,
+                          uint32_t capo, int nb, int kind, int kw, double alpha, double beta,
+                          long long ialpha, long long ibeta, int w_empty, unsigned int *flag,
+                          unsigned long long *total);
 int rimu_launch_norm(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb,
                      uint32_t capv, int val_kind, unsigned long long *acc3, int kw);
 int rimu_launch_lookup(rimu_ctx *ctx, const void *recs, const uint32_t *count, int nb_bits,

@@ -111,7 +111,160 @@ int fail_arg(const std::string &msg) {
   return RIMU_ERR_BADARG;
 }
 
+// ---- scale! and add! (VectorInterface, src/DictVectors/abstractdvec.jl:121-188) ----------
+// A value that becomes an exact zero is removed, as setindex! of a zero removes the key.
+// Integer lists take integer factors; their products and sums wrap as Int64 arithmetic does.
+
+__device__ __forceinline__ uint64_t scale_bits(uint64_t v, int kind, double a, long long ia) {
+  return kind == RIMU_VAL_I64 ? (uint64_t)(long long)v * (uint64_t)ia : dbits(__dmul_rn(a, bitsd(v)));
+}
+__device__ __forceinline__ bool nonzero_bits(uint64_t v, int kind) {
+  return kind == RIMU_VAL_I64 ? v != 0 : !is_zero_d(bitsd(v));
+}
+
+// scale!(v, alpha): one warp per bucket, the survivors compacted in place (a round's reads all
+// happen before the ballot, and its writes land below the next round's reads).
+template <class K>
+__global__ void k_vec_scale(RecT<K> *recs, uint32_t *count, int nb, uint32_t capv, int kind,
+                            double alpha, long long ialpha, unsigned long long *removed) {
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  unsigned long long rm = 0;
+  for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < nb; b += gridDim.x * warps) {
+    const uint32_t n = count[b] < capv ? count[b] : capv;
+    RecT<K> *rb = recs + (size_t)b * capv;
+    uint32_t out = 0;
+    for (uint32_t f0 = 0; f0 < n; f0 += 32) {
+      const uint32_t f = f0 + (uint32_t)lane;
+      RecT<K> rec{};
+      bool keep = false;
+      if (f < n) {
+        rec = rb[f];
+        rec.val = scale_bits(rec.val, kind, alpha, ialpha);
+        keep = nonzero_bits(rec.val, kind);
+        rm += keep ? 0 : 1;
+      }
+      const uint32_t m = __ballot_sync(0xffffffffu, keep);
+      if (keep) rb[out + (uint32_t)__popc(m & lt)] = rec;
+      out += (uint32_t)__popc(m);
+      __syncwarp();
+    }
+    if (lane == 0) count[b] = out;
+  }
+  for (int o = 16; o > 0; o >>= 1) rm += __shfl_down_sync(0xffffffffu, rm, o);
+  if (lane == 0 && rm) atomicAdd(removed, rm);
+}
+
+constexpr int AX_THREADS = 128;
+constexpr uint32_t AX_MAXV = 1024;   // entries of v's bucket held in shared memory
+
+// add!(w, v, alpha, beta) on two lists with the same buckets: out = beta*w + alpha*v per
+// address (scale!(w, beta), then w[key] += alpha*val), into a third list.  One CTA per bucket:
+// v's entries in shared memory, each of w's entries looks its address up there; then the
+// addresses only v has.  flag bit 0: a bucket of v larger than AX_MAXV; bit 1: an output
+// bucket over capacity.
+template <class K>
+__global__ void __launch_bounds__(AX_THREADS) k_vec_axpby(
+    const RecT<K> *rw, const uint32_t *cw, uint32_t capw, const RecT<K> *rv,
+    const uint32_t *cv, uint32_t capv, RecT<K> *ro, uint32_t *co, uint32_t capo, int nb, int kind,
+    double alpha, double beta, long long ialpha, long long ibeta, int w_empty, unsigned int *flag,
+    unsigned long long *total) {
+  __shared__ K vkey[AX_MAXV];
+  __shared__ uint64_t vval[AX_MAXV];
+  __shared__ uint8_t vtaken[AX_MAXV];
+  __shared__ uint32_t s_out;
+  const int tid = threadIdx.x;
+  unsigned long long tot = 0;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const uint32_t nv = cv[b] < capv ? cv[b] : capv;
+    const uint32_t nw = w_empty ? 0u : (cw[b] < capw ? cw[b] : capw);
+    if (nv > AX_MAXV) {                 // the same for every thread of the CTA
+      if (tid == 0) { atomicOr(flag, 1u); co[b] = 0; }
+      continue;
+    }
+    for (uint32_t e = tid; e < nv; e += AX_THREADS) {
+      const RecT<K> rec = rv[(size_t)b * capv + e];
+      vkey[e] = rec.key;
+      vval[e] = rec.val;
+      vtaken[e] = 0;
+    }
+    if (tid == 0) s_out = 0;
+    __syncthreads();
+    RecT<K> *ob = ro + (size_t)b * capo;
+    for (uint32_t e = tid; e < nw; e += AX_THREADS) {
+      const RecT<K> rec = rw[(size_t)b * capw + e];
+      int j = -1;
+      for (uint32_t i = 0; i < nv; ++i)
+        if (vkey[i] == rec.key) { j = (int)i; break; }
+      uint64_t x;
+      if (kind == RIMU_VAL_I64) {
+        x = scale_bits(rec.val, kind, beta, ibeta);
+        if (j >= 0) { vtaken[j] = 1; x += scale_bits(vval[j], kind, alpha, ialpha); }
+      } else {
+        double y = __dmul_rn(beta, bitsd(rec.val));
+        if (j >= 0) { vtaken[j] = 1; y = __dadd_rn(y, __dmul_rn(alpha, bitsd(vval[j]))); }
+        x = dbits(y);
+      }
+      if (nonzero_bits(x, kind)) {
+        const uint32_t pos = atomicAdd(&s_out, 1u);
+        if (pos < capo) ob[pos] = RecT<K>{rec.key, x};
+      }
+    }
+    __syncthreads();
+    for (uint32_t e = tid; e < nv; e += AX_THREADS) {
+      if (vtaken[e]) continue;
+      const uint64_t x = scale_bits(vval[e], kind, alpha, ialpha);   // zero + alpha*val
+      if (nonzero_bits(x, kind)) {
+        const uint32_t pos = atomicAdd(&s_out, 1u);
+        if (pos < capo) ob[pos] = RecT<K>{vkey[e], x};
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t o = s_out;
+      co[b] = o < capo ? o : capo;
+      if (o > capo) atomicOr(flag, 2u);
+      tot += o < capo ? o : capo;
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && tot) atomicAdd(total, tot);
+}
+
 }  // namespace
+
+int rimu_launch_vec_scale(rimu_ctx *ctx, void *recs, uint32_t *count, int nb, uint32_t capv,
+                          int kind, int kw, double alpha, long long ialpha,
+                          unsigned long long *removed) {
+  const int warps = 4;
+  const int want = (nb + warps - 1) / warps, cap = ctx->num_sms * 16;
+  const int grid = want < cap ? want : cap;
+  if (kw == 2)
+    k_vec_scale<Key128><<<grid, warps * 32, 0, ctx->stream>>>(static_cast<Rec2 *>(recs), count, nb,
+                                                              capv, kind, alpha, ialpha, removed);
+  else
+    k_vec_scale<uint64_t><<<grid, warps * 32, 0, ctx->stream>>>(static_cast<Rec *>(recs), count, nb,
+                                                                capv, kind, alpha, ialpha, removed);
+  return rimu_cuda_check(cudaGetLastError(), "k_vec_scale");
+}
+
+int rimu_launch_vec_axpby(rimu_ctx *ctx, const void *rw, const uint32_t *cw, uint32_t capw,
+                          const void *rv, const uint32_t *cv, uint32_t capv, void *ro, uint32_t *co,
+                          uint32_t capo, int nb, int kind, int kw, double alpha, double beta,
+                          long long ialpha, long long ibeta, int w_empty, unsigned int *flag,
+                          unsigned long long *total) {
+  const int cap = ctx->num_sms * 8;
+  const int grid = nb < cap ? nb : cap;
+  if (kw == 2)
+    k_vec_axpby<Key128><<<grid, AX_THREADS, 0, ctx->stream>>>(
+        static_cast<const Rec2 *>(rw), cw, capw, static_cast<const Rec2 *>(rv), cv, capv,
+        static_cast<Rec2 *>(ro), co, capo, nb, kind, alpha, beta, ialpha, ibeta, w_empty, flag, total);
+  else
+    k_vec_axpby<uint64_t><<<grid, AX_THREADS, 0, ctx->stream>>>(
+        static_cast<const Rec *>(rw), cw, capw, static_cast<const Rec *>(rv), cv, capv,
+        static_cast<Rec *>(ro), co, capo, nb, kind, alpha, beta, ialpha, ibeta, w_empty, flag, total);
+  return rimu_cuda_check(cudaGetLastError(), "k_vec_axpby");
+}
 
 extern "C" int rimu_vec_dot(rimu_vec *a, rimu_vec *b, double *out) {
   if (!a || !b || !out) return fail_arg("rimu_vec_dot: NULL argument");

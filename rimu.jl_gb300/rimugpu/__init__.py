@@ -11,8 +11,8 @@ from .hamiltonians import (CubicGrid, HardwallBoundaries, HubbardMom1D, HubbardR
                            continuum_dispersion, hubbard_dispersion)
 from .styles import (Exact, IsDeterministic, IsDynamicSemistochastic, IsStochasticInteger,
                      NoCompression, ThresholdCompression, WithReplacement, default_style)
-from .dvec import (FirstOrderTransitionOperator, GPUDVec, GPUWorkingMemory, apply_operator,
-                   dot_operator, mul, working_memory)
+from .dvec import (FirstOrderTransitionOperator, GPUDVec, GPUWorkingMemory, add_, apply_operator,
+                   dot_operator, mul, scale_, working_memory)
 from .problem import (AllOverlaps, DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUpdate,
                       LogUpdate, LogUpdateAfterTargetWalkers, NoStats, PMCSimulation,
                       ProjectedEnergy, ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)

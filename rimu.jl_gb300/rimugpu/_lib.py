@@ -29,6 +29,7 @@ EXPORTS = [
     "rimu_vec_walkernumber_and_length", "rimu_vec_lookup", "rimu_vec_copy", "rimu_vec_empty",
     "rimu_wm_create", "rimu_wm_destroy", "rimu_wm_set_projector", "rimu_wm_set_timing",
     "rimu_wm_set_launch_shape", "rimu_wm_set_annihilation", "rimu_wm_set_projector_w",
+    "rimu_vec_scale", "rimu_vec_add",
     "rimu_wm_timing", "rimu_apply_operator",
     "rimu_basis_dimension", "rimu_basis_keys", "rimu_hv_basis", "rimu_hv_basis_adjoint",
     "rimu_hv_basis_adjoint_noalloc",
@@ -138,6 +139,8 @@ def load(build_if_missing: bool = True):
         "rimu_wm_destroy": ([vp], C.c_int),
         "rimu_wm_set_projector": ([vp, u64p, f64p, f64p, C.c_int], C.c_int),
         "rimu_wm_set_projector_w": ([vp, u64p, f64p, f64p, C.c_int], C.c_int),
+        "rimu_vec_scale": ([vp, C.c_double], C.c_int),
+        "rimu_vec_add": ([vp, vp, C.c_double, C.c_double], C.c_int),
         "rimu_wm_set_timing": ([vp, C.c_int], C.c_int),
         "rimu_wm_set_launch_shape": ([vp, C.c_int, C.c_int], C.c_int),
         "rimu_wm_set_annihilation": ([vp, C.c_int], C.c_int),

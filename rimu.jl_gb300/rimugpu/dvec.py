@@ -183,6 +183,25 @@ class GPUDVec:
         _lib.check(_lib.load().rimu_vec_dot(self.handle, other.handle, C.byref(out)))
         return out.value
 
+    def scale_(self, alpha) -> "GPUDVec":
+        """scale!(v, alpha) (abstractdvec.jl:131-140), on the device."""
+        _lib.check(_lib.load().rimu_vec_scale(self.handle, float(alpha)))
+        return self
+
+    def add_(self, other: "GPUDVec", alpha=1.0, beta=1.0) -> "GPUDVec":
+        """add!(self, other, alpha, beta) = beta*self + alpha*other (abstractdvec.jl:180-188),
+        on the device."""
+        _lib.check(_lib.load().rimu_vec_add(self.handle, other.handle, float(alpha), float(beta)))
+        return self
+
+    def norm(self, p=2) -> float:
+        """norm(v, p) for p = 1 (the walker number) and 2 (abstractdvec.jl:233-246)."""
+        if p == 1:
+            return self.walkernumber()
+        if p == 2:
+            return math.sqrt(self.dot(self))
+        raise ValueError(f"{p}-norm is not implemented")
+
     def as_float(self) -> "GPUDVec":
         """A Float64 copy on the device (IsDeterministic style)."""
         w = GPUDVec(style=IsDeterministic(), address_type=self._addr(0))
@@ -319,6 +338,16 @@ def apply_operator(wm: GPUWorkingMemory, target: GPUDVec, source: GPUDVec, op, b
     stats = tuple(full[n] for n in names)
     wm.last_stats = full
     return names, stats, wm, target
+
+
+def scale_(v: GPUDVec, alpha) -> GPUDVec:
+    """scale!(v, alpha) (VectorInterface, abstractdvec.jl:131-140)."""
+    return v.scale_(alpha)
+
+
+def add_(w: GPUDVec, v: GPUDVec, alpha=1.0, beta=1.0) -> GPUDVec:
+    """add!(w, v, alpha, beta) = axpby!(alpha, v, beta, w) (abstractdvec.jl:180-208)."""
+    return w.add_(v, alpha, beta)
 
 
 def mul(y: GPUDVec, H, x: GPUDVec, wm: GPUWorkingMemory | None = None) -> GPUDVec:

@@ -13,7 +13,8 @@ from .styles import (Exact, IsDeterministic, IsDynamicSemistochastic, IsStochast
                      NoCompression, ThresholdCompression, WithReplacement, default_style)
 from .dvec import (FirstOrderTransitionOperator, GPUDVec, GPUWorkingMemory, add_, apply_operator,
                    dot_operator, mul, scale_, working_memory)
-from .problem import (AllOverlaps, DoubleLogUpdate, DoubleLogUpdateAfterTargetWalkers, DontUpdate,
+from .problem import (AllOverlaps, DoubleLogProjected, DoubleLogUpdate,
+                      DoubleLogUpdateAfterTargetWalkers, DontUpdate,
                       LogUpdate, LogUpdateAfterTargetWalkers, NoStats, PMCSimulation,
                       ProjectedEnergy, ProjectorMonteCarloProblem, ReportDFAndInfo, init, solve)
 from .stats import blocking_analysis, mean_and_se, projected_energy, shift_estimator

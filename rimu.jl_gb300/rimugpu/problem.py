@@ -81,6 +81,28 @@ class DoubleLogUpdateAfterTargetWalkers(DoubleLogUpdate):
         return {"shift": sp.shift, "norm": tnorm, "shift_mode": sp.shift_mode}, True
 
 
+class DoubleLogProjected:
+    """S -= ξ/dτ ln(P·ψ_new / target) + ζ/dτ ln(P·ψ_new / P·ψ_old) with a fixed projector P
+    (shiftstrategy.jl:280-300); P is a dict address => value, its dot products with the
+    device lists are lookups of P's addresses."""
+
+    needs_vectors = True
+
+    def __init__(self, target, projector, ζ=0.08, ξ=None):
+        self.target = float(target)
+        self.projector = dict(projector)
+        self.ζ = ζ
+        self.ξ = ζ ** 2 / 4 if ξ is None else ξ
+
+    def update(self, sp, tnorm, v_new=None, v_old=None):
+        dτ = sp.time_step
+        tp = v_new.dot(self.projector)
+        pp = v_old.dot(self.projector)
+        sp.shift -= self.ξ / dτ * math.log(tp / self.target) + self.ζ / dτ * math.log(tp / pp)
+        sp.pnorm = tnorm
+        return {"shift": sp.shift, "norm": tnorm, "tp": tp, "pp": pp}, True
+
+
 # ----------------------------------------------------------------------------------------
 # Post-step strategies
 # ----------------------------------------------------------------------------------------
@@ -295,7 +317,12 @@ class PMCSimulation:
         s.v, s.pv = pv, s.v
         full = s.wm.last_stats
         tnorm, length = full["norm"], full["len"]
-        shift_stats, proceed = p.shift_strategy.update(sp, tnorm) if length else ({"shift": sp.shift, "norm": tnorm}, True)
+        if not length:
+            shift_stats, proceed = {"shift": sp.shift, "norm": tnorm}, True
+        elif getattr(p.shift_strategy, "needs_vectors", False):
+            shift_stats, proceed = p.shift_strategy.update(sp, tnorm, s.v, s.pv)
+        else:
+            shift_stats, proceed = p.shift_strategy.update(sp, tnorm)
         if self.step % p.reporting_strategy.reporting_interval == 0:
             rep = self.report
             rep.add("len" + s.id, length)

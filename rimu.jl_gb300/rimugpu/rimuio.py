@@ -2,11 +2,12 @@
 (src/RimuIO/RimuIO.jl:92-195), so that a GPU run can resume from, or hand off to, a CPU run.
 
 An Arrow IPC file (zstd-compressed) with two columns, `key` and `value`, and the keyword
-arguments of save_state as string metadata.  A single-chunk BoseFS/FermiFS address is the
-Arrow extension type "JuliaLang.Rimu.BoseFS.BitString" (or "...FermiFS.BitString") with
-metadata "N.M.B" over a one-element fixed-size list of the chunk type (UInt8/16/32/64 for B
-bits, num_chunks in bitstring.jl:6-18; RimuIO/arrowtypes.jl).  Values are Float64 or Int64.
-pyarrow is imported only when a file is read or written.
+arguments of save_state as string metadata.  A BoseFS/FermiFS address is the Arrow extension
+type "JuliaLang.Rimu.BoseFS.BitString" (or "...FermiFS.BitString") with metadata "N.M.B" over
+a fixed-size list of its BitString chunks (RimuIO/arrowtypes.jl): one UInt8/16/32/64 chunk for
+B <= 64 bits, two UInt64 chunks for 65-128 bits, the most significant chunk first (num_chunks,
+bitstring.jl:6-18; chunk order, :250-252).  Values are Float64 or Int64.  pyarrow is imported
+only when a file is read or written.
 """
 from __future__ import annotations
 
@@ -29,9 +30,9 @@ def _chunk_dtype(bits: int):
         return np.uint16
     if bits <= 32:
         return np.uint32
-    if bits <= 64:
+    if bits <= 128:
         return np.uint64
-    raise ValueError("addresses of more than 64 bits are not supported")
+    raise ValueError("addresses of more than 128 bits are not supported")
 
 
 def _address_info(proto):
@@ -77,15 +78,21 @@ def save_pairs(filename, keys, vals, proto, **metadata):
     """Write (address key, value) pairs of addresses like `proto` in the save_state format."""
     import pyarrow as pa
     kind, N, M, B = _address_info(proto)
-    keys = np.ascontiguousarray(keys, dtype=np.uint64)
     vals = np.asarray(vals)
     if vals.dtype.kind in "iu":
         vals = vals.astype(np.int64)
     else:
         vals = vals.astype(np.float64)
     dt = _chunk_dtype(B)
-    chunk = pa.array(keys.astype(dt))
-    key_arr = pa.FixedSizeListArray.from_arrays(chunk, 1)
+    if B > 64:                          # two chunks per address, (hi, lo)
+        ik = [int(k) for k in keys]
+        words = np.zeros(2 * len(ik), dtype=np.uint64)
+        for i, k in enumerate(ik):
+            words[2 * i], words[2 * i + 1] = k >> 64, k & ((1 << 64) - 1)
+        key_arr = pa.FixedSizeListArray.from_arrays(pa.array(words), 2)
+    else:
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        key_arr = pa.FixedSizeListArray.from_arrays(pa.array(keys.astype(dt)), 1)
     key_field = pa.field("key", key_arr.type, nullable=False,
                          metadata={_EXT_NAME: f"JuliaLang.Rimu.{kind}.BitString",
                                    _EXT_META: f"{N}.{M}.{B}"})
@@ -113,9 +120,15 @@ def load_pairs(filename):
         raise ValueError(f"`{filename}`: unsupported address type {name!r}")
     N, M, B = (int(x) for x in meta.split("."))
     col = table.column("key").combine_chunks()
-    if col.type.list_size != 1:
-        raise ValueError("addresses of more than one chunk are not supported")
-    keys = np.asarray(col.flatten().to_numpy(zero_copy_only=False), dtype=np.uint64)
+    nchunks = 1 if B <= 64 else (B - 1) // 64 + 1
+    if col.type.list_size != nchunks or nchunks > 2:
+        raise ValueError(f"`{filename}`: {col.type.list_size} chunks for {B}-bit addresses")
+    flat = np.asarray(col.flatten().to_numpy(zero_copy_only=False), dtype=np.uint64)
+    if nchunks == 1:
+        keys = flat
+    else:                               # (hi, lo) chunks: Python ints
+        keys = np.array([(int(flat[2 * i]) << 64) | int(flat[2 * i + 1])
+                         for i in range(len(flat) // 2)], dtype=object)
     vals = table.column("value").to_numpy()
     proto = (BoseFS if "BoseFS" in name else FermiFS).from_key(0, N, M)
     smeta = {k.decode(): _parse(v.decode()) for k, v in (table.schema.metadata or {}).items()}

@@ -87,3 +87,31 @@ def test_empty_vectors_of_both_value_types(tmp_path, dtype):
     rimuio.save_pairs(f, np.zeros(0, dtype=np.uint64), np.zeros(0, dtype=dtype), R.BoseFS([1, 1, 1, 1]))
     k, v, _, meta = rimuio.load_pairs(f)
     assert len(k) == 0 and len(v) == 0 and meta["RIMU_PACKAGE_VERSION"] == "0.14.0"
+
+
+@pytest.mark.parametrize("proto", [R.BoseFS([1] * 50), R.FermiFS([1] * 10 + [0] * 90)],
+                         ids=["bose-99", "fermi-100"])
+def test_two_chunk_addresses(tmp_path, proto):
+    """Addresses of 65-128 bits: a BitString of two UInt64 chunks (num_chunks,
+    bitstring.jl:6-18), stored most significant chunk first (:250-252), as a two-element
+    fixed-size list; round trip key for key."""
+    B = proto.nbits
+    assert 64 < B <= 128
+    rng = np.random.default_rng(3)
+    keys = sorted({int(rng.integers(0, 1 << 62)) | (int(rng.integers(0, 1 << (B - 64))) << 64)
+                   for _ in range(300)})
+    vals = rng.normal(size=len(keys))
+    f = tmp_path / "wide.arrow"
+    rimuio.save_pairs(f, np.array(keys, dtype=object), vals, proto, step=12)
+    k, v, p, meta = rimuio.load_pairs(f)
+    assert [int(x) for x in k] == keys and np.array_equal(v, vals) and meta["step"] == 12
+    assert type(p) is type(proto) and (p.N, p.M) == (proto.N, proto.M)
+    with pa.memory_map(str(f)) as src:
+        t = pa.ipc.open_file(src).read_all()
+    kf = t.schema.field("key")
+    assert kf.type == pa.list_(pa.uint64(), 2)
+    kind = "BoseFS" if isinstance(proto, R.BoseFS) else "FermiFS"
+    assert kf.metadata[b"ARROW:extension:metadata"] == f"{proto.N}.{proto.M}.{B}".encode()
+    assert kf.metadata[b"ARROW:extension:name"] == f"JuliaLang.Rimu.{kind}.BitString".encode()
+    first = t.column("key").combine_chunks()[0].as_py()
+    assert first == [keys[0] >> 64, keys[0] & ((1 << 64) - 1)]

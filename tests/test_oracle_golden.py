@@ -64,10 +64,43 @@ def test_exact_energies(case):
     elif case["model"] == "mom1d":
         onr = case["start"]
         E = O.ground_energy(O.mom1d(sum(onr), len(onr), case["u"], case["t"]), O.bose_key(onr))
+    elif case["model"] == "realspace_multi":
+        E = O.ground_energy(O.realspace_multi(tuple((bool(f), n) for f, n in case["comps"]),
+                                              tuple(case["dims"]), t=case["ct"], u=case["cu"]))
     else:
         E = O.ground_energy(O.realspace(case["N"], tuple(case["dims"]), u=case["u"], t=case["t"],
                                         fermion=True))
     assert E == pytest.approx(case["E0"], abs=case["atol"])
+
+
+def test_krylov_sector_of_a_4x4_fermion_address():
+    """test/Hamiltonians.jl:439-444: exact_energy (:13-17, eigsolve from the starting address)
+    of five free fermions on the periodic 4x4 lattice started from
+    FermiFS((1,0,1,0,1,0,1,0,1,0,0,...)) is -10, although the closed-shell ground state of the
+    whole basis is -4 + 4*(-2) = -12: the start address has no overlap with that state, so a
+    Krylov space built from it reaches -10 first.  Restated on the dense matrix: the lowest
+    eigenvalue whose eigenspace the start address overlaps.  This pins the fermionic hopping
+    signs across the periodic boundaries."""
+    c = G["krylov_sector"]
+    onr = c["start"]
+    m = O.realspace(sum(onr), tuple(c["dims"]), u=0.0, t=c["t"], fermion=True)
+    keys = O.basis(m)
+    start = sum(1 << i for i, x in enumerate(onr) if x)
+    H = O.sparse_matrix(m, keys).toarray()
+    w, V = np.linalg.eigh(H)
+    assert w[0] == pytest.approx(-12.0, abs=1e-9)
+    j = int(np.searchsorted(keys, start))
+    # group degenerate levels and take the first the start address overlaps
+    e_first, i = None, 0
+    while i < len(w):
+        k = i
+        while k < len(w) and w[k] - w[i] < 1e-8:
+            k += 1
+        if np.linalg.norm(V[j, i:k]) > 1e-8:
+            e_first = w[i]
+            break
+        i = k
+    assert e_first == pytest.approx(c["E0"], abs=c["atol"])
 
 
 def test_real1d_equals_realspace_1d():

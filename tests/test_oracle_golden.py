@@ -337,3 +337,33 @@ def test_oracle_hamiltonian_action_on_one_address(name, m, key):
     assert set(got) == set(want)
     for a, x in want.items():
         assert got[a] == pytest.approx(x, rel=1e-14, abs=1e-14), a
+
+
+def test_hubbard_models_with_t_or_u_zero():
+    """test/Hamiltonians.jl:217-250 on the oracle with the host's momentum grid and
+    dispersions: with t = 0 or u = 0 the diagonal or the offdiagonals vanish; with u = 0 the
+    hubbard dispersion of three bosons in the k = 0 mode gives -2tN and the continuum
+    dispersion 0; for BoseFS(3,3,3) the continuum diagonal is 6t(2pi/M)^2 and above the
+    shifted hubbard one."""
+    import rimugpu as R
+
+    def mom(h):
+        m = O.mom1d(h.N, h.M, h.u, h.t)
+        m.kes = np.array(h.kes)
+        return m
+
+    bs1, bs2, bs3 = R.BoseFS((0, 1, 0)), R.BoseFS((3, 3, 3)), R.BoseFS((0, 3, 0))
+    assert O.diagonal(mom(R.HubbardMom1D(bs1, t=0.0)), bs1.key) == 0
+    assert O.diagonal(O.real1d(bs2.N, bs2.M, 0.0, 1.0), bs2.key) == 0
+    assert all(v == 0 for _, v in O.offdiagonals(mom(R.HubbardMom1D(bs1, u=0.0)), bs1.key))
+    assert all(v == 0 for _, v in O.offdiagonals(O.real1d(bs2.N, bs2.M, 1.0, 0.0), bs2.key))
+    t = 1.0
+    c3 = R.HubbardMom1D(bs3, u=0.0, t=t, dispersion=R.hamiltonians.continuum_dispersion)
+    h3 = R.HubbardMom1D(bs3, u=0.0, t=t)
+    assert O.diagonal(mom(c3), bs3.key) == 0
+    assert 2 * t * bs3.N + O.diagonal(mom(h3), bs3.key) == 0
+    c2 = R.HubbardMom1D(bs2, u=0.0, t=t, dispersion=R.hamiltonians.continuum_dispersion)
+    h2 = R.HubbardMom1D(bs2, u=0.0, t=t)
+    d2 = O.diagonal(mom(c2), bs2.key)
+    assert d2 > 2 * t * bs2.N + O.diagonal(mom(h2), bs2.key)
+    assert d2 == pytest.approx(6 * t * (2 * np.pi / bs2.M) ** 2)

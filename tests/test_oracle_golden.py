@@ -367,3 +367,17 @@ def test_hubbard_models_with_t_or_u_zero():
     d2 = O.diagonal(mom(c2), bs2.key)
     assert d2 > 2 * t * bs2.N + O.diagonal(mom(h2), bs2.key)
     assert d2 == pytest.approx(6 * t * (2 * np.pi / bs2.M) ** 2)
+
+
+@pytest.mark.parametrize("fermion,onr", [(False, (1, 1, 1, 0, 0, 0)), (True, (1, 0, 0, 0, 1, 0))],
+                         ids=["bose", "fermi"])
+def test_hardwall_lattice_orientation(fermion, onr):
+    """test/Hamiltonians.jl:472-484: HubbardRealSpace with default u and t on hard-wall 2x3 and
+    3x2 lattices has the same ground energy from the same start address (eigsolve from the
+    starting address: here the block connected to it)."""
+    start = sum(1 << i for i, x in enumerate(onr) if x) if fermion else O.bose_key(list(onr))
+    e = []
+    for dims in ((2, 3), (3, 2)):
+        m = O.realspace(sum(onr), dims, u=1.0, t=1.0, periodic=(False, False), fermion=fermion)
+        e.append(O.ground_energy(m, start))
+    assert e[0] == pytest.approx(e[1], rel=1e-12)
